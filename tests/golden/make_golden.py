@@ -1,0 +1,366 @@
+"""Generate golden vectors by executing NetKet's own source in this container.
+
+NetKet cannot be imported here (jax, flax, numba and igraph are absent), but the
+functions that pin the hot path are plain numpy / numba-kernel code.  This
+script parses the reference source files, extracts the named functions, strips
+their decorators (``numba.jit`` becomes a plain Python function, ``jax.jit`` is
+dropped) and executes them with numpy standing in for ``jax.numpy``.  Nothing
+from the reference is copied into the repository: only the input/output arrays
+are written, to ``tests/golden/*.npz``.
+
+Covered:
+  edges.npz      get_nn_edges (graph/_lattice_edge_logic.py:102-137) on several lattices
+  ising.npz      IsingNumba._flattened_kernel (operator/_ising/numba.py:101-132)
+  localop.npz    pack_internals + LocalOperatorNumba._get_conn_flattened_kernel
+                 (operator/_local_operator/compile_helpers.py:29-171,
+                 operator/_local_operator/numba.py:132-240) for Heisenberg
+                 (operator/_heisenberg.py:33-132 via operator/_graph_operator.py:47-145)
+                 and Ising-as-LocalOperator
+  logcosh.npz    log_cosh (nn/activation.py:78-84)
+  stats.npz      _statistics (stats/mc_stats_old.py:88-196)
+  ngd.npz        _prepare_input + _compute_srt_update + _compute_sr_update
+                 (_src/ngd/sr_srt_common.py:45-101, _src/ngd/srt.py:22-96,
+                 _src/ngd/sr.py:23-80) with cholesky / pinv_smooth /
+                 cholesky_with_fallback (optimizer/solver/solvers.py,
+                 _src/solvers/nan_fallback.py:22-45)
+
+Run:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+(default reference root: /root/reference).
+"""
+import __future__
+import ast
+import os
+import sys
+import types
+
+import numpy as np
+import scipy.linalg
+import scipy.sparse
+from scipy.sparse import find, triu
+from scipy.spatial import cKDTree
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+NK = os.path.join(REF, "netket")
+
+
+def load(relpath, names, ns, class_name=None):
+    """Exec the named top-level (or class-level) functions of a reference file."""
+    path = os.path.join(NK, relpath)
+    tree = ast.parse(open(path).read(), filename=path)
+    body = tree.body
+    if class_name is not None:
+        body = next(n for n in tree.body if isinstance(n, ast.ClassDef)
+                    and n.name == class_name).body
+    nodes = [n for n in body if isinstance(n, ast.FunctionDef) and n.name in names]
+    missing = set(names) - {n.name for n in nodes}
+    if missing:
+        raise RuntimeError(f"{relpath}: functions not found: {missing}")
+    for n in nodes:
+        n.decorator_list = []
+    mod = ast.Module(body=nodes, type_ignores=[])
+    code = compile(mod, path, "exec", flags=__future__.annotations.compiler_flag,
+                   dont_inherit=True)
+    exec(code, ns)
+    return ns
+
+
+# ---------------------------------------------------------------- shims
+numba_stub = types.SimpleNamespace(jit=lambda *a, **k: (lambda f: f))
+
+
+def lax_cond(pred, true_fun, false_fun, *operands):
+    return true_fun(*operands) if bool(pred) else false_fun(*operands)
+
+
+jax_stub = types.SimpleNamespace(
+    lax=types.SimpleNamespace(cond=lax_cond, add=np.add,
+                              collapse=lambda x, a, b: x.reshape((-1,) + x.shape[b:])),
+    Array=np.ndarray,
+)
+
+
+class FakeHilbert:
+    def __init__(self, N):
+        self.size = N
+        self.shape = [2] * N
+
+    def size_at_index(self, i):
+        return 2
+
+
+def ravel_identity(x):
+    x = np.asarray(x)
+    return x, (lambda y: y)
+
+
+# ---------------------------------------------------------------- edges
+def gen_edges():
+    ns = {"np": np, "cKDTree": cKDTree, "find": find, "triu": triu}
+    load("utils/float.py", ["comparable"], ns)
+    load("graph/_lattice_edge_logic.py",
+         ["create_site_positions", "site_to_idx", "create_padded_sites",
+          "get_naive_edges", "get_nn_edges"], ns)
+    cases = {
+        "chain16": ([16], True, 1), "chain5": ([5], True, 1), "chain8_obc": ([8], False, 1),
+        "chain14_nnn": ([14], True, 2), "square4": ([4, 4], True, 1),
+        "square6_nnn": ([6, 6], True, 2), "square10_nnn": ([10, 10], True, 2),
+        "square16": ([16, 16], True, 1), "cube3": ([3, 3, 3], True, 1),
+    }
+    out = {}
+    for name, (extent, pbc, order) in cases.items():
+        d = len(extent)
+        e = ns["get_nn_edges"](np.eye(d), np.asarray(extent), np.zeros((1, d)),
+                               np.array([pbc] * d), 1e-5, order)
+        out[name] = np.array(e, dtype=np.int64).reshape(-1, 3)
+        out[name + "__meta"] = np.array(extent + [int(pbc), order], dtype=np.int64)
+    np.savez_compressed(os.path.join(HERE, "edges.npz"), **out)
+    return out
+
+
+# ---------------------------------------------------------------- operators
+def gen_ising(edges):
+    ns = {"np": np}
+    load("operator/_ising/numba.py", ["_flattened_kernel"], ns, class_name="IsingNumba")
+    rng = np.random.default_rng(1234)
+    out = {}
+    for name, N, h, J in [("chain16", 16, 1.0, 1.0), ("chain5", 5, 0.7, -1.3),
+                          ("square4", 16, 0.5, 1.0)]:
+        e = edges[name][:, :2]
+        x_ids = rng.integers(0, 2, size=(37, N)).astype(np.int8)
+        sections = np.zeros(x_ids.shape[0], dtype=np.int64)
+        xp_ids, mels = ns["_flattened_kernel"](x_ids, sections, e.astype(np.intp),
+                                               np.float64(h), np.float64(J))
+        out[name + "__x_ids"] = x_ids
+        out[name + "__xp_ids"] = xp_ids
+        out[name + "__mels"] = mels
+        out[name + "__hJ"] = np.array([h, J])
+    np.savez_compressed(os.path.join(HERE, "ising.npz"), **out)
+
+
+def gen_localop(edges):
+    from oracle import graph as og, operator as oop
+    ns = {"np": np, "numba": numba_stub, "sparse": scipy.sparse}
+    load("operator/_local_operator/compile_helpers.py",
+         ["pack_internals", "_append_matrix", "_append_matrix_sparse",
+          "_number_to_state", "max_nonzero_per_row"], ns)
+    load("operator/_local_operator/numba.py", ["_get_conn_flattened_kernel"], ns,
+         class_name="LocalOperatorNumba")
+    # GraphOperator / Heisenberg term construction, recorded through a fake class
+    rec = {}
+
+    def recorder(hilbert, operators, acting_on, dtype=None):
+        rec["ops"], rec["aon"] = operators, acting_on
+        return rec
+
+    gns = {"np": np, "Sequence": (list, tuple), "Graph": None, "_LocalOperator": recorder}
+    load("operator/_graph_operator.py", ["check_acting_on_subspace", "GraphOperator"], gns)
+    load("operator/_heisenberg.py", ["Heisenberg"], gns)
+
+    rng = np.random.default_rng(4321)
+    out = {}
+    cases = [
+        ("heis_chain16", "chain16", 1.0, None), ("heis_square4", "square4", 1.0, None),
+        ("heis_square4_nosign", "square4", 1.0, False),
+        ("j1j2_square6", "square6_nnn", [1.0, 0.5], None),
+        ("j1j2_chain14", "chain14_nnn", [1.0, 0.2], None),
+        ("j1j2_square10", "square10_nnn", [1.0, 0.5], None),
+    ]
+    for name, gname, J, sr in cases:
+        e = edges[gname]
+        meta = edges[gname + "__meta"]
+        N = int(np.prod(meta[:-2]))
+        g = og.Graph([tuple(r) for r in e], N)
+        kwargs = {"cls": recorder}
+        if sr is not None:
+            kwargs["sign_rule"] = sr
+        gns["Heisenberg"](FakeHilbert(N), g, J, **kwargs)
+        ops = [np.asarray(o, dtype=np.float64) for o in rec["ops"]]
+        aon = [tuple(int(s) for s in a) for a in rec["aon"]]
+        _store_localop(ns, out, name, N, ops, aon, rng, oop)
+    # Ising as a LocalOperator: 1-site and 2-site groups
+    e = edges["chain5"][:, :2]
+    ops = [-0.7 * oop.SIGMAX for _ in range(5)] + [1.3 * np.kron(oop.SIGMAZ, oop.SIGMAZ)
+                                                   for _ in e]
+    aon = [(i,) for i in range(5)] + [tuple(int(s) for s in r) for r in e]
+    _store_localop(ns, out, "ising_local_chain5", 5, ops, aon, rng, oop)
+    np.savez_compressed(os.path.join(HERE, "localop.npz"), **out)
+
+
+def _store_localop(ns, out, name, N, ops, aon, rng, oop):
+    # _operators_dict summation (base.py:135-147); acting_on are sorted already
+    d = {}
+    for o, a in zip(ops, aon):
+        assert list(a) == sorted(a)
+        d[a] = d[a] + o if a in d else o
+    packed = ns["pack_internals"](FakeHilbert(N), d, np.float64(0.0), np.float64, 1e-10)
+    n = 23
+    x_ids = rng.integers(0, 2, size=(n, N)).astype(np.int8)
+    sections = np.zeros(n, dtype=np.int64)
+    xp_ids, mels = ns["_get_conn_flattened_kernel"](
+        x_ids, sections, packed["basis"], np.array(0.0), packed["diag_mels"],
+        packed["n_conns"], packed["mels"], packed["x_prime"], packed["acting_on"],
+        packed["acting_size"], packed["nonzero_diagonal"], False)
+    out[name + "__N"] = np.array(N)
+    out[name + "__aon"] = np.array([list(a) + [-1] * (2 - len(a)) for a in d.keys()])
+    out[name + "__ops"] = np.array([np.pad(m, ((0, 4 - m.shape[0]), (0, 4 - m.shape[1])))
+                                    for m in d.values()])
+    out[name + "__sizes"] = np.array([len(a) for a in d.keys()])
+    out[name + "__x_ids"] = x_ids
+    out[name + "__xp_ids"] = xp_ids
+    out[name + "__mels"] = mels
+    out[name + "__sections"] = sections
+    out[name + "__max_conn_numba"] = np.array(packed["max_conn_size"])
+    # max_conn_size of the JAX packer (compile_helpers.py:174-218), via the same helper
+    sizes = np.array([len(a) for a in d.keys()])
+    K, nz = 0, False
+    for s in np.unique(sizes):
+        sub = {a: m for a, m in d.items() if len(a) == s}
+        p = ns["pack_internals"](FakeHilbert(N), sub, 0, np.float64, 1e-10)
+        k = int(p["max_conn_size"]) - (1 if p["nonzero_diagonal"] else 0)
+        K += k
+        nz = nz or bool(p["nonzero_diagonal"])
+    out[name + "__max_conn_jax"] = np.array(K + (1 if nz else 0))
+
+
+# ---------------------------------------------------------------- log_cosh
+def gen_logcosh():
+    ns = {"jnp": np}
+    load("nn/activation.py", ["log_cosh"], ns)
+    x = np.concatenate([np.linspace(-30, 30, 601), np.array([0.0, -0.0, 1e-12, -1e-8, 50.0,
+                                                               -700.0, 700.0])])
+    rng = np.random.default_rng(7)
+    x = np.concatenate([x, rng.normal(0, 2, 500)])
+    np.savez_compressed(os.path.join(HERE, "logcosh.npz"), x=x, y=ns["log_cosh"](x))
+
+
+# ---------------------------------------------------------------- stats
+def gen_stats():
+    jnp = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("_")})
+    jnp.clip = lambda a, lo=None, hi=None: np.clip(a, lo, hi)
+    ns = {
+        "np": np, "jnp": jnp, "jax": jax_stub,
+        "nkjax": types.SimpleNamespace(dtype_real=lambda dt: np.float64),
+        "config": types.SimpleNamespace(netket_use_plain_rhat=False),
+        "Stats": lambda *a: np.array(a, dtype=np.float64),
+    }
+    load("stats/mc_stats_old.py", ["_get_blocks", "_block_variance", "_batch_variance",
+                                   "_statistics"], ns)
+    rng = np.random.default_rng(99)
+    out = {}
+    cases = {
+        "c1": rng.normal(-20, 1.0, size=(16, 63)),
+        "c2": rng.normal(-50, 3.0, size=(1024, 4)),
+        "odd": rng.normal(0, 1, size=(40, 7)),
+        "onechain": rng.normal(1, 1, size=(1, 100)),
+        "wide": rng.normal(0, 1, size=(64, 64)),
+    }
+    # correlated chains (AR(1)) so that tau > 0 and the block path is exercised
+    ar = np.zeros((8, 1024))
+    for t in range(1, 1024):
+        ar[:, t] = 0.95 * ar[:, t - 1] + rng.normal(size=8)
+    cases["ar1_blocks"] = ar
+    cases["ar1_slow"] = np.cumsum(rng.normal(size=(40, 64)), axis=1)
+    for k, v in cases.items():
+        out[k + "__data"] = v
+        out[k + "__stats"] = ns["_statistics"](v, 32)
+    np.savez_compressed(os.path.join(HERE, "stats.npz"), **out)
+
+
+# ---------------------------------------------------------------- NGD
+def gen_ngd():
+    jnp = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("_")})
+    # XLA's factorisations return NaN instead of raising; mirror that
+    def cho_factor(A, lower=False):
+        try:
+            return scipy.linalg.cho_factor(A, lower=lower, check_finite=False)
+        except np.linalg.LinAlgError:
+            return np.full_like(A, np.nan), lower
+
+    def cho_solve(cl, b):
+        return scipy.linalg.cho_solve(cl, b, check_finite=False)
+
+    def eigh(A):
+        if not np.all(np.isfinite(A)):
+            return np.full(A.shape[0], np.nan), np.full_like(A, np.nan)
+        return np.linalg.eigh(A)
+
+    jnp.linalg = types.SimpleNamespace(eigh=eigh)
+    jsp = types.SimpleNamespace(linalg=types.SimpleNamespace(cho_factor=cho_factor,
+                                                             cho_solve=cho_solve))
+    ns = {"np": np, "jnp": jnp, "jax": jax_stub, "jsp": jsp,
+          "ravel_pytree": ravel_identity,
+          "config": types.SimpleNamespace(netket_sharding=False),
+          "nkjax": types.SimpleNamespace(tree_leaf_iscomplex=lambda s: False),
+          "ensure_accepts_kwargs": lambda f, *names: (lambda A, b, **kw: f(A, b)),
+          "warn_deprecation": lambda *a, **k: None,
+          "Union": object}
+    load("_src/ngd/sr_srt_common.py", ["_prepare_input"], ns)
+    load("_src/ngd/srt.py", ["_compute_srt_update"], ns)
+    load("_src/ngd/sr.py", ["_compute_sr_update"], ns)
+    load("optimizer/solver/solvers.py", ["cholesky", "pinv_smooth", "cholesky_with_fallback"], ns)
+    load("_src/solvers/nan_fallback.py", ["_nan_fallback_solver"], ns)
+    # cholesky_with_fallback builds pinv_smooth(rtol=..) through partial_from_kwargs;
+    # restore that behaviour for keyword-only calls
+    pinv = ns["pinv_smooth"]
+
+    def pinv_kw(A=None, b=None, **kw):
+        if A is None:
+            return lambda A_, b_, x0=None: pinv(A_, b_, **kw)
+        return pinv(A, b, **kw)
+    ns["pinv_smooth"] = pinv_kw
+
+    rng = np.random.default_rng(2024)
+    out = {}
+    for name, n, P, shift in [("minsr", 48, 120, 1e-4), ("sr", 96, 40, 1e-2),
+                              ("minsr_big_shift", 32, 64, 0.1)]:
+        O = rng.normal(size=(n, P))
+        O = O - O.mean(axis=0)
+        e = rng.normal(-3, 1, size=n)
+        O_L, dv = ns["_prepare_input"](O, e, mode="real", scaling_factor=1.0 / n)
+        solver = ns["cholesky_with_fallback"]
+        if name.startswith("minsr"):
+            upd, _, info = ns["_compute_srt_update"](O_L, dv, diag_shift=shift,
+                                                     solver_fn=solver, mode="real",
+                                                     params_structure=None)
+        else:
+            upd, _, info = ns["_compute_sr_update"](O_L, dv, diag_shift=shift,
+                                                    solver_fn=solver, mode="real",
+                                                    params_structure=None)
+        out[name + "__O"] = O
+        out[name + "__e"] = e
+        out[name + "__shift"] = np.array(shift)
+        out[name + "__update"] = np.asarray(upd)
+        out[name + "__fallback"] = np.array(bool(info["solver_fallback"]))
+    # fallback: NaN in the matrix routes to pinv_smooth
+    A = rng.normal(size=(12, 12))
+    A = A @ A.T + 1e-3 * np.eye(12)
+    b = rng.normal(size=12)
+    x, info = ns["cholesky_with_fallback"](A, b)
+    out["solve_spd__A"], out["solve_spd__b"], out["solve_spd__x"] = A, b, np.asarray(x)
+    Ab = A.copy()
+    Ab[0, 0] = np.nan
+    xb, infob = ns["cholesky_with_fallback"](Ab, b)
+    out["solve_nan__x"] = np.asarray(xb)
+    out["solve_nan__fallback"] = np.array(bool(infob["solver_fallback"]))
+    # singular matrix: pinv_smooth directly
+    U = rng.normal(size=(10, 4))
+    S = U @ U.T
+    xs, _ = ns["pinv_smooth"](S, b[:10])
+    out["pinv_singular__A"], out["pinv_singular__b"], out["pinv_singular__x"] = S, b[:10], xs
+    np.savez_compressed(os.path.join(HERE, "ngd.npz"), **out)
+
+
+if __name__ == "__main__":
+    edges = gen_edges()
+    gen_ising(edges)
+    gen_localop(edges)
+    gen_logcosh()
+    gen_stats()
+    gen_ngd()
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")

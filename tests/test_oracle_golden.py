@@ -1,0 +1,167 @@
+"""Pin the CPU oracle against golden vectors produced by NetKet's own source
+(tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+from oracle import graph as og
+from oracle import hilbert as oh
+from oracle import operator as oop
+from oracle import rbm as orbm
+from oracle import stats as ost
+from oracle import ngd as ongd
+
+EDGE_CASES = ["chain16", "chain5", "chain8_obc", "chain14_nnn", "square4", "square6_nnn",
+              "square10_nnn", "square16", "cube3"]
+
+
+@pytest.mark.parametrize("name", EDGE_CASES)
+def test_edges_match_reference_order(golden, name):
+    g = golden("edges")
+    meta = g[name + "__meta"]
+    extent, pbc, order = list(meta[:-2]), bool(meta[-2]), int(meta[-1])
+    mine = np.array(og.lattice_edges(extent, pbc, order), dtype=np.int64).reshape(-1, 3)
+    np.testing.assert_array_equal(mine, g[name])
+
+
+@pytest.mark.parametrize("name", ["chain16", "chain5", "square4"])
+def test_ising_conn_matches_numba_kernel(golden, name):
+    gi = golden("ising")
+    edges = golden("edges")[name][:, :2]
+    h, J = gi[name + "__hJ"]
+    x = oh.local_indices_to_states(gi[name + "__x_ids"])
+    xp, mels = oop.ising_get_conn_padded(x, edges, h, J)
+    n, K, N = xp.shape
+    ref_xp = oh.local_indices_to_states(gi[name + "__xp_ids"]).reshape(n, K, N)
+    np.testing.assert_array_equal(xp, ref_xp)
+    np.testing.assert_array_equal(mels, gi[name + "__mels"].reshape(n, K))
+
+
+LOCALOP_CASES = ["heis_chain16", "heis_square4", "heis_square4_nosign", "j1j2_square6",
+                 "j1j2_chain14", "j1j2_square10", "ising_local_chain5"]
+
+
+def _build_local(gl, name, golden):
+    N = int(gl[name + "__N"])
+    ops, aon = [], []
+    for a, m, s in zip(gl[name + "__aon"], gl[name + "__ops"], gl[name + "__sizes"]):
+        d = 2**int(s)
+        ops.append(m[:d, :d])
+        aon.append([int(v) for v in a[:s]])
+    return N, oop.LocalOperator(N, ops, aon)
+
+
+def _heis_from_graph(golden, name):
+    table = {"heis_chain16": ("chain16", 1.0, None), "heis_square4": ("square4", 1.0, None),
+             "heis_square4_nosign": ("square4", 1.0, False),
+             "j1j2_square6": ("square6_nnn", [1.0, 0.5], None),
+             "j1j2_chain14": ("chain14_nnn", [1.0, 0.2], None),
+             "j1j2_square10": ("square10_nnn", [1.0, 0.5], None)}
+    gname, J, sr = table[name]
+    ge = golden("edges")
+    meta = ge[gname + "__meta"]
+    N = int(np.prod(meta[:-2]))
+    g = og.Graph([tuple(r) for r in ge[gname]], N)
+    return oop.heisenberg(N, g, J, sign_rule=sr)
+
+
+@pytest.mark.parametrize("name", LOCALOP_CASES)
+def test_localop_terms_match_reference_construction(golden, name):
+    """Heisenberg/GraphOperator term order and matrices equal NetKet's."""
+    if name == "ising_local_chain5":
+        pytest.skip("built directly from terms")
+    gl = golden("localop")
+    op = _heis_from_graph(golden, name)
+    assert [list(a) for a in op.acting_on] == [list(a[:s]) for a, s in
+                                               zip(gl[name + "__aon"], gl[name + "__sizes"])]
+    for m, ref in zip(op.operators, gl[name + "__ops"]):
+        np.testing.assert_array_equal(m, ref[:m.shape[0], :m.shape[1]])
+
+
+@pytest.mark.parametrize("name", LOCALOP_CASES)
+def test_localop_conn_matches_numba_kernel(golden, name):
+    gl = golden("localop")
+    N, op = _build_local(gl, name, golden)
+    assert op.max_conn_size == int(gl[name + "__max_conn_jax"])
+    x = oh.local_indices_to_states(gl[name + "__x_ids"])
+    sections = gl[name + "__sections"]
+    ref_xp = oh.local_indices_to_states(gl[name + "__xp_ids"])
+    ref_m = gl[name + "__mels"]
+    # numba order, unfiltered, per sample
+    flat = op.get_conn_flattened_numba_order(x)
+    start = 0
+    for b, (xs, ms) in enumerate(flat):
+        stop = sections[b]
+        np.testing.assert_array_equal(xs, ref_xp[start:stop])
+        np.testing.assert_array_equal(ms, ref_m[start:stop])
+        start = stop
+    # padded JAX order == numba order with |mel| <= cutoff dropped, when all
+    # terms act on the same number of sites (one group)
+    xp, mels = op.get_conn_padded(x)
+    single_group = len(set(gl[name + "__sizes"].tolist())) == 1
+    start = 0
+    for b in range(x.shape[0]):
+        stop = sections[b]
+        keep = np.abs(ref_m[start:stop]) > 1e-10
+        rx, rm = ref_xp[start:stop][keep], ref_m[start:stop][keep]
+        k = len(rm)
+        if single_group:
+            np.testing.assert_array_equal(xp[b, :k], rx)
+            np.testing.assert_array_equal(mels[b, :k], rm)
+        else:  # canonicalised comparison (test/operator/test_hamiltonian.py:160-218)
+            o1 = np.lexsort(xp[b, :k].T)
+            o2 = np.lexsort(rx.T)
+            np.testing.assert_array_equal(xp[b, :k][o1], rx[o2])
+            np.testing.assert_array_equal(mels[b, :k][o1], rm[o2])
+        assert np.all(mels[b, k:] == 0)
+        assert np.all(xp[b, k:] == x[b])
+        start = stop
+
+
+def test_log_cosh(golden):
+    g = golden("logcosh")
+    np.testing.assert_array_equal(orbm.log_cosh(g["x"]), g["y"])
+
+
+@pytest.mark.parametrize("name", ["c1", "c2", "odd", "onechain", "wide", "ar1_blocks",
+                                  "ar1_slow"])
+def test_stats(golden, name):
+    g = golden("stats")
+    s = ost.statistics(g[name + "__data"]).as_array()
+    np.testing.assert_allclose(s, g[name + "__stats"], rtol=1e-12, atol=1e-14,
+                               equal_nan=True)
+
+
+@pytest.mark.parametrize("name", ["minsr", "sr", "minsr_big_shift"])
+def test_ngd_updates(golden, name):
+    g = golden("ngd")
+    O, e, shift = g[name + "__O"], g[name + "__e"], float(g[name + "__shift"])
+    if name.startswith("minsr"):
+        upd, info = ongd.srt_update(O, e, shift)
+    else:
+        upd, info = ongd.sr_update(O, e, shift)
+    np.testing.assert_allclose(upd, g[name + "__update"], rtol=1e-10, atol=1e-12)
+    assert info["solver_fallback"] == bool(g[name + "__fallback"])
+
+
+def test_solvers(golden):
+    g = golden("ngd")
+    x, info = ongd.cholesky_with_fallback(g["solve_spd__A"], g["solve_spd__b"])
+    np.testing.assert_allclose(x, g["solve_spd__x"], rtol=1e-12)
+    assert not info["solver_fallback"]
+    A = g["solve_spd__A"].copy()
+    A[0, 0] = np.nan
+    _, info = ongd.cholesky_with_fallback(A, g["solve_spd__b"])
+    assert info["solver_fallback"] and bool(g["solve_nan__fallback"])
+    xs, _ = ongd.pinv_smooth(g["pinv_singular__A"], g["pinv_singular__b"])
+    np.testing.assert_allclose(xs, g["pinv_singular__x"], rtol=1e-8, atol=1e-10)
+
+
+def test_minsr_equals_sr():
+    """Woodbury identity, as NetKet's test/driver/test_srt.py:98-175 (atol 1e-10)."""
+    rng = np.random.default_rng(0)
+    O = rng.normal(size=(40, 25))
+    O -= O.mean(0)
+    e = rng.normal(size=40)
+    a, _ = ongd.srt_update(O, e, 1e-3)
+    b, _ = ongd.sr_update(O, e, 1e-3)
+    np.testing.assert_allclose(a, b, atol=1e-10)
