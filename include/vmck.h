@@ -1,0 +1,252 @@
+/*
+ * vmck.h - C ABI of the GB300-native VMC hot loop (libvmck.so).
+ *
+ * One function per hot-path kernel.  Every pointer argument is a DEVICE pointer
+ * unless stated otherwise; the caller owns all input and output buffers.  Calls
+ * are stream-ordered on the given stream (a cudaStream_t passed as void*; NULL is
+ * the legacy default stream) and return a host status code (VMCK_OK == 0).
+ * Conditions found on the device (non-finite values, a failed factorisation)
+ * are OR-ed into an optional int32 device status word, read by the host once per
+ * step.  No kernel traps.
+ *
+ * Spin configurations are int8 values in {+1, -1} (NetKet's Spin(1/2) states,
+ * netket/hilbert/spin.py:167-172).  RBM parameters are one flat buffer in NetKet's
+ * ravel order: [Dense.bias (M) | Dense.kernel (N*M, row-major) | visible_bias (N)]
+ * (netket/models/rbm.py:57-81 under jax.flatten_util.ravel_pytree).
+ */
+#ifndef VMCK_H
+#define VMCK_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VMCK_ABI_VERSION 1
+
+/* host status codes */
+#define VMCK_OK 0
+#define VMCK_ERR_ARG 1         /* null pointer, bad size */
+#define VMCK_ERR_UNSUPPORTED 2 /* dtype / shape outside what the kernel handles */
+#define VMCK_ERR_CUDA 3        /* a CUDA runtime call or launch failed */
+#define VMCK_ERR_LIBRARY 4     /* cuBLAS / cuSOLVER failure */
+#define VMCK_ERR_NOMEM 5       /* workspace allocation failed */
+
+/* device status bits */
+#define VMCK_DEV_NONFINITE 1   /* NaN or Inf in a solver input or output */
+#define VMCK_DEV_NOT_SPD 2     /* Cholesky info != 0 */
+#define VMCK_DEV_NO_CONVERGE 4 /* iterative refinement did not reach tolerance */
+
+/* element types */
+#define VMCK_F64 0
+#define VMCK_F32 1
+#define VMCK_BF16 2
+
+typedef void *vmck_stream; /* cudaStream_t */
+typedef struct vmck_ctx vmck_ctx;
+
+int vmck_abi_version(void);
+const char *vmck_error_string(int code);
+/* Last CUDA / library error text recorded by this thread (host string). */
+const char *vmck_last_error(void);
+
+/* Library context: owns cuBLAS / cuSOLVER handles and the solver workspace.
+ * Replaces the XLA-managed handles behind jax.scipy.linalg.cho_factor
+ * (netket/optimizer/solver/solvers.py:242-271). */
+int vmck_ctx_create(vmck_ctx **out);
+int vmck_ctx_destroy(vmck_ctx *ctx);
+
+/* ---------------------------------------------------------------- a1
+ * Random spin states.  n_down < 0: every site +1/-1 uniformly
+ * (netket/hilbert/random/homogeneous.py:37-47); n_down >= 0: a uniformly random
+ * arrangement of exactly n_down down spins (the Sz-constrained permutation draw,
+ * netket/hilbert/random/fock.py:92-101).  Philox4x32-10 keyed by seed. */
+int vmck_random_states(vmck_stream s, int8_t *out, int64_t n_batches, int32_t N,
+                       int32_t n_down, uint64_t seed, uint64_t stream_id);
+
+/* ---------------------------------------------------------------- a7
+ * IsingJax.get_conn_padded (netket/operator/_ising/jax.py:82-88, 125-165).
+ * x (n, N) -> xp (n, K, N), mels (n, K) with K = N+1 (K = 1 when h_is_zero).
+ * Row 0: x, mel J * sum_e (2 [x_u == x_v] - 1).  Row k: x with site k-1 flipped,
+ * mel -h.  n_conn (nullable, int32 (n,)): IsingJax.n_conn (jax.py:168-175). */
+int vmck_get_conn_ising(vmck_stream s, const int8_t *x, int64_t n, int32_t N,
+                        const int32_t *edges, int32_t n_edges, double h, double J,
+                        int32_t h_is_zero, int8_t *xp, double *mels, int32_t *n_conn);
+
+/* ---------------------------------------------------------------- a8
+ * Packed LocalOperator for spin-1/2 terms acting on <= 4 sites, the device form
+ * of pack_internals_jax (netket/operator/_local_operator/compile_helpers.py:
+ * 29-218).  Terms are stored in output order: grouped by acting size
+ * (ascending), insertion order inside a group.  All pointers are device
+ * pointers.  Row index of a term = sum_s idx(x[acting_on[s]]) * 2^(size-1-s)
+ * with idx(+1) = 0, idx(-1) = 1. */
+typedef struct {
+  int32_t n_sites;          /* N */
+  int32_t n_terms;          /* T */
+  int32_t max_sites;        /* S: stride of acting_on / x_prime (<= 4) */
+  int32_t max_rows;         /* R = 2^S */
+  int32_t max_conns;        /* C: stride of mels / x_prime */
+  int32_t max_conn_size;    /* K: padded output width */
+  int32_t nonzero_diagonal; /* the diagonal candidate exists */
+  int32_t n_groups;         /* number of acting-size groups */
+  double constant;          /* identity shift */
+  double mel_cutoff;        /* keep an entry only if |mel| > mel_cutoff */
+  const int32_t *acting_on; /* [T][S] */
+  const int32_t *acting_size; /* [T] */
+  const int32_t *group_end; /* [n_groups] exclusive end term index of each group */
+  const double *diag_mels;  /* [T][R] */
+  const int32_t *n_conns;   /* [T][R] */
+  const double *mels;       /* [T][R][C] */
+  const int8_t *x_prime;    /* [T][R][C][S] new spin values (+1/-1) */
+} vmck_local_op;
+
+/* LocalOperatorJax.get_conn_padded (netket/operator/_local_operator/jax.py:
+ * 74-201, 256-288): candidates [diagonal] + per term, per stored column; those
+ * with |mel| > mel_cutoff are compacted to the front; the rest of the K slots
+ * hold (x, 0.0).  n_conn (nullable) receives the number kept. */
+int vmck_get_conn_local(vmck_stream s, const vmck_local_op *op, const int8_t *x,
+                        int64_t n, int8_t *xp, double *mels, int32_t *n_conn);
+
+/* ---------------------------------------------------------------- a5
+ * RBM.__call__ (netket/models/rbm.py:57-81) with log_cosh
+ * (netket/nn/activation.py:78-84): logpsi(x) = sum_j log_cosh(theta_j) + a.x,
+ * theta = b + x W.  dtype VMCK_F64 or VMCK_F32 (params and outputs in dtype).
+ * theta_out / tanh_out (nullable): (n, M) in dtype. */
+int vmck_rbm_logpsi(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                    int32_t M, const int8_t *x, int64_t n, void *logpsi,
+                    void *theta_out, void *tanh_out);
+
+/* ---------------------------------------------------------------- a9 (plain)
+ * local_value_kernel_jax reduction (netket/vqs/mc/kernels.py:62-71) from
+ * precomputed log-amplitudes: eloc[i] = sum_k mels[i,k] exp(lp_conn[i,k] - lp[i]).
+ * lp / lp_conn in dtype (F64 or F32); eloc is FP64. */
+int vmck_eloc_from_logpsi(vmck_stream s, int32_t dtype, const void *lp,
+                          const void *lp_conn, const double *mels, int64_t n,
+                          int32_t K, double *eloc);
+
+/* ---------------------------------------------------------------- a6 + a9 (fused)
+ * Local energies without materialising connected states: for each sample the
+ * RBM log-ratio of every connected element is formed from theta and the rows of
+ * W of the changed sites.  Replaces get_conn_padded + logpsi on every row +
+ * the reduction (netket/vqs/mc/kernels.py:62-71).  logpsi_out nullable. */
+int vmck_rbm_eloc_ising(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                        int32_t M, const int8_t *x, int64_t n, const int32_t *edges,
+                        int32_t n_edges, double h, double J, double *eloc,
+                        void *logpsi_out);
+int vmck_rbm_eloc_local(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                        int32_t M, const int8_t *x, int64_t n, const vmck_local_op *op,
+                        double *eloc, void *logpsi_out);
+
+/* ---------------------------------------------------------------- a2 - a4
+ * MetropolisSampler sweep (netket/sampler/metropolis.py:416-505) with the RBM
+ * log-amplitude updated incrementally.  rule 0: LocalRule (rules/local.py:40-49);
+ * rule 1: ExchangeRule (rules/exchange.py:143-218) over clusters (C, 2).
+ * Runs n_discard + chain_length sweeps of sweep_size proposals per chain and
+ * stores the state after each of the last chain_length sweeps:
+ * samples (B, chain_length, N).  sigma (B, N) is read and written; log_prob (B,)
+ * FP64 receives 2 Re logpsi of the final state; n_accepted (B,) is incremented.
+ * The random stream is Philox4x32-10 with key = seed and counter =
+ * (proposal index counter + k, chain, 0); callers advance counter by
+ * (n_discard + chain_length) * sweep_size between calls. */
+int vmck_metropolis_sample(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                           int32_t M, int8_t *sigma, double *log_prob,
+                           int64_t *n_accepted, int32_t B, int32_t sweep_size,
+                           int32_t n_discard, int32_t chain_length, int8_t *samples,
+                           uint64_t seed, uint64_t counter, int32_t rule,
+                           const int32_t *clusters, int32_t n_clusters);
+
+/* ---------------------------------------------------------------- a10
+ * netket.stats.statistics, blocking estimator (netket/stats/mc_stats_old.py:
+ * 88-196) in FP64 over data (n_chains, chain_length):
+ * out5 = [mean, error_of_mean, variance, tau_corr, R_hat].
+ * workspace: vmck_stats_workspace_size() doubles. */
+int64_t vmck_stats_workspace_size(int32_t n_chains, int32_t chain_length);
+int vmck_stats_f64(vmck_stream s, const double *data, int32_t n_chains,
+                   int32_t chain_length, int32_t plain_rhat, double *out5,
+                   double *workspace, int64_t workspace_len);
+
+/* ---------------------------------------------------------------- a11 / a12 / a14
+ * out = O^T v for the RBM Jacobian O (n, P) without materialising it
+ * (the VJP of netket/vqs/mc/mc_state/expect_forces.py:99-106 and the
+ * O_L^T aux contraction of netket/_src/ngd/srt.py:83-84):
+ *   out[bias_j] = sum_s t_sj v_s, out[kernel_ij] = sum_s x_si t_sj v_s,
+ *   out[visible_i] = sum_s x_si v_s,  t = tanh(theta) (n, M) in dtype.
+ * v (n,) and out (P,) are FP64.  workspace: vmck_ot_v_workspace_size() doubles. */
+int64_t vmck_ot_v_workspace_size(int32_t N, int32_t M, int64_t n);
+int vmck_rbm_ot_v(vmck_stream s, int32_t dtype, const void *tanh_theta,
+                  const int8_t *x, int32_t N, int32_t M, int64_t n, const double *v,
+                  double *out, double *workspace, int64_t workspace_len);
+
+/* Dense centred, scaled Jacobian O_L = (O - mean O) * scale, (n, P) in out_dtype,
+ * from tanh(theta) (dtype) and the column means (FP64, P) -- nkjax.jacobian
+ * (netket/jax/_jacobian/logic.py:48-384, center=True) followed by
+ * _prepare_input (netket/_src/ngd/sr_srt_common.py:45-101). */
+int vmck_rbm_jacobian(vmck_stream s, int32_t dtype, const void *tanh_theta,
+                      const int8_t *x, int32_t N, int32_t M, int64_t n,
+                      const double *col_mean, double scale, int32_t out_dtype, void *O);
+
+/* ---------------------------------------------------------------- a14 (structured)
+ * minSR matrix T = O_L O_L^T + diag_shift I for the RBM without O:
+ *   O(s).O(s') = (t_s.t_s')(1 + x_s.x_s') + x_s.x_s',
+ *   T = (G - g 1^T - 1 g^T + c 11^T) / n + diag_shift I, g = O obar, c = |obar|^2.
+ * obar (P, FP64): column means.  Only the lower triangle (row >= col) is written;
+ * T64 (n, n) FP64 row-major; T32 (nullable) receives an FP32 copy.
+ * mode 0: FP64 contraction; mode 1: FP32 contraction; mode 2: BF16 tensor-core
+ * contraction with FP32 accumulation (tcgen05). */
+int64_t vmck_gram_workspace_size(int32_t N, int32_t M, int64_t n);
+int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t dtype,
+                  const void *tanh_theta, const int8_t *x, int32_t N, int32_t M,
+                  int64_t n, const double *obar, double diag_shift, double *T64,
+                  float *T32, double *workspace, int64_t workspace_len);
+
+/* Dense T = O_L O_L^T + diag_shift I (lower triangle) or S = O_L^T O_L + shift I
+ * (transpose = 1) with cuBLAS, from a materialised O_L (rows, cols) in dtype
+ * (netket/_src/ngd/srt.py:53-60, netket/_src/ngd/sr.py:54-60). */
+int vmck_gram_dense(vmck_ctx *ctx, vmck_stream s, int32_t dtype, const void *O_L,
+                    int64_t rows, int64_t cols, int32_t transpose, double diag_shift,
+                    void *out);
+
+/* ---------------------------------------------------------------- a15
+ * cholesky (netket/optimizer/solver/solvers.py:242-271): solve A x = b for SPD A
+ * (n, n) whose LOWER triangle is read (row-major; A is preserved).  dtype F64 or
+ * F32.  On info != 0 or a non-finite x, VMCK_DEV_NOT_SPD / VMCK_DEV_NONFINITE is
+ * OR-ed into *status; the caller then takes the pinv_smooth fallback
+ * (solvers.py:305-340, netket/_src/solvers/nan_fallback.py:22-45). */
+int vmck_cholesky_solve(vmck_ctx *ctx, vmck_stream s, int32_t dtype, const void *A,
+                        const void *b, void *x, int64_t n, int32_t *status);
+/* FP32 Cholesky factor of A32 (lower triangle, overwritten) refined against the
+ * FP64 matrix A64 (lower triangle) until ||b - A64 x|| <= tol ||b|| (FP64). */
+int vmck_cholesky_solve_refined(vmck_ctx *ctx, vmck_stream s, const double *A64,
+                                float *A32, const double *b, double *x, int64_t n,
+                                int32_t max_iter, double tol, int32_t *status,
+                                double *residual_out);
+/* pinv_smooth (solvers.py:33-139) via a symmetric eigendecomposition (FP64). */
+int vmck_pinv_smooth_solve(vmck_ctx *ctx, vmck_stream s, const double *A,
+                           const double *b, double *x, int64_t n, double rtol,
+                           double rtol_smooth);
+
+/* ---------------------------------------------------------------- a14 helpers
+ * dv = 2 (e - mean) * scale with mean = *mean_dev (netket/_src/ngd/
+ * sr_srt_common.py:86-88); all FP64. */
+int vmck_center_scale(vmck_stream s, const double *e, const double *mean_dev,
+                      int64_t n, double factor, double *out);
+/* update = scale * (raw - obar * sum(aux)) with sum(aux) computed on the device:
+ * turns O^T aux into O_L^T aux for the centred Jacobian (srt.py:83-84). */
+int vmck_center_update(vmck_stream s, const double *raw, const double *obar,
+                       const double *aux, int64_t n, int64_t P, double scale,
+                       double *update);
+
+/* ---------------------------------------------------------------- a16
+ * optax.sgd step (netket/optimizer/__init__.py:33-60 via
+ * netket/_src/driver/abstract_optimization_driver.py:86-92):
+ * p64 -= lr * update; p32 (nullable) receives the FP32 copy. */
+int vmck_sgd(vmck_stream s, double *p64, const double *update, int64_t P, double lr,
+             float *p32);
+/* Cast FP64 -> FP32 (n elements). */
+int vmck_cast_f64_f32(vmck_stream s, const double *in, float *out, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VMCK_H */

@@ -1,0 +1,23 @@
+"""netket_gb300: NetKet's VMC hot loop (Metropolis sampling, RBM amplitudes,
+local energies, Jacobian contractions and the SR/minSR solve) as hand-written
+sm_103a CUDA kernels behind a C ABI (``include/vmck.h``, ``libvmck.so``), with a
+host API that mirrors ``netket``: ``hilbert``, ``graph``, ``operator``,
+``models``, ``sampler``, ``vqs``, ``stats``, ``optimizer``, ``driver``,
+``exact``.
+"""
+from . import _native
+from . import graph
+from . import hilbert
+from . import operator
+from . import models
+from . import sampler
+from . import stats
+from . import kernels
+from . import ngd
+from . import optimizer
+from . import vqs
+from . import driver
+from . import exact
+
+__all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd",
+           "optimizer", "vqs", "driver", "exact"]

@@ -1,0 +1,146 @@
+"""ctypes binding of libvmck.so (the C ABI declared in include/vmck.h).
+
+The library is built in-tree by ``netket_gb300.build``.  There is no CPU
+fallback: if the library or a CUDA device is missing, every operation raises.
+"""
+import ctypes
+import os
+import threading
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libvmck.so")
+
+F64, F32, BF16 = 0, 1, 2
+DEV_NONFINITE, DEV_NOT_SPD, DEV_NO_CONVERGE = 1, 2, 4
+
+c_i32, c_i64, c_u64, c_dbl, c_vp = (ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64,
+                                    ctypes.c_double, ctypes.c_void_p)
+
+
+class VmckError(RuntimeError):
+    pass
+
+
+class LocalOpStruct(ctypes.Structure):
+    """Mirror of ``vmck_local_op`` (include/vmck.h)."""
+    _fields_ = [
+        ("n_sites", c_i32), ("n_terms", c_i32), ("max_sites", c_i32), ("max_rows", c_i32),
+        ("max_conns", c_i32), ("max_conn_size", c_i32), ("nonzero_diagonal", c_i32),
+        ("n_groups", c_i32), ("constant", c_dbl), ("mel_cutoff", c_dbl),
+        ("acting_on", c_vp), ("acting_size", c_vp), ("group_end", c_vp), ("diag_mels", c_vp),
+        ("n_conns", c_vp), ("mels", c_vp), ("x_prime", c_vp),
+    ]
+
+
+_SIGNATURES = {
+    "vmck_abi_version": ([], c_i32),
+    "vmck_error_string": ([c_i32], ctypes.c_char_p),
+    "vmck_last_error": ([], ctypes.c_char_p),
+    "vmck_ctx_create": ([ctypes.POINTER(c_vp)], c_i32),
+    "vmck_ctx_destroy": ([c_vp], c_i32),
+    "vmck_random_states": ([c_vp, c_vp, c_i64, c_i32, c_i32, c_u64, c_u64], c_i32),
+    "vmck_get_conn_ising": ([c_vp, c_vp, c_i64, c_i32, c_vp, c_i32, c_dbl, c_dbl, c_i32, c_vp,
+                             c_vp, c_vp], c_i32),
+    "vmck_get_conn_local": ([c_vp, ctypes.POINTER(LocalOpStruct), c_vp, c_i64, c_vp, c_vp, c_vp],
+                            c_i32),
+    "vmck_rbm_logpsi": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp], c_i32),
+    "vmck_eloc_from_logpsi": ([c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp], c_i32),
+    "vmck_rbm_eloc_ising": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64, c_vp, c_i32, c_dbl,
+                             c_dbl, c_vp, c_vp], c_i32),
+    "vmck_rbm_eloc_local": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64,
+                             ctypes.POINTER(LocalOpStruct), c_vp, c_vp], c_i32),
+    "vmck_metropolis_sample": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32,
+                                c_i32, c_i32, c_vp, c_u64, c_u64, c_i32, c_vp, c_i32], c_i32),
+    "vmck_stats_workspace_size": ([c_i32, c_i32], c_i64),
+    "vmck_stats_f64": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp, c_i64], c_i32),
+    "vmck_ot_v_workspace_size": ([c_i32, c_i32, c_i64], c_i64),
+    "vmck_rbm_ot_v": ([c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_i64],
+                      c_i32),
+    "vmck_rbm_jacobian": ([c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_dbl, c_i32,
+                           c_vp], c_i32),
+    "vmck_gram_workspace_size": ([c_i32, c_i32, c_i64], c_i64),
+    "vmck_rbm_gram": ([c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_dbl,
+                       c_vp, c_vp, c_vp, c_i64], c_i32),
+    "vmck_gram_dense": ([c_vp, c_vp, c_i32, c_vp, c_i64, c_i64, c_i32, c_dbl, c_vp], c_i32),
+    "vmck_cholesky_solve": ([c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp], c_i32),
+    "vmck_cholesky_solve_refined": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i32, c_dbl,
+                                     c_vp, c_vp], c_i32),
+    "vmck_pinv_smooth_solve": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_dbl, c_dbl], c_i32),
+    "vmck_center_scale": ([c_vp, c_vp, c_vp, c_i64, c_dbl, c_vp], c_i32),
+    "vmck_center_update": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_dbl, c_vp], c_i32),
+    "vmck_sgd": ([c_vp, c_vp, c_vp, c_i64, c_dbl, c_vp], c_i32),
+    "vmck_cast_f64_f32": ([c_vp, c_vp, c_vp, c_i64], c_i32),
+}
+
+_lib = None
+_lock = threading.Lock()
+_ctx = {}
+
+
+def lib():
+    """Load libvmck.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not os.path.exists(LIB_PATH):
+                    raise VmckError(f"libvmck.so is not built ({LIB_PATH}); run "
+                                    "`python -m netket_gb300.build`")
+                L = ctypes.CDLL(LIB_PATH)
+                for name, (args, res) in _SIGNATURES.items():
+                    f = getattr(L, name)
+                    f.argtypes = args
+                    f.restype = res
+                _lib = L
+    return _lib
+
+
+def declared_symbols():
+    return list(_SIGNATURES)
+
+
+def check(rc):
+    if rc != 0:
+        L = lib()
+        raise VmckError(f"{L.vmck_error_string(rc).decode()}: {L.vmck_last_error().decode()}")
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise VmckError("netket_gb300 needs a CUDA device (GB300, sm_103a); none is visible")
+
+
+def device():
+    require_cuda()
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def ctx():
+    """Per-device library context (cuBLAS / cuSOLVER handles, solver workspace)."""
+    require_cuda()
+    dev = torch.cuda.current_device()
+    if dev not in _ctx:
+        with _lock:
+            if dev not in _ctx:
+                h = c_vp()
+                check(lib().vmck_ctx_create(ctypes.byref(h)))
+                _ctx[dev] = h
+    return _ctx[dev]
+
+
+def dtype_code(dt):
+    if dt == torch.float64:
+        return F64
+    if dt == torch.float32:
+        return F32
+    raise VmckError(f"unsupported dtype {dt}")

@@ -1,0 +1,34 @@
+// ABI version, status strings and the per-thread last-error text.
+#include <cstdarg>
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace vmck {
+
+static thread_local char g_last_error[512] = "";
+
+void set_last_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+}
+
+}  // namespace vmck
+
+extern "C" int vmck_abi_version(void) { return VMCK_ABI_VERSION; }
+
+extern "C" const char *vmck_last_error(void) { return vmck::g_last_error; }
+
+extern "C" const char *vmck_error_string(int code) {
+  switch (code) {
+    case VMCK_OK: return "ok";
+    case VMCK_ERR_ARG: return "invalid argument";
+    case VMCK_ERR_UNSUPPORTED: return "unsupported dtype or shape";
+    case VMCK_ERR_CUDA: return "CUDA runtime error";
+    case VMCK_ERR_LIBRARY: return "cuBLAS / cuSOLVER error";
+    case VMCK_ERR_NOMEM: return "workspace allocation failed";
+    default: return "unknown status";
+  }
+}

@@ -1,0 +1,124 @@
+// Shared device helpers for libvmck: status handling, Philox4x32-10,
+// log_cosh, warp/block reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/vmck.h"
+
+namespace vmck {
+
+// ----------------------------------------------------------------- host status
+void set_last_error(const char *fmt, ...);
+
+inline int check_launch(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_last_error("%s: %s", what, cudaGetErrorString(e));
+    return VMCK_ERR_CUDA;
+  }
+  return VMCK_OK;
+}
+
+#define VMCK_CUDA(call)                                                        \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ::vmck::set_last_error("%s:%d %s: %s", __FILE__, __LINE__, #call,        \
+                             cudaGetErrorString(e_));                          \
+      return VMCK_ERR_CUDA;                                                    \
+    }                                                                          \
+  } while (0)
+
+#define VMCK_REQUIRE(cond, msg)                                                \
+  do {                                                                         \
+    if (!(cond)) {                                                             \
+      ::vmck::set_last_error("argument check failed: %s", msg);                \
+      return VMCK_ERR_ARG;                                                     \
+    }                                                                          \
+  } while (0)
+
+inline cudaStream_t as_stream(vmck_stream s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int ceil_div(int64_t a, int64_t b) { return static_cast<int>((a + b - 1) / b); }
+
+// ----------------------------------------------------------------- Philox4x32-10
+// Counter-based generator of Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3" (SC'11): ten rounds of two 32x32->64 multiplies
+// with the paper's multipliers and Weyl key increments.
+struct u32x4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// uniform in [0, 1) with 24 random bits
+__device__ __forceinline__ float u01f(uint32_t v) { return (v >> 8) * (1.0f / 16777216.0f); }
+// uniform in [0, 1) with 53 random bits
+__device__ __forceinline__ double u01d(uint32_t a, uint32_t b) {
+  uint64_t v = (static_cast<uint64_t>(a) << 21) ^ static_cast<uint64_t>(b >> 11);
+  return static_cast<double>(v & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0);
+}
+// integer in [0, n) by multiply-shift
+__device__ __forceinline__ uint32_t below(uint32_t v, uint32_t n) { return __umulhi(v, n); }
+
+// ----------------------------------------------------------------- log_cosh
+// log(cosh(x)) = |x| + log1p(exp(-2|x|)) - log(2), the stable form of
+// netket/nn/activation.py:78-84.
+__device__ __forceinline__ double log_cosh(double x) {
+  x = fabs(x);
+  return x + log1p(exp(-2.0 * x)) - 0.69314718055994530942;
+}
+__device__ __forceinline__ float log_cosh(float x) {
+  x = fabsf(x);
+  return x + log1pf(expf(-2.0f * x)) - 0.693147180559945309f;
+}
+
+// ----------------------------------------------------------------- reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum; every thread receives the result.  `red` must hold
+// blockDim.x/32 elements of T.  Deterministic (fixed tree).
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  T t = (lane < nw) ? red[lane] : T(0);
+  t = warp_sum(t);
+  return t;
+}
+
+template <typename T>
+struct Real;
+template <>
+struct Real<double> {
+  static constexpr int code = VMCK_F64;
+};
+template <>
+struct Real<float> {
+  static constexpr int code = VMCK_F32;
+};
+
+}  // namespace vmck

@@ -1,0 +1,390 @@
+// Library context and the dense linear algebra of the SR / minSR step:
+// Cholesky solves (FP64, FP32, FP32 factor + FP64 refinement), the pinv_smooth
+// fallback, cuBLAS SYRK Gram matrices for the materialised-Jacobian path, and
+// the small vector kernels around them.
+//
+// Matrix convention of the whole ABI: square matrices are row-major and only
+// their LOWER triangle (row >= col) is read or written.  Seen by the
+// column-major libraries that memory is the UPPER triangle of the same
+// symmetric matrix, hence CUBLAS_FILL_MODE_UPPER below.
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstring>
+
+#include "common.cuh"
+
+struct vmck_ctx {
+  int device = 0;
+  cublasHandle_t blas = nullptr;
+  cusolverDnHandle_t solver = nullptr;
+  cusolverDnParams_t params = nullptr;
+  void *dwork = nullptr;
+  size_t dwork_bytes = 0;
+  void *hwork = nullptr;
+  size_t hwork_bytes = 0;
+  void *aux = nullptr;
+  size_t aux_bytes = 0;
+  int *d_info = nullptr;
+};
+
+namespace vmck {
+
+#define VMCK_BLAS(call)                                                        \
+  do {                                                                         \
+    cublasStatus_t st_ = (call);                                               \
+    if (st_ != CUBLAS_STATUS_SUCCESS) {                                        \
+      ::vmck::set_last_error("%s:%d %s: cublas status %d", __FILE__, __LINE__, \
+                             #call, (int)st_);                                 \
+      return VMCK_ERR_LIBRARY;                                                 \
+    }                                                                          \
+  } while (0)
+
+#define VMCK_SOLVER(call)                                                      \
+  do {                                                                         \
+    cusolverStatus_t st_ = (call);                                             \
+    if (st_ != CUSOLVER_STATUS_SUCCESS) {                                      \
+      ::vmck::set_last_error("%s:%d %s: cusolver status %d", __FILE__,         \
+                             __LINE__, #call, (int)st_);                       \
+      return VMCK_ERR_LIBRARY;                                                 \
+    }                                                                          \
+  } while (0)
+
+static int grow(void **p, size_t *cap, size_t need, cudaStream_t st) {
+  if (need <= *cap) return VMCK_OK;
+  if (*p) {
+    VMCK_CUDA(cudaStreamSynchronize(st));
+    VMCK_CUDA(cudaFree(*p));
+    *p = nullptr;
+    *cap = 0;
+  }
+  size_t bytes = std::max<size_t>(need, 1 << 20);
+  if (cudaMalloc(p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    set_last_error("workspace allocation of %zu bytes failed", bytes);
+    return VMCK_ERR_NOMEM;
+  }
+  *cap = bytes;
+  return VMCK_OK;
+}
+
+static int grow_host(vmck_ctx *c, size_t need) {
+  if (need <= c->hwork_bytes) return VMCK_OK;
+  free(c->hwork);
+  c->hwork = malloc(std::max<size_t>(need, 64));
+  if (!c->hwork) {
+    c->hwork_bytes = 0;
+    return VMCK_ERR_NOMEM;
+  }
+  c->hwork_bytes = std::max<size_t>(need, 64);
+  return VMCK_OK;
+}
+
+static int bind(vmck_ctx *c, cudaStream_t st) {
+  VMCK_BLAS(cublasSetStream(c->blas, st));
+  VMCK_SOLVER(cusolverDnSetStream(c->solver, st));
+  return VMCK_OK;
+}
+
+// ------------------------------------------------------------ small kernels
+__global__ void add_diag_kernel(void *A, int dtype, int64_t n, double shift) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (dtype == VMCK_F64)
+    static_cast<double *>(A)[i * n + i] += shift;
+  else
+    static_cast<float *>(A)[i * n + i] += (float)shift;
+}
+
+template <typename T>
+__global__ void solve_check_kernel(const int *info, const T *x, const T *b, int64_t n,
+                                   int32_t *status) {
+  __shared__ int red[32];
+  int bad = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+    bad |= !isfinite((double)x[i]) || !isfinite((double)b[i]);
+  bad = block_sum(bad, red);
+  if (threadIdx.x == 0 && status) {
+    int s = 0;
+    if (*info != 0) s |= VMCK_DEV_NOT_SPD;
+    if (bad) s |= VMCK_DEV_NONFINITE;
+    if (s) atomicOr(status, s);
+  }
+}
+
+__global__ void d2f_kernel(const double *in, float *out, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
+__global__ void axpy_f2d_kernel(double *x, const float *d, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) x[i] += (double)d[i];
+}
+
+__global__ void refine_check_kernel(const double *nr, const double *nb, const int *info,
+                                    double tol, int32_t *status, double *res_out) {
+  double rel = *nr / *nb;
+  if (res_out) *res_out = rel;
+  if (status) {
+    int s = 0;
+    if (*info != 0) s |= VMCK_DEV_NOT_SPD;
+    if (!isfinite(rel)) s |= VMCK_DEV_NONFINITE;
+    else if (!(rel <= tol)) s |= VMCK_DEV_NO_CONVERGE;
+    if (s) atomicOr(status, s);
+  }
+}
+
+__global__ void pinv_filter_kernel(const double *w, double *y, int64_t n, double rtol,
+                                   double rtol_smooth) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double wmax = w[n - 1];
+  const double rel = fabs(w[i] / wmax);
+  double inv = rel > rtol ? 1.0 / w[i] : 0.0;
+  double q = rtol_smooth / rel;
+  double q2 = q * q;
+  inv *= 1.0 / (1.0 + q2 * q2 * q2);
+  y[i] *= inv;
+}
+
+__global__ void center_scale_kernel(const double *e, const double *mean, int64_t n, double f,
+                                    double *out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = f * (e[i] - *mean);
+}
+
+__global__ void center_update_kernel(const double *raw, const double *obar, const double *aux,
+                                     int64_t n, int64_t P, double scale, double *upd) {
+  __shared__ double red[32];
+  double s = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += aux[i];
+  s = block_sum(s, red);
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P;
+       p += (int64_t)gridDim.x * blockDim.x)
+    upd[p] = scale * (raw[p] - obar[p] * s);
+}
+
+__global__ void sgd_kernel(double *p, const double *u, int64_t P, double lr, float *p32) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  double v = p[i] - lr * u[i];
+  p[i] = v;
+  if (p32) p32[i] = (float)v;
+}
+
+static int num_sms() {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+}  // namespace vmck
+
+using namespace vmck;
+
+extern "C" int vmck_ctx_create(vmck_ctx **out) {
+  VMCK_REQUIRE(out, "ctx out pointer");
+  vmck_ctx *c = new vmck_ctx();
+  cudaGetDevice(&c->device);
+  if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS ||
+      cusolverDnCreate(&c->solver) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnCreateParams(&c->params) != CUSOLVER_STATUS_SUCCESS ||
+      cudaMalloc(&c->d_info, sizeof(int)) != cudaSuccess) {
+    set_last_error("vmck_ctx_create: cuBLAS / cuSOLVER initialisation failed");
+    vmck_ctx_destroy(c);
+    return VMCK_ERR_LIBRARY;
+  }
+  *out = c;
+  return VMCK_OK;
+}
+
+extern "C" int vmck_ctx_destroy(vmck_ctx *c) {
+  if (!c) return VMCK_OK;
+  cudaDeviceSynchronize();
+  if (c->params) cusolverDnDestroyParams(c->params);
+  if (c->solver) cusolverDnDestroy(c->solver);
+  if (c->blas) cublasDestroy(c->blas);
+  cudaFree(c->dwork);
+  cudaFree(c->aux);
+  cudaFree(c->d_info);
+  free(c->hwork);
+  delete c;
+  return VMCK_OK;
+}
+
+extern "C" int vmck_cholesky_solve(vmck_ctx *c, vmck_stream s, int32_t dtype, const void *A,
+                                   const void *b, void *x, int64_t n, int32_t *status) {
+  VMCK_REQUIRE(c && A && b && x && n > 0, "cholesky_solve arguments");
+  VMCK_REQUIRE(dtype == VMCK_F64 || dtype == VMCK_F32, "cholesky_solve dtype");
+  cudaStream_t st = as_stream(s);
+  int rc = bind(c, st);
+  if (rc) return rc;
+  const size_t es = dtype == VMCK_F64 ? 8 : 4;
+  const cudaDataType dt = dtype == VMCK_F64 ? CUDA_R_64F : CUDA_R_32F;
+  size_t dsize = 0, hsize = 0;
+  VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, dt, A,
+                                          n, dt, &dsize, &hsize));
+  const size_t fbytes = (size_t)n * n * es;
+  const size_t off = (fbytes + 255) & ~size_t(255);
+  if ((rc = grow(&c->dwork, &c->dwork_bytes, off + dsize + 256, st))) return rc;
+  if ((rc = grow_host(c, hsize))) return rc;
+  void *F = c->dwork;
+  void *work = static_cast<char *>(c->dwork) + off;
+  VMCK_CUDA(cudaMemcpyAsync(F, A, fbytes, cudaMemcpyDeviceToDevice, st));
+  VMCK_CUDA(cudaMemcpyAsync(x, b, (size_t)n * es, cudaMemcpyDeviceToDevice, st));
+  VMCK_SOLVER(cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, dt, F, n, dt, work,
+                               dsize, c->hwork, hsize, c->d_info));
+  VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, dt, F, n, dt, x,
+                               n, c->d_info));
+  if (dtype == VMCK_F64)
+    solve_check_kernel<double><<<1, 1024, 0, st>>>(c->d_info, static_cast<const double *>(x),
+                                                   static_cast<const double *>(b), n, status);
+  else
+    solve_check_kernel<float><<<1, 1024, 0, st>>>(c->d_info, static_cast<const float *>(x),
+                                                  static_cast<const float *>(b), n, status);
+  return check_launch("cholesky_solve check");
+}
+
+extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const double *A64,
+                                           float *A32, const double *b, double *x, int64_t n,
+                                           int32_t max_iter, double tol, int32_t *status,
+                                           double *residual_out) {
+  VMCK_REQUIRE(c && A64 && A32 && b && x && n > 0 && max_iter >= 1, "refined solve arguments");
+  cudaStream_t st = as_stream(s);
+  int rc = bind(c, st);
+  if (rc) return rc;
+  size_t dsize = 0, hsize = 0;
+  VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
+                                          CUDA_R_32F, A32, n, CUDA_R_32F, &dsize, &hsize));
+  if ((rc = grow(&c->dwork, &c->dwork_bytes, dsize + 256, st))) return rc;
+  if ((rc = grow_host(c, hsize))) return rc;
+  // aux: r (n double), r32 (n float), two norms
+  const size_t need = (size_t)n * 8 + (size_t)n * 4 + 64;
+  if ((rc = grow(&c->aux, &c->aux_bytes, need, st))) return rc;
+  double *r = static_cast<double *>(c->aux);
+  float *r32 = reinterpret_cast<float *>(r + n);
+  double *norms = reinterpret_cast<double *>(
+      (reinterpret_cast<uintptr_t>(r32 + n) + 15) & ~uintptr_t(15));
+  VMCK_SOLVER(cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, CUDA_R_32F, A32, n,
+                               CUDA_R_32F, c->dwork, dsize, c->hwork, hsize, c->d_info));
+  VMCK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
+  const int blocks = ceil_div(n, 256);
+  const double one = 1.0, mone = -1.0;
+  for (int it = 0; it < max_iter; ++it) {
+    VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    if (it > 0) VMCK_BLAS(cublasDsymv(c->blas, CUBLAS_FILL_MODE_UPPER, (int)n, &mone, A64, (int)n, x, 1, &one, r, 1));
+    d2f_kernel<<<blocks, 256, 0, st>>>(r, r32, n);
+    VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, CUDA_R_32F,
+                                 A32, n, CUDA_R_32F, r32, n, c->d_info));
+    axpy_f2d_kernel<<<blocks, 256, 0, st>>>(x, r32, n);
+  }
+  VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+  VMCK_BLAS(cublasDsymv(c->blas, CUBLAS_FILL_MODE_UPPER, (int)n, &mone, A64, (int)n, x, 1, &one, r, 1));
+  VMCK_BLAS(cublasSetPointerMode(c->blas, CUBLAS_POINTER_MODE_DEVICE));
+  cublasStatus_t s1 = cublasDnrm2(c->blas, (int)n, r, 1, norms);
+  cublasStatus_t s2 = cublasDnrm2(c->blas, (int)n, b, 1, norms + 1);
+  cublasSetPointerMode(c->blas, CUBLAS_POINTER_MODE_HOST);
+  if (s1 != CUBLAS_STATUS_SUCCESS || s2 != CUBLAS_STATUS_SUCCESS) {
+    set_last_error("refined solve: cublasDnrm2 failed");
+    return VMCK_ERR_LIBRARY;
+  }
+  refine_check_kernel<<<1, 1, 0, st>>>(norms, norms + 1, c->d_info, tol, status, residual_out);
+  return check_launch("refined solve");
+}
+
+extern "C" int vmck_pinv_smooth_solve(vmck_ctx *c, vmck_stream s, const double *A, const double *b,
+                                      double *x, int64_t n, double rtol, double rtol_smooth) {
+  VMCK_REQUIRE(c && A && b && x && n > 0, "pinv_smooth arguments");
+  cudaStream_t st = as_stream(s);
+  int rc = bind(c, st);
+  if (rc) return rc;
+  const size_t fbytes = (size_t)n * n * 8;
+  const size_t off = (fbytes + 255) & ~size_t(255);
+  // aux: eigenvalues w (n), y (n)
+  if ((rc = grow(&c->aux, &c->aux_bytes, (size_t)n * 16 + 64, st))) return rc;
+  double *w = static_cast<double *>(c->aux);
+  double *y = w + n;
+  size_t dsize = 0, hsize = 0;
+  VMCK_SOLVER(cusolverDnXsyevd_bufferSize(c->solver, c->params, CUSOLVER_EIG_MODE_VECTOR,
+                                          CUBLAS_FILL_MODE_UPPER, n, CUDA_R_64F, A, n, CUDA_R_64F,
+                                          w, CUDA_R_64F, &dsize, &hsize));
+  if ((rc = grow(&c->dwork, &c->dwork_bytes, off + dsize + 256, st))) return rc;
+  if ((rc = grow_host(c, hsize))) return rc;
+  double *U = static_cast<double *>(c->dwork);
+  void *work = static_cast<char *>(c->dwork) + off;
+  VMCK_CUDA(cudaMemcpyAsync(U, A, fbytes, cudaMemcpyDeviceToDevice, st));
+  VMCK_SOLVER(cusolverDnXsyevd(c->solver, c->params, CUSOLVER_EIG_MODE_VECTOR,
+                               CUBLAS_FILL_MODE_UPPER, n, CUDA_R_64F, U, n, CUDA_R_64F, w,
+                               CUDA_R_64F, work, dsize, c->hwork, hsize, c->d_info));
+  const double one = 1.0, zero = 0.0;
+  VMCK_BLAS(cublasDgemv(c->blas, CUBLAS_OP_T, (int)n, (int)n, &one, U, (int)n, b, 1, &zero, y, 1));
+  pinv_filter_kernel<<<ceil_div(n, 256), 256, 0, st>>>(w, y, n, rtol, rtol_smooth);
+  VMCK_BLAS(cublasDgemv(c->blas, CUBLAS_OP_N, (int)n, (int)n, &one, U, (int)n, y, 1, &zero, x, 1));
+  return check_launch("pinv_smooth");
+}
+
+extern "C" int vmck_gram_dense(vmck_ctx *c, vmck_stream s, int32_t dtype, const void *O_L,
+                               int64_t rows, int64_t cols, int32_t transpose, double diag_shift,
+                               void *out) {
+  VMCK_REQUIRE(c && O_L && out && rows > 0 && cols > 0, "gram_dense arguments");
+  VMCK_REQUIRE(rows < (1ll << 31) && cols < (1ll << 31), "gram_dense sizes");
+  cudaStream_t st = as_stream(s);
+  int rc = bind(c, st);
+  if (rc) return rc;
+  // O_L row-major (rows, cols) == column-major X (cols x rows), ld = cols
+  const int64_t m = transpose ? cols : rows;
+  const cublasOperation_t op = transpose ? CUBLAS_OP_N : CUBLAS_OP_T;
+  const int k = (int)(transpose ? rows : cols);
+  if (dtype == VMCK_F64) {
+    const double one = 1.0, zero = 0.0;
+    VMCK_BLAS(cublasDsyrk(c->blas, CUBLAS_FILL_MODE_UPPER, op, (int)m, k, &one,
+                          static_cast<const double *>(O_L), (int)cols, &zero,
+                          static_cast<double *>(out), (int)m));
+  } else if (dtype == VMCK_F32) {
+    const float one = 1.0f, zero = 0.0f;
+    VMCK_BLAS(cublasSsyrk(c->blas, CUBLAS_FILL_MODE_UPPER, op, (int)m, k, &one,
+                          static_cast<const float *>(O_L), (int)cols, &zero,
+                          static_cast<float *>(out), (int)m));
+  } else {
+    set_last_error("gram_dense dtype");
+    return VMCK_ERR_UNSUPPORTED;
+  }
+  if (diag_shift != 0.0) add_diag_kernel<<<ceil_div(m, 256), 256, 0, st>>>(out, dtype, m, diag_shift);
+  return check_launch("gram_dense");
+}
+
+extern "C" int vmck_center_scale(vmck_stream s, const double *e, const double *mean_dev, int64_t n,
+                                 double factor, double *out) {
+  VMCK_REQUIRE(e && mean_dev && out && n > 0, "center_scale arguments");
+  center_scale_kernel<<<ceil_div(n, 256), 256, 0, as_stream(s)>>>(e, mean_dev, n, factor, out);
+  return check_launch("center_scale");
+}
+
+extern "C" int vmck_center_update(vmck_stream s, const double *raw, const double *obar,
+                                  const double *aux, int64_t n, int64_t P, double scale,
+                                  double *update) {
+  VMCK_REQUIRE(raw && obar && aux && update && n > 0 && P > 0, "center_update arguments");
+  int grid = (int)std::min<int64_t>(ceil_div(P, 256), (int64_t)num_sms() * 2);
+  center_update_kernel<<<grid, 256, 0, as_stream(s)>>>(raw, obar, aux, n, P, scale, update);
+  return check_launch("center_update");
+}
+
+extern "C" int vmck_sgd(vmck_stream s, double *p64, const double *update, int64_t P, double lr,
+                        float *p32) {
+  VMCK_REQUIRE(p64 && update && P > 0, "sgd arguments");
+  sgd_kernel<<<ceil_div(P, 256), 256, 0, as_stream(s)>>>(p64, update, P, lr, p32);
+  return check_launch("sgd");
+}
+
+extern "C" int vmck_cast_f64_f32(vmck_stream s, const double *in, float *out, int64_t n) {
+  VMCK_REQUIRE(in && out && n >= 0, "cast arguments");
+  if (n == 0) return VMCK_OK;
+  d2f_kernel<<<ceil_div(n, 256), 256, 0, as_stream(s)>>>(in, out, n);
+  return check_launch("cast");
+}

@@ -1,0 +1,256 @@
+// Metropolis sweeps for the RBM with Local and Exchange transition rules.
+//
+// One warp owns one chain for the whole launch (all discarded and kept
+// sweeps).  Per chain the warp keeps in shared memory: the configuration
+// x (N int8), theta = b + x W (M), log_cosh(theta) (M) and the proposal's
+// theta' / log_cosh(theta') (2M).  A proposal changing sites {u (, v)} costs
+// M log_cosh evaluations and 1-2 FMAs per hidden unit -- instead of the full
+// N*M forward pass NetKet's sampler runs per proposal
+// (netket/sampler/metropolis.py:438).  theta is recomputed exactly at the start
+// of every sweep, so incremental rounding never builds up over more than one
+// sweep.
+//
+// Acceptance follows netket/sampler/metropolis.py:440-450:
+//   accept iff u < exp(2 Re[logpsi(x') - logpsi(x)] + corr).
+// Exchange (netket/sampler/rules/exchange.py:143-184): pick uniformly among the
+// clusters (u, v) with x_u != x_v, swap, corr = log #hoppable(x) - log #hoppable(x').
+// With no hoppable cluster the proposal is x itself with a NaN correction in
+// NetKet, which is never accepted; here it is rejected directly.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace vmck {
+
+template <typename T>
+struct ChainSmem {
+  T *th, *lc, *tn, *ln;
+  int8_t *xs;
+};
+
+template <typename T>
+__device__ inline void chain_recompute(const T *__restrict__ b, const T *__restrict__ W,
+                                       const T *__restrict__ a, int N, int M, ChainSmem<T> c,
+                                       T *logpsi) {
+  const int lane = threadIdx.x & 31;
+  T part = 0;
+  for (int j = lane; j < M; j += 32) {
+    T acc = b[j];
+    for (int i = 0; i < N; ++i) acc += (T)c.xs[i] * W[(int64_t)i * M + j];
+    c.th[j] = acc;
+    T l = log_cosh(acc);
+    c.lc[j] = l;
+    part += l;
+  }
+  for (int i = lane; i < N; i += 32) part += (T)c.xs[i] * a[i];
+  part = warp_sum(part);
+  *logpsi = part;
+  __syncwarp();
+}
+
+template <typename T, int RULE>
+__global__ void metropolis_kernel(const T *__restrict__ params, int N, int M, int8_t *sigma,
+                                  double *log_prob, int64_t *n_accepted, int B, int sweep,
+                                  int n_discard, int L, int8_t *samples, uint32_t k0, uint32_t k1,
+                                  uint64_t counter, const int32_t *__restrict__ clusters, int C,
+                                  int wpb) {
+  extern __shared__ unsigned char smem_raw[];
+  const T *bvec = params, *W = params + M, *a = params + M + (int64_t)N * M;
+  int16_t *cl = reinterpret_cast<int16_t *>(smem_raw);
+  unsigned char *base = smem_raw + ((4 * (size_t)C + 15) & ~size_t(15));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t per_warp = 4 * (size_t)M * sizeof(T) + ((N + 15) & ~15);
+  ChainSmem<T> c;
+  c.th = reinterpret_cast<T *>(base + warp * per_warp);
+  c.lc = c.th + M;
+  c.tn = c.lc + M;
+  c.ln = c.tn + M;
+  c.xs = reinterpret_cast<int8_t *>(c.ln + M);
+  if (RULE == 1)
+    for (int q = threadIdx.x; q < 2 * C; q += blockDim.x) cl[q] = (int16_t)clusters[q];
+  __syncthreads();
+  const int b = blockIdx.x * wpb + warp;
+  if (b >= B) return;
+
+  for (int i = lane; i < N; i += 32) c.xs[i] = sigma[(int64_t)b * N + i];
+  __syncwarp();
+  T logpsi;
+  int hop = 0;
+  if (RULE == 1) {
+    for (int q0 = 0; q0 < C; q0 += 32) {
+      int q = q0 + lane;
+      bool h = q < C && c.xs[cl[2 * q]] != c.xs[cl[2 * q + 1]];
+      hop += __popc(__ballot_sync(0xffffffffu, h));
+    }
+  }
+  int64_t acc_count = 0;
+  const int total = n_discard + L;
+  for (int step = 0; step < total; ++step) {
+    chain_recompute(bvec, W, a, N, M, c, &logpsi);
+    for (int p = 0; p < sweep; ++p) {
+      const uint64_t pidx = counter + (uint64_t)step * sweep + p;
+      u32x4 r = philox4x32_10(u32x4{(uint32_t)pidx, (uint32_t)(pidx >> 32), (uint32_t)b, 0u}, k0, k1);
+      int su, sv = -1;
+      T du, dv = 0;
+      T corr = 0;
+      int hop_new = hop;
+      if (RULE == 0) {
+        su = (int)below(r.x, (uint32_t)N);
+        du = (T)(-2 * c.xs[su]);
+      } else {
+        if (hop == 0) continue;  // no move possible: rejected (see header)
+        int k = (int)below(r.x, (uint32_t)hop);
+        int pick = -1;
+        for (int q0 = 0; q0 < C && pick < 0; q0 += 32) {
+          int q = q0 + lane;
+          bool h = q < C && c.xs[cl[2 * q]] != c.xs[cl[2 * q + 1]];
+          unsigned m = __ballot_sync(0xffffffffu, h);
+          int pc = __popc(m);
+          if (k < pc) {
+            for (int z = 0; z < k; ++z) m &= m - 1;
+            pick = q0 + __ffs(m) - 1;
+          } else {
+            k -= pc;
+          }
+        }
+        if (pick < 0) continue;  // unreachable while hop is consistent; never index out of range
+        su = cl[2 * pick];
+        sv = cl[2 * pick + 1];
+        const int8_t xu = c.xs[su], xv = c.xs[sv];
+        du = (T)(xv - xu);
+        dv = (T)(xu - xv);
+        // hoppable count of the proposed configuration
+        __syncwarp();
+        if (lane == 0) {
+          c.xs[su] = xv;
+          c.xs[sv] = xu;
+        }
+        __syncwarp();
+        hop_new = 0;
+        for (int q0 = 0; q0 < C; q0 += 32) {
+          int q = q0 + lane;
+          bool h = q < C && c.xs[cl[2 * q]] != c.xs[cl[2 * q + 1]];
+          hop_new += __popc(__ballot_sync(0xffffffffu, h));
+        }
+        __syncwarp();
+        if (lane == 0) {
+          c.xs[su] = xu;
+          c.xs[sv] = xv;
+        }
+        __syncwarp();
+        corr = log((T)hop) - log((T)hop_new);
+      }
+      // log-ratio of the RBM amplitude
+      T s = 0;
+      const T *Wu = W + (int64_t)su * M;
+      const T *Wv = (sv >= 0) ? W + (int64_t)sv * M : Wu;
+      for (int j = lane; j < M; j += 32) {
+        T t = c.th[j] + du * Wu[j];
+        if (RULE == 1) t += dv * Wv[j];
+        T l = log_cosh(t);
+        c.tn[j] = t;
+        c.ln[j] = l;
+        s += l - c.lc[j];
+      }
+      s = warp_sum(s);
+      s += du * a[su];
+      if (RULE == 1) s += dv * a[sv];
+      const T dlp = (T)2 * s;
+      bool accept;
+      if (sizeof(T) == 8) {
+        double u = u01d(r.y, r.z);
+        accept = u < exp((double)(dlp + corr));
+      } else {
+        float u = u01f(r.y);
+        accept = u < expf((float)(dlp + corr));
+      }
+      if (accept) {
+        for (int j = lane; j < M; j += 32) {
+          c.th[j] = c.tn[j];
+          c.lc[j] = c.ln[j];
+        }
+        __syncwarp();
+        if (lane == 0) {
+          c.xs[su] = (int8_t)(c.xs[su] + (int)du);
+          if (RULE == 1) c.xs[sv] = (int8_t)(c.xs[sv] + (int)dv);
+        }
+        hop = hop_new;
+        logpsi += s;
+        ++acc_count;
+      }
+      __syncwarp();
+    }
+    if (step >= n_discard) {
+      int8_t *dst = samples + ((int64_t)b * L + (step - n_discard)) * N;
+      for (int i = lane; i < N; i += 32) dst[i] = c.xs[i];
+    }
+  }
+  chain_recompute(bvec, W, a, N, M, c, &logpsi);
+  for (int i = lane; i < N; i += 32) sigma[(int64_t)b * N + i] = c.xs[i];
+  if (lane == 0) {
+    log_prob[b] = 2.0 * (double)logpsi;
+    n_accepted[b] += acc_count;
+  }
+}
+
+template <typename T>
+int launch_metropolis(cudaStream_t st, const void *params, int N, int M, int8_t *sigma,
+                      double *log_prob, int64_t *n_acc, int B, int sweep, int n_discard, int L,
+                      int8_t *samples, uint64_t seed, uint64_t counter, int rule,
+                      const int32_t *clusters, int C) {
+  const size_t per_warp = 4 * (size_t)M * sizeof(T) + ((N + 15) & ~15);
+  const size_t cl_bytes = (rule == 1) ? ((4 * (size_t)C + 15) & ~size_t(15)) : 0;
+  const size_t budget = 200 * 1024;
+  VMCK_REQUIRE(cl_bytes + per_warp <= budget, "M too large for the Metropolis kernel");
+  int wpb = (int)std::min<size_t>(4, (budget - cl_bytes) / per_warp);
+  if (wpb < 1) wpb = 1;
+  size_t smem = cl_bytes + wpb * per_warp;
+  int grid = (B + wpb - 1) / wpb;
+  const T *p = static_cast<const T *>(params);
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  if (rule == 0) {
+    if (smem > 48 * 1024)
+      VMCK_CUDA(cudaFuncSetAttribute(metropolis_kernel<T, 0>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    metropolis_kernel<T, 0><<<grid, 32 * wpb, smem, st>>>(p, N, M, sigma, log_prob, n_acc, B, sweep,
+                                                         n_discard, L, samples, k0, k1, counter,
+                                                         clusters, 0, wpb);
+  } else {
+    if (smem > 48 * 1024)
+      VMCK_CUDA(cudaFuncSetAttribute(metropolis_kernel<T, 1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    metropolis_kernel<T, 1><<<grid, 32 * wpb, smem, st>>>(p, N, M, sigma, log_prob, n_acc, B, sweep,
+                                                         n_discard, L, samples, k0, k1, counter,
+                                                         clusters, C, wpb);
+  }
+  return check_launch("metropolis_sample");
+}
+
+}  // namespace vmck
+
+using namespace vmck;
+
+extern "C" int vmck_metropolis_sample(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                                      int32_t M, int8_t *sigma, double *log_prob,
+                                      int64_t *n_accepted, int32_t B, int32_t sweep_size,
+                                      int32_t n_discard, int32_t chain_length, int8_t *samples,
+                                      uint64_t seed, uint64_t counter, int32_t rule,
+                                      const int32_t *clusters, int32_t n_clusters) {
+  VMCK_REQUIRE(params && sigma && log_prob && n_accepted && N > 0 && N < 32768 && M > 0 && B > 0,
+               "metropolis arguments");
+  VMCK_REQUIRE(sweep_size >= 0 && n_discard >= 0 && chain_length >= 0, "metropolis lengths");
+  VMCK_REQUIRE(chain_length == 0 || samples, "samples buffer");
+  VMCK_REQUIRE(rule == 0 || rule == 1, "rule must be 0 (local) or 1 (exchange)");
+  VMCK_REQUIRE(rule == 0 || (clusters && n_clusters > 0), "exchange clusters");
+  cudaStream_t st = as_stream(s);
+  if (dtype == VMCK_F64)
+    return launch_metropolis<double>(st, params, N, M, sigma, log_prob, n_accepted, B, sweep_size,
+                                     n_discard, chain_length, samples, seed, counter, rule,
+                                     clusters, n_clusters);
+  if (dtype == VMCK_F32)
+    return launch_metropolis<float>(st, params, N, M, sigma, log_prob, n_accepted, B, sweep_size,
+                                    n_discard, chain_length, samples, seed, counter, rule, clusters,
+                                    n_clusters);
+  set_last_error("metropolis_sample: dtype %d unsupported", dtype);
+  return VMCK_ERR_UNSUPPORTED;
+}

@@ -1,0 +1,147 @@
+// Monte Carlo statistics in FP64: the blocking estimator of
+// netket/stats/mc_stats_old.py:88-196 over data (n_chains B, chain_length L).
+//
+// Pass 1 (one CTA per chain): per-chain sum, the two half-chain sums used by
+// split-R-hat and the block sums (block length max(1, L / 32)), written to the
+// workspace.  Pass 2 (one CTA): mean, two-pass population variance, variance of
+// chain means, of block means and of half-chain means, then NetKet's choice of
+// error estimate and R-hat.  Every reduction runs in a fixed order, so results
+// are bit-reproducible run to run.
+#include "common.cuh"
+
+namespace vmck {
+
+struct StatsLayout {
+  int B, L, l_block, nb, h;
+  int64_t chain_off, half_off, block_off, total;
+};
+
+__host__ __device__ inline StatsLayout stats_layout(int B, int L) {
+  StatsLayout s;
+  s.B = B;
+  s.L = L;
+  s.l_block = L / 32 > 1 ? L / 32 : 1;
+  s.nb = L / s.l_block;
+  s.h = L / 2;
+  s.chain_off = 0;
+  s.half_off = B;
+  s.block_off = 3 * (int64_t)B;
+  s.total = 3 * (int64_t)B + (int64_t)B * s.nb;
+  return s;
+}
+
+__global__ void stats_pass1(const double *__restrict__ data, StatsLayout lay, double *ws) {
+  __shared__ double red[32];
+  const int b = blockIdx.x;
+  const double *row = data + (int64_t)b * lay.L;
+  double s = 0, s0 = 0, s1 = 0;
+  for (int l = threadIdx.x; l < lay.L; l += blockDim.x) {
+    double v = row[l];
+    s += v;
+    if (l < lay.h)
+      s0 += v;
+    else if (l < 2 * lay.h)
+      s1 += v;
+  }
+  s = block_sum(s, red);
+  s0 = block_sum(s0, red);
+  s1 = block_sum(s1, red);
+  if (threadIdx.x == 0) {
+    ws[lay.chain_off + b] = s;
+    ws[lay.half_off + 2 * b] = s0;
+    ws[lay.half_off + 2 * b + 1] = s1;
+  }
+  // block sums: one thread per block (blocks are short: l_block = L/32)
+  for (int k = threadIdx.x; k < lay.nb; k += blockDim.x) {
+    double t = 0;
+    for (int q = 0; q < lay.l_block; ++q) t += row[k * lay.l_block + q];
+    ws[lay.block_off + (int64_t)b * lay.nb + k] = t;
+  }
+}
+
+// population variance of v[i] * scale over count entries (two-pass)
+__device__ double pop_var(const double *v, int64_t count, double scale, double *red) {
+  double s = 0;
+  for (int64_t i = threadIdx.x; i < count; i += blockDim.x) s += v[i] * scale;
+  double mean = block_sum(s, red) / (double)count;
+  double q = 0;
+  for (int64_t i = threadIdx.x; i < count; i += blockDim.x) {
+    double d = v[i] * scale - mean;
+    q += d * d;
+  }
+  return block_sum(q, red) / (double)count;
+}
+
+__global__ void stats_pass2(const double *__restrict__ data, StatsLayout lay, int plain_rhat,
+                            const double *ws, double *out5) {
+  __shared__ double red[32];
+  const int64_t ts = (int64_t)lay.B * lay.L;
+  double s = 0;
+  for (int b = threadIdx.x; b < lay.B; b += blockDim.x) s += ws[lay.chain_off + b];
+  const double mean = block_sum(s, red) / (double)ts;
+  double q = 0;
+  for (int64_t i = threadIdx.x; i < ts; i += blockDim.x) {
+    double d = data[i] - mean;
+    q += d * d;
+  }
+  const double variance = block_sum(q, red) / (double)ts;
+  double batch_var = pop_var(ws + lay.chain_off, lay.B, 1.0 / lay.L, red);
+  const int n_batches = lay.B;
+  const int64_t n_blocks = (int64_t)lay.B * lay.nb;
+  double block_var = n_blocks > 0 ? pop_var(ws + lay.block_off, n_blocks, 1.0 / lay.l_block, red)
+                                  : nan("");
+  double split_var = 0;
+  if (!plain_rhat && n_batches > 1 && lay.h > 0)
+    split_var = pop_var(ws + lay.half_off, 2 * (int64_t)lay.B, 1.0 / lay.h, red);
+  if (threadIdx.x == 0) {
+    const int batch_size = 32;
+    double tau_batch = (((double)ts / n_batches) * batch_var / variance - 1) * 0.5;
+    double tau_block = (((double)ts / (double)n_blocks) * block_var / variance - 1) * 0.5;
+    bool batch_good = (tau_batch < 6.0 * lay.L) && (n_batches >= batch_size);
+    bool block_good = (tau_block < 6.0 * lay.l_block) && (n_blocks >= batch_size);
+    double err, tau;
+    if (batch_good) {
+      err = sqrt(batch_var / n_batches);
+      tau = tau_batch < 0 ? 0.0 : tau_batch;
+    } else if (block_good) {
+      err = sqrt(block_var / (double)n_blocks);
+      tau = tau_block < 0 ? 0.0 : tau_block;
+    } else {
+      err = nan("");
+      tau = nan("");
+    }
+    double rhat = nan("");
+    if (n_batches > 1) {
+      double bv = plain_rhat ? batch_var : (lay.h > 0 ? split_var : nan(""));
+      rhat = sqrt((double)(lay.L - 1) / lay.L + bv / variance);
+    }
+    out5[0] = mean;
+    out5[1] = err;
+    out5[2] = variance;
+    out5[3] = tau;
+    out5[4] = rhat;
+  }
+}
+
+}  // namespace vmck
+
+using namespace vmck;
+
+extern "C" int64_t vmck_stats_workspace_size(int32_t n_chains, int32_t chain_length) {
+  if (n_chains <= 0 || chain_length <= 0) return 0;
+  return stats_layout(n_chains, chain_length).total;
+}
+
+extern "C" int vmck_stats_f64(vmck_stream s, const double *data, int32_t n_chains,
+                              int32_t chain_length, int32_t plain_rhat, double *out5,
+                              double *workspace, int64_t workspace_len) {
+  VMCK_REQUIRE(data && out5 && workspace && n_chains > 0 && chain_length > 0, "stats arguments");
+  StatsLayout lay = stats_layout(n_chains, chain_length);
+  VMCK_REQUIRE(workspace_len >= lay.total, "stats workspace too small");
+  cudaStream_t st = as_stream(s);
+  stats_pass1<<<n_chains, 128, 0, st>>>(data, lay, workspace);
+  int rc = check_launch("stats pass 1");
+  if (rc) return rc;
+  stats_pass2<<<1, 1024, 0, st>>>(data, lay, plain_rhat, workspace, out5);
+  return check_launch("stats pass 2");
+}

@@ -1,0 +1,147 @@
+"""Drivers (``netket.driver``): ``VMC`` and ``VMC_SR``.
+
+The run loop mirrors ``netket/_src/driver/abstract_variational_driver.py:349-478``
+(compute the loss and update, apply the optimiser, log, callbacks);
+``VMC.compute_loss_and_update`` is ``netket/driver/vmc.py:141-158`` and
+``VMC_SR.compute_loss_and_update`` is ``netket/_src/driver/vmc_sr.py:438-510``.
+One step reads back exactly one small device buffer (the energy statistics and
+the solver status).
+"""
+import time
+
+import torch
+
+from .ngd import minsr_update, sr_update
+from .optimizer import identity_preconditioner
+from .stats import Stats
+
+
+class RuntimeLog:
+    """In-memory log of the per-step quantities (``RuntimeLog``)."""
+
+    def __init__(self):
+        self.data = {}
+
+    def __call__(self, step, item):
+        for k, v in item.items():
+            self.data.setdefault(k, {"iters": [], "value": []})
+            self.data[k]["iters"].append(step)
+            self.data[k]["value"].append(v)
+
+    def __getitem__(self, k):
+        return self.data[k]
+
+
+class AbstractVariationalDriver:
+    def __init__(self, variational_state, optimizer, minimized_quantity_name="Energy"):
+        self.state = variational_state
+        self.optimizer = optimizer
+        self._loss_name = minimized_quantity_name
+        self._loss_stats = None
+        self._dp = None
+        self.step_count = 0
+        self.info = None
+
+    def compute_loss_and_update(self):
+        raise NotImplementedError
+
+    def reset(self):
+        self.step_count = 0
+        self.state.reset()
+
+    def advance(self, steps=1):
+        for _ in range(steps):
+            self._loss_stats, self._dp = self.compute_loss_and_update()
+            self.optimizer.apply(self.state, self._dp, self.step_count)
+            self.step_count += 1
+        return self._loss_stats
+
+    def iter(self, n_steps, step=1):
+        for _ in range(0, n_steps, step):
+            self.advance(step)
+            yield self.step_count
+
+    def run(self, n_iter, out=None, callback=None, timeit=False):
+        """Run ``n_iter`` steps.  ``out`` is a logger called with
+        (step, {loss_name: Stats-as-dict}); ``callback(step, log_data, driver)``
+        may return False to stop (``abstract_variational_driver.py:444-478``)."""
+        if out is None:
+            out = RuntimeLog()
+        loggers = out if isinstance(out, (list, tuple)) else [out]
+        callbacks = callback if isinstance(callback, (list, tuple)) else (
+            [callback] if callback else [])
+        t0 = time.perf_counter()
+        for _ in range(n_iter):
+            step = self.step_count
+            stats = self.advance(1)
+            log_data = {self._loss_name: stats.to_dict()}
+            for lg in loggers:
+                lg(step, log_data)
+            if any(cb(step, log_data, self) is False for cb in callbacks):
+                break
+        self.wall_time = time.perf_counter() - t0
+        return loggers
+
+    @property
+    def energy(self):
+        return self._loss_stats
+
+
+class VMC(AbstractVariationalDriver):
+    """``expect_and_grad`` then an optional preconditioner (e.g. ``SR``)."""
+
+    def __init__(self, hamiltonian, optimizer, *, variational_state, preconditioner=None):
+        super().__init__(variational_state, optimizer)
+        self._ham = hamiltonian
+        self.preconditioner = preconditioner or identity_preconditioner
+
+    def compute_loss_and_update(self):
+        self.state.reset()
+        stats, grad = self.state.expect_and_grad(self._ham)
+        dp = self.preconditioner(self.state, self.state.model.flatten(grad), self.step_count)
+        return stats, dp
+
+
+class VMC_SR(AbstractVariationalDriver):
+    """Natural-gradient VMC: minSR (``use_ntk=True``) or SR.
+
+    ``use_ntk=None`` picks minSR when n_parameters > n_samples
+    (``vmc_sr.py:356-357``).  ``gram``/``solve``/``gram_mode`` select the
+    implementation of the minSR linear algebra (see ``netket_gb300.ngd``).
+    """
+
+    def __init__(self, hamiltonian, optimizer, *, diag_shift, variational_state, use_ntk=None,
+                 gram="structured", gram_mode=None, solve=None, refine_iters=4,
+                 refine_tol=1e-10, jac_dtype=None, proj_reg=None, momentum=None):
+        super().__init__(variational_state, optimizer)
+        if proj_reg is not None or momentum is not None:
+            raise NotImplementedError("proj_reg / momentum are not supported")
+        self._ham = hamiltonian
+        self.diag_shift = diag_shift
+        if use_ntk is None:
+            use_ntk = variational_state.n_parameters > variational_state.n_samples
+        self.use_ntk = bool(use_ntk)
+        self.gram = gram
+        self.gram_mode = gram_mode
+        if solve is None:
+            solve = "refined" if variational_state.precision == "mixed" else "cholesky"
+        self.solve = solve
+        self.refine_iters = refine_iters
+        self.refine_tol = refine_tol
+        self.jac_dtype = jac_dtype
+
+    def compute_loss_and_update(self):
+        st = self.state
+        st.reset()
+        c = st._forward_cache(self._ham)
+        shift = self.diag_shift(self.step_count) if callable(self.diag_shift) else self.diag_shift
+        if self.use_ntk:
+            dp, self.info = minsr_update(c["t"], c["x"], st.N, st.M, c["e"], c["stats_dev"][0:1],
+                                         shift, gram=self.gram, gram_mode=self.gram_mode,
+                                         solve=self.solve, refine_iters=self.refine_iters,
+                                         refine_tol=self.refine_tol, jac_dtype=self.jac_dtype)
+        else:
+            dp, self.info = sr_update(c["t"], c["x"], st.N, st.M, c["e"], c["stats_dev"][0:1],
+                                      shift, jac_dtype=self.jac_dtype)
+        stats = Stats.from_array(c["stats_dev"].cpu().numpy())
+        return stats, dp

@@ -1,0 +1,95 @@
+"""Spin-1/2 Hilbert space (``netket.hilbert.Spin`` for s = 1/2).
+
+States are int8 tensors with values +1 / -1 (NetKet's new ordering,
+``netket/hilbert/spin.py:167-172``); local index 0 <-> +1, 1 <-> -1.
+Random states come from the CUDA kernel ``vmck_random_states``.
+"""
+import itertools
+
+import numpy as np
+import torch
+
+from . import _native as nat
+
+
+class Spin:
+    def __init__(self, s=0.5, N=1, total_sz=None):
+        if s != 0.5:
+            raise NotImplementedError("only spin-1/2 is supported")
+        self.s = 0.5
+        self.N = int(N)
+        if total_sz is not None:
+            two_sz = round(2 * total_sz)
+            if (self.N + two_sz) % 2 != 0 or abs(two_sz) > self.N:
+                raise ValueError(f"total_sz={total_sz} is incompatible with N={self.N}")
+        self.total_sz = total_sz
+
+    @property
+    def size(self):
+        return self.N
+
+    @property
+    def local_size(self):
+        return 2
+
+    @property
+    def local_states(self):
+        return [1, -1]
+
+    @property
+    def shape(self):
+        return (2,) * self.N
+
+    @property
+    def constrained(self):
+        return self.total_sz is not None
+
+    @property
+    def n_down(self):
+        """Number of down spins fixed by ``total_sz`` (None if unconstrained)."""
+        if self.total_sz is None:
+            return None
+        return (self.N - round(2 * self.total_sz)) // 2
+
+    def random_state(self, seed, size, stream_id=0):
+        """(size, N) int8 device tensor: uniform, or a uniformly random
+        arrangement of the fixed number of down spins."""
+        out = torch.empty((int(size), self.N), dtype=torch.int8, device=nat.device())
+        nd = -1 if self.n_down is None else self.n_down
+        nat.check(nat.lib().vmck_random_states(nat.stream(), nat.ptr(out), int(size), self.N, nd,
+                                               int(seed) & (2**64 - 1), int(stream_id)))
+        return out
+
+    @staticmethod
+    def states_to_local_indices(x):
+        return ((1 - x.to(torch.int16)) // 2).to(torch.int8)
+
+    @staticmethod
+    def local_indices_to_states(i):
+        return (1 - 2 * i.to(torch.int16)).to(torch.int8)
+
+    @property
+    def n_states(self):
+        if self.total_sz is None:
+            return 2**self.N
+        from math import comb
+        return comb(self.N, self.n_down)
+
+    def all_states(self):
+        """Every basis state (device int8), first site most significant."""
+        if self.N > 26:
+            raise ValueError("Hilbert space too large to enumerate")
+        idx = np.array(list(itertools.product([0, 1], repeat=self.N)), dtype=np.int8)
+        if self.n_down is not None:
+            idx = idx[idx.sum(axis=1) == self.n_down]
+        return torch.from_numpy(1 - 2 * idx).to(nat.device())
+
+    def __eq__(self, other):
+        return isinstance(other, Spin) and (self.N, self.total_sz) == (other.N, other.total_sz)
+
+    def __hash__(self):
+        return hash((self.N, self.total_sz))
+
+    def __repr__(self):
+        tsz = "" if self.total_sz is None else f", total_sz={self.total_sz}"
+        return f"Spin(s=1/2{tsz}, N={self.N})"

@@ -1,0 +1,76 @@
+"""The RBM (``netket.models.RBM``, ``netket/models/rbm.py:33-81``).
+
+logpsi(x) = sum_j log_cosh(b_j + sum_i x_i W_ij) + sum_i a_i x_i.
+
+Parameters follow NetKet's pytree ``{"Dense": {"bias": (M,), "kernel": (N, M)},
+"visible_bias": (N,)}`` and its ravel order (sorted keys): bias, kernel
+(row-major), visible_bias.  On the device they live in one flat buffer in that
+order, which is the layout every kernel takes.
+"""
+import torch
+
+from . import _native as nat
+
+
+class RBM:
+    def __init__(self, alpha=1, param_dtype=torch.float64, use_hidden_bias=True,
+                 use_visible_bias=True, kernel_init_std=0.01, hidden_bias_init_std=0.01,
+                 visible_bias_init_std=0.01):
+        if not (use_hidden_bias and use_visible_bias):
+            raise NotImplementedError("the RBM kernels take both biases")
+        self.alpha = alpha
+        self.param_dtype = param_dtype
+        self.stds = (hidden_bias_init_std, kernel_init_std, visible_bias_init_std)
+
+    def n_hidden(self, N):
+        return int(self.alpha * N)
+
+    def n_parameters(self, N):
+        M = self.n_hidden(N)
+        return M + N * M + N
+
+    def init_flat(self, seed, N):
+        """Flat FP64 parameters, each leaf ~ Normal(0, std) (``rbm.py:29``)."""
+        M = self.n_hidden(N)
+        g = torch.Generator().manual_seed(int(seed))
+        sb, sk, sv = self.stds
+        flat = torch.cat([torch.randn(M, generator=g, dtype=torch.float64) * sb,
+                          torch.randn(N * M, generator=g, dtype=torch.float64) * sk,
+                          torch.randn(N, generator=g, dtype=torch.float64) * sv])
+        if self.param_dtype == torch.float32:
+            flat = flat.to(torch.float32).to(torch.float64)
+        return flat.to(nat.device())
+
+    @staticmethod
+    def unflatten(flat, N, M):
+        return {"Dense": {"bias": flat[:M], "kernel": flat[M:M + N * M].view(N, M)},
+                "visible_bias": flat[M + N * M:]}
+
+    @staticmethod
+    def flatten(params):
+        return torch.cat([params["Dense"]["bias"].reshape(-1), params["Dense"]["kernel"].reshape(-1),
+                          params["visible_bias"].reshape(-1)])
+
+    @staticmethod
+    def sizes_from_flat(P, N):
+        M = (P - N) // (N + 1)
+        if M + N * M + N != P:
+            raise ValueError("parameter vector does not match an RBM on N sites")
+        return M
+
+    def apply(self, flat, x, dtype=None):
+        """logpsi(x) for x (..., N) int8 with flat parameters (device)."""
+        dtype = dtype or flat.dtype
+        x = x.to(device=flat.device, dtype=torch.int8)
+        N = x.shape[-1]
+        M = self.sizes_from_flat(flat.numel(), N)
+        p = flat.to(dtype).contiguous()
+        x2 = x.reshape(-1, N).contiguous()
+        out = torch.empty(x2.shape[0], dtype=dtype, device=flat.device)
+        nat.check(nat.lib().vmck_rbm_logpsi(nat.stream(), nat.dtype_code(dtype), nat.ptr(p), N, M,
+                                            nat.ptr(x2), x2.shape[0], nat.ptr(out), None, None))
+        return out.reshape(x.shape[:-1])
+
+    def __repr__(self):
+        return f"RBM(alpha={self.alpha}, param_dtype={self.param_dtype})"
+

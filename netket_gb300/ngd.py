@@ -1,0 +1,111 @@
+"""SR / minSR natural-gradient updates on the GPU.
+
+``minsr_update`` is ``netket/_src/ngd/srt.py:22-96`` (with ``_prepare_input``,
+``netket/_src/ngd/sr_srt_common.py:45-101``): ``T = O_L O_L^T + lambda I``,
+``aux = T^-1 dv``, ``delta = O_L^T aux`` with ``O_L = (O - mean O)/sqrt(n)`` and
+``dv = 2 (E - mean E)/sqrt(n)``.  ``sr_update`` is ``netket/_src/ngd/sr.py:23-80``.
+
+Two ways to form T:
+  * ``gram="structured"`` (default): the RBM identity
+    ``O(s).O(s') = (t_s.t_s')(1 + x_s.x_s') + x_s.x_s'`` (t = tanh theta) turns
+    the (n x n x P) contraction into (n x n x M), and O is never stored;
+  * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
+    and a cuBLAS SYRK.
+Solvers (``solve=``):
+  * ``"cholesky"``: cuSOLVER Cholesky in the Jacobian's precision;
+  * ``"refined"``: FP32 Cholesky refined against the FP64 matrix (iterative
+    refinement) until the FP64 residual is below ``tol``;
+with NetKet's ``cholesky_with_fallback`` behaviour: a failed factorisation or a
+non-finite result switches to ``pinv_smooth`` (``netket/optimizer/solver/
+solvers.py:305-340``).
+"""
+import math
+
+import torch
+
+from . import _native as nat
+from . import kernels as K
+
+
+class SolveInfo(dict):
+    pass
+
+
+def _status():
+    return torch.zeros(1, dtype=torch.int32, device=nat.device())
+
+
+def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram_mode=None,
+                 solve="cholesky", refine_iters=4, refine_tol=1e-10, rtol=1e-14,
+                 rtol_smooth=1e-14, jac_dtype=None, check=True):
+    """Returns (delta (P,) FP64, info).  ``t`` = tanh(theta) (n, M) in the compute
+    dtype, ``e`` = local energies (n,) FP64, ``mean_dev`` = their mean (device)."""
+    n = x.shape[0]
+    s = 1.0 / math.sqrt(n)
+    obar = K.column_means(t, x, N, M)
+    dv = K.center_scale(e, mean_dev, 2.0 * s)
+    status = _status()
+    info = SolveInfo(solver_fallback=False)
+    if gram == "structured":
+        mode = gram_mode if gram_mode is not None else (0 if t.dtype == torch.float64 else 1)
+        T64, T32 = K.gram_structured(t, x, N, M, obar, diag_shift, mode,
+                                     want_f32=(solve == "refined"))
+        if solve == "refined":
+            aux, res = K.cholesky_solve_refined(T64, T32, dv, status, refine_iters, refine_tol)
+            info["residual_dev"] = res
+        else:
+            aux = K.cholesky_solve(T64, dv, status)
+        Tfb = T64
+    elif gram == "dense":
+        jd = jac_dtype or t.dtype
+        O_L = K.jacobian_dense(t, x, N, M, obar, s, jd)
+        T = K.gram_dense(O_L, diag_shift)
+        del O_L
+        if T.dtype == torch.float64:
+            aux = K.cholesky_solve(T, dv, status)
+        else:
+            aux = K.cholesky_solve(T, dv.to(torch.float32), status).to(torch.float64)
+        Tfb = T
+    else:
+        raise ValueError("gram must be 'structured' or 'dense'")
+    info["status_dev"] = status
+    if check:
+        st = int(status.item())
+        if st & (nat.DEV_NOT_SPD | nat.DEV_NONFINITE):
+            A = Tfb.to(torch.float64)
+            A = torch.tril(A) + torch.tril(A, -1).T
+            aux = K.pinv_smooth_solve(A.contiguous(), dv, rtol, rtol_smooth)
+            info["solver_fallback"] = True
+        info["status"] = st
+    raw = K.ot_v(t, x, N, M, aux)
+    delta = K.center_update(raw, obar, aux, s)
+    return delta, info
+
+
+def sr_update(t, x, N, M, e, mean_dev, diag_shift, *, jac_dtype=None, rtol=1e-14,
+              rtol_smooth=1e-14):
+    """SR with the dense QGT: (O_L^T O_L + lambda I) delta = O_L^T dv."""
+    n = x.shape[0]
+    s = 1.0 / math.sqrt(n)
+    obar = K.column_means(t, x, N, M)
+    dv = K.center_scale(e, mean_dev, 2.0 * s)
+    raw = K.ot_v(t, x, N, M, dv)
+    F = K.center_update(raw, obar, dv, s)
+    jd = jac_dtype or torch.float64
+    O_L = K.jacobian_dense(t, x, N, M, obar, s, jd)
+    S = K.gram_dense(O_L, diag_shift, transpose=True)
+    return solve_with_fallback(S.to(torch.float64), F, rtol, rtol_smooth)
+
+
+def solve_with_fallback(A, b, rtol=1e-14, rtol_smooth=1e-14):
+    """``cholesky_with_fallback`` for an SPD matrix whose lower triangle is set."""
+    status = _status()
+    x = K.cholesky_solve(A, b, status)
+    info = SolveInfo(solver_fallback=False)
+    st = int(status.item())
+    if st & (nat.DEV_NOT_SPD | nat.DEV_NONFINITE):
+        full = torch.tril(A) + torch.tril(A, -1).T
+        x = K.pinv_smooth_solve(full.contiguous(), b, rtol, rtol_smooth)
+        info["solver_fallback"] = True
+    info["status"] = st
+    return x, info

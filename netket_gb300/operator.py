@@ -1,0 +1,364 @@
+"""Hamiltonians of the hot path: ``Ising``, ``LocalOperator``, ``Heisenberg``,
+``GraphOperator`` (``netket.operator`` for spin-1/2).
+
+``get_conn_padded(x)`` follows NetKet's JAX operators (``IsingJax``,
+``LocalOperatorJax``): for x (..., N) it returns x' (..., K, N) int8 and
+mels (..., K) float64 with ``K = max_conn_size``, computed on the GPU by
+``vmck_get_conn_ising`` / ``vmck_get_conn_local``.  Operator tables are packed
+on the host once (the work of
+``netket/operator/_local_operator/compile_helpers.py:29-218``) and kept
+resident on the device.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .hilbert import Spin
+
+
+def _as_x(x, N):
+    if not isinstance(x, torch.Tensor):
+        x = torch.as_tensor(np.asarray(x))
+    x = x.to(device=nat.device(), dtype=torch.int8)
+    if x.shape[-1] != N:
+        raise ValueError(f"last dimension {x.shape[-1]} != N={N}")
+    return x.contiguous()
+
+
+class DiscreteOperator:
+    """Shared API of the device operators."""
+
+    is_hermitian = True
+
+    def __init__(self, hilbert):
+        self.hilbert = hilbert
+
+    def get_conn_padded(self, x):
+        x = _as_x(x, self.hilbert.size)
+        batch = x.shape[:-1]
+        x2 = x.reshape(-1, self.hilbert.size)
+        xp, mels, _ = self._conn(x2)
+        K = mels.shape[-1]
+        return xp.reshape(*batch, K, self.hilbert.size), mels.reshape(*batch, K)
+
+    def n_conn(self, x):
+        x = _as_x(x, self.hilbert.size)
+        _, _, n = self._conn(x.reshape(-1, self.hilbert.size))
+        return n.reshape(x.shape[:-1])
+
+    def to_sparse(self):
+        import scipy.sparse as sp
+        states = self.hilbert.all_states()
+        xp, mels = self.get_conn_padded(states)
+        n, K, N = xp.shape
+        w = torch.tensor([1 << (N - 1 - i) for i in range(N)], dtype=torch.int64,
+                         device=states.device)
+        code_x = (((1 - states.to(torch.int64)) // 2) * w).sum(-1)
+        code_xp = (((1 - xp.to(torch.int64)) // 2) * w).sum(-1)
+        order = torch.argsort(code_x)
+        pos = torch.searchsorted(code_x[order], code_xp.reshape(-1))
+        pos = order[pos.clamp(max=n - 1)].reshape(n, K)
+        m = mels.cpu().numpy()
+        cols = pos.cpu().numpy()
+        rows = np.repeat(np.arange(n), K)
+        keep = m.reshape(-1) != 0
+        return sp.csr_matrix((m.reshape(-1)[keep], (rows[keep], cols.reshape(-1)[keep])),
+                             shape=(n, n))
+
+    def to_dense(self):
+        return self.to_sparse().toarray()
+
+
+class Ising(DiscreteOperator):
+    """``-h sum_i X_i + J sum_<ij> Z_i Z_j`` (``netket/operator/_ising/jax.py``)."""
+
+    def __init__(self, hilbert, graph, h, J=1.0, dtype=None):
+        super().__init__(hilbert)
+        if hasattr(graph, "edges"):
+            edges = np.asarray(graph.edges(), dtype=np.int64).reshape(-1, 2)
+        else:
+            edges = np.asarray(graph, dtype=np.int64).reshape(-1, 2)
+        self.edges = edges
+        self.h = float(h)
+        self.J = float(J)
+        self._dev = {}
+
+    @property
+    def max_conn_size(self):
+        return self.hilbert.size + 1
+
+    def _edges_dev(self):
+        d = torch.cuda.current_device()
+        if d not in self._dev:
+            self._dev[d] = torch.as_tensor(self.edges.astype(np.int32), device=nat.device())
+        return self._dev[d]
+
+    def _conn(self, x):
+        n, N = x.shape
+        K = 1 if self.h == 0 else N + 1
+        xp = torch.empty((n, K, N), dtype=torch.int8, device=x.device)
+        mels = torch.empty((n, K), dtype=torch.float64, device=x.device)
+        nc = torch.empty((n,), dtype=torch.int32, device=x.device)
+        e = self._edges_dev()
+        nat.check(nat.lib().vmck_get_conn_ising(nat.stream(), nat.ptr(x), n, N, nat.ptr(e),
+                                                len(self.edges), self.h, self.J,
+                                                int(self.h == 0), nat.ptr(xp), nat.ptr(mels),
+                                                nat.ptr(nc)))
+        return xp, mels, nc
+
+    def to_local_operator(self):
+        """``IsingBase.to_local_operator``: -h X_i terms, then J Z_i Z_j per edge."""
+        ops, aon = [], []
+        if self.h != 0:
+            for i in range(self.hilbert.size):
+                ops.append(-self.h * SIGMAX)
+                aon.append([i])
+        if self.J != 0:
+            for i, j in self.edges:
+                ops.append(self.J * np.kron(SIGMAZ, SIGMAZ))
+                aon.append([int(i), int(j)])
+        return LocalOperator(self.hilbert, ops, aon)
+
+    def __repr__(self):
+        return f"Ising(J={self.J}, h={self.h}; dim={self.hilbert.size})"
+
+
+SIGMAX = np.array([[0.0, 1.0], [1.0, 0.0]])
+SIGMAZ = np.array([[1.0, 0.0], [0.0, -1.0]])
+SZSZ = np.diag([1.0, -1.0, -1.0, 1.0])
+EXCHANGE = np.array([[0, 0, 0, 0], [0, 0, 2, 0], [0, 2, 0, 0], [0, 0, 0, 0]], dtype=np.float64)
+
+
+def _sort_sites(mat, sites):
+    """Sort the sites of a k-local matrix, permuting its tensor factors
+    (first site = most significant digit of the row index)."""
+    sites = [int(s) for s in sites]
+    if len(set(sites)) != len(sites):
+        raise ValueError(f"operator acts on duplicated sites {sites}")
+    order = sorted(range(len(sites)), key=lambda q: sites[q])
+    if order == list(range(len(sites))):
+        return np.array(mat, dtype=np.float64), tuple(sites)
+    k = len(sites)
+    t = np.asarray(mat, dtype=np.float64).reshape((2,) * (2 * k))
+    t = np.transpose(t, order + [k + q for q in order])
+    return t.reshape(2**k, 2**k), tuple(sites[q] for q in order)
+
+
+class LocalOperator(DiscreteOperator):
+    """Sum of k-local spin-1/2 terms (k <= 4), NetKet's ``LocalOperator``."""
+
+    def __init__(self, hilbert, operators=(), acting_on=(), constant=0.0, dtype=None,
+                 mel_cutoff=1e-10):
+        super().__init__(hilbert)
+        self.constant = float(constant)
+        self.mel_cutoff = float(mel_cutoff)
+        self._terms = {}
+        if len(acting_on) and np.isscalar(acting_on[0]):
+            operators, acting_on = [operators], [acting_on]
+        for op, aon in zip(operators, acting_on):
+            self._add(np.asarray(op, dtype=np.float64), aon)
+        self._tables = None
+        self._dev = {}
+
+    def _add(self, mat, aon):
+        if any(a < 0 or a >= self.hilbert.size for a in aon):
+            raise ValueError("An operator acts on an invalid set of sites.")
+        if mat.shape != (2 ** len(aon), 2 ** len(aon)):
+            raise ValueError(f"matrix shape {mat.shape} does not match sites {list(aon)}")
+        m, key = _sort_sites(mat, aon)
+        self._terms[key] = self._terms[key] + m if key in self._terms else m
+        self._tables = None
+        self._dev = {}
+
+    @property
+    def acting_on(self):
+        return [list(k) for k in self._terms]
+
+    @property
+    def operators(self):
+        return list(self._terms.values())
+
+    @property
+    def n_operators(self):
+        return len(self._terms)
+
+    def copy(self):
+        new = LocalOperator(self.hilbert, constant=self.constant, mel_cutoff=self.mel_cutoff)
+        new._terms = {k: v.copy() for k, v in self._terms.items()}
+        return new
+
+    def __add__(self, other):
+        new = self.copy()
+        if isinstance(other, LocalOperator):
+            for k, v in other._terms.items():
+                new._add(v, k)
+            new.constant += other.constant
+        elif np.isscalar(other):
+            new.constant += float(other)
+        else:
+            return NotImplemented
+        return new
+
+    __radd__ = __add__
+
+    def __mul__(self, s):
+        if not np.isscalar(s):
+            return NotImplemented
+        new = LocalOperator(self.hilbert, constant=self.constant * s, mel_cutoff=self.mel_cutoff)
+        new._terms = {k: v * s for k, v in self._terms.items()}
+        return new
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return self * -1.0
+
+    def __sub__(self, other):
+        return self + (-other)
+
+    # ---------------------------------------------------------------- packing
+    def _pack(self):
+        """Device tables in JAX-packer order: terms grouped by acting size
+        (ascending), insertion order within a group."""
+        if self._tables is not None:
+            return self._tables
+        items = list(self._terms.items())
+        sizes = sorted({len(k) for k, _ in items})
+        ordered = [(k, m) for s in sizes for (k, m) in items if len(k) == s]
+        group_end, acc = [], 0
+        for s in sizes:
+            acc += sum(1 for k, _ in items if len(k) == s)
+            group_end.append(acc)
+        T = len(ordered)
+        S = max(sizes) if sizes else 1
+        if S > 4:
+            raise NotImplementedError("terms acting on more than 4 sites are not supported")
+        R = 2**S
+        cut = self.mel_cutoff
+        per_row = []
+        K = 0
+        nonzero_diag = abs(self.constant) >= cut
+        for k, m in ordered:
+            off = np.abs(m) > cut
+            np.fill_diagonal(off, False)
+            per_row.append(off)
+            kept = np.abs(m) >= cut
+            np.fill_diagonal(kept, False)
+            K += int(kept.sum(axis=1).max())
+            nonzero_diag = nonzero_diag or bool(np.any(np.abs(np.diag(m)) >= cut))
+        C = max([int(o.sum(axis=1).max()) for o in per_row], default=0)
+        if nonzero_diag:
+            K += 1
+        acting_on = np.full((T, S), -1, dtype=np.int32)
+        acting_size = np.zeros(T, dtype=np.int32)
+        diag = np.zeros((T, R))
+        n_conns = np.zeros((T, R), dtype=np.int32)
+        mels = np.zeros((T, R, max(C, 1)))
+        xprime = np.zeros((T, R, max(C, 1), S), dtype=np.int8)
+        for t, ((key, m), off) in enumerate(zip(ordered, per_row)):
+            sz = len(key)
+            acting_on[t, :sz] = key
+            acting_size[t] = sz
+            for r in range(2**sz):
+                diag[t, r] = m[r, r]
+                cols = np.flatnonzero(off[r])
+                n_conns[t, r] = len(cols)
+                for c, col in enumerate(cols):
+                    mels[t, r, c] = m[r, col]
+                    bits = [(col >> (sz - 1 - q)) & 1 for q in range(sz)]
+                    xprime[t, r, c, :sz] = [1 - 2 * b for b in bits]
+        self._tables = dict(T=T, S=S, R=R, C=max(C, 1), K=K, nonzero_diag=bool(nonzero_diag),
+                            acting_on=acting_on, acting_size=acting_size,
+                            group_end=np.array(group_end, dtype=np.int32), diag=diag,
+                            n_conns=n_conns, mels=mels, xprime=xprime)
+        return self._tables
+
+    @property
+    def max_conn_size(self):
+        return self._pack()["K"]
+
+    def device_struct(self):
+        """(ctypes ``vmck_local_op``, tensors kept alive) on the current device."""
+        d = torch.cuda.current_device()
+        if d not in self._dev:
+            tb = self._pack()
+            dev = nat.device()
+            keep = {k: torch.as_tensor(np.ascontiguousarray(tb[k]), device=dev)
+                    for k in ("acting_on", "acting_size", "group_end", "diag", "n_conns", "mels",
+                              "xprime")}
+            st = nat.LocalOpStruct(
+                n_sites=self.hilbert.size, n_terms=tb["T"], max_sites=tb["S"], max_rows=tb["R"],
+                max_conns=tb["C"], max_conn_size=tb["K"], nonzero_diagonal=int(tb["nonzero_diag"]),
+                n_groups=len(tb["group_end"]), constant=self.constant, mel_cutoff=self.mel_cutoff,
+                acting_on=keep["acting_on"].data_ptr(), acting_size=keep["acting_size"].data_ptr(),
+                group_end=keep["group_end"].data_ptr(), diag_mels=keep["diag"].data_ptr(),
+                n_conns=keep["n_conns"].data_ptr(), mels=keep["mels"].data_ptr(),
+                x_prime=keep["xprime"].data_ptr())
+            self._dev[d] = (st, keep)
+        return self._dev[d][0]
+
+    def _conn(self, x):
+        n, N = x.shape
+        st = self.device_struct()
+        K = st.max_conn_size
+        xp = torch.empty((n, K, N), dtype=torch.int8, device=x.device)
+        mels = torch.empty((n, K), dtype=torch.float64, device=x.device)
+        nc = torch.empty((n,), dtype=torch.int32, device=x.device)
+        if K == 0:
+            return xp, mels, nc.zero_()
+        nat.check(nat.lib().vmck_get_conn_local(nat.stream(), ctypes.byref(st), nat.ptr(x), n,
+                                                nat.ptr(xp), nat.ptr(mels), nat.ptr(nc)))
+        return xp, mels, nc
+
+    def __repr__(self):
+        return (f"LocalOperator(dim={self.hilbert.size}, #acting_on={len(self._terms)} "
+                f"locations, constant={self.constant})")
+
+
+def GraphOperator(hilbert, graph, site_ops=(), bond_ops=(), bond_ops_colors=()):
+    """Sum of site operators on every node and bond operators on every edge
+    (coloured edges select their operator), NetKet's term order
+    (``netket/operator/_graph_operator.py:103-145``)."""
+    if len(site_ops) == 0 and len(bond_ops) == 0:
+        raise ValueError("Must input at least site_ops or bond_ops.")
+    ops, aon = [], []
+    for i in range(graph.n_nodes):
+        for so in site_ops:
+            ops.append(so)
+            aon.append([i])
+    if len(bond_ops_colors) > 0:
+        if len(bond_ops) != len(bond_ops_colors):
+            raise ValueError("The sizes of bond_ops and bond_ops_colors do not match.")
+        for u, v, color in graph.edges(return_color=True):
+            for c, bc in enumerate(bond_ops_colors):
+                if bc == color:
+                    ops.append(bond_ops[c])
+                    aon.append([u, v])
+    else:
+        if len(bond_ops) != 1:
+            raise ValueError("without colours exactly one bond operator is expected")
+        for u, v in graph.edges():
+            ops.append(bond_ops[0])
+            aon.append([u, v])
+    return LocalOperator(hilbert, ops, aon)
+
+
+def Heisenberg(hilbert, graph, J=1.0, sign_rule=None):
+    """``J (Sz Sz +/- 2 (S+S- + S-S+))`` per bond (``netket/operator/_heisenberg.py``);
+    the minus sign applies Marshall's sign rule (default: bipartite graph for a
+    scalar J, ``False`` per colour for a J list)."""
+    if isinstance(J, (list, tuple)):
+        if len(J) != max(graph.edge_colors) + 1:
+            raise ValueError("one coupling per edge colour is expected")
+        if sign_rule is None:
+            sign_rule = [False] * len(J)
+        bond_ops = [J[i] * (SZSZ - EXCHANGE if sign_rule[i] else SZSZ + EXCHANGE)
+                    for i in range(len(J))]
+        return GraphOperator(hilbert, graph, bond_ops=bond_ops, bond_ops_colors=list(range(len(J))))
+    if sign_rule is None:
+        sign_rule = graph.is_bipartite()
+    elif sign_rule and not graph.is_bipartite():
+        raise ValueError("sign_rule=True specified for a non-bipartite lattice")
+    return GraphOperator(hilbert, graph, bond_ops=[J * (SZSZ - EXCHANGE if sign_rule else SZSZ + EXCHANGE)])

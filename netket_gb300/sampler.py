@@ -1,0 +1,158 @@
+"""Metropolis samplers (``netket.sampler``): ``MetropolisSampler`` with the
+``LocalRule`` / ``ExchangeRule`` transition rules and the ``MetropolisLocal`` /
+``MetropolisExchange`` constructors.
+
+The whole chain (discarded plus kept sweeps) runs in ONE launch of
+``vmck_metropolis_sample``: a warp per chain, the RBM pre-activations kept
+in shared memory and updated per proposal.  Samples come back shaped
+(n_chains, chain_length, N) as in ``netket/sampler/metropolis.py:496-500``.
+The random stream is Philox4x32-10, keyed by the sampler seed, with a
+proposal counter carried in the sampler state.
+"""
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as nat
+
+
+class MetropolisRule:
+    code = None
+
+    def device_clusters(self):
+        return None, 0
+
+
+class LocalRule(MetropolisRule):
+    """Flip one uniformly chosen site (``netket/sampler/rules/local.py:40-49``)."""
+    code = 0
+
+    def __repr__(self):
+        return "LocalRule()"
+
+
+class ExchangeRule(MetropolisRule):
+    """Swap the spins of a uniformly chosen cluster (i, j) with x_i != x_j
+    (``netket/sampler/rules/exchange.py:143-218``).  Clusters are all pairs
+    with graph distance <= d_max, in row-major order."""
+    code = 1
+
+    def __init__(self, *, clusters=None, graph=None, d_max=1):
+        if clusters is None:
+            if graph is None:
+                raise ValueError("pass clusters or a graph")
+            dist = np.asarray(graph.distances())
+            cl = np.argwhere(dist <= d_max)
+            clusters = cl[cl[:, 0] < cl[:, 1]]
+        self.clusters = np.asarray(clusters, dtype=np.int64).reshape(-1, 2)
+        self._dev = {}
+
+    def device_clusters(self):
+        d = torch.cuda.current_device()
+        if d not in self._dev:
+            self._dev[d] = torch.as_tensor(self.clusters.astype(np.int32), device=nat.device())
+        return self._dev[d], len(self.clusters)
+
+    def __repr__(self):
+        return f"ExchangeRule(# of clusters: {len(self.clusters)})"
+
+
+@dataclass
+class MetropolisSamplerState:
+    """Chain state (``netket/sampler/metropolis.py:42-95``)."""
+    σ: torch.Tensor
+    log_prob: torch.Tensor
+    seed: int
+    counter: int
+    n_accepted_proc: torch.Tensor
+    n_steps_proc: int = 0
+
+    @property
+    def acceptance(self):
+        if self.n_steps_proc == 0:
+            return None
+        return float(self.n_accepted_proc.sum().item()) / self.n_steps_proc
+
+    @property
+    def n_accepted(self):
+        return int(self.n_accepted_proc.sum().item())
+
+
+class MetropolisSampler:
+    machine_pow = 2
+    is_exact = False
+
+    def __init__(self, hilbert, rule, *, n_chains=None, n_chains_per_rank=None, sweep_size=None,
+                 reset_chains=False, dtype=torch.int8):
+        if not isinstance(rule, MetropolisRule):
+            raise TypeError("rule must be a MetropolisRule")
+        if n_chains is None:
+            n_chains = n_chains_per_rank if n_chains_per_rank is not None else 16
+        self.hilbert = hilbert
+        self.rule = rule
+        self.n_chains = int(n_chains)
+        self.sweep_size = hilbert.size if sweep_size is None else int(sweep_size)
+        self.reset_chains = bool(reset_chains)
+        if self.reset_chains:
+            raise NotImplementedError("reset_chains=True is not supported")
+        self.dtype = dtype
+
+    @property
+    def n_batches(self):
+        return self.n_chains
+
+    def init_state(self, machine, params, seed=0):
+        σ = self.hilbert.random_state(seed, self.n_chains, stream_id=1)
+        lp = torch.full((self.n_chains,), -np.inf, dtype=torch.float64, device=σ.device)
+        acc = torch.zeros(self.n_chains, dtype=torch.int64, device=σ.device)
+        return MetropolisSamplerState(σ=σ, log_prob=lp, seed=int(seed) & (2**64 - 1), counter=0,
+                                      n_accepted_proc=acc)
+
+    def reset(self, machine, params, state):
+        """Recompute log_prob for the current parameters and zero the counters
+        (``netket/sampler/metropolis.py:382-414``)."""
+        N = self.hilbert.size
+        M = machine.sizes_from_flat(params.numel(), N)
+        from .kernels import rbm_forward
+        lp, _, _ = rbm_forward(params, state.σ, N, M)
+        state.log_prob = 2.0 * lp.to(torch.float64)
+        state.n_accepted_proc = torch.zeros_like(state.n_accepted_proc)
+        state.n_steps_proc = 0
+        return state
+
+    def sample(self, machine, params, *, state=None, chain_length=1, n_discard=0):
+        """Run ``n_discard`` discarded sweeps then ``chain_length`` kept sweeps.
+
+        ``params`` is the flat parameter vector in the compute dtype (FP64 or
+        FP32).  Returns samples (n_chains, chain_length, N) and the new state.
+        """
+        if state is None:
+            state = self.init_state(machine, params)
+        N = self.hilbert.size
+        M = machine.sizes_from_flat(params.numel(), N)
+        B = self.n_chains
+        L = int(chain_length)
+        samples = torch.empty((B, L, N), dtype=torch.int8, device=state.σ.device)
+        cl, C = self.rule.device_clusters()
+        nat.check(nat.lib().vmck_metropolis_sample(
+            nat.stream(), nat.dtype_code(params.dtype), nat.ptr(params.contiguous()), N, M,
+            nat.ptr(state.σ), nat.ptr(state.log_prob), nat.ptr(state.n_accepted_proc), B,
+            self.sweep_size, int(n_discard), L, nat.ptr(samples), state.seed, state.counter,
+            self.rule.code, nat.ptr(cl), C))
+        state.counter += (int(n_discard) + L) * self.sweep_size
+        state.n_steps_proc += (int(n_discard) + L) * self.sweep_size * B
+        return samples, state
+
+    def __repr__(self):
+        return (f"MetropolisSampler(rule={self.rule}, n_chains={self.n_chains}, "
+                f"sweep_size={self.sweep_size})")
+
+
+def MetropolisLocal(hilbert, **kwargs):
+    return MetropolisSampler(hilbert, LocalRule(), **kwargs)
+
+
+def MetropolisExchange(hilbert, *, clusters=None, graph=None, d_max=1, **kwargs):
+    return MetropolisSampler(hilbert, ExchangeRule(clusters=clusters, graph=graph, d_max=d_max),
+                             **kwargs)

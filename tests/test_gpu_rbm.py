@@ -1,0 +1,95 @@
+"""RBM log-amplitudes and local energies on the GPU against the FP64 oracle.
+Tolerances: FP64 kernels 1e-10 relative (the benchmark spec's bound for FP64 paths);
+FP32 kernels 2e-5 relative on log-amplitudes and 1e-4 on local energies."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_common import oracle_heisenberg, oracle_params
+from oracle import operator as oop
+from oracle import rbm as orbm
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nk():
+    import netket_gb300
+    netket_gb300._native.require_cuda()
+    return netket_gb300
+
+
+def _setup(nk, N, alpha, seed, std=0.1):
+    model = nk.models.RBM(alpha=alpha, kernel_init_std=std, hidden_bias_init_std=std,
+                          visible_bias_init_std=std)
+    flat = model.init_flat(seed, N)
+    return model, flat, model.n_hidden(N)
+
+
+@pytest.mark.parametrize("N,alpha", [(16, 1), (100, 4), (37, 2), (256, 1)])
+def test_logpsi(nk, N, alpha):
+    model, flat, M = _setup(nk, N, alpha, N)
+    x = nk.hilbert.Spin(0.5, N).random_state(seed=1, size=1000)
+    lp64 = model.apply(flat, x, dtype=torch.float64).cpu().numpy()
+    lp32 = model.apply(flat, x, dtype=torch.float32).cpu().numpy()
+    ref = orbm.logpsi(oracle_params(flat, N, M), x.cpu().numpy())
+    np.testing.assert_allclose(lp64, ref, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(lp32, ref, rtol=2e-5, atol=2e-5)
+    _, th, tt = nk.kernels.rbm_forward(flat, x, N, M, want_theta=True, want_tanh=True)
+    rth = orbm.theta(oracle_params(flat, N, M), x.cpu().numpy())
+    np.testing.assert_allclose(th.cpu().numpy(), rth, rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(tt.cpu().numpy(), np.tanh(rth), rtol=1e-12, atol=1e-13)
+
+
+@pytest.mark.parametrize("N,h,J", [(16, 1.0, 1.0), (24, 0.6, -1.0), (9, 0.0, 1.0)])
+def test_eloc_ising(nk, N, h, J):
+    model, flat, M = _setup(nk, N, 2, 3)
+    g = nk.graph.Chain(N)
+    H = nk.operator.Ising(nk.hilbert.Spin(0.5, N), g, h=h, J=J)
+    x = nk.hilbert.Spin(0.5, N).random_state(seed=2, size=777)
+    p = oracle_params(flat, N, M)
+    ref = orbm.local_energies(p, x.cpu().numpy(),
+                              lambda s: oop.ising_get_conn_padded(s, np.array(g.edges()), h, J))
+    e64 = nk.kernels.local_energies_fused(H, flat, x, N, M).cpu().numpy()
+    d64 = nk.kernels.local_energies_dense(H, flat, x, N, M).cpu().numpy()
+    e32 = nk.kernels.local_energies_fused(H, flat.float(), x, N, M).cpu().numpy()
+    d32 = nk.kernels.local_energies_dense(H, flat.float(), x, N, M).cpu().numpy()
+    np.testing.assert_allclose(e64, ref, rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(d64, ref, rtol=1e-10, atol=1e-10)
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(e32, ref, rtol=1e-4, atol=1e-4 * scale)
+    np.testing.assert_allclose(d32, ref, rtol=1e-4, atol=1e-4 * scale)
+
+
+@pytest.mark.parametrize("L,J,order", [(4, 1.0, 1), (6, [1.0, 0.5], 2), (10, [1.0, 0.5], 2)])
+def test_eloc_heisenberg(nk, L, J, order):
+    N = L * L
+    model, flat, M = _setup(nk, N, 2, 4)
+    g = nk.graph.Square(L, max_neighbor_order=order)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    H = nk.operator.Heisenberg(hi, g, J=J)
+    x = hi.random_state(seed=9, size=300)
+    ref = orbm.local_energies(oracle_params(flat, N, M), x.cpu().numpy(),
+                              oracle_heisenberg(g, J).get_conn_padded)
+    e64 = nk.kernels.local_energies_fused(H, flat, x, N, M).cpu().numpy()
+    d64 = nk.kernels.local_energies_dense(H, flat, x, N, M).cpu().numpy()
+    e32 = nk.kernels.local_energies_fused(H, flat.float(), x, N, M).cpu().numpy()
+    np.testing.assert_allclose(e64, ref, rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(d64, ref, rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(e32, ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
+
+
+def test_eloc_general_local_operator(nk):
+    """1-site and 2-site terms together (Ising written as a LocalOperator) plus
+    a constant: fused == dense == oracle."""
+    N = 10
+    model, flat, M = _setup(nk, N, 1, 5)
+    hi = nk.hilbert.Spin(0.5, N)
+    H = nk.operator.Ising(hi, nk.graph.Chain(N), h=0.8, J=1.1).to_local_operator() + 0.25
+    x = hi.random_state(seed=4, size=200)
+    ref_op = oop.LocalOperator(N, H.operators, H.acting_on, constant=0.25)
+    ref = orbm.local_energies(oracle_params(flat, N, M), x.cpu().numpy(), ref_op.get_conn_padded)
+    e = nk.kernels.local_energies_fused(H, flat, x, N, M).cpu().numpy()
+    d = nk.kernels.local_energies_dense(H, flat, x, N, M).cpu().numpy()
+    np.testing.assert_allclose(e, ref, rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(d, ref, rtol=1e-10, atol=1e-10)

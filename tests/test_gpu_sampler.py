@@ -1,0 +1,124 @@
+"""Metropolis sampling on the GPU.  As in NetKet (test/sampler/test_sampler.py:
+400-458) parity is distributional: the histogram of samples on a small system
+must follow |psi|^2 (chi-squared, Fisher-combined p-value > 0.01).  Also:
+determinism, Sz conservation, acceptance bookkeeping, log_prob consistency."""
+import numpy as np
+import pytest
+import torch
+from scipy import stats as sps
+
+from gpu_common import oracle_params
+from oracle import hilbert as oh
+from oracle import rbm as orbm
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nk():
+    import netket_gb300
+    netket_gb300._native.require_cuda()
+    return netket_gb300
+
+
+def _chi2_pvalues(nk, make_sampler, model, flat, N, total_sz, dtype, reps=6, independent=True):
+    """Fisher-combined chi-squared p-value of the sample histogram against |psi|^2.
+
+    independent=True: one sample per chain per repetition, 30 sweeps apart, with
+    many chains -- the samples inside a repetition are independent, so the test
+    stays valid for strongly peaked distributions.  independent=False: NetKet's
+    form (consecutive samples of 64 chains, n_samples = 40 * n_states), valid
+    for near-uniform distributions only."""
+    states = oh.all_states(N, total_sz)
+    p = oracle_params(flat, N, model.n_hidden(N))
+    lp = orbm.logpsi(p, states)
+    prob = np.exp(2 * (lp - lp.max()))
+    prob /= prob.sum()
+    w = 2 ** np.arange(N - 1, -1, -1)
+    code = {int(c): i for i, c in enumerate(oh.states_to_local_indices(states).astype(np.int64) @ w)}
+    n_samples = max(40 * len(states), 100)
+    n_chains = n_samples if independent else 64
+    sampler = make_sampler(n_chains)
+    chain_length = 1 if independent else int(np.ceil(n_samples / n_chains))
+    n_discard = 30 if independent else 0
+    pvals = []
+    params = flat.to(dtype)
+    state = sampler.init_state(model, params, seed=123)
+    samples, state = sampler.sample(model, params, state=state, chain_length=1, n_discard=50)
+    for _ in range(reps):
+        samples, state = sampler.sample(model, params, state=state, chain_length=chain_length,
+                                        n_discard=n_discard)
+        s = samples.reshape(-1, N).cpu().numpy()
+        idx = np.array([code[int(c)] for c in oh.states_to_local_indices(s).astype(np.int64) @ w])
+        hist = np.bincount(idx, minlength=len(states))
+        pvals.append(sps.chisquare(hist, prob * len(idx)).pvalue)
+    return sps.combine_pvalues(pvals, method="fisher").pvalue
+
+
+def _model(nk, std):
+    return nk.models.RBM(alpha=1, kernel_init_std=std, hidden_bias_init_std=std,
+                         visible_bias_init_std=std)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("std,independent", [(0.1, False), (0.5, True)])
+def test_local_rule_distribution(nk, dtype, std, independent):
+    N = 6
+    model = _model(nk, std)
+    flat = model.init_flat(7, N)
+    hi = nk.hilbert.Spin(0.5, N)
+    make = lambda nc: nk.sampler.MetropolisLocal(hi, n_chains=nc)
+    assert _chi2_pvalues(nk, make, model, flat, N, None, dtype, independent=independent) > 0.01
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("std,independent", [(0.1, False), (0.5, True)])
+def test_exchange_rule_distribution(nk, dtype, std, independent):
+    N = 8
+    model = _model(nk, std)
+    flat = model.init_flat(8, N)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    g = nk.graph.Chain(N, max_neighbor_order=2)
+    make = lambda nc: nk.sampler.MetropolisExchange(hi, graph=g, d_max=1, n_chains=nc)
+    assert len(make(1).rule.clusters) == 16
+    assert _chi2_pvalues(nk, make, model, flat, N, 0, dtype, independent=independent) > 0.01
+
+
+def test_sampler_bookkeeping(nk):
+    N = 20
+    model = nk.models.RBM(alpha=2)
+    flat = model.init_flat(1, N)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    sampler = nk.sampler.MetropolisExchange(hi, graph=nk.graph.Chain(N), n_chains=128)
+    s1 = sampler.init_state(model, flat, seed=5)
+    a, s1 = sampler.sample(model, flat, state=s1, chain_length=7, n_discard=3)
+    s2 = sampler.init_state(model, flat, seed=5)
+    b, s2 = sampler.sample(model, flat, state=s2, chain_length=7, n_discard=3)
+    assert a.shape == (128, 7, N)
+    assert torch.equal(a, b), "same seed must give identical chains"
+    assert torch.all(a.to(torch.int32).sum(-1) == 0)
+    assert torch.equal(a[:, -1], s1.σ)
+    lp = 2 * model.apply(flat, s1.σ)
+    torch.testing.assert_close(s1.log_prob, lp, rtol=1e-12, atol=1e-12)
+    assert s1.n_steps_proc == 128 * 10 * N
+    acc = s1.acceptance
+    assert 0.05 < acc <= 1.0
+    c, s1 = sampler.sample(model, flat, state=s1, chain_length=2)
+    assert not torch.equal(c[:, 0], a[:, 0])
+
+
+def test_local_sampler_fp32_matches_fp64_marginals(nk):
+    """FP32 and FP64 sampling of the same model agree on <x_i x_j> within error."""
+    N = 16
+    model = nk.models.RBM(alpha=1, kernel_init_std=0.3, hidden_bias_init_std=0.3,
+                          visible_bias_init_std=0.3)
+    flat = model.init_flat(3, N)
+    hi = nk.hilbert.Spin(0.5, N)
+    corr = []
+    for dt in (torch.float64, torch.float32):
+        sampler = nk.sampler.MetropolisLocal(hi, n_chains=1024)
+        st = sampler.init_state(model, flat.to(dt), seed=11)
+        s, st = sampler.sample(model, flat.to(dt), state=st, chain_length=64, n_discard=32)
+        s = s.reshape(-1, N).to(torch.float64)
+        corr.append((s[:, :-1] * s[:, 1:]).mean(0).cpu().numpy())
+    assert np.all(np.abs(corr[0] - corr[1]) < 0.03)

@@ -1,0 +1,115 @@
+"""End-to-end VMC on the GPU: expect / expect_and_grad against the oracle on
+the same sample set, the gradient against an exact full-sum gradient, and the
+1D transverse-field Ising chain (N=16, h=J=1) converging to the Lanczos
+ground-state energy."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_common import oracle_heisenberg, oracle_params
+from oracle import exact as oex
+from oracle import operator as oop
+from oracle import rbm as orbm
+from oracle import stats as ost
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nk():
+    import netket_gb300
+    netket_gb300._native.require_cuda()
+    return netket_gb300
+
+
+def test_expect_and_grad_matches_oracle(nk):
+    L = 4
+    g = nk.graph.Square(L)
+    hi = nk.hilbert.Spin(0.5, N=16, total_sz=0)
+    H = nk.operator.Heisenberg(hi, g)
+    vs = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=g, n_chains=64),
+                        nk.models.RBM(alpha=2), n_samples=2048, seed=2, precision="fp64")
+    st, grad = vs.expect_and_grad(H)
+    s = vs.samples.reshape(-1, 16).cpu().numpy()
+    p = oracle_params(vs.flat_parameters, 16, vs.M)
+    e = orbm.local_energies(p, s, oracle_heisenberg(g).get_conn_padded)
+    ref_stats = ost.statistics(e.reshape(64, -1))
+    np.testing.assert_allclose(st.as_array(), ref_stats.as_array(), rtol=1e-10, equal_nan=True)
+    _, ref_grad = orbm.forces_and_grad(p, s, e)
+    got = vs.model.flatten(grad).cpu().numpy()
+    np.testing.assert_allclose(got, ref_grad, rtol=1e-9, atol=1e-11 * np.abs(ref_grad).max())
+    F_stats, F = vs.expect_and_forces(H)
+    np.testing.assert_array_equal(2 * vs.model.flatten(F).cpu().numpy(), got)
+
+
+def test_gradient_matches_full_sum(nk):
+    """Monte Carlo gradient within 5 sigma-ish of the exact gradient (N=10)."""
+    N = 10
+    g = nk.graph.Chain(N)
+    hi = nk.hilbert.Spin(0.5, N)
+    H = nk.operator.Ising(hi, g, h=0.9)
+    model = nk.models.RBM(alpha=1, kernel_init_std=0.2, hidden_bias_init_std=0.2,
+                          visible_bias_init_std=0.2)
+    vs = nk.vqs.MCState(nk.sampler.MetropolisLocal(hi, n_chains=512), model, n_samples=512 * 256,
+                        n_discard_per_chain=64, seed=3, precision="fp64")
+    st, grad = vs.expect_and_grad(H)
+    p = oracle_params(vs.flat_parameters, N, vs.M)
+    E, G = oex.full_sum_energy_and_grad(
+        p, lambda s: oop.ising_get_conn_padded(s, np.array(g.edges()), 0.9, 1.0), N)
+    assert abs(st.mean - E) < 5 * st.error_of_mean + 1e-3
+    got = vs.model.flatten(grad).cpu().numpy()
+    assert np.linalg.norm(got - G) < 0.05 * np.linalg.norm(G) + 5e-3
+
+
+@pytest.mark.slow
+def test_tfim_chain16_vmc_sr_converges(nk):
+    """Configuration of the 1D TFIM benchmark: N=16, J=1, h=1, RBM alpha=1 FP64,
+    MetropolisLocal 16 chains, 1008 samples, 32 discarded sweeps, SR
+    diag_shift=0.01, sgd lr=0.01.  After 300 steps the energy is within 1% of
+    the exact ground state (NetKet's RBM reaches the same band)."""
+    N = 16
+    g = nk.graph.Chain(N)
+    hi = nk.hilbert.Spin(0.5, N)
+    H = nk.operator.Ising(hi, g, h=1.0, J=1.0)
+    E0 = oex.lanczos_ed(lambda s: oop.ising_get_conn_padded(s, np.array(g.edges()), 1.0, 1.0), N)[0]
+    assert abs(E0 - oex.tfim_ground_energy(N, 1.0, 1.0)) < 1e-8
+    vs = nk.vqs.MCState(nk.sampler.MetropolisLocal(hi, n_chains=16), nk.models.RBM(alpha=1),
+                        n_samples=1008, n_discard_per_chain=32, seed=0, precision="fp64")
+    drv = nk.driver.VMC(H, nk.optimizer.Sgd(0.01), variational_state=vs,
+                        preconditioner=nk.optimizer.SR(diag_shift=0.01))
+    log = drv.run(300)[0]
+    tail = np.array([d["Mean"] for d in log["Energy"]["value"][-50:]])
+    assert abs(tail.mean() - E0) / abs(E0) < 1e-2
+    # the state's own estimate with more samples
+    st = vs.expect(H)
+    assert abs(st.mean - E0) / abs(E0) < 1e-2
+
+
+def test_vmc_sr_minsr_step_mixed_matches_fp64(nk):
+    """One minSR step of a 6x6 J1-J2 model: the mixed path (FP32 kernels, FP64-
+    refined solve) agrees with the FP64 path on the same samples."""
+    L = 6
+    g = nk.graph.Square(L, max_neighbor_order=2)
+    hi = nk.hilbert.Spin(0.5, N=L * L, total_sz=0)
+    H = nk.operator.Heisenberg(hi, g, J=[1.0, 0.5])
+    out = {}
+    for prec in ("fp64", "mixed"):
+        vs = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=g, n_chains=256),
+                            nk.models.RBM(alpha=2), n_samples=1024, seed=1, precision=prec)
+        if prec == "mixed":
+            vs._samples = out["fp64"][2]
+        drv = nk.driver.VMC_SR(H, nk.optimizer.Sgd(0.01), diag_shift=1e-4, variational_state=vs,
+                               use_ntk=True)
+        if prec == "mixed":
+            c = vs._forward_cache(H)
+        stats, dp = drv.compute_loss_and_update() if prec == "fp64" else (None, None)
+        if prec == "mixed":
+            from netket_gb300.ngd import minsr_update
+            dp, info = minsr_update(c["t"], c["x"], vs.N, vs.M, c["e"], c["stats_dev"][0:1], 1e-4,
+                                    solve="refined", refine_iters=8)
+            stats = nk.stats.Stats.from_array(c["stats_dev"].cpu().numpy())
+        out[prec] = (stats, dp, vs.samples.clone())
+    e64, e32 = out["fp64"][0].mean, out["mixed"][0].mean
+    assert abs(e64 - e32) / abs(e64) < 1e-5
+    d64, d32 = out["fp64"][1].cpu().numpy(), out["mixed"][1].cpu().numpy()
+    assert np.linalg.norm(d64 - d32) / np.linalg.norm(d64) < 5e-2

@@ -1,0 +1,135 @@
+"""CPU tests of the product's host side: lattice edges, operator packing, the
+C-ABI library (loads and exports every declared symbol), and loud failure
+without a GPU.  No kernel is launched here."""
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import hilbert as oh
+from oracle import operator as oop
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    from netket_gb300 import build
+    return build.build()
+
+
+def test_philox_known_answers():
+    """Random123 known-answer vectors for Philox4x32-10."""
+    from philox_ref import philox4x32_10
+    assert philox4x32_10((0, 0, 0, 0), (0, 0)) == (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)
+    F = 0xFFFFFFFF
+    assert philox4x32_10((F, F, F, F), (F, F)) == (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)
+    assert philox4x32_10((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344),
+                         (0xA4093822, 0x299F31D0)) == (0xD16CFE09, 0x94FDCCEB, 0x5001E420,
+                                                       0x24126EA1)
+
+
+@pytest.mark.parametrize("name", ["chain16", "chain5", "chain8_obc", "chain14_nnn", "square4",
+                                  "square6_nnn", "square10_nnn", "square16", "cube3"])
+def test_product_lattice_edges_match_reference(golden, name):
+    from netket_gb300 import graph
+    g = golden("edges")
+    meta = g[name + "__meta"]
+    L = graph.Lattice(list(meta[:-2]), bool(meta[-2]), int(meta[-1]))
+    np.testing.assert_array_equal(np.array(L.edges(return_color=True)).reshape(-1, 3), g[name])
+
+
+def test_graph_distances_and_bipartite():
+    from netket_gb300 import graph
+    g = graph.Chain(6)
+    d = g.distances()
+    assert d[0, 3] == 3 and d[0, 5] == 1
+    assert g.is_bipartite() and not graph.Chain(5).is_bipartite()
+    assert not graph.Square(4, max_neighbor_order=2).is_bipartite()
+
+
+LOCALOP_CASES = ["heis_chain16", "heis_square4", "heis_square4_nosign", "j1j2_square6",
+                 "j1j2_chain14", "j1j2_square10", "ising_local_chain5"]
+
+
+@pytest.mark.parametrize("name", LOCALOP_CASES)
+def test_product_packing_matches_reference(golden, name):
+    """The device tables reproduce the reference packer's max_conn_size and the
+    oracle's term order / connections (checked on the host copy of the tables)."""
+    from netket_gb300 import hilbert, operator
+    gl = golden("localop")
+    N = int(gl[name + "__N"])
+    ops, aon = [], []
+    for a, m, s in zip(gl[name + "__aon"], gl[name + "__ops"], gl[name + "__sizes"]):
+        d = 2**int(s)
+        ops.append(m[:d, :d])
+        aon.append([int(v) for v in a[:s]])
+    op = operator.LocalOperator(hilbert.Spin(0.5, N), ops, aon)
+    assert op.max_conn_size == int(gl[name + "__max_conn_jax"])
+    ref = oop.LocalOperator(N, ops, aon)
+    tb = op._pack()
+    # emulate the device enumeration on the host tables for a few samples
+    x = oh.local_indices_to_states(gl[name + "__x_ids"])[:5]
+    rxp, rm = ref.get_conn_padded(x)
+    for b in range(len(x)):
+        cand = []
+        rows = []
+        for t in range(tb["T"]):
+            sz = tb["acting_size"][t]
+            r = 0
+            for q in range(sz):
+                r = (r << 1) | int(x[b, tb["acting_on"][t, q]] < 0)
+            rows.append(r)
+        if tb["nonzero_diag"]:
+            tot, t = 0.0, 0
+            for ge in tb["group_end"]:
+                gs = 0.0
+                while t < ge:
+                    gs += tb["diag"][t, rows[t]]
+                    t += 1
+                tot += gs
+            d = 0.0 + tot
+            if abs(d) > 1e-10:
+                cand.append(d)
+        for t in range(tb["T"]):
+            for c in range(tb["n_conns"][t, rows[t]]):
+                cand.append(tb["mels"][t, rows[t], c])
+        K = tb["K"]
+        got = np.zeros(K)
+        got[:len(cand)] = cand
+        np.testing.assert_array_equal(got, rm[b])
+
+
+def test_header_symbols_exported(built_lib):
+    """Every entry point declared in include/vmck.h is exported by libvmck.so and
+    has a ctypes signature."""
+    import ctypes
+    from netket_gb300 import _native
+    hdr = open(os.path.join(ROOT, "include", "vmck.h")).read()
+    declared = set(re.findall(r"\b(vmck_[a-z0-9_]+)\s*\(", hdr))
+    lib = ctypes.CDLL(built_lib)
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared == set(_native.declared_symbols())
+    L = _native.lib()
+    assert L.vmck_abi_version() == 1
+    assert L.vmck_error_string(1) == b"invalid argument"
+
+
+def test_argument_errors_are_reported(built_lib):
+    """Host-side argument checks return an error code without touching a GPU."""
+    from netket_gb300 import _native
+    L = _native.lib()
+    rc = L.vmck_get_conn_ising(None, None, 4, 8, None, 0, 1.0, 1.0, 0, None, None, None)
+    assert rc == 1 and b"argument" in L.vmck_last_error()
+    assert L.vmck_stats_workspace_size(16, 63) == 3 * 16 + 16 * (63 // 1)
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU behaviour")
+def test_fails_loudly_without_gpu(built_lib):
+    import netket_gb300 as nk
+    hi = nk.hilbert.Spin(0.5, N=4)
+    with pytest.raises(nk._native.VmckError):
+        hi.random_state(0, 3)
