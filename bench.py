@@ -1,0 +1,360 @@
+"""Benchmark: VMC steps/s of the 10x10 J1-J2 Heisenberg minSR step on one GB300.
+
+Workload (the configuration the metric is quoted on): 10x10 periodic square
+lattice, J1 = 1, J2 = 0.5, total Sz = 0; RBM alpha = 4 (M = 400, P = 40,500);
+MetropolisExchange on the 400 nearest and next-nearest bonds, 4096 chains,
+16,384 samples per step (4 per chain), 5 discarded sweeps per chain; minSR with
+T = O_L O_L^T + 1e-4 I (16,384 x 16,384) solved in FP64; SGD lr 0.01.
+Synthetic: random RBM initialisation (Normal(0, 0.01)), no dataset.
+
+A step = one VMC_SR step (sample, local energies, statistics, T, solve,
+parameter update), through ``netket_gb300.driver.VMC_SR.advance``.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference algorithm on the host cores (the
+numpy FP64 restatement in ``oracle/``; NetKet's own JAX path cannot be
+installed here) on a bounded sample of the same workload and scales it to the
+full step phase by phase.  Under torchrun every rank runs an independent
+replica (the path has no cross-GPU exchange on a single-GPU machine); rank 0
+prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics as pystats
+import subprocess
+import sys
+import time
+
+NPROC = os.cpu_count() or 1
+for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(var, str(NPROC))
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {
+    "workload": "j1j2_10x10_minsr",
+    "lattice": "10x10 periodic square, J1=1, J2=0.5, total_sz=0, sign_rule=[True, False]",
+    "model": "RBM alpha=4 (M=400, P=40500)",
+    "sampler": "MetropolisExchange nn+nnn bonds (400 clusters)",
+    "n_chains": 4096, "n_samples": 16384, "n_discard_per_chain": 5,
+    "solver": "minSR, T 16384x16384, diag_shift=1e-4", "lr": 0.01,
+}
+METRIC = "VMC steps/s"
+
+
+def build_problem(nk, precision, seed=0, n_chains=4096, n_samples=16384):
+    g = nk.graph.Square(10, max_neighbor_order=2)
+    hi = nk.hilbert.Spin(0.5, N=100, total_sz=0)
+    # Marshall's sign rule on the bipartite J1 bonds (a positive RBM cannot carry
+    # the J1 sign structure; with NetKet's default [False, False] the FP64 and
+    # the mixed runs both diverge after ~15 steps)
+    H = nk.operator.Heisenberg(hi, g, J=[1.0, 0.5], sign_rule=[True, False])
+    sampler = nk.sampler.MetropolisExchange(hi, graph=g, d_max=1, n_chains=n_chains)
+    vs = nk.vqs.MCState(sampler, nk.models.RBM(alpha=4), n_samples=n_samples,
+                        n_discard_per_chain=5, seed=seed, precision=precision)
+    drv = nk.driver.VMC_SR(H, nk.optimizer.Sgd(0.01), diag_shift=1e-4, variational_state=vs,
+                           use_ntk=True)
+    return H, vs, drv
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"vmck_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        try:
+            for line in open(self.path):
+                f = [v.strip() for v in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1].split()[0]))
+                    mx = float(f[2].split()[0])
+                except ValueError:
+                    continue
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                         "sw_power_cap"]
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        except OSError:
+            pass
+        return {"sm_mhz": pystats.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_ours(args):
+    import torch
+    import netket_gb300 as nk
+    from netket_gb300 import _native
+    from netket_gb300.driver import PhaseTimer
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    H, vs, drv = build_problem(nk, args.precision, seed=rank)
+    drv.advance(args.warmup)
+    barrier()
+    L = _native.lib()
+    launches0 = L.vmck_launch_count()
+    drv.phase_timer = PhaseTimer()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        start.record()
+        for _ in range(args.steps):
+            st = drv.advance(1)
+        stop.record()
+        barrier()
+    launches = L.vmck_launch_count() - launches0
+    phases = drv.phase_timer.summary()
+    drv.phase_timer = None
+    ms = start.elapsed_time(stop) / args.steps
+    t_tot = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t_tot, op=dist.ReduceOp.MAX)
+    ms_max = float(t_tot.item())
+    value = world * 1000.0 / ms_max
+    energy = st.mean / 100
+
+    # ---------------- end to end through the public API, host buffers
+    P = vs.n_parameters
+    h_params = torch.empty(P, dtype=torch.float64).pin_memory()
+    h_params.copy_(vs.flat_parameters.cpu())
+    h_out = torch.empty(P + 5, dtype=torch.float64).pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        vs.flat_parameters.copy_(h_params, non_blocking=True)
+        vs.params_changed()
+        st = drv.advance(1)
+        h_out[:P].copy_(vs.flat_parameters, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        h_out[P:] = torch.tensor([st.mean, st.error_of_mean, st.variance, st.tau_corr, st.R_hat])
+        h_params.copy_(h_out[:P])
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    t_e2e = torch.tensor([e2e_ms], device="cuda")
+    if dist:
+        dist.all_reduce(t_e2e, op=dist.ReduceOp.MAX)
+    e2e_value = world * 1000.0 / float(t_e2e.item())
+
+    # ---------------- the plain FP32 GPU path (reference algorithm on the GPU)
+    plain = None
+    if args.plain_steps > 0:
+        _, vs32, drv32 = build_problem(nk, "fp32", seed=rank)
+        vs32.local_estimator = "dense"
+        drv32.gram = "dense"
+        drv32.solve = "cholesky"
+        drv32.advance(2)
+        barrier()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record()
+        for _ in range(args.plain_steps):
+            st32 = drv32.advance(1)
+        p1.record()
+        barrier()
+        pms = p0.elapsed_time(p1) / args.plain_steps
+        plain = {"path": "fp32 dense: get_conn + logpsi on every row, materialised Jacobian, "
+                         "cuBLAS SSYRK T, cuSOLVER SPOTRF",
+                 "ms_per_step": round(pms, 3), "steps_per_s": round(1000.0 / pms, 4),
+                 "speedup_of_value": round(pms / ms_max, 3)}
+        del vs32, drv32
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return None
+    gram_ms = phases.get("gram")
+    n = 16384
+    flops = float(n) * (n + 1) * 400  # lower triangle of t t^T (n x n x M), 2 flop per FMA
+    roof = None
+    if gram_ms:
+        peaks = load_peaks()
+        achieved = flops / (gram_ms * 1e-3) / 1e12
+        roof = {"kernel": "structured Gram T = O_L O_L^T (vmck_rbm_gram)", "bound": "tensor",
+                "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": round(achieved / peaks["bf16_tflops"], 5), "traffic": args.gram_traffic,
+                "peak_source": peaks["source"], "algorithmic_flops_per_launch": flops,
+                "launch_ms": round(gram_ms, 4)}
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = run_cpu_baseline(n_samples=args.cpu_samples)
+    line = {
+        "metric": METRIC, "value": round(value, 5), "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else args.precision, "data": "synthetic",
+        "config": dict(WORKLOAD, precision=args.precision, parallelism=f"replicas{world}",
+                       l2="per-step working set > L2: T64 2.1 GB + T32 1.1 GB"),
+        "samples_per_s": round(value * 16384, 1),
+        "energy_per_site": round(energy, 8),
+        "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+        "plain_fp32": plain,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_value, 5), "unit": "steps/s",
+                "h2d_bytes_per_step": P * 8, "d2h_bytes_per_step": P * 8 + 6 * 8},
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": round(launches / args.steps, 2),
+        "clocks": clk.summary(),
+    }
+    if dist:
+        dist.destroy_process_group()
+    return line
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "source": "fallback"}
+
+
+def run_cpu_baseline(n_samples=512, repeats=1):
+    """The reference algorithm (numpy FP64, all host threads) on a bounded
+    sample: n_samples samples from n_samples/4 chains (chain length 4, 5
+    discarded sweeps) of the same 10x10 J1-J2 / alpha=4 problem; each phase is
+    scaled to 16,384 samples by its complexity (sampling, local energies,
+    Jacobian and update ~ n; T ~ n^2; Cholesky ~ n^3)."""
+    import numpy as np
+    from oracle import graph as og, hilbert as oh, operator as oop, rbm as orbm, vmc_step
+
+    g = og.Square(10, max_neighbor_order=2)
+    op = oop.heisenberg(100, g, [1.0, 0.5], sign_rule=[True, False])
+    tables = vmc_step.two_site_tables(op)
+    clusters = np.array(g.edges(), dtype=np.int64)
+    clusters = np.sort(clusters, axis=1)
+    order = np.lexsort((clusters[:, 1], clusters[:, 0]))
+    clusters = clusters[order]
+    import scipy.linalg as sla
+    rng = np.random.default_rng(0)
+    params = orbm.init_params(rng, 100, 4, 0.01)
+    B = max(1, n_samples // 4)
+    x = oh.random_state(rng, B, 100, 0)
+    best = None
+    t_start = time.perf_counter()
+    for _ in range(repeats):
+        params, x, st, t = vmc_step.timed_step(params, x, rng, clusters, tables, 5, 4, 1e-4, 0.01)
+        # the Cholesky of a few-hundred matrix is overhead-bound: time it at n_c
+        n_c = 3072
+        A = rng.normal(size=(n_c, 256))
+        A = A @ A.T / 256 + 1e-4 * np.eye(n_c)
+        b = rng.normal(size=n_c)
+        c0 = time.perf_counter()
+        cf = sla.cho_factor(A, lower=False, overwrite_a=True, check_finite=False)
+        sla.cho_solve(cf, b, check_finite=False)
+        t["solve"] = (time.perf_counter() - c0) * (B * 4 / n_c) ** 3
+        tot = sum(t[k] * (16384 / (B * 4)) ** vmc_step.PHASE_SCALING[k] for k in t)
+        if best is None or tot < best[0]:
+            best = (tot, t)
+    wall = time.perf_counter() - t_start
+    full_s, phases = best
+    return {"value": round(1.0 / full_s, 6), "unit": "steps/s", "cores": NPROC, "kind": "port",
+            "sample": (f"{B * 4} samples ({B} chains x 4, 5 discarded sweeps) of the same "
+                       f"workload (Cholesky timed at n=3072), numpy FP64 reference algorithm, "
+                       f"each phase scaled to 16384 samples by its complexity; "
+                       f"measured {wall:.1f} s"),
+            "phase_s_at_sample": {k: round(v, 4) for k, v in phases.items()},
+            "full_step_s": round(full_s, 3)}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return None
+    vals = []
+    for _ in range(args.warmup):
+        run_cpu_baseline(n_samples=args.cpu_samples)
+    for _ in range(args.steps):
+        vals.append(run_cpu_baseline(n_samples=args.cpu_samples))
+    v = pystats.median([c["value"] for c in vals])
+    c = vals[-1]
+    return {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / v, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": dict(WORKLOAD, precision="fp64",
+                                            parallelism="host cores"),
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": NPROC, "kind": "port",
+                         "sample": c["sample"]},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "NetKet's JAX CPU path cannot be installed here (no jax/flax/optax/numba); "
+                "the numpy FP64 restatement of the same algorithm is timed instead",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
+    ap.add_argument("--plain-steps", type=int, default=4)
+    ap.add_argument("--cpu-samples", type=int, default=512)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gram-traffic", type=float, default=None)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

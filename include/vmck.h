@@ -50,6 +50,9 @@ int vmck_abi_version(void);
 const char *vmck_error_string(int code);
 /* Last CUDA / library error text recorded by this thread (host string). */
 const char *vmck_last_error(void);
+/* Number of kernels this library has launched in this process (diagnostic;
+ * cuBLAS / cuSOLVER launches are not included). */
+int64_t vmck_launch_count(void);
 
 /* Library context: owns cuBLAS / cuSOLVER handles and the solver workspace.
  * Replaces the XLA-managed handles behind jax.scipy.linalg.cho_factor
@@ -216,11 +219,15 @@ int vmck_gram_dense(vmck_ctx *ctx, vmck_stream s, int32_t dtype, const void *O_L
 int vmck_cholesky_solve(vmck_ctx *ctx, vmck_stream s, int32_t dtype, const void *A,
                         const void *b, void *x, int64_t n, int32_t *status);
 /* FP32 Cholesky factor of A32 (lower triangle, overwritten) refined against the
- * FP64 matrix A64 (lower triangle) until ||b - A64 x|| <= tol ||b|| (FP64). */
+ * FP64 matrix A64 (lower triangle): max_iter correction solves, each from the
+ * FP64 residual b - A64 x; the final relative residual goes to residual_out
+ * (device, nullable) and VMCK_DEV_NO_CONVERGE is raised if it exceeds tol.
+ * fp32_emulation != 0 factorises with FP32-accurate BF16x9 tensor-core
+ * emulation (cuSOLVER CUSOLVER_FP32_EMULATED_BF16X9_MATH). */
 int vmck_cholesky_solve_refined(vmck_ctx *ctx, vmck_stream s, const double *A64,
                                 float *A32, const double *b, double *x, int64_t n,
-                                int32_t max_iter, double tol, int32_t *status,
-                                double *residual_out);
+                                int32_t max_iter, double tol, int32_t fp32_emulation,
+                                int32_t *status, double *residual_out);
 /* pinv_smooth (solvers.py:33-139) via a symmetric eigendecomposition (FP64). */
 int vmck_pinv_smooth_solve(vmck_ctx *ctx, vmck_stream s, const double *A,
                            const double *b, double *x, int64_t n, double rtol,

@@ -38,6 +38,7 @@ _SIGNATURES = {
     "vmck_abi_version": ([], c_i32),
     "vmck_error_string": ([c_i32], ctypes.c_char_p),
     "vmck_last_error": ([], ctypes.c_char_p),
+    "vmck_launch_count": ([], c_i64),
     "vmck_ctx_create": ([ctypes.POINTER(c_vp)], c_i32),
     "vmck_ctx_destroy": ([c_vp], c_i32),
     "vmck_random_states": ([c_vp, c_vp, c_i64, c_i32, c_i32, c_u64, c_u64], c_i32),
@@ -66,7 +67,7 @@ _SIGNATURES = {
     "vmck_gram_dense": ([c_vp, c_vp, c_i32, c_vp, c_i64, c_i64, c_i32, c_dbl, c_vp], c_i32),
     "vmck_cholesky_solve": ([c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp], c_i32),
     "vmck_cholesky_solve_refined": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i32, c_dbl,
-                                     c_vp, c_vp], c_i32),
+                                     c_i32, c_vp, c_vp], c_i32),
     "vmck_pinv_smooth_solve": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_dbl, c_dbl], c_i32),
     "vmck_center_scale": ([c_vp, c_vp, c_vp, c_i64, c_dbl, c_vp], c_i32),
     "vmck_center_update": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_dbl, c_vp], c_i32),

@@ -1,4 +1,5 @@
 // ABI version, status strings and the per-thread last-error text.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 
@@ -15,7 +16,13 @@ void set_last_error(const char *fmt, ...) {
   va_end(ap);
 }
 
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 }  // namespace vmck
+
+extern "C" int64_t vmck_launch_count(void) { return vmck::g_launches.load(); }
 
 extern "C" int vmck_abi_version(void) { return VMCK_ABI_VERSION; }
 

@@ -13,7 +13,12 @@ namespace vmck {
 // ----------------------------------------------------------------- host status
 void set_last_error(const char *fmt, ...);
 
+void count_launch();
+
+// Every kernel launch of the library is followed by check_launch, which also
+// counts it (vmck_launch_count).
 inline int check_launch(const char *what) {
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_last_error("%s: %s", what, cudaGetErrorString(e));

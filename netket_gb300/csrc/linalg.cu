@@ -177,6 +177,86 @@ __global__ void sgd_kernel(double *p, const double *u, int64_t P, double lr, flo
   if (p32) p32[i] = (float)v;
 }
 
+// ------------------------------------------------------------ symmetric residual
+// r = b - A x for a symmetric A stored as its lower triangle (row-major), each
+// stored element read exactly once.  Tile (I, J), I >= J, of 64 x 64 adds
+// A_IJ x_J to the rows of block I (slot J) and A_IJ^T x_I to the rows of block J
+// (slot I); on a diagonal tile both go to slot I.  Every (slot, row) of
+// ws[n_tiles][n] is written exactly once; the second kernel sums the slots in
+// a fixed order.  HBM-bound: n(n+1)/2 * 8 bytes per call.
+constexpr int SY_T = 64;
+
+__device__ inline void sy_tri_tile(int64_t bid, int64_t &I, int64_t &J) {
+  int64_t i = (int64_t)((sqrt(8.0 * (double)bid + 1.0) - 1.0) * 0.5);
+  while (i * (i + 1) / 2 > bid) --i;
+  while ((i + 1) * (i + 2) / 2 <= bid) ++i;
+  I = i;
+  J = bid - i * (i + 1) / 2;
+}
+
+__global__ void __launch_bounds__(256) symv_lower_partial_kernel(const double *__restrict__ A,
+                                                                 int64_t n,
+                                                                 const double *__restrict__ x,
+                                                                 double *__restrict__ ws) {
+  __shared__ double xr[SY_T], xc[SY_T];
+  __shared__ double rowpart[2][SY_T];
+  __shared__ double colpart[4][SY_T];
+  int64_t I, J;
+  sy_tri_tile(blockIdx.x, I, J);
+  const int tid = threadIdx.x, c = tid & 63, g = tid >> 6, half = (tid >> 5) & 1;
+  const int lane = tid & 31;
+  const int64_t r0 = I * SY_T, c0 = J * SY_T;
+  if (tid < SY_T) xc[tid] = (c0 + tid < n) ? x[c0 + tid] : 0.0;
+  else if (tid < 2 * SY_T) xr[tid - SY_T] = (r0 + tid - SY_T < n) ? x[r0 + tid - SY_T] : 0.0;
+  __syncthreads();
+  const bool diag = (I == J);
+  const bool cok = (c0 + c) < n;
+  double colacc = 0.0;
+#pragma unroll 4
+  for (int k = 0; k < 16; ++k) {
+    const int r = g + 4 * k;
+    const bool rok = (r0 + r) < n;
+    double a = 0.0;
+    if (rok && cok && (!diag || r >= c)) a = A[(r0 + r) * n + c0 + c];
+    double v = a * xc[c];
+    v = warp_sum(v);
+    if (lane == 0) rowpart[half][r] = v;
+    if (!diag || r > c) colacc += a * xr[r];
+  }
+  colpart[g][c] = colacc;
+  __syncthreads();
+  if (tid < SY_T) {
+    const int r = tid;
+    const double rs = rowpart[0][r] + rowpart[1][r];
+    const double cs = colpart[0][r] + colpart[1][r] + colpart[2][r] + colpart[3][r];
+    if (diag) {
+      if (r0 + r < n) ws[I * n + r0 + r] = rs + cs;
+    } else {
+      if (r0 + r < n) ws[J * n + r0 + r] = rs;
+      if (c0 + r < n) ws[I * n + c0 + r] = cs;
+    }
+  }
+}
+
+__global__ void symv_residual_reduce_kernel(const double *__restrict__ ws, int64_t n, int nt,
+                                            const double *__restrict__ b, double *__restrict__ r) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int k = 0; k < nt; ++k) s += ws[k * n + i];
+  r[i] = b[i] - s;
+}
+
+static int symv_residual(cudaStream_t st, const double *A, int64_t n, const double *x,
+                         const double *b, double *r, double *ws) {
+  const int64_t nt = (n + SY_T - 1) / SY_T;
+  symv_lower_partial_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, st>>>(A, n, x, ws);
+  int rc = check_launch("symv partial");
+  if (rc) return rc;
+  symv_residual_reduce_kernel<<<ceil_div(n, 256), 256, 0, st>>>(ws, n, (int)nt, b, r);
+  return check_launch("symv reduce");
+}
+
 static int num_sms() {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
@@ -253,39 +333,55 @@ extern "C" int vmck_cholesky_solve(vmck_ctx *c, vmck_stream s, int32_t dtype, co
 
 extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const double *A64,
                                            float *A32, const double *b, double *x, int64_t n,
-                                           int32_t max_iter, double tol, int32_t *status,
-                                           double *residual_out) {
+                                           int32_t max_iter, double tol, int32_t fp32_emulation,
+                                           int32_t *status, double *residual_out) {
   VMCK_REQUIRE(c && A64 && A32 && b && x && n > 0 && max_iter >= 1, "refined solve arguments");
   cudaStream_t st = as_stream(s);
   int rc = bind(c, st);
   if (rc) return rc;
+  VMCK_SOLVER(cusolverDnSetMathMode(c->solver, fp32_emulation ? CUSOLVER_FP32_EMULATED_BF16X9_MATH
+                                                              : CUSOLVER_DEFAULT_MATH));
+  if (fp32_emulation)
+    VMCK_SOLVER(cusolverDnSetEmulationStrategy(c->solver, CUDA_EMULATION_STRATEGY_EAGER));
   size_t dsize = 0, hsize = 0;
   VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
                                           CUDA_R_32F, A32, n, CUDA_R_32F, &dsize, &hsize));
   if ((rc = grow(&c->dwork, &c->dwork_bytes, dsize + 256, st))) return rc;
   if ((rc = grow_host(c, hsize))) return rc;
-  // aux: r (n double), r32 (n float), two norms
-  const size_t need = (size_t)n * 8 + (size_t)n * 4 + 64;
+  // aux: r (n double), r32 (n float), two norms, symv slots (n_tiles x n double)
+  const int64_t nt = (n + SY_T - 1) / SY_T;
+  const size_t ws_off = (((size_t)n * 12 + 64) + 255) & ~size_t(255);
+  const size_t need = ws_off + (size_t)nt * n * 8;
   if ((rc = grow(&c->aux, &c->aux_bytes, need, st))) return rc;
   double *r = static_cast<double *>(c->aux);
   float *r32 = reinterpret_cast<float *>(r + n);
   double *norms = reinterpret_cast<double *>(
       (reinterpret_cast<uintptr_t>(r32 + n) + 15) & ~uintptr_t(15));
-  VMCK_SOLVER(cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, CUDA_R_32F, A32, n,
-                               CUDA_R_32F, c->dwork, dsize, c->hwork, hsize, c->d_info));
+  double *sws = reinterpret_cast<double *>(static_cast<char *>(c->aux) + ws_off);
+  cusolverStatus_t fs = cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
+                                         CUDA_R_32F, A32, n, CUDA_R_32F, c->dwork, dsize,
+                                         c->hwork, hsize, c->d_info);
+  cusolverDnSetMathMode(c->solver, CUSOLVER_DEFAULT_MATH);
+  if (fs != CUSOLVER_STATUS_SUCCESS) {
+    set_last_error("refined solve: cusolverDnXpotrf status %d", (int)fs);
+    return VMCK_ERR_LIBRARY;
+  }
   VMCK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
   const int blocks = ceil_div(n, 256);
-  const double one = 1.0, mone = -1.0;
   for (int it = 0; it < max_iter; ++it) {
-    VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-    if (it > 0) VMCK_BLAS(cublasDsymv(c->blas, CUBLAS_FILL_MODE_UPPER, (int)n, &mone, A64, (int)n, x, 1, &one, r, 1));
+    if (it == 0) {
+      VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    } else if ((rc = symv_residual(st, A64, n, x, b, r, sws))) {
+      return rc;
+    }
     d2f_kernel<<<blocks, 256, 0, st>>>(r, r32, n);
+    if ((rc = check_launch("refined solve cast"))) return rc;
     VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, CUDA_R_32F,
                                  A32, n, CUDA_R_32F, r32, n, c->d_info));
     axpy_f2d_kernel<<<blocks, 256, 0, st>>>(x, r32, n);
+    if ((rc = check_launch("refined solve update"))) return rc;
   }
-  VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-  VMCK_BLAS(cublasDsymv(c->blas, CUBLAS_FILL_MODE_UPPER, (int)n, &mone, A64, (int)n, x, 1, &one, r, 1));
+  if ((rc = symv_residual(st, A64, n, x, b, r, sws))) return rc;
   VMCK_BLAS(cublasSetPointerMode(c->blas, CUBLAS_POINTER_MODE_DEVICE));
   cublasStatus_t s1 = cublasDnrm2(c->blas, (int)n, r, 1, norms);
   cublasStatus_t s2 = cublasDnrm2(c->blas, (int)n, b, 1, norms + 1);
@@ -325,8 +421,9 @@ extern "C" int vmck_pinv_smooth_solve(vmck_ctx *c, vmck_stream s, const double *
   const double one = 1.0, zero = 0.0;
   VMCK_BLAS(cublasDgemv(c->blas, CUBLAS_OP_T, (int)n, (int)n, &one, U, (int)n, b, 1, &zero, y, 1));
   pinv_filter_kernel<<<ceil_div(n, 256), 256, 0, st>>>(w, y, n, rtol, rtol_smooth);
+  if ((rc = check_launch("pinv_smooth filter"))) return rc;
   VMCK_BLAS(cublasDgemv(c->blas, CUBLAS_OP_N, (int)n, (int)n, &one, U, (int)n, y, 1, &zero, x, 1));
-  return check_launch("pinv_smooth");
+  return VMCK_OK;
 }
 
 extern "C" int vmck_gram_dense(vmck_ctx *c, vmck_stream s, int32_t dtype, const void *O_L,
@@ -355,7 +452,8 @@ extern "C" int vmck_gram_dense(vmck_ctx *c, vmck_stream s, int32_t dtype, const 
     set_last_error("gram_dense dtype");
     return VMCK_ERR_UNSUPPORTED;
   }
-  if (diag_shift != 0.0) add_diag_kernel<<<ceil_div(m, 256), 256, 0, st>>>(out, dtype, m, diag_shift);
+  if (diag_shift == 0.0) return VMCK_OK;
+  add_diag_kernel<<<ceil_div(m, 256), 256, 0, st>>>(out, dtype, m, diag_shift);
   return check_launch("gram_dense");
 }
 

@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(EL_THREADS) eloc_ising_kernel(
         int site = k;
         T d = (T)(-2 * xs[k]);
         T lr = warp_log_ratio(P, th, lc, &site, &d, 1);
-        if (lane == 0) acc += -h * (double)exp(lr);
+        if (lane == 0) acc += -h * exp((double)lr);
       }
     }
     if (threadIdx.x == 0) acc += J * (double)tot;
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(EL_THREADS) eloc_local_kernel(
         if (lane == 0) acc += mel;
       } else {
         T lr = warp_log_ratio(P, th, lc, site, d, ns);
-        if (lane == 0) acc += mel * (double)exp(lr);
+        if (lane == 0) acc += mel * exp((double)lr);
       }
     }
     double e = block_sum(acc, redd);

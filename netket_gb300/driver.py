@@ -11,7 +11,8 @@ import time
 
 import torch
 
-from .ngd import minsr_update, sr_update
+from ._native import DEV_NONFINITE, DEV_NOT_SPD
+from .ngd import minsr_fallback, minsr_update, sr_update
 from .optimizer import identity_preconditioner
 from .stats import Stats
 
@@ -32,6 +33,38 @@ class RuntimeLog:
         return self.data[k]
 
 
+class PhaseTimer:
+    """CUDA events recorded between the phases of a step on the current stream
+    (no host synchronisation); ``summary()`` syncs once and returns the mean
+    milliseconds per phase.  The GPU counterpart of NetKet's ``timeit``
+    (``netket/utils/timing.py``)."""
+
+    def __init__(self):
+        self.steps = []
+        self._cur = None
+
+    def mark(self, name):
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record()
+        if name == "start":
+            self._cur = [("start", ev)]
+            self.steps.append(self._cur)
+        elif self._cur is not None:
+            self._cur.append((name, ev))
+
+    def summary(self):
+        torch.cuda.synchronize()
+        acc = {}
+        for marks in self.steps:
+            for (_, a), (name, b) in zip(marks[:-1], marks[1:]):
+                acc.setdefault(name, []).append(a.elapsed_time(b))
+        return {k: sum(v) / len(v) for k, v in acc.items()}
+
+    def reset(self):
+        self.steps = []
+        self._cur = None
+
+
 class AbstractVariationalDriver:
     def __init__(self, variational_state, optimizer, minimized_quantity_name="Energy"):
         self.state = variational_state
@@ -41,6 +74,7 @@ class AbstractVariationalDriver:
         self._dp = None
         self.step_count = 0
         self.info = None
+        self.phase_timer = None
 
     def compute_loss_and_update(self):
         raise NotImplementedError
@@ -132,16 +166,32 @@ class VMC_SR(AbstractVariationalDriver):
 
     def compute_loss_and_update(self):
         st = self.state
+        ph = self.phase_timer
         st.reset()
+        if ph:
+            ph.mark("start")
+        st.sample()
+        if ph:
+            ph.mark("sample")
         c = st._forward_cache(self._ham)
+        if ph:
+            ph.mark("local_energy")
         shift = self.diag_shift(self.step_count) if callable(self.diag_shift) else self.diag_shift
         if self.use_ntk:
             dp, self.info = minsr_update(c["t"], c["x"], st.N, st.M, c["e"], c["stats_dev"][0:1],
                                          shift, gram=self.gram, gram_mode=self.gram_mode,
                                          solve=self.solve, refine_iters=self.refine_iters,
-                                         refine_tol=self.refine_tol, jac_dtype=self.jac_dtype)
+                                         refine_tol=self.refine_tol, jac_dtype=self.jac_dtype,
+                                         check=False, phase_timer=ph)
+            # one host read per step: energy statistics and solver status together
+            host = torch.cat([c["stats_dev"], self.info["status_dev"].to(torch.float64)]).cpu()
+            status = int(host[5].item())
+            self.info["status"] = status
+            if status & (DEV_NOT_SPD | DEV_NONFINITE):
+                dp = minsr_fallback(self.info)
+            stats = Stats.from_array(host[:5].numpy())
         else:
             dp, self.info = sr_update(c["t"], c["x"], st.N, st.M, c["e"], c["stats_dev"][0:1],
                                       shift, jac_dtype=self.jac_dtype)
-        stats = Stats.from_array(c["stats_dev"].cpu().numpy())
+            stats = Stats.from_array(c["stats_dev"].cpu().numpy())
         return stats, dp

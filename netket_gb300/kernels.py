@@ -148,13 +148,16 @@ def cholesky_solve(A, b, status):
     return x
 
 
-def cholesky_solve_refined(A64, A32, b, status, max_iter=4, tol=1e-10):
+def cholesky_solve_refined(A64, A32, b, status, max_iter=4, tol=1e-10, emulation=True):
+    """FP32 Cholesky (BF16x9 tensor-core emulation when ``emulation``) refined to
+    an FP64 residual; A32 is overwritten by its factor."""
     x = torch.empty_like(b)
     res = torch.empty(1, dtype=torch.float64, device=b.device)
     nat.check(nat.lib().vmck_cholesky_solve_refined(nat.ctx(), nat.stream(), nat.ptr(A64),
                                                     nat.ptr(A32), nat.ptr(b), nat.ptr(x),
                                                     A64.shape[0], int(max_iter), float(tol),
-                                                    nat.ptr(status), nat.ptr(res)))
+                                                    int(bool(emulation)), nat.ptr(status),
+                                                    nat.ptr(res)))
     return x, res
 
 

@@ -37,9 +37,14 @@ def _status():
 
 def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram_mode=None,
                  solve="cholesky", refine_iters=4, refine_tol=1e-10, rtol=1e-14,
-                 rtol_smooth=1e-14, jac_dtype=None, check=True):
+                 rtol_smooth=1e-14, jac_dtype=None, check=True, phase_timer=None):
     """Returns (delta (P,) FP64, info).  ``t`` = tanh(theta) (n, M) in the compute
-    dtype, ``e`` = local energies (n,) FP64, ``mean_dev`` = their mean (device)."""
+    dtype, ``e`` = local energies (n,) FP64, ``mean_dev`` = their mean (device).
+
+    With ``check=False`` the device status is not read here: ``info["status_dev"]``
+    holds it and ``minsr_fallback(info)`` recomputes delta with pinv_smooth if the
+    caller finds a failed factorisation (one host read per step)."""
+    ph = phase_timer
     n = x.shape[0]
     s = 1.0 / math.sqrt(n)
     obar = K.column_means(t, x, N, M)
@@ -50,6 +55,8 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
         mode = gram_mode if gram_mode is not None else (0 if t.dtype == torch.float64 else 1)
         T64, T32 = K.gram_structured(t, x, N, M, obar, diag_shift, mode,
                                      want_f32=(solve == "refined"))
+        if ph:
+            ph.mark("gram")
         if solve == "refined":
             aux, res = K.cholesky_solve_refined(T64, T32, dv, status, refine_iters, refine_tol)
             info["residual_dev"] = res
@@ -61,6 +68,8 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
         O_L = K.jacobian_dense(t, x, N, M, obar, s, jd)
         T = K.gram_dense(O_L, diag_shift)
         del O_L
+        if ph:
+            ph.mark("gram")
         if T.dtype == torch.float64:
             aux = K.cholesky_solve(T, dv, status)
         else:
@@ -69,17 +78,30 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     else:
         raise ValueError("gram must be 'structured' or 'dense'")
     info["status_dev"] = status
+    if ph:
+        ph.mark("solve")
+    info["_fallback_args"] = (t, x, N, M, obar, dv, Tfb, s, rtol, rtol_smooth)
     if check:
         st = int(status.item())
-        if st & (nat.DEV_NOT_SPD | nat.DEV_NONFINITE):
-            A = Tfb.to(torch.float64)
-            A = torch.tril(A) + torch.tril(A, -1).T
-            aux = K.pinv_smooth_solve(A.contiguous(), dv, rtol, rtol_smooth)
-            info["solver_fallback"] = True
         info["status"] = st
+        if st & (nat.DEV_NOT_SPD | nat.DEV_NONFINITE):
+            return minsr_fallback(info), info
     raw = K.ot_v(t, x, N, M, aux)
     delta = K.center_update(raw, obar, aux, s)
+    if ph:
+        ph.mark("update")
     return delta, info
+
+
+def minsr_fallback(info):
+    """delta from pinv_smooth on the same T (``cholesky_with_fallback``)."""
+    t, x, N, M, obar, dv, T, s, rtol, rtol_smooth = info["_fallback_args"]
+    A = T.to(torch.float64)
+    A = torch.tril(A) + torch.tril(A, -1).T
+    aux = K.pinv_smooth_solve(A.contiguous(), dv, rtol, rtol_smooth)
+    info["solver_fallback"] = True
+    raw = K.ot_v(t, x, N, M, aux)
+    return K.center_update(raw, obar, aux, s)
 
 
 def sr_update(t, x, N, M, e, mean_dev, diag_shift, *, jac_dtype=None, rtol=1e-14,

@@ -165,3 +165,16 @@ def test_minsr_equals_sr():
     a, _ = ongd.srt_update(O, e, 1e-3)
     b, _ = ongd.sr_update(O, e, 1e-3)
     np.testing.assert_allclose(a, b, atol=1e-10)
+
+
+@pytest.mark.parametrize("name", ["heis_square4", "j1j2_square6", "j1j2_square10"])
+def test_vectorised_conn_equals_loop_oracle(golden, name):
+    from oracle import vmc_step
+    gl = golden("localop")
+    N, op = _build_local(gl, name, golden)
+    rng = np.random.default_rng(5)
+    x = oh.local_indices_to_states(rng.integers(0, 2, size=(40, N)))
+    xp, m = vmc_step.conn_two_site(x, vmc_step.two_site_tables(op))
+    rxp, rm = op.get_conn_padded(x)
+    np.testing.assert_array_equal(xp, rxp)
+    np.testing.assert_array_equal(m, rm)
