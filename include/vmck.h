@@ -169,6 +169,25 @@ int vmck_stats_f64(vmck_stream s, const double *data, int32_t n_chains,
                    int32_t chain_length, int32_t plain_rhat, double *out5,
                    double *workspace, int64_t workspace_len);
 
+/* Allocation-free form of vmck_stats_f64.  It has no counterpart in the
+ * reference: it exists for callers that cannot allocate device memory while
+ * they run -- an XLA custom call / FFI handler, or a host runtime whose memory
+ * pool owns the device -- where a cudaMalloc / cudaFree would synchronise the
+ * device or fail.  The caller still provides data and out5.  The scratch is a
+ * fixed array of VMCK_STATS_NOALLOC_MAX_DOUBLES doubles (2 MiB) compiled into
+ * the library; every GPU that loads the library holds it until the process
+ * exits.  Sizes needing more scratch than that
+ * (vmck_stats_workspace_size(n_chains, chain_length) > the maximum, roughly
+ * n_chains > 3900 for long chains) are rejected with VMCK_ERR_ARG.
+ * The first call on a device looks up the array's device address (set-up, no
+ * allocation); make that first call before any stream capture.  All calls share
+ * the one array and it keeps the last call's contents (each call overwrites what
+ * it reads, so nothing needs clearing); calls that overlap on the GPU (other
+ * streams, other host threads) race on it and must be serialised by the caller. */
+#define VMCK_STATS_NOALLOC_MAX_DOUBLES 262144
+int vmck_stats_f64_noalloc(vmck_stream s, const double *data, int32_t n_chains,
+                           int32_t chain_length, int32_t plain_rhat, double *out5);
+
 /* ---------------------------------------------------------------- a11 / a12 / a14
  * out = O^T v for the RBM Jacobian O (n, P) without materialising it
  * (the VJP of netket/vqs/mc/mc_state/expect_forces.py:99-106 and the

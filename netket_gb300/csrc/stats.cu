@@ -7,6 +7,8 @@
 // chain means, of block means and of half-chain means, then NetKet's choice of
 // error estimate and R-hat.  Every reduction runs in a fixed order, so results
 // are bit-reproducible run to run.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace vmck {
@@ -126,6 +128,63 @@ __global__ void stats_pass2(const double *__restrict__ data, StatsLayout lay, in
 }  // namespace vmck
 
 using namespace vmck;
+
+// ------------------------------------------------------------ allocation-free variant
+// Scratch for vmck_stats_f64_noalloc: a fixed array that lives in every device's
+// global memory from library load until process exit, so the entry point never
+// allocates.  Host code cannot use the symbol itself as a pointer (on the host
+// it only names a shadow variable); the device address is fetched once per
+// device with cudaGetSymbolAddress while that device is current.
+static __device__ __align__(256) double g_stats_scratch[VMCK_STATS_NOALLOC_MAX_DOUBLES];
+
+namespace {
+std::mutex g_scratch_mutex;
+double *g_scratch_ptr[64] = {nullptr};
+}  // namespace
+
+static int stats_scratch_for_current_device(double **out) {
+  int dev = 0;
+  VMCK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_last_error("stats_f64_noalloc: device ordinal %d out of range", dev);
+    return VMCK_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_stats_scratch);
+    if (e != cudaSuccess || !p) {
+      set_last_error("stats_f64_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return VMCK_ERR_CUDA;
+    }
+    g_scratch_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return VMCK_OK;
+}
+
+extern "C" int vmck_stats_f64_noalloc(vmck_stream s, const double *data, int32_t n_chains,
+                                      int32_t chain_length, int32_t plain_rhat, double *out5) {
+  VMCK_REQUIRE(data && out5 && n_chains > 0 && chain_length > 0, "stats_noalloc arguments");
+  StatsLayout lay = stats_layout(n_chains, chain_length);
+  if (lay.total > VMCK_STATS_NOALLOC_MAX_DOUBLES) {
+    set_last_error("stats_f64_noalloc: %d chains x %d samples need %lld scratch doubles, more "
+                   "than the fixed %d; use vmck_stats_f64 with a caller workspace",
+                   n_chains, chain_length, (long long)lay.total, VMCK_STATS_NOALLOC_MAX_DOUBLES);
+    return VMCK_ERR_ARG;
+  }
+  double *scratch = nullptr;
+  int rc = stats_scratch_for_current_device(&scratch);
+  if (rc) return rc;
+  // Pass 1 overwrites every scratch element pass 2 reads, so the contents left
+  // by an earlier call need no clearing.
+  cudaStream_t st = as_stream(s);
+  stats_pass1<<<n_chains, 128, 0, st>>>(data, lay, scratch);
+  rc = check_launch("stats_noalloc pass 1");
+  if (rc) return rc;
+  stats_pass2<<<1, 1024, 0, st>>>(data, lay, plain_rhat, scratch, out5);
+  return check_launch("stats_noalloc pass 2");
+}
 
 extern "C" int64_t vmck_stats_workspace_size(int32_t n_chains, int32_t chain_length) {
   if (n_chains <= 0 || chain_length <= 0) return 0;
