@@ -37,6 +37,7 @@ extern "C" {
 #define VMCK_DEV_NONFINITE 1   /* NaN or Inf in a solver input or output */
 #define VMCK_DEV_NOT_SPD 2     /* Cholesky info != 0 */
 #define VMCK_DEV_NO_CONVERGE 4 /* iterative refinement did not reach tolerance */
+#define VMCK_DEV_TIMEOUT 8     /* a bounded device-side wait ran out (kernel wound down) */
 
 /* element types */
 #define VMCK_F64 0
@@ -214,13 +215,20 @@ int vmck_rbm_jacobian(vmck_stream s, int32_t dtype, const void *tanh_theta,
  *   T = (G - g 1^T - 1 g^T + c 11^T) / n + diag_shift I, g = O obar, c = |obar|^2.
  * obar (P, FP64): column means.  Only the lower triangle (row >= col) is written;
  * T64 (n, n) FP64 row-major; T32 (nullable) receives an FP32 copy.
- * mode 0: FP64 contraction; mode 1: FP32 contraction; mode 2: BF16 tensor-core
- * contraction with FP32 accumulation (tcgen05). */
+ * mode 0: FP64 contraction (CUDA cores); 1: FP32 contraction (CUDA cores);
+ * 2: tensor cores (tcgen05, TMA) on t rounded to hi + lo BF16 pairs (all four
+ * products, FP32 accumulation); 3: tensor cores on t rounded to one BF16.
+ * Modes 1-3 take tanh_theta in FP32 and contract the shifted c = t - fp32(tbar)
+ * (tbar = obar[0:M]), adding the shift back exactly in a double-float epilogue,
+ * so T is the exact Gram matrix of the contracted Jacobian (positive
+ * definite) with no cancellation against the mean.  status (nullable device int32) receives
+ * VMCK_DEV_TIMEOUT if a tensor-core CTA's bounded wait ran out. */
 int64_t vmck_gram_workspace_size(int32_t N, int32_t M, int64_t n);
+
 int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t dtype,
                   const void *tanh_theta, const int8_t *x, int32_t N, int32_t M,
                   int64_t n, const double *obar, double diag_shift, double *T64,
-                  float *T32, double *workspace, int64_t workspace_len);
+                  float *T32, double *workspace, int64_t workspace_len, int32_t *status);
 
 /* Dense T = O_L O_L^T + diag_shift I (lower triangle) or S = O_L^T O_L + shift I
  * (transpose = 1) with cuBLAS, from a materialised O_L (rows, cols) in dtype
@@ -241,11 +249,12 @@ int vmck_cholesky_solve(vmck_ctx *ctx, vmck_stream s, int32_t dtype, const void 
  * FP64 matrix A64 (lower triangle): max_iter correction solves, each from the
  * FP64 residual b - A64 x; the final relative residual goes to residual_out
  * (device, nullable) and VMCK_DEV_NO_CONVERGE is raised if it exceeds tol.
- * fp32_emulation != 0 factorises with FP32-accurate BF16x9 tensor-core
- * emulation (cuSOLVER CUSOLVER_FP32_EMULATED_BF16X9_MATH). */
+ * factor_mode 0: cuSOLVER SPOTRF; 1: cuSOLVER SPOTRF with FP32-accurate BF16x9
+ * tensor-core emulation; 2: recursive Cholesky whose TRSM / SYRK are recursive
+ * GEMMs on BF16x9-emulated tensor cores (cuSOLVER / cuBLAS at <= 1024 leaves). */
 int vmck_cholesky_solve_refined(vmck_ctx *ctx, vmck_stream s, const double *A64,
                                 float *A32, const double *b, double *x, int64_t n,
-                                int32_t max_iter, double tol, int32_t fp32_emulation,
+                                int32_t max_iter, double tol, int32_t factor_mode,
                                 int32_t *status, double *residual_out);
 /* pinv_smooth (solvers.py:33-139) via a symmetric eigendecomposition (FP64). */
 int vmck_pinv_smooth_solve(vmck_ctx *ctx, vmck_stream s, const double *A,

@@ -13,7 +13,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libvmck.so")
 
 F64, F32, BF16 = 0, 1, 2
-DEV_NONFINITE, DEV_NOT_SPD, DEV_NO_CONVERGE = 1, 2, 4
+DEV_NONFINITE, DEV_NOT_SPD, DEV_NO_CONVERGE, DEV_TIMEOUT = 1, 2, 4, 8
 
 c_i32, c_i64, c_u64, c_dbl, c_vp = (ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64,
                                     ctypes.c_double, ctypes.c_void_p)
@@ -64,7 +64,7 @@ _SIGNATURES = {
                            c_vp], c_i32),
     "vmck_gram_workspace_size": ([c_i32, c_i32, c_i64], c_i64),
     "vmck_rbm_gram": ([c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_dbl,
-                       c_vp, c_vp, c_vp, c_i64], c_i32),
+                       c_vp, c_vp, c_vp, c_i64, c_vp], c_i32),
     "vmck_gram_dense": ([c_vp, c_vp, c_i32, c_vp, c_i64, c_i64, c_i32, c_dbl, c_vp], c_i32),
     "vmck_cholesky_solve": ([c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp], c_i32),
     "vmck_cholesky_solve_refined": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i32, c_dbl,

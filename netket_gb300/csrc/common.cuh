@@ -92,6 +92,61 @@ __device__ __forceinline__ float log_cosh(float x) {
   x = fabsf(x);
   return x + log1pf(expf(-2.0f * x)) - 0.693147180559945309f;
 }
+// Same formula on the special-function units (__expf / __logf, one MUFU op
+// each): 1 + exp(-2|x|) lies in (1, 2], so log(1 + e) loses nothing to the
+// missing log1p; absolute error ~1e-7, used by the FP32 sampler and local-energy
+// kernels (whose results carry a 1e-4 relative bound).
+__device__ __forceinline__ float log_cosh_fast(float x) {
+  x = fabsf(x);
+  return x + __logf(1.0f + __expf(-2.0f * x)) - 0.693147180559945309f;
+}
+__device__ __forceinline__ double log_cosh_fast(double x) { return log_cosh(x); }
+
+// ----------------------------------------------------------------- double-float
+// Pairs (hi, lo) of FP32 values carrying ~48 significant bits, with the
+// error-free transformations of Knuth (TwoSum) and Dekker (TwoProduct via FMA).
+// Used where GB300's FP64 pipe would be the bottleneck (it issues roughly two
+// FP64 FMAs per clock per SM) but FP32 accuracy is not enough.
+struct df32 {
+  float hi, lo;
+};
+__device__ __forceinline__ df32 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ df32 df_quick_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df32 df_two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+  const df32 s = df_two_sum(a.hi, b.hi);
+  return df_quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df32 df_add(df32 a, float b) {
+  const df32 s = df_two_sum(a.hi, b);
+  return df_quick_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+__device__ __forceinline__ df32 df_neg(df32 a) { return {-a.hi, -a.lo}; }
+// a * b for a float b (error of the lo * b product is below the pair's precision)
+__device__ __forceinline__ df32 df_mul(df32 a, float b) {
+  const df32 p = df_two_prod(a.hi, b);
+  return df_quick_two_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
+  const df32 p = df_two_prod(a.hi, b.hi);
+  return df_quick_two_sum(p.hi, __fadd_rn(p.lo, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi))));
+}
+__device__ __forceinline__ df32 df_from(double d) {
+  const float h = __double2float_rn(d);
+  return {h, __double2float_rn(d - (double)h)};
+}
+__device__ __forceinline__ double df_to_double(df32 a) { return (double)a.hi + (double)a.lo; }
 
 // ----------------------------------------------------------------- reductions
 template <typename T>

@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "gram_tc.cuh"
 
@@ -83,12 +85,151 @@ __global__ void __launch_bounds__(256) g_vector_kernel(const T *__restrict__ t,
   }
 }
 
+// Double-float form for FP32 tanh(theta): the ~6.5e8 accumulations per call
+// would otherwise run on the FP64 pipe.  t enters as c + s0 (the shifted,
+// rounded values of gram_shift_kernel plus the shift), exactly as the
+// contraction sees it; obar_df holds (hi, lo) pairs of obar.
+__global__ void __launch_bounds__(256) g_vector_df_kernel(const float *__restrict__ c,
+                                                          const float *__restrict__ s0,
+                                                          const int8_t *__restrict__ x, int N,
+                                                          int M, int64_t n,
+                                                          const float2 *__restrict__ obar_df,
+                                                          const double *__restrict__ obar,
+                                                          double *__restrict__ g) {
+  __shared__ int8_t xs[G_SPB][G_NMAX];
+  __shared__ double part[G_SPB][8];
+  const int64_t s0i = (int64_t)blockIdx.x * G_SPB;
+  const float2 *Kbar = obar_df + M;
+  const double *xbar = obar + M + (int64_t)N * M;
+  const int ns = (int)std::min<int64_t>(G_SPB, n - s0i);
+  for (int e = threadIdx.x; e < G_SPB * N; e += blockDim.x) {
+    int q = e / N, i = e % N;
+    xs[q][i] = (q < ns) ? x[(s0i + q) * N + i] : int8_t(0);
+  }
+  __syncthreads();
+  df32 gp[G_SPB];
+#pragma unroll
+  for (int q = 0; q < G_SPB; ++q) gp[q] = {0.0f, 0.0f};
+  for (int j = threadIdx.x; j < M; j += blockDim.x) {
+    df32 y[G_SPB];
+    const float2 tb = obar_df[j];
+    const float sj = s0[j];
+#pragma unroll
+    for (int q = 0; q < G_SPB; ++q) y[q] = {tb.x, tb.y};
+    for (int i = 0; i < N; ++i) {
+      const float2 kb = Kbar[(int64_t)i * M + j];
+      const df32 kp = {kb.x, kb.y}, km = {-kb.x, -kb.y};
+#pragma unroll
+      for (int q = 0; q < G_SPB; ++q) y[q] = df_add(y[q], xs[q][i] > 0 ? kp : km);
+    }
+#pragma unroll
+    for (int q = 0; q < G_SPB; ++q)
+      if (q < ns) gp[q] = df_add(gp[q], df_mul(y[q], df_two_sum(c[(s0i + q) * M + j], sj)));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < G_SPB; ++q) {
+    double v = warp_sum(df_to_double(gp[q]));
+    if (lane == 0) part[q][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < ns) {
+    const int q = threadIdx.x;
+    double v = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += part[q][w];
+    for (int i = 0; i < N; ++i) v += xs[q][i] > 0 ? xbar[i] : -xbar[i];
+    g[s0i + q] = v;
+  }
+}
+
+// Shift of the FP32 contraction: s0 = fp32(mean of t) from obar, and
+// c = round(t - s0) with terms = 0 (FP32), 1 (one BF16) or 2 (hi + lo BF16);
+// c is exactly what the contraction multiplies.  A = t t^T is then
+// c c^T + w 1^T + 1 w^T + |s0|^2 with w_s = c_s . s0, and only c c^T is
+// accumulated in FP32 -- its entries are small where hidden units are biased,
+// which keeps the centred T free of catastrophic cancellation.
+__global__ void gram_shift_kernel(const float *__restrict__ t, const double *__restrict__ obar,
+                                  int64_t n, int M, int terms, float *__restrict__ c,
+                                  float *__restrict__ s0) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e < M) s0[e] = __double2float_rn(obar[e]);
+  if (e >= n * M) return;
+  const int j = (int)(e % M);
+  const float v = __fsub_rn(t[e], __double2float_rn(obar[j]));
+  if (terms == 0) {
+    c[e] = v;
+  } else {
+    const float hi = __bfloat162float(__float2bfloat16(v));
+    c[e] = (terms == 1) ? hi : __fadd_rn(hi, __bfloat162float(__float2bfloat16(__fsub_rn(v, hi))));
+  }
+}
+
+// w_s = c_s . s0 (one warp per sample, FP64) and |s0|^2, as double-float pairs
+__global__ void gram_shift_dot_kernel(const float *__restrict__ c, const float *__restrict__ s0,
+                                      int64_t n, int M, float2 *__restrict__ w,
+                                      float2 *__restrict__ s0sq) {
+  const int64_t s = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s < n) {
+    double acc = 0.0;
+    for (int j = lane; j < M; j += 32) acc += (double)c[s * M + j] * (double)s0[j];
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      const df32 d = df_from(acc);
+      w[s] = make_float2(d.hi, d.lo);
+    }
+  }
+  if (blockIdx.x == 0 && (threadIdx.x >> 5) == 0) {
+    double q = 0.0;
+    for (int j = lane; j < M; j += 32) q += (double)s0[j] * (double)s0[j];
+    q = warp_sum(q);
+    if (lane == 0) {
+      const df32 d = df_from(q);
+      *s0sq = make_float2(d.hi, d.lo);
+    }
+  }
+}
+
+__global__ void to_df_kernel(const double *__restrict__ v, int64_t P, float2 *__restrict__ out) {
+  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const df32 d = df_from(v[p]);
+  out[p] = make_float2(d.hi, d.lo);
+}
+
 __global__ void sumsq_kernel(const double *__restrict__ v, int64_t P, double *out) {
   __shared__ double red[32];
   double s = 0;
   for (int64_t p = threadIdx.x; p < P; p += blockDim.x) s += v[p] * v[p];
   s = block_sum(s, red);
   if (threadIdx.x == 0) *out = s;
+}
+
+// h_s = g_s - c / 2 as a double-float pair, so that T = (G - h_s - h_s') / n
+__global__ void h_df_kernel(const double *__restrict__ g, const double *__restrict__ cptr,
+                            int64_t n, float2 *__restrict__ h) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const df32 d = df_from(g[s] - 0.5 * (*cptr));
+  h[s] = make_float2(d.hi, d.lo);
+}
+
+// Gram epilogue value in double-float arithmetic: Ac = c_s.c_s' from the FP32
+// contraction, the shift terms w, |s0|^2, B = x.x' exact, h = g - |obar|^2 / 2.
+// Returns (((Ac + w_s + w_s' + |s0|^2)(1 + B) + B) - h_s - h_s') / n (+ shift).
+__device__ __forceinline__ df32 gram_value_df(float Ac, float2 ws, float2 wc, df32 s0sq, int B,
+                                              float2 hs, float2 hc, float inv_n, bool diag,
+                                              df32 shift) {
+  df32 a = df_add(df32{ws.x, ws.y}, df32{wc.x, wc.y});
+  a = df_add(a, s0sq);
+  a = df_add(a, Ac);
+  df32 v = df_mul(a, (float)(1 + B));
+  v = df_add(v, (float)B);
+  v = df_add(v, df32{-hs.x, -hs.y});
+  v = df_add(v, df32{-hc.x, -hc.y});
+  v = df_mul(v, inv_n);
+  if (diag) v = df_add(v, shift);
+  return v;
 }
 
 // ---------------------------------------------------------------- SIMT Gram
@@ -105,7 +246,8 @@ __device__ inline void tri_tile(int64_t bid, int64_t &I, int64_t &J) {
 template <typename T>
 __global__ void __launch_bounds__(256) gram_simt_kernel(
     const T *__restrict__ t, const uint32_t *__restrict__ bits, int words, int N, int M, int64_t n,
-    const double *__restrict__ g, const double *__restrict__ cptr, double inv_n,
+    const double *__restrict__ g, const double *__restrict__ cptr, const float2 *__restrict__ hdf,
+    const float2 *__restrict__ wdf, const float2 *__restrict__ s0sq_p, double inv_n,
     double diag_shift, double *__restrict__ T64, float *__restrict__ T32) {
   __shared__ T ta[GK][GT];
   __shared__ T tb[GK][GT];
@@ -150,6 +292,7 @@ __global__ void __launch_bounds__(256) gram_simt_kernel(
   }
   __syncthreads();
   const double c = *cptr;
+  const df32 shift_df = {(float)diag_shift, (float)(diag_shift - (double)(float)diag_shift)};
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int64_t s = r0 + tr * 4 + i;
@@ -159,12 +302,20 @@ __global__ void __launch_bounds__(256) gram_simt_kernel(
       if (s < n && sp <= s) {
         int diff = 0;
         for (int w = 0; w < words; ++w) diff += __popc(ba[tr * 4 + i][w] ^ bb[tc * 4 + j][w]);
-        const double B = (double)(N - 2 * diff);
-        const double A = (double)acc[i][j];
-        double v = (A * (1.0 + B) + B - g[s] - g[sp] + c) * inv_n;
-        if (s == sp) v += diag_shift;
-        T64[s * n + sp] = v;
-        if (T32) T32[s * n + sp] = (float)v;
+        const int B = N - 2 * diff;
+        if (sizeof(T) == 8) {
+          const double A = (double)acc[i][j];
+          double v = (A * (1.0 + B) + B - g[s] - g[sp] + c) * inv_n;
+          if (s == sp) v += diag_shift;
+          if (T64) T64[s * n + sp] = v;
+          if (T32) T32[s * n + sp] = (float)v;
+        } else {
+          const float2 q = *s0sq_p;
+          const df32 v = gram_value_df((float)acc[i][j], wdf[s], wdf[sp], df32{q.x, q.y}, B,
+                                       hdf[s], hdf[sp], (float)inv_n, s == sp, shift_df);
+          if (T64) T64[s * n + sp] = df_to_double(v);
+          if (T32) T32[s * n + sp] = v.hi + v.lo;
+        }
       }
     }
   }
@@ -176,59 +327,98 @@ using namespace vmck;
 
 static int64_t gram_words(int N) { return (N + 31) / 32; }
 
+struct GramWs {
+  double *g, *cptr;
+  uint32_t *bits;
+  float2 *obar_df, *hdf, *wdf, *s0sq;
+  float *c, *s0;
+  double *tc;
+};
+
+static GramWs gram_ws_layout(double *ws, int N, int M, int64_t n) {
+  const int64_t words = gram_words(N);
+  const int64_t P = (int64_t)M + (int64_t)N * M + N;
+  GramWs w;
+  w.g = ws;
+  w.cptr = ws + n;
+  w.bits = reinterpret_cast<uint32_t *>(ws + n + 2);
+  double *p = ws + n + 2 + (n * words + 1) / 2;
+  w.obar_df = reinterpret_cast<float2 *>(p);
+  p += P;
+  w.hdf = reinterpret_cast<float2 *>(p);
+  p += n;
+  w.wdf = reinterpret_cast<float2 *>(p);
+  p += n;
+  w.s0sq = reinterpret_cast<float2 *>(p);
+  p += 2;
+  w.s0 = reinterpret_cast<float *>(p);
+  p += (M + 1) / 2 + 2;
+  w.c = reinterpret_cast<float *>(p);
+  p += (n * (int64_t)M + 1) / 2 + 2;
+  w.tc = p;
+  return w;
+}
+
 extern "C" int64_t vmck_gram_workspace_size(int32_t N, int32_t M, int64_t n) {
-  (void)M;
-  int64_t words = gram_words(N);
-  return n /*g*/ + 2 /*c*/ + (n * words + 1) / 2 /*bits*/ + vmck::gram_tc_workspace_doubles(M, n) + 8;
+  const int64_t words = gram_words(N);
+  const int64_t P = (int64_t)M + (int64_t)N * M + N;
+  return n + 2 + (n * words + 1) / 2 + P + n + n + 2 + (M + 1) / 2 + 2 + (n * (int64_t)M + 1) / 2 +
+         2 + vmck::gram_tc_workspace_doubles(M, n) + 8;
 }
 
 extern "C" int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t dtype,
                              const void *tanh_theta, const int8_t *x, int32_t N, int32_t M,
                              int64_t n, const double *obar, double diag_shift, double *T64,
-                             float *T32, double *workspace, int64_t workspace_len) {
-  VMCK_REQUIRE(tanh_theta && x && obar && T64 && workspace && N > 0 && M > 0 && n > 0,
+                             float *T32, double *workspace, int64_t workspace_len,
+                             int32_t *status) {
+  VMCK_REQUIRE(tanh_theta && x && obar && (T64 || T32) && workspace && N > 0 && M > 0 && n > 0,
                "rbm_gram arguments");
   VMCK_REQUIRE(N <= 288, "rbm_gram supports N <= 288");
   VMCK_REQUIRE(workspace_len >= vmck_gram_workspace_size(N, M, n), "rbm_gram workspace too small");
-  VMCK_REQUIRE((mode == 0 && dtype == VMCK_F64) || (mode == 1 && dtype == VMCK_F32) ||
-                   (mode == 2 && dtype == VMCK_F32),
-               "rbm_gram: mode/dtype combination (0:F64, 1:F32, 2:F32 tanh input)");
+  VMCK_REQUIRE((mode == 0 && dtype == VMCK_F64) || (mode >= 1 && mode <= 3 && dtype == VMCK_F32),
+               "rbm_gram: mode/dtype combination (0: F64, 1-3: F32 tanh input)");
+  VMCK_REQUIRE(mode < 2 || T32, "rbm_gram: tensor-core modes write T32");
   cudaStream_t st = as_stream(s);
   const int words = (int)gram_words(N);
-  double *g = workspace;
-  double *cptr = workspace + n;
-  uint32_t *bits = reinterpret_cast<uint32_t *>(workspace + n + 2);
-  double *tc_ws = workspace + n + 2 + (n * words + 1) / 2;
+  GramWs w = gram_ws_layout(workspace, N, M, n);
   const int64_t P = (int64_t)M + (int64_t)N * M + N;
-  sign_bits_kernel<<<ceil_div(n * words, 256), 256, 0, st>>>(x, n, N, words, bits);
+  sign_bits_kernel<<<ceil_div(n * words, 256), 256, 0, st>>>(x, n, N, words, w.bits);
   int rc = check_launch("gram sign bits");
   if (rc) return rc;
-  const unsigned gblocks = (unsigned)((n + 15) / 16);
-  if (dtype == VMCK_F64)
-    g_vector_kernel<double><<<gblocks, 256, 0, st>>>(static_cast<const double *>(tanh_theta), x, N,
-                                                     M, n, obar, g);
-  else
-    g_vector_kernel<float><<<gblocks, 256, 0, st>>>(static_cast<const float *>(tanh_theta), x, N,
-                                                    M, n, obar, g);
-  rc = check_launch("gram g vector");
-  if (rc) return rc;
-  sumsq_kernel<<<1, 1024, 0, st>>>(obar, P, cptr);
-  rc = check_launch("gram |obar|^2");
-  if (rc) return rc;
+  const unsigned gblocks = (unsigned)((n + G_SPB - 1) / G_SPB);
+  if (dtype == VMCK_F64) {
+    g_vector_kernel<double><<<gblocks, 256, 0, st>>>(static_cast<const double *>(tanh_theta), x,
+                                                     N, M, n, obar, w.g);
+  } else {
+    const int terms = mode == 2 ? 2 : (mode == 3 ? 1 : 0);
+    gram_shift_kernel<<<ceil_div(n * (int64_t)M, 256), 256, 0, st>>>(
+        static_cast<const float *>(tanh_theta), obar, n, M, terms, w.c, w.s0);
+    if ((rc = check_launch("gram shift"))) return rc;
+    gram_shift_dot_kernel<<<ceil_div(n, 8), 256, 0, st>>>(w.c, w.s0, n, M, w.wdf, w.s0sq);
+    if ((rc = check_launch("gram shift dot"))) return rc;
+    to_df_kernel<<<ceil_div(P, 256), 256, 0, st>>>(obar, P, w.obar_df);
+    if ((rc = check_launch("gram obar pairs"))) return rc;
+    g_vector_df_kernel<<<gblocks, 256, 0, st>>>(w.c, w.s0, x, N, M, n, w.obar_df, obar, w.g);
+  }
+  if ((rc = check_launch("gram g vector"))) return rc;
+  sumsq_kernel<<<1, 1024, 0, st>>>(obar, P, w.cptr);
+  if ((rc = check_launch("gram |obar|^2"))) return rc;
+  h_df_kernel<<<ceil_div(n, 256), 256, 0, st>>>(w.g, w.cptr, n, w.hdf);
+  if ((rc = check_launch("gram h pairs"))) return rc;
   const double inv_n = 1.0 / (double)n;
-  if (mode == 2)
-    return gram_tc_launch(ctx, st, static_cast<const float *>(tanh_theta), bits, words, N, M, n, g,
-                          cptr, inv_n, diag_shift, T64, T32, tc_ws);
+  if (mode >= 2)
+    return gram_tc_launch(ctx, st, w.c, w.bits, words, N, M, n, w.hdf, w.wdf, w.s0sq, inv_n,
+                          diag_shift, T64, T32, w.tc, mode == 2 ? 1 : 0, status);
   const int64_t nt = (n + GT - 1) / GT;
   const int64_t tiles = nt * (nt + 1) / 2;
   VMCK_REQUIRE(tiles < (1ll << 31), "too many tiles");
   if (dtype == VMCK_F64)
     gram_simt_kernel<double><<<(unsigned)tiles, 256, 0, st>>>(
-        static_cast<const double *>(tanh_theta), bits, words, N, M, n, g, cptr, inv_n, diag_shift,
-        T64, T32);
+        static_cast<const double *>(tanh_theta), w.bits, words, N, M, n, w.g, w.cptr, w.hdf,
+        w.wdf, w.s0sq, inv_n, diag_shift, T64, T32);
   else
     gram_simt_kernel<float><<<(unsigned)tiles, 256, 0, st>>>(
-        static_cast<const float *>(tanh_theta), bits, words, N, M, n, g, cptr, inv_n, diag_shift,
-        T64, T32);
+        w.c, w.bits, words, N, M, n, w.g, w.cptr, w.hdf, w.wdf, w.s0sq, inv_n, diag_shift, T64,
+        T32);
   return check_launch("gram simt");
 }

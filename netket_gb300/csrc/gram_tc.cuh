@@ -8,8 +8,11 @@ namespace vmck {
 
 int64_t gram_tc_workspace_doubles(int M, int64_t n);
 
-int gram_tc_launch(vmck_ctx *ctx, cudaStream_t st, const float *tanh_theta, const uint32_t *bits,
-                   int words, int N, int M, int64_t n, const double *g, const double *cptr,
-                   double inv_n, double diag_shift, double *T64, float *T32, double *ws);
+// c: shifted, rounded tanh(theta); h, w, s0sq: double-float epilogue terms
+// (see gram.cu); T64 nullable.
+int gram_tc_launch(vmck_ctx *ctx, cudaStream_t st, const float *c, const uint32_t *bits,
+                   int words, int N, int M, int64_t n, const float2 *h, const float2 *w,
+                   const float2 *s0sq, double inv_n, double diag_shift, double *T64, float *T32,
+                   double *ws, int split, int32_t *status);
 
 }  // namespace vmck

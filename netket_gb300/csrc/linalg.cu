@@ -177,6 +177,80 @@ __global__ void sgd_kernel(double *p, const double *u, int64_t P, double lr, flo
   if (p32) p32[i] = (float)v;
 }
 
+// ------------------------------------------------------------ recursive Cholesky
+// Upper Cholesky A = U^T U of a column-major FP32 matrix (our row-major lower
+// triangle), in place, by recursive halving (Gustavson / Elmroth style): every
+// flop outside the leaves is a GEMM, and the GEMMs run with cuBLAS'
+// FP32-accurate BF16x9 tensor-core emulation.  Leaves (<= CHOL_LEAF) use
+// cuSOLVER POTRF, cuBLAS TRSM / SYRK.
+constexpr int64_t CHOL_LEAF = 1024;
+
+static int64_t half_split(int64_t n) {
+  int64_t h = ((n / 2) + 255) / 256 * 256;
+  return (h >= n) ? n / 2 : h;
+}
+
+__global__ void info_accumulate_kernel(const int *info, int32_t *status) {
+  if (*info != 0 && status) atomicOr(status, VMCK_DEV_NOT_SPD);
+}
+
+struct RecChol {
+  vmck_ctx *c;
+  cudaStream_t st;
+  int32_t *status;
+  size_t dsize, hsize;
+};
+
+// C (n x n, upper) -= A^T A with A (k x n)
+static int syrk_rec(RecChol &R, float *C, int64_t ldc, int64_t n, const float *A, int64_t lda,
+                    int64_t k) {
+  const float mone = -1.0f, one = 1.0f;
+  if (n <= CHOL_LEAF) {
+    VMCK_BLAS(cublasSsyrk(R.c->blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, (int)n, (int)k, &mone, A,
+                          (int)lda, &one, C, (int)ldc));
+    return VMCK_OK;
+  }
+  const int64_t n1 = half_split(n), n2 = n - n1;
+  int rc = syrk_rec(R, C, ldc, n1, A, lda, k);
+  if (rc) return rc;
+  VMCK_BLAS(cublasSgemm(R.c->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n1, (int)n2, (int)k, &mone, A,
+                        (int)lda, A + n1 * lda, (int)lda, &one, C + n1 * ldc, (int)ldc));
+  return syrk_rec(R, C + n1 + n1 * ldc, ldc, n2, A + n1 * lda, lda, k);
+}
+
+// B (m x nrhs) <- U^-T B, U upper (m x m)
+static int trsm_rec(RecChol &R, const float *U, int64_t ldu, int64_t m, float *B, int64_t ldb,
+                    int64_t nrhs) {
+  const float mone = -1.0f, one = 1.0f;
+  if (m <= CHOL_LEAF) {
+    VMCK_BLAS(cublasStrsm(R.c->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
+                          CUBLAS_DIAG_NON_UNIT, (int)m, (int)nrhs, &one, U, (int)ldu, B, (int)ldb));
+    return VMCK_OK;
+  }
+  const int64_t m1 = half_split(m), m2 = m - m1;
+  int rc = trsm_rec(R, U, ldu, m1, B, ldb, nrhs);
+  if (rc) return rc;
+  VMCK_BLAS(cublasSgemm(R.c->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)m2, (int)nrhs, (int)m1, &mone,
+                        U + m1 * ldu, (int)ldu, B, (int)ldb, &one, B + m1, (int)ldb));
+  return trsm_rec(R, U + m1 + m1 * ldu, ldu, m2, B + m1, ldb, nrhs);
+}
+
+static int chol_rec(RecChol &R, float *A, int64_t lda, int64_t n) {
+  if (n <= CHOL_LEAF) {
+    VMCK_SOLVER(cusolverDnXpotrf(R.c->solver, R.c->params, CUBLAS_FILL_MODE_UPPER, n, CUDA_R_32F,
+                                 A, lda, CUDA_R_32F, R.c->dwork, R.dsize, R.c->hwork, R.hsize,
+                                 R.c->d_info));
+    info_accumulate_kernel<<<1, 1, 0, R.st>>>(R.c->d_info, R.status);
+    return check_launch("cholesky leaf info");
+  }
+  const int64_t n1 = half_split(n), n2 = n - n1;
+  int rc = chol_rec(R, A, lda, n1);
+  if (rc) return rc;
+  if ((rc = trsm_rec(R, A, lda, n1, A + n1 * lda, lda, n2))) return rc;
+  if ((rc = syrk_rec(R, A + n1 + n1 * lda, lda, n2, A + n1 * lda, lda, n1))) return rc;
+  return chol_rec(R, A + n1 + n1 * lda, lda, n2);
+}
+
 // ------------------------------------------------------------ symmetric residual
 // r = b - A x for a symmetric A stored as its lower triangle (row-major), each
 // stored element read exactly once.  Tile (I, J), I >= J, of 64 x 64 adds
@@ -333,18 +407,22 @@ extern "C" int vmck_cholesky_solve(vmck_ctx *c, vmck_stream s, int32_t dtype, co
 
 extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const double *A64,
                                            float *A32, const double *b, double *x, int64_t n,
-                                           int32_t max_iter, double tol, int32_t fp32_emulation,
+                                           int32_t max_iter, double tol, int32_t factor_mode,
                                            int32_t *status, double *residual_out) {
   VMCK_REQUIRE(c && A64 && A32 && b && x && n > 0 && max_iter >= 1, "refined solve arguments");
+  VMCK_REQUIRE(factor_mode >= 0 && factor_mode <= 2, "factor_mode must be 0, 1 or 2");
+  VMCK_REQUIRE(n < (1ll << 31), "refined solve size");
   cudaStream_t st = as_stream(s);
   int rc = bind(c, st);
   if (rc) return rc;
-  VMCK_SOLVER(cusolverDnSetMathMode(c->solver, fp32_emulation ? CUSOLVER_FP32_EMULATED_BF16X9_MATH
-                                                              : CUSOLVER_DEFAULT_MATH));
-  if (fp32_emulation)
+  const bool emulate = factor_mode != 0;
+  VMCK_SOLVER(cusolverDnSetMathMode(c->solver, emulate ? CUSOLVER_FP32_EMULATED_BF16X9_MATH
+                                                       : CUSOLVER_DEFAULT_MATH));
+  if (emulate)
     VMCK_SOLVER(cusolverDnSetEmulationStrategy(c->solver, CUDA_EMULATION_STRATEGY_EAGER));
   size_t dsize = 0, hsize = 0;
-  VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
+  const int64_t fn = factor_mode == 2 ? std::min<int64_t>(n, CHOL_LEAF) : n;
+  VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, fn,
                                           CUDA_R_32F, A32, n, CUDA_R_32F, &dsize, &hsize));
   if ((rc = grow(&c->dwork, &c->dwork_bytes, dsize + 256, st))) return rc;
   if ((rc = grow_host(c, hsize))) return rc;
@@ -358,13 +436,25 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
   double *norms = reinterpret_cast<double *>(
       (reinterpret_cast<uintptr_t>(r32 + n) + 15) & ~uintptr_t(15));
   double *sws = reinterpret_cast<double *>(static_cast<char *>(c->aux) + ws_off);
-  cusolverStatus_t fs = cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
-                                         CUDA_R_32F, A32, n, CUDA_R_32F, c->dwork, dsize,
-                                         c->hwork, hsize, c->d_info);
-  cusolverDnSetMathMode(c->solver, CUSOLVER_DEFAULT_MATH);
-  if (fs != CUSOLVER_STATUS_SUCCESS) {
-    set_last_error("refined solve: cusolverDnXpotrf status %d", (int)fs);
-    return VMCK_ERR_LIBRARY;
+  if (factor_mode == 2) {
+    VMCK_BLAS(cublasSetMathMode(c->blas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
+    VMCK_BLAS(cublasSetEmulationStrategy(c->blas, CUBLAS_EMULATION_STRATEGY_EAGER));
+    RecChol R{c, st, status, dsize, hsize};
+    rc = chol_rec(R, A32, n, n);
+    cublasSetMathMode(c->blas, CUBLAS_DEFAULT_MATH);
+    cusolverDnSetMathMode(c->solver, CUSOLVER_DEFAULT_MATH);
+    if (rc) return rc;
+  } else {
+    cusolverStatus_t fs = cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
+                                           CUDA_R_32F, A32, n, CUDA_R_32F, c->dwork, dsize,
+                                           c->hwork, hsize, c->d_info);
+    cusolverDnSetMathMode(c->solver, CUSOLVER_DEFAULT_MATH);
+    if (fs != CUSOLVER_STATUS_SUCCESS) {
+      set_last_error("refined solve: cusolverDnXpotrf status %d", (int)fs);
+      return VMCK_ERR_LIBRARY;
+    }
+    info_accumulate_kernel<<<1, 1, 0, st>>>(c->d_info, status);
+    if ((rc = check_launch("refined solve info"))) return rc;
   }
   VMCK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
   const int blocks = ceil_div(n, 256);

@@ -140,7 +140,7 @@ __device__ inline void theta_and_logpsi(const RbmParams<T> &P, const int8_t *xs,
     T acc = P.b[j];
     for (int i = 0; i < N; ++i) acc += (T)xs[i] * P.W[(int64_t)i * M + j];
     th[j] = acc;
-    T l = log_cosh(acc);
+    T l = log_cosh_fast(acc);
     lc[j] = l;
     part += l;
   }
@@ -157,7 +157,7 @@ __device__ inline T warp_log_ratio(const RbmParams<T> &P, const T *th, const T *
   for (int j = lane; j < M; j += 32) {
     T t = th[j];
     for (int q = 0; q < ns; ++q) t += d[q] * P.W[(int64_t)site[q] * M + j];
-    s += log_cosh(t) - lc[j];
+    s += log_cosh_fast(t) - lc[j];
   }
   s = warp_sum(s);
   for (int q = 0; q < ns; ++q) s += d[q] * P.a[site[q]];

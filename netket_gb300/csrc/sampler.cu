@@ -38,7 +38,7 @@ __device__ inline void chain_recompute(const T *__restrict__ b, const T *__restr
     T acc = b[j];
     for (int i = 0; i < N; ++i) acc += (T)c.xs[i] * W[(int64_t)i * M + j];
     c.th[j] = acc;
-    T l = log_cosh(acc);
+    T l = log_cosh_fast(acc);
     c.lc[j] = l;
     part += l;
   }
@@ -147,7 +147,7 @@ __global__ void metropolis_kernel(const T *__restrict__ params, int N, int M, in
       for (int j = lane; j < M; j += 32) {
         T t = c.th[j] + du * Wu[j];
         if (RULE == 1) t += dv * Wv[j];
-        T l = log_cosh(t);
+        T l = log_cosh_fast(t);
         c.tn[j] = t;
         c.ln[j] = l;
         s += l - c.lc[j];

@@ -11,7 +11,7 @@ import time
 
 import torch
 
-from ._native import DEV_NONFINITE, DEV_NOT_SPD
+from ._native import DEV_NONFINITE, DEV_NOT_SPD, DEV_TIMEOUT, VmckError
 from .ngd import minsr_fallback, minsr_update, sr_update
 from .optimizer import identity_preconditioner
 from .stats import Stats
@@ -145,7 +145,7 @@ class VMC_SR(AbstractVariationalDriver):
     """
 
     def __init__(self, hamiltonian, optimizer, *, diag_shift, variational_state, use_ntk=None,
-                 gram="structured", gram_mode=None, solve=None, refine_iters=4,
+                 gram="structured", gram_mode=None, solve=None, refine_iters=3,
                  refine_tol=1e-10, jac_dtype=None, proj_reg=None, momentum=None):
         super().__init__(variational_state, optimizer)
         if proj_reg is not None or momentum is not None:
@@ -187,6 +187,8 @@ class VMC_SR(AbstractVariationalDriver):
             host = torch.cat([c["stats_dev"], self.info["status_dev"].to(torch.float64)]).cpu()
             status = int(host[5].item())
             self.info["status"] = status
+            if status & DEV_TIMEOUT:
+                raise VmckError("a device-side wait timed out in the minSR step")
             if status & (DEV_NOT_SPD | DEV_NONFINITE):
                 dp = minsr_fallback(self.info)
             stats = Stats.from_array(host[:5].numpy())

@@ -115,8 +115,10 @@ def jacobian_dense(tanh_t, x, N, M, col_mean, scale, out_dtype):
     return O
 
 
-def gram_structured(tanh_t, x, N, M, obar, diag_shift, mode, want_f32=False):
-    """Lower triangle of T = O_L O_L^T + diag_shift I (n, n) FP64 (+ FP32 copy)."""
+def gram_structured(tanh_t, x, N, M, obar, diag_shift, mode, want_f32=False, status=None):
+    """Lower triangle of T = O_L O_L^T + diag_shift I (n, n) FP64 (+ FP32 copy).
+    mode 0: FP64 CUDA cores; 1: FP32 CUDA cores; 2: tcgen05 BF16 hi/lo split;
+    3: tcgen05 single BF16."""
     n = x.shape[0]
     T64 = torch.empty((n, n), dtype=torch.float64, device=x.device)
     T32 = torch.empty((n, n), dtype=torch.float32, device=x.device) if want_f32 else None
@@ -125,7 +127,7 @@ def gram_structured(tanh_t, x, N, M, obar, diag_shift, mode, want_f32=False):
     nat.check(nat.lib().vmck_rbm_gram(nat.ctx(), nat.stream(), int(mode),
                                       nat.dtype_code(tanh_t.dtype), nat.ptr(tanh_t), nat.ptr(x), N,
                                       M, n, nat.ptr(obar), float(diag_shift), nat.ptr(T64),
-                                      nat.ptr(T32), nat.ptr(ws), ws.numel()))
+                                      nat.ptr(T32), nat.ptr(ws), ws.numel(), nat.ptr(status)))
     return T64, T32
 
 
@@ -148,15 +150,17 @@ def cholesky_solve(A, b, status):
     return x
 
 
-def cholesky_solve_refined(A64, A32, b, status, max_iter=4, tol=1e-10, emulation=True):
-    """FP32 Cholesky (BF16x9 tensor-core emulation when ``emulation``) refined to
-    an FP64 residual; A32 is overwritten by its factor."""
+def cholesky_solve_refined(A64, A32, b, status, max_iter=3, tol=1e-10, factor_mode=2):
+    """FP32-accurate Cholesky of A32 (overwritten by its factor) refined to an
+    FP64 residual against A64.  factor_mode 0: cuSOLVER SPOTRF; 1: SPOTRF with
+    BF16x9 emulation; 2: recursive GEMM-based factorisation on BF16x9-emulated
+    tensor cores."""
     x = torch.empty_like(b)
     res = torch.empty(1, dtype=torch.float64, device=b.device)
     nat.check(nat.lib().vmck_cholesky_solve_refined(nat.ctx(), nat.stream(), nat.ptr(A64),
                                                     nat.ptr(A32), nat.ptr(b), nat.ptr(x),
                                                     A64.shape[0], int(max_iter), float(tol),
-                                                    int(bool(emulation)), nat.ptr(status),
+                                                    int(factor_mode), nat.ptr(status),
                                                     nat.ptr(res)))
     return x, res
 

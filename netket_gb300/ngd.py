@@ -8,7 +8,13 @@
 Two ways to form T:
   * ``gram="structured"`` (default): the RBM identity
     ``O(s).O(s') = (t_s.t_s')(1 + x_s.x_s') + x_s.x_s'`` (t = tanh theta) turns
-    the (n x n x P) contraction into (n x n x M), and O is never stored;
+    the (n x n x P) contraction into (n x n x M), and O is never stored.  For an
+    FP32 t the contraction is shifted by the column mean and the shift is added
+    back in double-float (no cancellation); ``gram_mode=1`` (default) contracts
+    in FP32 on the CUDA cores, ``2`` / ``3`` on the tensor cores (tcgen05) with t
+    rounded to hi + lo BF16 pairs / one BF16.  At n = 16,384 and diag_shift
+    1e-4 an entrywise T error of ~1e-6 already has a spectral norm close to the
+    shift, so only mode 1 keeps T positive definite there (see the design notes);
   * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
     and a cuBLAS SYRK.
 Solvers (``solve=``):
@@ -36,7 +42,7 @@ def _status():
 
 
 def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram_mode=None,
-                 solve="cholesky", refine_iters=4, refine_tol=1e-10, rtol=1e-14,
+                 solve="cholesky", refine_iters=3, refine_tol=1e-10, rtol=1e-14,
                  rtol_smooth=1e-14, jac_dtype=None, check=True, phase_timer=None):
     """Returns (delta (P,) FP64, info).  ``t`` = tanh(theta) (n, M) in the compute
     dtype, ``e`` = local energies (n,) FP64, ``mean_dev`` = their mean (device).
@@ -47,14 +53,16 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     ph = phase_timer
     n = x.shape[0]
     s = 1.0 / math.sqrt(n)
+    mode = None
+    if gram == "structured":
+        mode = gram_mode if gram_mode is not None else (0 if t.dtype == torch.float64 else 1)
     obar = K.column_means(t, x, N, M)
     dv = K.center_scale(e, mean_dev, 2.0 * s)
     status = _status()
     info = SolveInfo(solver_fallback=False)
     if gram == "structured":
-        mode = gram_mode if gram_mode is not None else (0 if t.dtype == torch.float64 else 1)
         T64, T32 = K.gram_structured(t, x, N, M, obar, diag_shift, mode,
-                                     want_f32=(solve == "refined"))
+                                     want_f32=(solve == "refined" or mode >= 2), status=status)
         if ph:
             ph.mark("gram")
         if solve == "refined":

@@ -73,11 +73,6 @@ def test_structured_gram(nk, N, alpha, n):
     T64, _ = nk.kernels.gram_structured(t, x, N, M, obar, 1e-3, mode=0)
     np.testing.assert_allclose(T64.cpu().numpy()[low], ref[low], rtol=1e-10,
                                atol=1e-12 * np.abs(ref).max())
-    T64b, T32 = nk.kernels.gram_structured(t.float(), x, N, M, obar, 1e-3, mode=1, want_f32=True)
-    np.testing.assert_allclose(T64b.cpu().numpy()[low], ref[low], rtol=1e-4,
-                               atol=1e-5 * np.abs(ref).max())
-    np.testing.assert_allclose(T32.cpu().numpy()[low], ref[low], rtol=1e-4,
-                               atol=1e-5 * np.abs(ref).max())
     OL = nk.kernels.jacobian_dense(t, x, N, M, obar, 1 / math.sqrt(n), torch.float64)
     Td = nk.kernels.gram_dense(OL, 1e-3)
     np.testing.assert_allclose(Td.cpu().numpy()[low], ref[low], rtol=1e-10,
@@ -88,6 +83,50 @@ def test_structured_gram(nk, N, alpha, n):
     lowP = np.tril_indices(P)
     np.testing.assert_allclose(S.cpu().numpy()[lowP], refS[lowP], rtol=1e-10,
                                atol=1e-12 * np.abs(refS).max())
+
+
+def _jacobian_from_t(t, x):
+    n, N = x.shape
+    M = t.shape[1]
+    return np.concatenate([t, (x[:, :, None] * t[:, None, :]).reshape(n, N * M), x], axis=1)
+
+
+def _round_terms(v, terms):
+    if terms == 0:
+        return v
+    hi = v.to(torch.bfloat16).float()
+    return hi if terms == 1 else hi + (v - hi).to(torch.bfloat16).float()
+
+
+@pytest.mark.parametrize("N,alpha,n", [(16, 1, 300), (100, 4, 700), (36, 2, 1030)])
+def test_fp32_and_tensor_core_gram(nk, N, alpha, n):
+    """FP32 Gram modes contract c = round(t - s0) (s0 = fp32 column mean of t;
+    mode 1 FP32, mode 2 hi + lo BF16 pairs on tcgen05, mode 3 one BF16 on
+    tcgen05) and add the shift back exactly: T equals the FP64 Gram of the
+    Jacobian of t_eff = c + s0 centred at the given obar, to FP32 accumulation
+    accuracy, and is positive definite."""
+    model, flat, M, x, t, p = _problem(nk, N, alpha, n)
+    xs = x.cpu().numpy().astype(np.float64)
+    low = np.tril_indices(n)
+    t32 = t.float().contiguous()
+    obar = nk.kernels.column_means(t, x, N, M)
+    s0 = obar[:M].float()
+    ob = obar.cpu().numpy()
+    for mode, terms in ((1, 0), (2, 2), (3, 1)):
+        teff = (_round_terms(t32 - s0, terms).double() + s0.double()).cpu().numpy()
+        O = (_jacobian_from_t(teff, xs) - ob) / math.sqrt(n)
+        ref = O @ O.T + 1e-3 * np.eye(n)
+        scale = np.abs(ref).max()
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        T64, T32 = nk.kernels.gram_structured(t32, x, N, M, obar, 1e-3, mode=mode, want_f32=True,
+                                              status=st)
+        assert st.item() == 0
+        got = T64.cpu().numpy()
+        err = np.abs(got[low] - ref[low]).max() / scale
+        assert err < 2e-6, (mode, err)
+        np.testing.assert_allclose(T32.cpu().numpy()[low], got[low], rtol=1e-6, atol=1e-7 * scale)
+        full = np.tril(got) + np.tril(got, -1).T
+        np.linalg.cholesky(full)  # positive definite
 
 
 def test_solvers(nk, golden):
@@ -109,19 +148,36 @@ def test_solvers(nk, golden):
     assert info2["solver_fallback"]
 
 
-def test_refined_solve(nk):
+@pytest.mark.parametrize("n,mode", [(700, 2), (2500, 0), (2500, 1), (2500, 2), (4100, 2)])
+def test_refined_solve(nk, n, mode):
+    """FP32-accurate factorisation (cuSOLVER, emulated cuSOLVER, recursive GEMM
+    Cholesky) + FP64 refinement reaches the FP64 solution."""
     rng = np.random.default_rng(3)
-    n = 700
-    U = rng.normal(size=(n, 200))
-    A = U @ U.T / 200 + 1e-3 * np.eye(n)
+    U = rng.normal(size=(n, 300))
+    A = U @ U.T / 300 + 1e-3 * np.eye(n)
     b = rng.normal(size=n)
     At = torch.as_tensor(A, device="cuda")
+    A32 = At.float().contiguous()
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
-    x, res = nk.kernels.cholesky_solve_refined(At, At.float().contiguous(), torch.as_tensor(b, device="cuda"),
-                                               st, max_iter=6, tol=1e-12)
-    np.testing.assert_allclose(x.cpu().numpy(), np.linalg.solve(A, b), rtol=1e-9,
-                               atol=1e-9 * np.abs(np.linalg.solve(A, b)).max())
-    assert res.item() < 1e-12 and st.item() == 0
+    x, res = nk.kernels.cholesky_solve_refined(At, A32, torch.as_tensor(b, device="cuda"),
+                                               st, max_iter=6, tol=1e-11, factor_mode=mode)
+    ref = np.linalg.solve(A, b)
+    np.testing.assert_allclose(x.cpu().numpy(), ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max())
+    assert res.item() < 1e-11 and st.item() == 0
+    # the factor itself: U^T U == A to FP32 accuracy (upper triangle, column-major
+    # == lower triangle, row-major)
+    L = torch.tril(A32).double()
+    np.testing.assert_allclose((L @ L.T).cpu().numpy(), A, atol=2e-5 * np.abs(A).max())
+
+
+def test_refined_solve_flags_non_spd(nk):
+    n = 1500
+    A = -np.eye(n)
+    At = torch.as_tensor(A, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nk.kernels.cholesky_solve_refined(At, At.float().contiguous(), torch.ones(n, device="cuda",
+                                      dtype=torch.float64), st, max_iter=2, factor_mode=2)
+    assert st.item() & nk._native.DEV_NOT_SPD
 
 
 @pytest.mark.parametrize("name", ["minsr", "sr", "minsr_big_shift"])
