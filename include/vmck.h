@@ -160,6 +160,55 @@ int vmck_metropolis_sample(vmck_stream s, int32_t dtype, const void *params, int
                            uint64_t seed, uint64_t counter, int32_t rule,
                            const int32_t *clusters, int32_t n_clusters);
 
+/* ---------------------------------------------------------------- batched (C3)
+ * Many independent problems of uneven size in one persistent launch.  Each
+ * instance's chains run exactly as vmck_metropolis_sample would run them
+ * (same per-chain code, same Philox stream keyed by the instance seed and the
+ * chain index), so an instance's samples are identical alone and in a batch.
+ * The instance table and the work list live in device memory; work holds
+ * (instance, first chain) pairs of chains_per_item chains each, ordered by the
+ * caller (largest cost first); queue is a device int32 the call resets.
+ * Persistent CTAs (n_ctas of them, chains_per_item warps each) take items from
+ * the queue with an atomic counter.  Each instance's counter is advanced by
+ * (n_discard + chain_length) * sweep_size at the end of the call.  Local rule
+ * only.  No counterpart function in the reference: it batches
+ * MetropolisSampler._sample_chain (netket/sampler/metropolis.py:466-505) over
+ * independent samplers. */
+typedef struct {
+  const void *params;  /* flat RBM parameters of the instance, in dtype */
+  int8_t *sigma;       /* (n_chains, N) chain states, read and written */
+  double *log_prob;    /* (n_chains,) */
+  int64_t *n_accepted; /* (n_chains,) incremented */
+  int8_t *samples;     /* (n_chains, chain_length, N) */
+  uint64_t seed;       /* Philox key */
+  uint64_t counter;    /* proposal counter, advanced by the call */
+  int32_t N, M, n_chains, sweep_size;
+} vmck_batch_chains;
+
+int vmck_batched_metropolis_local(vmck_stream s, int32_t dtype, vmck_batch_chains *inst,
+                                  int32_t n_inst, const int32_t *work, int32_t n_items,
+                                  int32_t chains_per_item, int32_t *queue, int32_t n_discard,
+                                  int32_t chain_length, int32_t max_N, int32_t max_M,
+                                  int32_t n_ctas);
+
+/* Batched fused Ising local energies (vmck_rbm_eloc_ising per instance, in one
+ * persistent launch): work holds (instance, first sample) pairs of
+ * samples_per_item samples each. */
+typedef struct {
+  const void *params;
+  const int8_t *x;      /* (n, N) */
+  double *eloc;         /* (n,) */
+  const int32_t *edges; /* (n_edges, 2) */
+  int64_t n;
+  double h, J;
+  int32_t N, M, n_edges, pad;
+} vmck_batch_ising;
+
+int vmck_batched_eloc_ising(vmck_stream s, int32_t dtype, const vmck_batch_ising *inst,
+                            int32_t n_inst, const int32_t *work, int32_t n_items,
+                            int32_t samples_per_item, int32_t *queue, int32_t max_N,
+                            int32_t max_M, int32_t n_ctas);
+
 /* ---------------------------------------------------------------- a10
  * netket.stats.statistics, blocking estimator (netket/stats/mc_stats_old.py:
  * 88-196) in FP64 over data (n_chains, chain_length):

@@ -18,6 +18,7 @@ from . import optimizer
 from . import vqs
 from . import driver
 from . import exact
+from . import batched
 
-__all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd",
+__all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd", "batched",
            "optimizer", "vqs", "driver", "exact"]

@@ -34,6 +34,20 @@ class LocalOpStruct(ctypes.Structure):
     ]
 
 
+class BatchChainsStruct(ctypes.Structure):
+    """Mirror of ``vmck_batch_chains``."""
+    _fields_ = [("params", c_vp), ("sigma", c_vp), ("log_prob", c_vp), ("n_accepted", c_vp),
+                ("samples", c_vp), ("seed", c_u64), ("counter", c_u64), ("N", c_i32),
+                ("M", c_i32), ("n_chains", c_i32), ("sweep_size", c_i32)]
+
+
+class BatchIsingStruct(ctypes.Structure):
+    """Mirror of ``vmck_batch_ising``."""
+    _fields_ = [("params", c_vp), ("x", c_vp), ("eloc", c_vp), ("edges", c_vp), ("n", c_i64),
+                ("h", c_dbl), ("J", c_dbl), ("N", c_i32), ("M", c_i32), ("n_edges", c_i32),
+                ("pad", c_i32)]
+
+
 _SIGNATURES = {
     "vmck_abi_version": ([], c_i32),
     "vmck_error_string": ([c_i32], ctypes.c_char_p),
@@ -54,6 +68,10 @@ _SIGNATURES = {
                              ctypes.POINTER(LocalOpStruct), c_vp, c_vp], c_i32),
     "vmck_metropolis_sample": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32,
                                 c_i32, c_i32, c_vp, c_u64, c_u64, c_i32, c_vp, c_i32], c_i32),
+    "vmck_batched_metropolis_local": ([c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32,
+                                       c_i32, c_i32, c_i32, c_i32], c_i32),
+    "vmck_batched_eloc_ising": ([c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32, c_i32,
+                                 c_i32], c_i32),
     "vmck_stats_workspace_size": ([c_i32, c_i32], c_i64),
     "vmck_stats_f64": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp, c_i64], c_i32),
     "vmck_stats_f64_noalloc": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_vp], c_i32),
@@ -127,17 +145,37 @@ def ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+_slot = threading.local()
+
+
+class use_ctx:
+    """Select library context ``slot`` on this thread (a context holds one
+    cuBLAS / cuSOLVER handle pair and its workspace, so work that runs
+    concurrently on several streams uses one slot per stream)."""
+
+    def __init__(self, slot):
+        self.slot = int(slot)
+
+    def __enter__(self):
+        self.prev = getattr(_slot, "value", 0)
+        _slot.value = self.slot
+
+    def __exit__(self, *a):
+        _slot.value = self.prev
+
+
 def ctx():
-    """Per-device library context (cuBLAS / cuSOLVER handles, solver workspace)."""
+    """Library context of the current device and slot (cuBLAS / cuSOLVER
+    handles, solver workspace)."""
     require_cuda()
-    dev = torch.cuda.current_device()
-    if dev not in _ctx:
+    key = (torch.cuda.current_device(), getattr(_slot, "value", 0))
+    if key not in _ctx:
         with _lock:
-            if dev not in _ctx:
+            if key not in _ctx:
                 h = c_vp()
                 check(lib().vmck_ctx_create(ctypes.byref(h)))
-                _ctx[dev] = h
-    return _ctx[dev]
+                _ctx[key] = h
+    return _ctx[key]
 
 
 def dtype_code(dt):

@@ -164,6 +164,34 @@ __device__ inline T warp_log_ratio(const RbmParams<T> &P, const T *th, const T *
   return s;
 }
 
+// Local energy of one sample for the Ising Hamiltonian, by the whole CTA.
+// xs must hold the configuration (visible to all threads); returns E_loc on
+// every thread.
+template <typename T>
+__device__ double eloc_ising_sample(const RbmParams<T> &P, const int8_t *xs,
+                                    const int32_t *__restrict__ edges, int n_edges, double h,
+                                    double J, T *th, T *lc, T *red, double *redd, int *redi,
+                                    T *logpsi_out) {
+  const int N = P.N;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  theta_and_logpsi(P, xs, th, lc, red, logpsi_out);
+  int same = 0;
+  for (int e = threadIdx.x; e < n_edges; e += blockDim.x)
+    same += (xs[edges[2 * e]] == xs[edges[2 * e + 1]]) ? 1 : -1;
+  int tot = block_sum(same, redi);
+  double acc = 0.0;
+  if (h != 0.0) {
+    for (int k = warp; k < N; k += nw) {
+      int site = k;
+      T d = (T)(-2 * xs[k]);
+      T lr = warp_log_ratio(P, th, lc, &site, &d, 1);
+      if (lane == 0) acc += -h * exp((double)lr);
+    }
+  }
+  if (threadIdx.x == 0) acc += J * (double)tot;
+  return block_sum(acc, redd);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(EL_THREADS) eloc_ising_kernel(
     RbmParams<T> P, const int8_t *__restrict__ x, int64_t n, const int32_t *__restrict__ edges,
@@ -176,28 +204,47 @@ __global__ void __launch_bounds__(EL_THREADS) eloc_ising_kernel(
   __shared__ T red[32];
   __shared__ double redd[32];
   __shared__ int redi[32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int64_t b = blockIdx.x; b < n; b += gridDim.x) {
     for (int i = threadIdx.x; i < N; i += blockDim.x) xs[i] = x[b * N + i];
     __syncthreads();
-    theta_and_logpsi(P, xs, th, lc, red, logpsi_out ? logpsi_out + b : nullptr);
-    int same = 0;
-    for (int e = threadIdx.x; e < n_edges; e += blockDim.x)
-      same += (xs[edges[2 * e]] == xs[edges[2 * e + 1]]) ? 1 : -1;
-    int tot = block_sum(same, redi);
-    double acc = 0.0;
-    if (h != 0.0) {
-      for (int k = warp; k < N; k += nw) {
-        int site = k;
-        T d = (T)(-2 * xs[k]);
-        T lr = warp_log_ratio(P, th, lc, &site, &d, 1);
-        if (lane == 0) acc += -h * exp((double)lr);
-      }
-    }
-    if (threadIdx.x == 0) acc += J * (double)tot;
-    double e = block_sum(acc, redd);
+    double e = eloc_ising_sample(P, xs, edges, n_edges, h, J, th, lc, red, redd, redi,
+                                 logpsi_out ? logpsi_out + b : nullptr);
     if (threadIdx.x == 0) eloc[b] = e;
     __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(EL_THREADS) batched_eloc_ising_kernel(
+    const vmck_batch_ising *__restrict__ inst, const int32_t *__restrict__ work, int n_items,
+    int32_t *queue, int spi, int max_M) {
+  extern __shared__ unsigned char smem_raw[];
+  T *th = reinterpret_cast<T *>(smem_raw);
+  T *lc = th + max_M;
+  int8_t *xs = reinterpret_cast<int8_t *>(lc + max_M);
+  __shared__ T red[32];
+  __shared__ double redd[32];
+  __shared__ int redi[32];
+  __shared__ int item_s;
+  while (true) {
+    if (threadIdx.x == 0) item_s = atomicAdd(queue, 1);
+    __syncthreads();
+    const int item = item_s;
+    __syncthreads();
+    if (item >= n_items) break;
+    const vmck_batch_ising I = inst[work[2 * item]];
+    const RbmParams<T> P = rbm_view<T>(I.params, I.N, I.M);
+    const int64_t first = work[2 * item + 1];
+    for (int q = 0; q < spi; ++q) {
+      const int64_t b = first + q;
+      if (b >= I.n) break;  // uniform across the CTA
+      for (int i = threadIdx.x; i < I.N; i += blockDim.x) xs[i] = I.x[b * I.N + i];
+      __syncthreads();
+      double e = eloc_ising_sample(P, xs, I.edges, I.n_edges, I.h, I.J, th, lc, red, redd, redi,
+                                   (T *)nullptr);
+      if (threadIdx.x == 0) I.eloc[b] = e;
+      __syncthreads();
+    }
   }
 }
 
@@ -536,4 +583,33 @@ extern "C" int vmck_rbm_jacobian(vmck_stream s, int32_t dtype, const void *tanh_
     return VMCK_ERR_UNSUPPORTED;
   }
   return check_launch("rbm_jacobian");
+}
+
+extern "C" int vmck_batched_eloc_ising(vmck_stream s, int32_t dtype, const vmck_batch_ising *inst,
+                                       int32_t n_inst, const int32_t *work, int32_t n_items,
+                                       int32_t samples_per_item, int32_t *queue, int32_t max_N,
+                                       int32_t max_M, int32_t n_ctas) {
+  VMCK_REQUIRE(inst && work && queue && n_inst > 0 && n_items >= 0 && samples_per_item > 0 &&
+                   max_N > 0 && max_M > 0 && n_ctas > 0,
+               "batched_eloc_ising arguments");
+  cudaStream_t st = as_stream(s);
+  VMCK_CUDA(cudaMemsetAsync(queue, 0, sizeof(int32_t), st));
+  const size_t es = dtype == VMCK_F64 ? 8 : 4;
+  const size_t smem = 2 * es * (size_t)max_M + align16(max_N);
+  VMCK_REQUIRE(smem <= 200 * 1024, "batched_eloc_ising: max_M too large");
+  if (dtype == VMCK_F32) {
+    VMCK_CUDA(cudaFuncSetAttribute(batched_eloc_ising_kernel<float>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    batched_eloc_ising_kernel<float><<<n_ctas, EL_THREADS, smem, st>>>(
+        inst, work, n_items, queue, samples_per_item, max_M);
+  } else if (dtype == VMCK_F64) {
+    VMCK_CUDA(cudaFuncSetAttribute(batched_eloc_ising_kernel<double>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    batched_eloc_ising_kernel<double><<<n_ctas, EL_THREADS, smem, st>>>(
+        inst, work, n_items, queue, samples_per_item, max_M);
+  } else {
+    set_last_error("batched_eloc_ising: dtype %d unsupported", dtype);
+    return VMCK_ERR_UNSUPPORTED;
+  }
+  return check_launch("batched_eloc_ising");
 }

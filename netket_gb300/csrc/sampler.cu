@@ -48,31 +48,17 @@ __device__ inline void chain_recompute(const T *__restrict__ b, const T *__restr
   __syncwarp();
 }
 
+// One chain, driven by one warp: n_discard + L sweeps of `sweep` proposals,
+// the state after each of the last L sweeps written to samples_chain (L x N).
+// b is the chain's index in its problem: it keys the Philox stream.
 template <typename T, int RULE>
-__global__ void metropolis_kernel(const T *__restrict__ params, int N, int M, int8_t *sigma,
-                                  double *log_prob, int64_t *n_accepted, int B, int sweep,
-                                  int n_discard, int L, int8_t *samples, uint32_t k0, uint32_t k1,
-                                  uint64_t counter, const int32_t *__restrict__ clusters, int C,
-                                  int wpb) {
-  extern __shared__ unsigned char smem_raw[];
+__device__ void run_chain(const T *__restrict__ params, int N, int M, int8_t *sigma_row,
+                          double *log_prob_b, int64_t *n_accepted_b, int b, int sweep,
+                          int n_discard, int L, int8_t *samples_chain, uint32_t k0, uint32_t k1,
+                          uint64_t counter, const int16_t *cl, int C, ChainSmem<T> c) {
+  const int lane = threadIdx.x & 31;
   const T *bvec = params, *W = params + M, *a = params + M + (int64_t)N * M;
-  int16_t *cl = reinterpret_cast<int16_t *>(smem_raw);
-  unsigned char *base = smem_raw + ((4 * (size_t)C + 15) & ~size_t(15));
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t per_warp = 4 * (size_t)M * sizeof(T) + ((N + 15) & ~15);
-  ChainSmem<T> c;
-  c.th = reinterpret_cast<T *>(base + warp * per_warp);
-  c.lc = c.th + M;
-  c.tn = c.lc + M;
-  c.ln = c.tn + M;
-  c.xs = reinterpret_cast<int8_t *>(c.ln + M);
-  if (RULE == 1)
-    for (int q = threadIdx.x; q < 2 * C; q += blockDim.x) cl[q] = (int16_t)clusters[q];
-  __syncthreads();
-  const int b = blockIdx.x * wpb + warp;
-  if (b >= B) return;
-
-  for (int i = lane; i < N; i += 32) c.xs[i] = sigma[(int64_t)b * N + i];
+  for (int i = lane; i < N; i += 32) c.xs[i] = sigma_row[i];
   __syncwarp();
   T logpsi;
   int hop = 0;
@@ -181,16 +167,82 @@ __global__ void metropolis_kernel(const T *__restrict__ params, int N, int M, in
       __syncwarp();
     }
     if (step >= n_discard) {
-      int8_t *dst = samples + ((int64_t)b * L + (step - n_discard)) * N;
+      int8_t *dst = samples_chain + (int64_t)(step - n_discard) * N;
       for (int i = lane; i < N; i += 32) dst[i] = c.xs[i];
     }
   }
   chain_recompute(bvec, W, a, N, M, c, &logpsi);
-  for (int i = lane; i < N; i += 32) sigma[(int64_t)b * N + i] = c.xs[i];
+  for (int i = lane; i < N; i += 32) sigma_row[i] = c.xs[i];
   if (lane == 0) {
-    log_prob[b] = 2.0 * (double)logpsi;
-    n_accepted[b] += acc_count;
+    *log_prob_b = 2.0 * (double)logpsi;
+    *n_accepted_b += acc_count;
   }
+}
+
+template <typename T, int RULE>
+__global__ void metropolis_kernel(const T *__restrict__ params, int N, int M, int8_t *sigma,
+                                  double *log_prob, int64_t *n_accepted, int B, int sweep,
+                                  int n_discard, int L, int8_t *samples, uint32_t k0, uint32_t k1,
+                                  uint64_t counter, const int32_t *__restrict__ clusters, int C,
+                                  int wpb) {
+  extern __shared__ unsigned char smem_raw[];
+  int16_t *cl = reinterpret_cast<int16_t *>(smem_raw);
+  unsigned char *base = smem_raw + ((4 * (size_t)C + 15) & ~size_t(15));
+  const int warp = threadIdx.x >> 5;
+  const size_t per_warp = 4 * (size_t)M * sizeof(T) + ((N + 15) & ~15);
+  ChainSmem<T> c;
+  c.th = reinterpret_cast<T *>(base + warp * per_warp);
+  c.lc = c.th + M;
+  c.tn = c.lc + M;
+  c.ln = c.tn + M;
+  c.xs = reinterpret_cast<int8_t *>(c.ln + M);
+  if (RULE == 1)
+    for (int q = threadIdx.x; q < 2 * C; q += blockDim.x) cl[q] = (int16_t)clusters[q];
+  __syncthreads();
+  const int b = blockIdx.x * wpb + warp;
+  if (b >= B) return;
+  run_chain<T, RULE>(params, N, M, sigma + (int64_t)b * N, log_prob + b, n_accepted + b, b, sweep,
+                     n_discard, L, samples + (int64_t)b * L * N, k0, k1, counter, cl, C, c);
+}
+
+// Persistent batched sampler: CTAs pull (instance, first chain) items.
+template <typename T>
+__global__ void batched_metropolis_kernel(const vmck_batch_chains *__restrict__ inst,
+                                          const int32_t *__restrict__ work, int n_items,
+                                          int32_t *queue, int n_discard, int L, int max_N,
+                                          int max_M) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ int item_s;
+  const int warp = threadIdx.x >> 5;
+  const size_t per_warp = 4 * (size_t)max_M * sizeof(T) + ((max_N + 15) & ~15);
+  unsigned char *mine = smem_raw + warp * per_warp;
+  while (true) {
+    if (threadIdx.x == 0) item_s = atomicAdd(queue, 1);
+    __syncthreads();
+    const int item = item_s;
+    __syncthreads();
+    if (item >= n_items) break;
+    const int i = work[2 * item];
+    const vmck_batch_chains I = inst[i];
+    const int b = work[2 * item + 1] + warp;
+    if (b < I.n_chains) {
+      ChainSmem<T> c;
+      c.th = reinterpret_cast<T *>(mine);
+      c.lc = c.th + I.M;
+      c.tn = c.lc + I.M;
+      c.ln = c.tn + I.M;
+      c.xs = reinterpret_cast<int8_t *>(c.ln + I.M);
+      run_chain<T, 0>(static_cast<const T *>(I.params), I.N, I.M, I.sigma + (int64_t)b * I.N,
+                      I.log_prob + b, I.n_accepted + b, b, I.sweep_size, n_discard, L,
+                      I.samples + (int64_t)b * L * I.N, (uint32_t)I.seed,
+                      (uint32_t)(I.seed >> 32), I.counter, nullptr, 0, c);
+    }
+  }
+}
+
+__global__ void batch_advance_counters_kernel(vmck_batch_chains *inst, int n_inst, int steps) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_inst) inst[i].counter += (uint64_t)steps * (uint64_t)inst[i].sweep_size;
 }
 
 template <typename T>
@@ -253,4 +305,43 @@ extern "C" int vmck_metropolis_sample(vmck_stream s, int32_t dtype, const void *
                                     n_clusters);
   set_last_error("metropolis_sample: dtype %d unsupported", dtype);
   return VMCK_ERR_UNSUPPORTED;
+}
+
+extern "C" int vmck_batched_metropolis_local(vmck_stream s, int32_t dtype, vmck_batch_chains *inst,
+                                             int32_t n_inst, const int32_t *work, int32_t n_items,
+                                             int32_t chains_per_item, int32_t *queue,
+                                             int32_t n_discard, int32_t chain_length,
+                                             int32_t max_N, int32_t max_M, int32_t n_ctas) {
+  VMCK_REQUIRE(inst && work && queue && n_inst > 0 && n_items >= 0 && chains_per_item > 0 &&
+                   chains_per_item <= 32 && max_N > 0 && max_N < 32768 && max_M > 0 && n_ctas > 0,
+               "batched_metropolis arguments");
+  VMCK_REQUIRE(n_discard >= 0 && chain_length >= 0, "batched_metropolis lengths");
+  cudaStream_t st = as_stream(s);
+  VMCK_CUDA(cudaMemsetAsync(queue, 0, sizeof(int32_t), st));
+  const size_t es = dtype == VMCK_F64 ? 8 : 4;
+  const size_t per_warp = 4 * (size_t)max_M * es + ((max_N + 15) & ~15);
+  const size_t smem = per_warp * chains_per_item;
+  VMCK_REQUIRE(smem <= 200 * 1024, "batched_metropolis: max_M too large");
+  const int threads = 32 * chains_per_item;
+  if (dtype == VMCK_F32) {
+    VMCK_CUDA(cudaFuncSetAttribute(batched_metropolis_kernel<float>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    batched_metropolis_kernel<float><<<n_ctas, threads, smem, st>>>(inst, work, n_items, queue,
+                                                                     n_discard, chain_length,
+                                                                     max_N, max_M);
+  } else if (dtype == VMCK_F64) {
+    VMCK_CUDA(cudaFuncSetAttribute(batched_metropolis_kernel<double>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    batched_metropolis_kernel<double><<<n_ctas, threads, smem, st>>>(inst, work, n_items, queue,
+                                                                      n_discard, chain_length,
+                                                                      max_N, max_M);
+  } else {
+    set_last_error("batched_metropolis: dtype %d unsupported", dtype);
+    return VMCK_ERR_UNSUPPORTED;
+  }
+  int rc = check_launch("batched_metropolis");
+  if (rc) return rc;
+  batch_advance_counters_kernel<<<ceil_div(n_inst, 128), 128, 0, st>>>(inst, n_inst,
+                                                                      n_discard + chain_length);
+  return check_launch("batched counters");
 }
