@@ -19,6 +19,7 @@ from . import vqs
 from . import driver
 from . import exact
 from . import batched
+from . import serving
 
-__all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd", "batched",
+__all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd", "batched", "serving",
            "optimizer", "vqs", "driver", "exact"]
