@@ -45,6 +45,17 @@ WORKLOAD = {
 METRIC = "VMC steps/s"
 
 
+def workload_config(args, world):
+    cfg = dict(WORKLOAD, precision=args.precision, parallelism=f"replicas{world}",
+               l2="per-step working set > L2: T64 2.1 GB + T32 1.1 GB")
+    if (args.n_chains, args.n_samples) != (WORKLOAD["n_chains"], WORKLOAD["n_samples"]):
+        n = args.n_samples
+        cfg.update(workload=f"j1j2_10x10_minsr_n{n}", n_chains=args.n_chains, n_samples=n,
+                   solver=f"minSR, T {n}x{n}, diag_shift=1e-4",
+                   l2=f"T64 {8 * n * n / 1e9:.2f} GB + T32 {4 * n * n / 1e9:.2f} GB")
+    return cfg
+
+
 def build_problem(nk, precision, seed=0, n_chains=4096, n_samples=16384):
     g = nk.graph.Square(10, max_neighbor_order=2)
     hi = nk.hilbert.Spin(0.5, N=100, total_sz=0)
@@ -136,7 +147,8 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    H, vs, drv = build_problem(nk, args.precision, seed=rank)
+    H, vs, drv = build_problem(nk, args.precision, seed=rank, n_chains=args.n_chains,
+                               n_samples=args.n_samples)
     drv.advance(args.warmup)
     barrier()
     L = _native.lib()
@@ -190,7 +202,8 @@ def run_ours(args):
     # ---------------- the plain FP32 GPU path (reference algorithm on the GPU)
     plain = None
     if args.plain_steps > 0:
-        _, vs32, drv32 = build_problem(nk, "fp32", seed=rank)
+        _, vs32, drv32 = build_problem(nk, "fp32", seed=rank, n_chains=args.n_chains,
+                                       n_samples=args.n_samples)
         vs32.local_estimator = "dense"
         drv32.gram = "dense"
         drv32.solve = "cholesky"
@@ -215,7 +228,7 @@ def run_ours(args):
             dist.destroy_process_group()
         return None
     gram_ms = phases.get("gram")
-    n = 16384
+    n = vs.n_samples
     flops = float(n) * (n + 1) * 400  # lower triangle of t t^T (n x n x M), 2 flop per FMA
     roof = None
     if gram_ms:
@@ -234,9 +247,8 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if args.precision == "mixed" else args.precision, "data": "synthetic",
-        "config": dict(WORKLOAD, precision=args.precision, parallelism=f"replicas{world}",
-                       l2="per-step working set > L2: T64 2.1 GB + T32 1.1 GB"),
-        "samples_per_s": round(value * 16384, 1),
+        "config": workload_config(args, world),
+        "samples_per_s": round(value * n, 1),
         "energy_per_site": round(energy, 8),
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         "plain_fp32": plain,
@@ -345,6 +357,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     ap.add_argument("--plain-steps", type=int, default=4)
+    ap.add_argument("--n-chains", type=int, default=WORKLOAD["n_chains"],
+                    help="smaller cases for profiling; the metric is quoted at the default")
+    ap.add_argument("--n-samples", type=int, default=WORKLOAD["n_samples"])
     ap.add_argument("--cpu-samples", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gram-traffic", type=float, default=None)
