@@ -298,9 +298,12 @@ int vmck_cholesky_solve(vmck_ctx *ctx, vmck_stream s, int32_t dtype, const void 
  * FP64 matrix A64 (lower triangle): max_iter correction solves, each from the
  * FP64 residual b - A64 x; the final relative residual goes to residual_out
  * (device, nullable) and VMCK_DEV_NO_CONVERGE is raised if it exceeds tol.
+ * The residual is evaluated in double-float arithmetic (~2^-46 per term).
  * factor_mode 0: cuSOLVER SPOTRF; 1: cuSOLVER SPOTRF with FP32-accurate BF16x9
  * tensor-core emulation; 2: recursive Cholesky whose TRSM / SYRK are recursive
- * GEMMs on BF16x9-emulated tensor cores (cuSOLVER / cuBLAS at <= 1024 leaves). */
+ * GEMMs on BF16x9-emulated tensor cores (cuSOLVER / cuBLAS at <= 1024 leaves);
+ * 3: blocked right-looking Cholesky (512-row panels, this library's 128 x 128
+ * leaf kernel, emulated-GEMM panel solves and trailing updates). */
 int vmck_cholesky_solve_refined(vmck_ctx *ctx, vmck_stream s, const double *A64,
                                 float *A32, const double *b, double *x, int64_t n,
                                 int32_t max_iter, double tol, int32_t factor_mode,

@@ -102,6 +102,15 @@ __device__ __forceinline__ float log_cosh_fast(float x) {
 }
 __device__ __forceinline__ double log_cosh_fast(double x) { return log_cosh(x); }
 
+// exp of a log-amplitude ratio in a local-energy sum: in FP32 (one accurate
+// expf) when the ratio cannot overflow, else in double.  GB300's FP64 pipe is
+// narrow enough that a double exp per connected element dominated the FP32
+// local-energy kernels.
+__device__ __forceinline__ double exp_ratio(float x) {
+  return x < 80.0f ? (double)expf(x) : exp((double)x);
+}
+__device__ __forceinline__ double exp_ratio(double x) { return exp(x); }
+
 // ----------------------------------------------------------------- double-float
 // Pairs (hi, lo) of FP32 values carrying ~48 significant bits, with the
 // error-free transformations of Knuth (TwoSum) and Dekker (TwoProduct via FMA).

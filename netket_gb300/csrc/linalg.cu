@@ -30,6 +30,12 @@ struct vmck_ctx {
   void *aux = nullptr;
   size_t aux_bytes = 0;
   int *d_info = nullptr;
+  // look-ahead Cholesky: a second stream / cuBLAS handle for the trailing
+  // updates and a pool of events (two per panel), created on first use
+  cudaStream_t side = nullptr;
+  cublasHandle_t blas2 = nullptr;
+  cudaEvent_t *events = nullptr;
+  int n_events = 0;
 };
 
 namespace vmck {
@@ -181,17 +187,520 @@ __global__ void sgd_kernel(double *p, const double *u, int64_t P, double lr, flo
 // Upper Cholesky A = U^T U of a column-major FP32 matrix (our row-major lower
 // triangle), in place, by recursive halving (Gustavson / Elmroth style): every
 // flop outside the leaves is a GEMM, and the GEMMs run with cuBLAS'
-// FP32-accurate BF16x9 tensor-core emulation.  Leaves (<= CHOL_LEAF) use
-// cuSOLVER POTRF, cuBLAS TRSM / SYRK.
+// FP32-accurate BF16x9 tensor-core emulation.  Leaves (<= R.leaf) use
+// cuSOLVER POTRF (factor_mode 2) or potrf_leaf_kernel (factor_mode 3), and
+// cuBLAS TRSM / SYRK.
 constexpr int64_t CHOL_LEAF = 1024;
+constexpr int LEAF_B = 128;        // potrf_leaf_kernel block
+constexpr int LEAF_THREADS = 512;
+constexpr int64_t PANEL_W = 512;   // blocked factorization panel
+constexpr int64_t STRIP_W = 2048;  // trailing-update GEMM strip width
 
 static int64_t half_split(int64_t n) {
   int64_t h = ((n / 2) + 255) / 256 * 256;
-  return (h >= n) ? n / 2 : h;
+  if (h >= n) h = ((n / 2) + LEAF_B - 1) / LEAF_B * LEAF_B;
+  return (h >= n || h <= 0) ? n / 2 : h;
 }
 
 __global__ void info_accumulate_kernel(const int *info, int32_t *status) {
   if (*info != 0 && status) atomicOr(status, VMCK_DEV_NOT_SPD);
+}
+
+// Leaf kernels of the blocked Cholesky.  Both keep a b x b (b <= 128) upper
+// factor in shared memory as Us[i * LEAF_LD + j] (row i, column j, i <= j; rows
+// 16-byte aligned) and work in 32-row panels:
+//   (a) a latency-bound 32-wide step done in registers with warp shuffles,
+//   (b) a rank-32 update of what remains, as 4 x 4 register tiles.
+constexpr int LEAF_LD = LEAF_B + 4;
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+// Load the upper triangle of the b x b column-major block A (lda) into Us
+// (LEAF_ROWS x LEAF_LD), zeros elsewhere: the 4 x 4 tiles of a block whose size
+// is not a multiple of 4 run up to 3 rows / columns past it.
+constexpr int LEAF_ROWS = LEAF_B + 4;
+__device__ inline void leaf_load_upper(float *Us, const float *A, int64_t lda, int b) {
+  constexpr int TOTAL = LEAF_ROWS * LEAF_LD, BATCH = 8;
+  for (int e0 = threadIdx.x; e0 < TOTAL; e0 += BATCH * blockDim.x) {
+    float v[BATCH];
+#pragma unroll
+    for (int u = 0; u < BATCH; ++u) {  // issue all loads of the batch first
+      const int e = e0 + u * blockDim.x;
+      const int j = e / LEAF_ROWS, i = e - j * LEAF_ROWS;
+      v[u] = (e < TOTAL && i <= j && j < b) ? A[(int64_t)j * lda + i] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < BATCH; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int j = e / LEAF_ROWS, i = e - j * LEAF_ROWS;
+      if (e < TOTAL) Us[i * LEAF_LD + j] = v[u];
+    }
+  }
+}
+
+// Store the upper triangle of Us back to the b x b column-major block A.
+__device__ inline void leaf_store_upper(const float *Us, float *A, int64_t lda, int b) {
+  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+    const int j = e / b, i = e - j * b;
+    if (i <= j) A[(int64_t)j * lda + i] = Us[i * LEAF_LD + j];
+  }
+}
+
+// Forward substitution U_pp^T X = V for one 32-row panel (rows p..p+pw-1) of a
+// column held by 4 consecutive lanes: lane quarter q owns rows p + 8q .. p + 8q + 7
+// (v[0..7]), so its slice of a row of U_pp is two 16-byte loads.  rinv[i] =
+// 1 / u_ii.  All 32 lanes of the warp must call it; p is a multiple of 32.
+__device__ __forceinline__ void panel_forward(const float *Us, const float *rinv, int p, int pw,
+                                              int q, float (&v)[8]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    if (k < pw) {
+      const float mine = v[k & 7] * rinv[p + k];
+      const float x = __shfl_sync(FULL_MASK, mine, (lane & ~3) | (k >> 3));
+      if (q == (k >> 3)) v[k & 7] = x;
+      if (8 * q + 7 > k) {  // rows of this quarter below k
+        const float4 u0 = *reinterpret_cast<const float4 *>(&Us[(p + k) * LEAF_LD + p + 8 * q]);
+        const float4 u1 = *reinterpret_cast<const float4 *>(&Us[(p + k) * LEAF_LD + p + 8 * q + 4]);
+        const float uv[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+          if (8 * q + r > k && 8 * q + r < pw) v[r] = __fmaf_rn(-uv[r], x, v[r]);
+      }
+    }
+  }
+}
+
+// Right-looking upper Cholesky of one b x b diagonal block (b <= 128) of a
+// column-major matrix.  Per 32-row panel: (a) warp 0 factors the 32 x 32
+// diagonal block in registers (lane l holds column l; the unused part of a short
+// panel is padded with the identity), (b) four lanes per column solve the panel
+// row, (c) rank-32 update of the trailing block.  A non-positive (or NaN) pivot
+// sets VMCK_DEV_NOT_SPD and is replaced by 1; the caller falls back on the
+// status word.
+__global__ void __launch_bounds__(LEAF_THREADS) potrf_leaf_kernel(float *A, int64_t lda, int b,
+                                                                  int32_t *status) {
+  extern __shared__ __align__(16) float Us[];
+  __shared__ float rinv[LEAF_B];
+  __shared__ __align__(16) float rowk[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  leaf_load_upper(Us, A, lda, b);
+  __syncthreads();
+  bool bad = false;
+  for (int p = 0; p < b; p += 32) {
+    const int pw = (b - p) < 32 ? (b - p) : 32;
+    if (warp == 0) {  // (a) lane l holds column p + l of the 32 x 32 diagonal block
+      float col[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        col[i] = (lane < pw && i <= lane) ? Us[(p + i) * LEAF_LD + p + lane] : (i == lane ? 1.0f : 0.0f);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const float d = __shfl_sync(FULL_MASK, col[k], k);
+        const bool ok = d > 0.0f;
+        if (k < pw) bad |= !ok;
+        const float ri = ok ? rsqrtf(d) : 1.0f;
+        col[k] = (lane == k) ? (ok ? d * ri : 1.0f) : col[k] * ri;  // row k scaled
+        if (k < 31) {  // rank-1 update of the rows below k; lanes left of a row update
+                       // lower-triangle entries, which are never read
+          rowk[lane] = col[k];
+          __syncwarp();
+          float rv[32];
+#pragma unroll
+          for (int g = 0; g < 8; ++g) {
+            const float4 t = reinterpret_cast<const float4 *>(rowk)[g];
+            rv[4 * g] = t.x;
+            rv[4 * g + 1] = t.y;
+            rv[4 * g + 2] = t.z;
+            rv[4 * g + 3] = t.w;
+          }
+#pragma unroll
+          for (int i = k + 1; i < 32; ++i) col[i] = __fmaf_rn(-rv[i], col[k], col[i]);
+          __syncwarp();
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        if (lane < pw && i <= lane) Us[(p + i) * LEAF_LD + p + lane] = col[i];
+      float dl = 1.0f;
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        if (i == lane) dl = col[i];
+      if (lane < pw) rinv[p + lane] = 1.0f / dl;
+    }
+    __syncthreads();
+    const int m = b - p - pw;  // trailing size
+    if (m <= 0) break;
+    {  // (b) panel row: 4 lanes per column j = p + pw + c
+      const int c = tid >> 2, q = tid & 3;
+      if (warp < (m + 7) / 8) {  // whole warps, 8 columns each
+        const bool valid = c < m;
+        const int j = p + pw + (valid ? c : 0);
+        float v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = (valid && 8 * q + r < pw) ? Us[(p + 8 * q + r) * LEAF_LD + j] : 0.0f;
+        panel_forward(Us, rinv, p, pw, q, v);
+        if (valid) {
+#pragma unroll
+          for (int r = 0; r < 8; ++r)
+            if (8 * q + r < pw) Us[(p + 8 * q + r) * LEAF_LD + j] = v[r];
+        }
+      }
+    }
+    __syncthreads();
+    {  // (c) U(i, j) -= sum_k X(p+k, i) X(p+k, j), 4 x 4 tiles with ti <= tj
+      const int nt = (m + 3) / 4, base = p + pw;
+      for (int t = tid; t < nt * nt; t += blockDim.x) {
+        const int ti = t / nt, tj = t - ti * nt;
+        if (ti > tj) continue;
+        const int i0 = base + 4 * ti, j0 = base + 4 * tj;
+        float acc[4][4] = {};
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+          const float4 a = *reinterpret_cast<const float4 *>(&Us[(p + k) * LEAF_LD + i0]);
+          const float4 bb = *reinterpret_cast<const float4 *>(&Us[(p + k) * LEAF_LD + j0]);
+          const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {bb.x, bb.y, bb.z, bb.w};
+#pragma unroll
+          for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int y = 0; y < 4; ++y) acc[x][y] = __fmaf_rn(av[x], bv[y], acc[x][y]);
+        }
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) Us[(i0 + x) * LEAF_LD + j0 + y] -= acc[x][y];
+      }
+    }
+    __syncthreads();
+  }
+  if (__syncthreads_or(bad) && tid == 0 && status) atomicOr(status, VMCK_DEV_NOT_SPD);
+  leaf_store_upper(Us, A, lda, b);
+}
+
+// B (m x nrhs, column-major) <- U^-T B for the m x m upper factor U (m <= 128)
+// of one leaf.  CTA c solves columns [64c, 64c + 64) with U and its column block
+// (Bs[k * TRSM_LD + c]) in shared memory, in the same 32-row panels: (a) four
+// lanes per column do the forward substitution of the panel, (b) a rank-32
+// update of the rows below.
+constexpr int TRSM_COLS = 64;
+constexpr int TRSM_LD = TRSM_COLS + 4;
+
+// Forward substitution Us^T X = Bs in place for an m x m upper Us (m <= 128) and a
+// 64-column Bs[k * TRSM_LD + c] in shared memory; rinv[i] = 1 / u_ii.
+__device__ void leaf_trsm_core(const float *Us, float *Bs, const float *rinv, int m) {
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int p = 0; p < m; p += 32) {
+    const int pw = (m - p) < 32 ? (m - p) : 32;
+    if (warp < 8) {  // (a) 256 threads: column c = tid >> 2, quarter q = tid & 3
+      const int c = tid >> 2, q = tid & 3;
+      float v[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = (8 * q + r < pw) ? Bs[(p + 8 * q + r) * TRSM_LD + c] : 0.0f;
+      panel_forward(Us, rinv, p, pw, q, v);
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+        if (8 * q + r < pw) Bs[(p + 8 * q + r) * TRSM_LD + c] = v[r];
+    }
+    __syncthreads();
+    const int rows = m - p - pw;
+    if (rows <= 0) break;
+    {  // (b) B(i, c) -= sum_k U(p+k, i) X(p+k, c), 4 x 4 tiles
+      const int nti = (rows + 3) / 4, base = p + pw;
+      for (int t = tid; t < nti * (TRSM_COLS / 4); t += blockDim.x) {
+        const int ti = t / (TRSM_COLS / 4), tc = t - ti * (TRSM_COLS / 4);
+        const int i0 = base + 4 * ti, cc0 = 4 * tc;
+        float acc[4][4] = {};
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+          const float4 a = *reinterpret_cast<const float4 *>(&Us[(p + k) * LEAF_LD + i0]);
+          const float4 x = *reinterpret_cast<const float4 *>(&Bs[(p + k) * TRSM_LD + cc0]);
+          const float av[4] = {a.x, a.y, a.z, a.w}, xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int y = 0; y < 4; ++y) acc[u][y] = __fmaf_rn(av[u], xv[y], acc[u][y]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) Bs[(i0 + u) * TRSM_LD + cc0 + y] -= acc[u][y];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(LEAF_THREADS) trsm_leaf_kernel(const float *__restrict__ Ug,
+                                                                 int64_t ldu, int m, float *B,
+                                                                 int64_t ldb, int64_t nrhs) {
+  extern __shared__ __align__(16) float sm[];
+  float *Us = sm;                         // LEAF_ROWS x LEAF_LD
+  float *Bs = sm + LEAF_ROWS * LEAF_LD;   // LEAF_ROWS x TRSM_LD
+  __shared__ float rinv[LEAF_B];
+  const int tid = threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.x * TRSM_COLS;
+  const int nc = (int)((nrhs - c0) < TRSM_COLS ? (nrhs - c0) : TRSM_COLS);
+  leaf_load_upper(Us, Ug, ldu, m);
+  {
+    constexpr int TOTAL = TRSM_LD * LEAF_ROWS, BATCH = 8;
+    for (int e0 = tid; e0 < TOTAL; e0 += BATCH * blockDim.x) {
+      float v[BATCH];
+#pragma unroll
+      for (int u = 0; u < BATCH; ++u) {
+        const int e = e0 + u * blockDim.x;
+        const int c = e / LEAF_ROWS, k = e - c * LEAF_ROWS;
+        v[u] = (e < TOTAL && c < nc && k < m) ? B[(c0 + c) * ldb + k] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < BATCH; ++u) {
+        const int e = e0 + u * blockDim.x;
+        const int c = e / LEAF_ROWS, k = e - c * LEAF_ROWS;
+        if (e < TOTAL) Bs[k * TRSM_LD + c] = v[u];
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < m) rinv[tid] = 1.0f / Us[tid * LEAF_LD + tid];
+  __syncthreads();
+  leaf_trsm_core(Us, Bs, rinv, m);
+  for (int e = tid; e < TRSM_COLS * m; e += blockDim.x) {
+    const int c = e / m, k = e - c * m;
+    if (c < nc) B[(c0 + c) * ldb + k] = Bs[k * TRSM_LD + c];
+  }
+}
+
+// ------------------------------------------------------------ blocked triangular solves
+// U^T y = r and U x = y for the FP32 upper factor U (column-major, ld n) in
+// 128-row blocks, for the refinement loop.  trsv_inv_kernel stores
+// Y_K = U_KK^-T (lower, column-major 128 x 128, zero-padded) for every diagonal
+// block, so a block's own solve is a 128 x 128 product.  The two solve kernels
+// are persistent: CTAs take block tickets in order from an atomic counter, so
+// every block a CTA waits for has been claimed by a CTA that is already running
+// and that never waits for a later block; a finished block is published with a
+// release store of the call's epoch into its flag.  Waits are bounded
+// (TRSV_WAIT_NS of wall time); a wait that runs out raises VMCK_DEV_TIMEOUT and
+// sets the abort word, which makes every other wait give up at once.
+constexpr int TB = 128;
+constexpr unsigned long long TRSV_WAIT_NS = 2000000000ull;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long wall_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Every lane of the warp spins; returns false if the solve was aborted.
+__device__ __forceinline__ bool trsv_wait(const unsigned *flag, unsigned epoch, unsigned *abort_w,
+                          int32_t *status) {
+  const unsigned long long t0 = wall_ns();
+  for (unsigned it = 0;; ++it) {
+    if (ld_acquire_u32(flag) == epoch) return true;
+    if (ld_acquire_u32(abort_w) == epoch) return false;
+    if ((it & 63) == 63 && wall_ns() - t0 > TRSV_WAIT_NS) {
+      if (status) atomicOr(status, VMCK_DEV_TIMEOUT);
+      atomicExch(abort_w, epoch);
+      return false;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(LEAF_THREADS) trsv_inv_kernel(const float *__restrict__ U,
+                                                                int64_t n, float *Yinv) {
+  extern __shared__ __align__(16) float sm[];
+  float *Us = sm;
+  float *Bs = sm + LEAF_ROWS * LEAF_LD;
+  __shared__ float rinv[LEAF_B];
+  const int tid = threadIdx.x;
+  const int64_t K = blockIdx.y, k0 = K * TB;
+  const int m = (int)((n - k0) < TB ? (n - k0) : TB);
+  const int cbase = blockIdx.x * TRSM_COLS;  // identity columns [cbase, cbase + 64)
+  leaf_load_upper(Us, U + k0 + k0 * n, n, m);
+  for (int e = tid; e < TRSM_LD * LEAF_ROWS; e += blockDim.x) {
+    const int c = e / LEAF_ROWS, k = e - c * LEAF_ROWS;
+    Bs[k * TRSM_LD + c] = (c < TRSM_COLS && k < m && k == cbase + c) ? 1.0f : 0.0f;
+  }
+  __syncthreads();
+  if (tid < m) rinv[tid] = 1.0f / Us[tid * LEAF_LD + tid];
+  __syncthreads();
+  leaf_trsm_core(Us, Bs, rinv, m);
+  float *Y = Yinv + K * TB * TB;
+  for (int e = tid; e < TRSM_COLS * TB; e += blockDim.x) {
+    const int c = e / TB, k = e - c * TB;
+    Y[(int64_t)(cbase + c) * TB + k] = (k < m && cbase + c < m) ? Bs[k * TRSM_LD + c] : 0.0f;
+  }
+}
+
+struct TrsvSync {
+  unsigned *flags;   // nb
+  unsigned *ticket;  // 1
+  unsigned *abort_w; // 1
+};
+
+// y = U^-T r.  Block K: z = r_K - sum_{J<K} U_JK^T y_J (warp w: columns 8w..8w+7 of
+// block K, each a 128-long contiguous column segment per J), then y_K = Y_K z.
+__global__ void __launch_bounds__(LEAF_THREADS) trsv_fwd_kernel(const float *__restrict__ U,
+                                                                int64_t n,
+                                                                const float *__restrict__ Yinv,
+                                                                const float *__restrict__ r,
+                                                                float *y, TrsvSync sy,
+                                                                unsigned epoch, int32_t *status) {
+  __shared__ float z[TB];
+  __shared__ float part[4][TB];
+  __shared__ int K_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nb = (int)((n + TB - 1) / TB);
+  while (true) {
+    __syncthreads();
+    if (tid == 0) K_s = (int)atomicAdd(sy.ticket, 1u);
+    __syncthreads();
+    const int K = K_s;
+    if (K >= nb) break;
+    const int64_t k0 = (int64_t)K * TB;
+    const int mk = (int)((n - k0) < TB ? (n - k0) : TB);
+    float acc[8] = {};
+    bool alive = true;
+    for (int J = 0; J < K && alive; ++J) {
+      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status);
+      if (!alive) break;
+      const float4 yj = __ldcg(reinterpret_cast<const float4 *>(y + (int64_t)J * TB) + lane);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int c = 8 * warp + q;
+        if (c < mk) {
+          const float4 u = __ldg(reinterpret_cast<const float4 *>(U + (k0 + c) * n + (int64_t)J * TB) + lane);
+          acc[q] = __fmaf_rn(u.x, yj.x, __fmaf_rn(u.y, yj.y, __fmaf_rn(u.z, yj.z, __fmaf_rn(u.w, yj.w, acc[q]))));
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float v = warp_sum(acc[q]);
+      const int c = 8 * warp + q;
+      if (lane == 0) z[c] = (c < mk) ? r[k0 + c] - v : 0.0f;
+    }
+    __syncthreads();
+    {  // y_K[c] = sum_c' Y_K(c, c') z[c'], thread (h, c): c' in [32h, 32h + 32)
+      const int c = tid & (TB - 1), h = tid >> 7;
+      const float *Y = Yinv + (int64_t)K * TB * TB;
+      float sacc = 0.0f;
+#pragma unroll 8
+      for (int i = 0; i < 32; ++i) sacc = __fmaf_rn(Y[(32 * h + i) * TB + c], z[32 * h + i], sacc);
+      part[h][c] = sacc;
+    }
+    __syncthreads();
+    if (tid < mk) {
+      __stcg(y + k0 + tid, (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+      __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) st_release_u32(sy.flags + K, epoch);
+  }
+}
+
+// x = U^-1 y.  Block K (taken from the last): w = y_K - sum_{J>K} U_KJ x_J (warp w:
+// columns 8w..8w+7 of every later block J; lane: rows 4 lane..4 lane+3), then
+// x_K = Y_K^T w.
+__global__ void __launch_bounds__(LEAF_THREADS) trsv_bwd_kernel(const float *__restrict__ U,
+                                                                int64_t n,
+                                                                const float *__restrict__ Yinv,
+                                                                const float *__restrict__ yv,
+                                                                float *x, TrsvSync sy,
+                                                                unsigned epoch, int32_t *status) {
+  __shared__ __align__(16) float wv[TB];
+  __shared__ float part[16][TB];
+  __shared__ int K_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nb = (int)((n + TB - 1) / TB);
+  while (true) {
+    __syncthreads();
+    if (tid == 0) K_s = nb - 1 - (int)atomicAdd(sy.ticket, 1u);
+    __syncthreads();
+    const int K = K_s;
+    if (K < 0) break;
+    const int64_t k0 = (int64_t)K * TB;
+    const int mk = (int)((n - k0) < TB ? (n - k0) : TB);
+    const bool full = (4 * lane + 3) < mk;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    bool alive = true;
+    for (int J = nb - 1; J > K && alive; --J) {
+      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status);
+      if (!alive) break;
+      const int64_t j0 = (int64_t)J * TB;
+      const int mj = (int)((n - j0) < TB ? (n - j0) : TB);
+      float xs[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) xs[q] = (8 * warp + q < mj) ? __ldcg(x + j0 + 8 * warp + q) : 0.0f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int cj = 8 * warp + q;
+        if (cj < mj) {
+          const float xj = xs[q];
+          const float *col = U + (j0 + cj) * n + k0;
+          if (full) {
+            const float4 u = __ldg(reinterpret_cast<const float4 *>(col) + lane);
+            a0 = __fmaf_rn(u.x, xj, a0);
+            a1 = __fmaf_rn(u.y, xj, a1);
+            a2 = __fmaf_rn(u.z, xj, a2);
+            a3 = __fmaf_rn(u.w, xj, a3);
+          } else {
+            const int rr = 4 * lane;
+            if (rr < mk) a0 = __fmaf_rn(col[rr], xj, a0);
+            if (rr + 1 < mk) a1 = __fmaf_rn(col[rr + 1], xj, a1);
+            if (rr + 2 < mk) a2 = __fmaf_rn(col[rr + 2], xj, a2);
+          }
+        }
+      }
+    }
+    part[warp][4 * lane] = a0;
+    part[warp][4 * lane + 1] = a1;
+    part[warp][4 * lane + 2] = a2;
+    part[warp][4 * lane + 3] = a3;
+    __syncthreads();
+    if (tid < TB) {
+      float sum = 0.0f;
+#pragma unroll
+      for (int w = 0; w < 16; ++w) sum += part[w][tid];
+      wv[tid] = (tid < mk) ? yv[k0 + tid] - sum : 0.0f;
+    }
+    __syncthreads();
+    {  // x_K[c] = sum_c' Y_K(c', c) w[c'] (column c of Y_K is contiguous): warp per 8 c
+      const float *Y = Yinv + (int64_t)K * TB * TB;
+      const float4 w4 = reinterpret_cast<const float4 *>(wv)[lane];
+      float4 yc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        yc[q] = __ldg(reinterpret_cast<const float4 *>(Y + (int64_t)(8 * warp + q) * TB) + lane);
+      float v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        v[q] = warp_sum(yc[q].x * w4.x + yc[q].y * w4.y + yc[q].z * w4.z + yc[q].w * w4.w);
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (8 * warp + q < mk) __stcg(x + k0 + 8 * warp + q, v[q]);
+        __threadfence();
+      }
+    }
+    __syncthreads();
+    if (tid == 0) st_release_u32(sy.flags + K, epoch);
+  }
+}
+
+constexpr size_t LEAF_SMEM = (size_t)LEAF_ROWS * LEAF_LD * sizeof(float);
+constexpr size_t TRSM_SMEM = (size_t)LEAF_ROWS * (LEAF_LD + TRSM_LD) * sizeof(float);
+
+static int num_sms() {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
 }
 
 struct RecChol {
@@ -199,13 +708,15 @@ struct RecChol {
   cudaStream_t st;
   int32_t *status;
   size_t dsize, hsize;
+  int64_t leaf;
+  bool own_leaf;
 };
 
 // C (n x n, upper) -= A^T A with A (k x n)
 static int syrk_rec(RecChol &R, float *C, int64_t ldc, int64_t n, const float *A, int64_t lda,
                     int64_t k) {
   const float mone = -1.0f, one = 1.0f;
-  if (n <= CHOL_LEAF) {
+  if (n <= R.leaf) {
     VMCK_BLAS(cublasSsyrk(R.c->blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, (int)n, (int)k, &mone, A,
                           (int)lda, &one, C, (int)ldc));
     return VMCK_OK;
@@ -222,7 +733,12 @@ static int syrk_rec(RecChol &R, float *C, int64_t ldc, int64_t n, const float *A
 static int trsm_rec(RecChol &R, const float *U, int64_t ldu, int64_t m, float *B, int64_t ldb,
                     int64_t nrhs) {
   const float mone = -1.0f, one = 1.0f;
-  if (m <= CHOL_LEAF) {
+  if (m <= R.leaf && R.own_leaf) {
+    trsm_leaf_kernel<<<(unsigned)((nrhs + TRSM_COLS - 1) / TRSM_COLS), LEAF_THREADS, TRSM_SMEM,
+                       R.st>>>(U, ldu, (int)m, B, ldb, nrhs);
+    return check_launch("trsm leaf");
+  }
+  if (m <= R.leaf) {
     VMCK_BLAS(cublasStrsm(R.c->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
                           CUBLAS_DIAG_NON_UNIT, (int)m, (int)nrhs, &one, U, (int)ldu, B, (int)ldb));
     return VMCK_OK;
@@ -236,7 +752,12 @@ static int trsm_rec(RecChol &R, const float *U, int64_t ldu, int64_t m, float *B
 }
 
 static int chol_rec(RecChol &R, float *A, int64_t lda, int64_t n) {
-  if (n <= CHOL_LEAF) {
+  if (n <= R.leaf) {
+    if (R.own_leaf) {
+      potrf_leaf_kernel<<<1, LEAF_THREADS, LEAF_SMEM, R.st>>>(
+          A, lda, (int)n, R.status);
+      return check_launch("cholesky leaf");
+    }
     VMCK_SOLVER(cusolverDnXpotrf(R.c->solver, R.c->params, CUBLAS_FILL_MODE_UPPER, n, CUDA_R_32F,
                                  A, lda, CUDA_R_32F, R.c->dwork, R.dsize, R.c->hwork, R.hsize,
                                  R.c->d_info));
@@ -251,14 +772,102 @@ static int chol_rec(RecChol &R, float *A, int64_t lda, int64_t n) {
   return chol_rec(R, A + n1 + n1 * lda, lda, n2);
 }
 
+// Blocked right-looking upper Cholesky with look-ahead.  Panel q (rows
+// [k_q, k_q+1) of the upper factor) is factored on the caller's stream: its
+// diagonal block by chol_rec (potrf_leaf_kernel leaves), its row by trsm_rec
+// (trsm_leaf_kernel leaves + emulated GEMMs), then the update of the next block
+// row by this panel.  The update of every later block row runs on the side
+// stream (first the block row q+2 as one GEMM, then column strips of what is
+// left), overlapping the next panels' latency-bound factorisation.  Events:
+// F[q] (panel q final) orders the side stream's use of it; U[q] (block row q+2
+// updated by panel q) orders the caller's update of that row by panel q+1.
+static int chol_lookahead_setup(vmck_ctx *c, int panels) {
+  if (!c->side) {
+    VMCK_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    VMCK_BLAS(cublasCreate(&c->blas2));
+  }
+  const int need = 2 * panels + 2;
+  if (c->n_events < need) {
+    cudaEvent_t *ev = static_cast<cudaEvent_t *>(malloc(sizeof(cudaEvent_t) * need));
+    if (!ev) return VMCK_ERR_NOMEM;
+    for (int i = 0; i < c->n_events; ++i) ev[i] = c->events[i];
+    for (int i = c->n_events; i < need; ++i)
+      VMCK_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+    free(c->events);
+    c->events = ev;
+    c->n_events = need;
+  }
+  VMCK_BLAS(cublasSetStream(c->blas2, c->side));
+  VMCK_BLAS(cublasSetMathMode(c->blas2, CUBLAS_FP32_EMULATED_BF16X9_MATH));
+  VMCK_BLAS(cublasSetEmulationStrategy(c->blas2, CUBLAS_EMULATION_STRATEGY_EAGER));
+  VMCK_BLAS(cublasSetEmulationSpecialValuesSupport(c->blas2,
+                                                    CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE));
+  return VMCK_OK;
+}
+
+static int chol_blocked(RecChol &R, float *A, int64_t lda, int64_t n) {
+  const float mone = -1.0f, one = 1.0f;
+  vmck_ctx *c = R.c;
+  const int panels = (int)((n + PANEL_W - 1) / PANEL_W);
+  int rc = chol_lookahead_setup(c, panels);
+  if (rc) return rc;
+  cudaEvent_t *F = c->events, *U = c->events + panels;
+  cudaEvent_t start = c->events[2 * panels], done = c->events[2 * panels + 1];
+  VMCK_CUDA(cudaEventRecord(start, R.st));
+  VMCK_CUDA(cudaStreamWaitEvent(c->side, start, 0));
+  for (int q = 0; q < panels; ++q) {
+    const int64_t k0 = q * PANEL_W, k1 = std::min<int64_t>(n, k0 + PANEL_W), w = k1 - k0;
+    const int64_t m = n - k1;
+    float *D = A + k0 + k0 * lda;
+    if ((rc = chol_rec(R, D, lda, w))) return rc;
+    if (m == 0) break;
+    float *P = A + k0 + k1 * lda;  // w x m panel row
+    if ((rc = trsm_rec(R, D, lda, w, P, lda, m))) return rc;
+    VMCK_CUDA(cudaEventRecord(F[q], R.st));
+    // caller's stream: block row q+1 (rows [k1, k2), columns [k1, n)) by panel q
+    const int64_t k2 = std::min<int64_t>(n, k1 + PANEL_W);
+    if (q >= 1) VMCK_CUDA(cudaStreamWaitEvent(R.st, U[q - 1], 0));
+    VMCK_BLAS(cublasSgemm(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)(k2 - k1), (int)m, (int)w, &mone,
+                          P, (int)lda, P, (int)lda, &one, A + k1 + k1 * lda, (int)lda));
+    if (k2 == n) continue;
+    // side stream: block row q+2, then the rest in column strips
+    VMCK_CUDA(cudaStreamWaitEvent(c->side, F[q], 0));
+    const int64_t k3 = std::min<int64_t>(n, k2 + PANEL_W);
+    VMCK_BLAS(cublasSgemm(c->blas2, CUBLAS_OP_T, CUBLAS_OP_N, (int)(k3 - k2), (int)(n - k2), (int)w,
+                          &mone, P + (k2 - k1) * lda, (int)lda, P + (k2 - k1) * lda, (int)lda, &one,
+                          A + k2 + k2 * lda, (int)lda));
+    VMCK_CUDA(cudaEventRecord(U[q], c->side));
+    const float *P3 = P + (k3 - k1) * lda;
+    const int64_t m3 = n - k3;
+    for (int64_t c0 = 0; c0 < m3; c0 += STRIP_W) {
+      const int64_t c1 = std::min<int64_t>(m3, c0 + STRIP_W);
+      // C[0:c1, c0:c1] -= P3[:, 0:c1]^T P3[:, c0:c1] (trailing matrix from k3)
+      VMCK_BLAS(cublasSgemm(c->blas2, CUBLAS_OP_T, CUBLAS_OP_N, (int)c1, (int)(c1 - c0), (int)w,
+                            &mone, P3, (int)lda, P3 + c0 * lda, (int)lda, &one,
+                            A + k3 + (k3 + c0) * lda, (int)lda));
+    }
+  }
+  VMCK_CUDA(cudaEventRecord(done, c->side));
+  VMCK_CUDA(cudaStreamWaitEvent(R.st, done, 0));
+  return VMCK_OK;
+}
+
 // ------------------------------------------------------------ symmetric residual
 // r = b - A x for a symmetric A stored as its lower triangle (row-major), each
 // stored element read exactly once.  Tile (I, J), I >= J, of 64 x 64 adds
 // A_IJ x_J to the rows of block I (slot J) and A_IJ^T x_I to the rows of block J
 // (slot I); on a diagonal tile both go to slot I.  Every (slot, row) of
 // ws[n_tiles][n] is written exactly once; the second kernel sums the slots in
-// a fixed order.  HBM-bound: n(n+1)/2 * 8 bytes per call.
+// a fixed order.
+//
+// GB300 issues about 1.4 FP64 instructions per clock per SM, so a plain FP64
+// symv is bound by the FP64 pipe (~0.6 ms at n = 16,384 even with two FMAs per
+// element) rather than by HBM.  Here each double is split into a (hi, lo) pair
+// of floats with integer operations only and the products are accumulated in
+// double-float arithmetic (~2^-46 relative per term) on the FP32 pipe, which
+// leaves the kernel HBM-bound: n(n+1)/2 * 8 bytes per call.
 constexpr int SY_T = 64;
+constexpr int SY_LD = SY_T + 1;  // smem row stride (floats): conflict-free rows and columns
 
 __device__ inline void sy_tri_tile(int64_t bid, int64_t &I, int64_t &J) {
   int64_t i = (int64_t)((sqrt(8.0 * (double)bid + 1.0) - 1.0) * 0.5);
@@ -268,46 +877,89 @@ __device__ inline void sy_tri_tile(int64_t bid, int64_t &I, int64_t &J) {
   J = bid - i * (i + 1) / 2;
 }
 
+// hi = the leading 24 significand bits of a, lo = the next 24 (both truncated,
+// same sign), from the IEEE bit fields: no FP64 instruction.  |a| < 2^-100
+// maps to (0, 0).
+__device__ __forceinline__ df32 df_split_bits(double a) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
+  const unsigned sign = (unsigned)(bits >> 32) & 0x80000000u;
+  const int e = (int)((bits >> 52) & 0x7FF);
+  if (e < 1023 - 100) return {0.0f, 0.0f};
+  if (e > 1023 + 127) return {__int_as_float(sign | 0x7F800000u), 0.0f};
+  const unsigned long long m = bits & ((1ull << 52) - 1);
+  const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(m >> 29));
+  const unsigned rem = (unsigned)(m & ((1u << 29) - 1));
+  // rem's bit 0 weighs 2^(e - 1075): scale by 2^(e - 1075 + 64) (a normal float for
+  // e >= 923), then by 2^-64 so that a subnormal lo rounds instead of vanishing
+  const float lo = __uint2float_rz(rem) * __uint_as_float((unsigned)(e - 1075 + 64 + 127) << 23) *
+                   __uint_as_float(0x1F800000u);
+  return {hi, __uint_as_float(__float_as_uint(lo) | sign)};
+}
+
+// acc += a * x for double-float a, x (the lo * lo term is below the pair's precision)
+__device__ __forceinline__ df32 df_fma(df32 acc, df32 a, df32 x) {
+  df32 p = df_two_prod(a.hi, x.hi);
+  p.lo = __fmaf_rn(a.hi, x.lo, __fmaf_rn(a.lo, x.hi, p.lo));
+  return df_add(acc, p);
+}
+
 __global__ void __launch_bounds__(256) symv_lower_partial_kernel(const double *__restrict__ A,
                                                                  int64_t n,
                                                                  const double *__restrict__ x,
                                                                  double *__restrict__ ws) {
-  __shared__ double xr[SY_T], xc[SY_T];
-  __shared__ double rowpart[2][SY_T];
-  __shared__ double colpart[4][SY_T];
+  __shared__ float ahi[SY_T * SY_LD], alo[SY_T * SY_LD];
+  __shared__ df32 xr[SY_T], xc[SY_T];
+  __shared__ df32 part[4][SY_T];  // [row half 0, row half 1, col half 0, col half 1]
   int64_t I, J;
   sy_tri_tile(blockIdx.x, I, J);
-  const int tid = threadIdx.x, c = tid & 63, g = tid >> 6, half = (tid >> 5) & 1;
-  const int lane = tid & 31;
+  const int tid = threadIdx.x;
   const int64_t r0 = I * SY_T, c0 = J * SY_T;
-  if (tid < SY_T) xc[tid] = (c0 + tid < n) ? x[c0 + tid] : 0.0;
-  else if (tid < 2 * SY_T) xr[tid - SY_T] = (r0 + tid - SY_T < n) ? x[r0 + tid - SY_T] : 0.0;
-  __syncthreads();
   const bool diag = (I == J);
-  const bool cok = (c0 + c) < n;
-  double colacc = 0.0;
+  if (tid < SY_T) xc[tid] = (c0 + tid < n) ? df_split_bits(x[c0 + tid]) : df32{0.0f, 0.0f};
+  else if (tid < 2 * SY_T)
+    xr[tid - SY_T] = (r0 + tid - SY_T < n) ? df_split_bits(x[r0 + tid - SY_T]) : df32{0.0f, 0.0f};
+  {
+    const int c = tid & 63, g = tid >> 6;
+    const bool cok = (c0 + c) < n;
 #pragma unroll 4
-  for (int k = 0; k < 16; ++k) {
-    const int r = g + 4 * k;
-    const bool rok = (r0 + r) < n;
-    double a = 0.0;
-    if (rok && cok && (!diag || r >= c)) a = A[(r0 + r) * n + c0 + c];
-    double v = a * xc[c];
-    v = warp_sum(v);
-    if (lane == 0) rowpart[half][r] = v;
-    if (!diag || r > c) colacc += a * xr[r];
+    for (int k = 0; k < 16; ++k) {
+      const int r = g + 4 * k;
+      df32 v{0.0f, 0.0f};
+      if (cok && (r0 + r) < n && (!diag || r >= c)) v = df_split_bits(A[(r0 + r) * n + c0 + c]);
+      ahi[r * SY_LD + c] = v.hi;
+      alo[r * SY_LD + c] = v.lo;
+    }
   }
-  colpart[g][c] = colacc;
+  __syncthreads();
+  // threads 0-127: row sums (row = tid & 63, column half = tid >> 6);
+  // threads 128-255: column sums over the strict lower part of a diagonal tile
+  const int u = tid & 63, h = (tid >> 6) & 1;
+  df32 acc{0.0f, 0.0f};
+  if (tid < 128) {
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const int c = 32 * h + i;
+      acc = df_fma(acc, df32{ahi[u * SY_LD + c], alo[u * SY_LD + c]}, xc[c]);
+    }
+  } else {
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const int r = 32 * h + i;
+      if (diag && r == u) continue;
+      acc = df_fma(acc, df32{ahi[r * SY_LD + u], alo[r * SY_LD + u]}, xr[r]);
+    }
+  }
+  part[tid >> 6][u] = acc;
   __syncthreads();
   if (tid < SY_T) {
     const int r = tid;
-    const double rs = rowpart[0][r] + rowpart[1][r];
-    const double cs = colpart[0][r] + colpart[1][r] + colpart[2][r] + colpart[3][r];
+    const df32 rs = df_add(part[0][r], part[1][r]);
+    const df32 cs = df_add(part[2][r], part[3][r]);
     if (diag) {
-      if (r0 + r < n) ws[I * n + r0 + r] = rs + cs;
+      if (r0 + r < n) ws[I * n + r0 + r] = df_to_double(df_add(rs, cs));
     } else {
-      if (r0 + r < n) ws[J * n + r0 + r] = rs;
-      if (c0 + r < n) ws[I * n + c0 + r] = cs;
+      if (r0 + r < n) ws[J * n + r0 + r] = df_to_double(rs);
+      if (c0 + r < n) ws[I * n + c0 + r] = df_to_double(cs);
     }
   }
 }
@@ -331,12 +983,6 @@ static int symv_residual(cudaStream_t st, const double *A, int64_t n, const doub
   return check_launch("symv reduce");
 }
 
-static int num_sms() {
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return sms;
-}
 
 }  // namespace vmck
 
@@ -361,6 +1007,10 @@ extern "C" int vmck_ctx_create(vmck_ctx **out) {
 extern "C" int vmck_ctx_destroy(vmck_ctx *c) {
   if (!c) return VMCK_OK;
   cudaDeviceSynchronize();
+  for (int i = 0; i < c->n_events; ++i) cudaEventDestroy(c->events[i]);
+  free(c->events);
+  if (c->blas2) cublasDestroy(c->blas2);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->params) cusolverDnDestroyParams(c->params);
   if (c->solver) cusolverDnDestroy(c->solver);
   if (c->blas) cublasDestroy(c->blas);
@@ -410,7 +1060,7 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
                                            int32_t max_iter, double tol, int32_t factor_mode,
                                            int32_t *status, double *residual_out) {
   VMCK_REQUIRE(c && A64 && A32 && b && x && n > 0 && max_iter >= 1, "refined solve arguments");
-  VMCK_REQUIRE(factor_mode >= 0 && factor_mode <= 2, "factor_mode must be 0, 1 or 2");
+  VMCK_REQUIRE(factor_mode >= 0 && factor_mode <= 3, "factor_mode must be 0, 1, 2 or 3");
   VMCK_REQUIRE(n < (1ll << 31), "refined solve size");
   cudaStream_t st = as_stream(s);
   int rc = bind(c, st);
@@ -426,24 +1076,59 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
                                           CUDA_R_32F, A32, n, CUDA_R_32F, &dsize, &hsize));
   if ((rc = grow(&c->dwork, &c->dwork_bytes, dsize + 256, st))) return rc;
   if ((rc = grow_host(c, hsize))) return rc;
-  // aux: r (n double), r32 (n float), two norms, symv slots (n_tiles x n double)
+  // aux: r (n double), r32 (n float), two norms, symv slots (n_tiles x n double);
+  // factor_mode 3 adds the blocked solves' inverse diagonal blocks (nb x 128^2
+  // float), y32 (n float) and their flags / tickets (2 nb + 4 uint)
   const int64_t nt = (n + SY_T - 1) / SY_T;
+  const bool own_trsv = factor_mode == 3 && n % 4 == 0;
+  const int64_t nb = (n + TB - 1) / TB;
   const size_t ws_off = (((size_t)n * 12 + 64) + 255) & ~size_t(255);
-  const size_t need = ws_off + (size_t)nt * n * 8;
+  const size_t yinv_off = (ws_off + (size_t)nt * n * 8 + 255) & ~size_t(255);
+  const size_t y32_off = (yinv_off + (own_trsv ? (size_t)nb * TB * TB * 4 : 0) + 255) & ~size_t(255);
+  const size_t sync_off = (y32_off + (own_trsv ? (size_t)n * 4 : 0) + 255) & ~size_t(255);
+  const size_t need = sync_off + (own_trsv ? (size_t)(2 * nb + 4) * 4 : 0);
   if ((rc = grow(&c->aux, &c->aux_bytes, need, st))) return rc;
+  char *aux = static_cast<char *>(c->aux);
   double *r = static_cast<double *>(c->aux);
   float *r32 = reinterpret_cast<float *>(r + n);
   double *norms = reinterpret_cast<double *>(
       (reinterpret_cast<uintptr_t>(r32 + n) + 15) & ~uintptr_t(15));
-  double *sws = reinterpret_cast<double *>(static_cast<char *>(c->aux) + ws_off);
-  if (factor_mode == 2) {
+  double *sws = reinterpret_cast<double *>(aux + ws_off);
+  float *yinv = reinterpret_cast<float *>(aux + yinv_off);
+  float *y32 = reinterpret_cast<float *>(aux + y32_off);
+  unsigned *sync = reinterpret_cast<unsigned *>(aux + sync_off);
+  const TrsvSync sync_f{sync, sync + 2 * nb, sync + 2 * nb + 2};
+  const TrsvSync sync_b{sync + nb, sync + 2 * nb + 1, sync + 2 * nb + 2};
+  if (factor_mode >= 2) {
     VMCK_BLAS(cublasSetMathMode(c->blas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
     VMCK_BLAS(cublasSetEmulationStrategy(c->blas, CUBLAS_EMULATION_STRATEGY_EAGER));
-    RecChol R{c, st, status, dsize, hsize};
-    rc = chol_rec(R, A32, n, n);
+    if (factor_mode == 2) {
+      RecChol R{c, st, status, dsize, hsize, CHOL_LEAF, false};
+      rc = chol_rec(R, A32, n, n);
+    } else {
+      VMCK_CUDA(cudaFuncSetAttribute(potrf_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)LEAF_SMEM));
+      VMCK_CUDA(cudaFuncSetAttribute(trsm_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)TRSM_SMEM));
+      // finite inputs: a NaN or Inf in A32 still ends as a failed pivot or an
+      // unconverged refinement, both reported in the status word
+      VMCK_BLAS(cublasSetEmulationSpecialValuesSupport(c->blas,
+                                                        CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE));
+      RecChol R{c, st, status, dsize, hsize, LEAF_B, true};
+      rc = chol_blocked(R, A32, n, n);
+      cublasSetEmulationSpecialValuesSupport(c->blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_DEFAULT);
+    }
     cublasSetMathMode(c->blas, CUBLAS_DEFAULT_MATH);
     cusolverDnSetMathMode(c->solver, CUSOLVER_DEFAULT_MATH);
     if (rc) return rc;
+    if (factor_mode == 3) VMCK_CUDA(cudaMemsetAsync(c->d_info, 0, sizeof(int), st));
+    if (own_trsv) {
+      VMCK_CUDA(cudaFuncSetAttribute(trsv_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)TRSM_SMEM));
+      trsv_inv_kernel<<<dim3(2, (unsigned)nb), LEAF_THREADS, TRSM_SMEM, st>>>(A32, n, yinv);
+      if ((rc = check_launch("refined solve inverse blocks"))) return rc;
+      VMCK_CUDA(cudaMemsetAsync(sync, 0, (size_t)(2 * nb + 4) * 4, st));
+    }
   } else {
     cusolverStatus_t fs = cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
                                            CUDA_R_32F, A32, n, CUDA_R_32F, c->dwork, dsize,
@@ -466,8 +1151,19 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
     }
     d2f_kernel<<<blocks, 256, 0, st>>>(r, r32, n);
     if ((rc = check_launch("refined solve cast"))) return rc;
-    VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, CUDA_R_32F,
-                                 A32, n, CUDA_R_32F, r32, n, c->d_info));
+    if (own_trsv) {
+      const unsigned grid = (unsigned)std::min<int64_t>(nb, 2 * (int64_t)num_sms());
+      VMCK_CUDA(cudaMemsetAsync(sync + 2 * nb, 0, 2 * sizeof(unsigned), st));  // tickets
+      trsv_fwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(A32, n, yinv, r32, y32, sync_f,
+                                                     (unsigned)(it + 1), status);
+      if ((rc = check_launch("refined solve forward"))) return rc;
+      trsv_bwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(A32, n, yinv, y32, r32, sync_b,
+                                                     (unsigned)(it + 1), status);
+      if ((rc = check_launch("refined solve backward"))) return rc;
+    } else {
+      VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, CUDA_R_32F,
+                                   A32, n, CUDA_R_32F, r32, n, c->d_info));
+    }
     axpy_f2d_kernel<<<blocks, 256, 0, st>>>(x, r32, n);
     if ((rc = check_launch("refined solve update"))) return rc;
   }

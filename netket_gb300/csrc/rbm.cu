@@ -185,7 +185,7 @@ __device__ double eloc_ising_sample(const RbmParams<T> &P, const int8_t *xs,
       int site = k;
       T d = (T)(-2 * xs[k]);
       T lr = warp_log_ratio(P, th, lc, &site, &d, 1);
-      if (lane == 0) acc += -h * exp((double)lr);
+      if (lane == 0) acc += -h * exp_ratio(lr);
     }
   }
   if (threadIdx.x == 0) acc += J * (double)tot;
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(EL_THREADS) eloc_local_kernel(
         if (lane == 0) acc += mel;
       } else {
         T lr = warp_log_ratio(P, th, lc, site, d, ns);
-        if (lane == 0) acc += mel * exp((double)lr);
+        if (lane == 0) acc += mel * exp_ratio(lr);
       }
     }
     double e = block_sum(acc, redd);

@@ -150,11 +150,12 @@ def cholesky_solve(A, b, status):
     return x
 
 
-def cholesky_solve_refined(A64, A32, b, status, max_iter=3, tol=1e-10, factor_mode=2):
+def cholesky_solve_refined(A64, A32, b, status, max_iter=3, tol=1e-10, factor_mode=3):
     """FP32-accurate Cholesky of A32 (overwritten by its factor) refined to an
     FP64 residual against A64.  factor_mode 0: cuSOLVER SPOTRF; 1: SPOTRF with
     BF16x9 emulation; 2: recursive GEMM-based factorisation on BF16x9-emulated
-    tensor cores."""
+    tensor cores; 3: blocked factorisation with this library's leaf kernel and
+    emulated-GEMM panel solves / trailing updates."""
     x = torch.empty_like(b)
     res = torch.empty(1, dtype=torch.float64, device=b.device)
     nat.check(nat.lib().vmck_cholesky_solve_refined(nat.ctx(), nat.stream(), nat.ptr(A64),
