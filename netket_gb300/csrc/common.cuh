@@ -155,7 +155,31 @@ __device__ __forceinline__ df32 df_from(double d) {
   const float h = __double2float_rn(d);
   return {h, __double2float_rn(d - (double)h)};
 }
-__device__ __forceinline__ double df_to_double(df32 a) { return (double)a.hi + (double)a.lo; }
+// (double)(hi + lo) assembled from the bit fields with integer operations: for a
+// normalised pair (|lo| <= ulp(hi) / 2) lo lands in the 29 low mantissa bits a
+// double has below hi's, so the result is exact (a subtraction that borrows
+// from hi's leading bit renormalises by one place).  GB300 issues roughly one
+// FP64 instruction per clock per SM, so two conversions and an add per element
+// would bound the Gram epilogues; zero / subnormal / non-finite hi and
+// non-normalised pairs take the FP64 route.
+__device__ __forceinline__ double df_to_double(df32 a) {
+  const uint32_t hb = __float_as_uint(a.hi), lb = __float_as_uint(a.lo);
+  const int he = (int)((hb >> 23) & 0xFFu), le = (int)((lb >> 23) & 0xFFu);
+  const int sh = (le > 0 ? le : 1) - he + 29;  // lo in units of hi's last double bit
+  if (he == 0 || he == 0xFF || le == 0xFF || sh > 5) return (double)a.hi + (double)a.lo;
+  long long X = (long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
+  const unsigned long long ml = (lb & 0x7FFFFFu) | (le ? 0x800000u : 0u);
+  const long long li = (long long)(sh >= 0 ? (ml << sh) : (sh > -40 ? (ml >> -sh) : 0ull));
+  X = ((hb ^ lb) >> 31) ? X - li : X + li;
+  int e = he - 127 + 1023;
+  if (X < (1ll << 52)) {
+    X <<= 1;
+    --e;
+  }
+  return __longlong_as_double((long long)(((unsigned long long)(hb >> 31) << 63) |
+                                          ((unsigned long long)e << 52) |
+                                          ((unsigned long long)X & ((1ull << 52) - 1))));
+}
 
 // ----------------------------------------------------------------- reductions
 template <typename T>

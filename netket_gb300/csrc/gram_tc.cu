@@ -2,23 +2,32 @@
 //
 // T = (A o (1 + B) + B - g 1^T - 1 g^T + c 1 1^T) / n + diag_shift I with
 // A = t t^T (t = tanh theta, n x M) and B = x x^T (exact, popcount).  A runs on
-// the 5th-generation tensor cores: each CTA owns one 128 x 128 lower-triangular
-// tile of T, streams K-slabs of the two operand panels with TMA
-// (cp.async.bulk.tensor, 128-byte swizzle) into a 4-stage shared-memory ring
-// guarded by mbarriers, issues tcgen05.mma (kind::f16, BF16 in, FP32
-// accumulate in tensor memory) from one thread, and the four warps read the
-// accumulator back with tcgen05.ld for the fused epilogue that writes T64 / T32.
+// the 5th-generation tensor cores in a persistent, warp-specialised kernel: one
+// CTA per SM walks the 128 x 128 lower-triangular tiles of T; warp 0 streams
+// K-slabs of the two operand panels with TMA (cp.async.bulk.tensor, 128-byte
+// swizzle) into a 4-stage shared-memory ring, warp 1 issues tcgen05.mma
+// (kind::f16, BF16 in, FP32 accumulate in tensor memory) from one thread, and
+// eight epilogue warps read the accumulators back with tcgen05.ld, form T in
+// double-float FP32 and write it with coalesced row segments staged through
+// shared memory.  Tensor memory holds two tile buffers, so the epilogue of one
+// tile overlaps the MMAs of the next.
 //
 // Precision: t arrives rounded to hi + lo (two BF16 terms) or to one BF16; the
-// operand panels [hi | hi | lo | lo] and [hi | lo | hi | lo] make one GEMM form
-// all four products, i.e. t t^T exactly up to FP32 accumulation.  Every other
-// ingredient of T (column means, g) is computed from the same rounded t, so T
-// is the exact Gram matrix of a slightly perturbed Jacobian and keeps its
-// positive definiteness.  The epilogue works in double-float FP32.
+// operand panels [hi | hi | lo | lo] and [hi | lo | hi | lo] (each segment
+// padded to a multiple of 64) make one GEMM form all four products, i.e. t t^T
+// exactly up to FP32 accumulation.  The hi * hi segment and the three small
+// cross segments accumulate in separate tensor-memory regions (single-BF16 mode:
+// alternate K-slabs), which keeps the tensor core's accumulation error on the
+// large part from growing with the number of steps; the epilogue adds the
+// regions in double-float.  Every other ingredient of T (column means, g) is
+// computed from the same rounded t, so T is the Gram matrix of a slightly
+// perturbed Jacobian.
 //
 // Every mbarrier wait is bounded by wall time (2 s, %globaltimer); a wait that
-// runs out sets VMCK_DEV_TIMEOUT in the status word and the CTA winds down
-// (waiting, again bounded, for its own TMA copies) instead of hanging.
+// runs out sets VMCK_DEV_TIMEOUT in the status word and an abort flag in shared
+// memory; every role then leaves its loop, the producer waits (bounded) for the
+// TMA copies it issued, the MMA thread for its last commit, and the CTA frees
+// its tensor memory and exits.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -35,10 +44,12 @@ constexpr int TC_BN = 128;     // tile cols (UMMA N)
 constexpr int TC_BK = 64;      // K slab: 64 bf16 = 128 bytes = one swizzle row
 constexpr int TC_STAGES = 4;
 constexpr int TC_UMMA_K = 16;  // K per tcgen05.mma for 16-bit inputs
-constexpr int TC_ACC = 4;           // accumulators the K-blocks rotate over
-constexpr int TC_TMEM_COLS = 512;  // TC_ACC x TC_BN columns: all of tensor memory
+constexpr int TC_TMEM_COLS = 512;  // 2 buffers x 2 regions x TC_BN columns
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;
-constexpr int TC_THREADS = 128;
+constexpr int TC_EPI_WARPS = 8;    // two per tensor-memory lane quarter, 64 columns each
+constexpr int TC_THREADS = 32 * (2 + TC_EPI_WARPS);
+constexpr int TC_CHUNK = 16;       // epilogue columns per tcgen05.ld
+constexpr int TC_STG_LD = TC_CHUNK + 1;
 
 // ------------------------------------------------------------ PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -156,29 +167,50 @@ __device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld_16cols(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // ------------------------------------------------------------ operand panels
 // Input t is already rounded (exactly hi + lo, or exactly one BF16), so
 //   split:  L = [hi | hi | lo | lo], R = [hi | lo | hi | lo]  ->  L R^T = t t^T,
 //   single: L = R = [bf16(t)]                                 ->  L R^T = t t^T,
-// exactly up to the FP32 accumulation: T is then the exact Gram matrix of the
-// rounded Jacobian and stays positive semidefinite.  Rows are Kp long
-// (zero padding to a multiple of 64).
-__global__ void tc_split_kernel(const float *__restrict__ t, int64_t n, int M, int Kp, int split,
-                                __nv_bfloat16 *__restrict__ L, __nv_bfloat16 *__restrict__ R) {
+// exactly up to the FP32 accumulation.  Each segment is Mp = M rounded up to a
+// multiple of 64 long (zero padded), so a K-slab never straddles two segments.
+__global__ void tc_split_kernel(const float *__restrict__ t, int64_t n, int M, int Mp, int Kp,
+                                int split, __nv_bfloat16 *__restrict__ L,
+                                __nv_bfloat16 *__restrict__ R) {
   int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= n * Kp) return;
   const int64_t s = e / Kp;
   const int k = (int)(e % Kp);
   __nv_bfloat16 lv = __float2bfloat16(0.0f), rv = lv;
-  const int seg = k / M, j = k % M;
-  if (!split) {
-    if (seg == 0) lv = rv = __float2bfloat16(t[s * M + j]);
-  } else if (seg < 4) {
-    const float v = t[s * M + j];
-    const __nv_bfloat16 hi = __float2bfloat16(v);
-    const __nv_bfloat16 lo = __float2bfloat16(v - __bfloat162float(hi));
-    lv = (seg < 2) ? hi : lo;
-    rv = (seg & 1) ? lo : hi;
+  const int seg = k / Mp, j = k % Mp;
+  if (j < M) {
+    if (!split) {
+      lv = rv = __float2bfloat16(t[s * M + j]);
+    } else {
+      const float v = t[s * M + j];
+      const __nv_bfloat16 hi = __float2bfloat16(v);
+      const __nv_bfloat16 lo = __float2bfloat16(v - __bfloat162float(hi));
+      lv = (seg < 2) ? hi : lo;
+      rv = (seg & 1) ? lo : hi;
+    }
   }
   L[e] = lv;
   R[e] = rv;
@@ -205,38 +237,38 @@ __device__ inline void tc_tri_tile(int64_t bid, int64_t &I, int64_t &J) {
   J = bid - i * (i + 1) / 2;
 }
 
+// num_kb K-slabs per tile; kb_hi: slabs of the hi * hi segment (split mode), or 0
+// (single mode: slabs alternate between the two regions).
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gram_tc_kernel(const __grid_constant__ CUtensorMap mapL,
-                   const __grid_constant__ CUtensorMap mapR, int num_kb, TcEpilogue ep) {
+                   const __grid_constant__ CUtensorMap mapR, int num_kb, int kb_hi,
+                   int64_t n_tiles, TcEpilogue ep) {
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
-  // 1024-byte alignment for the 128B-swizzled operand slabs
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
   constexpr int SLAB = TC_BM * TC_BK * 2;  // 16 KB
   unsigned char *slabA = smem;
   unsigned char *slabB = smem + TC_STAGES * SLAB;
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + 2 * TC_STAGES * SLAB);
+  // per epilogue warp: the chunk being written, as (hi, lo) pairs [32][TC_STG_LD]
+  float2 *stg = reinterpret_cast<float2 *>(smem + 2 * TC_STAGES * SLAB);
+  // per epilogue warp: its 64 columns' sign bits (N <= 128), w and h pairs
+  uint4 *cbits = reinterpret_cast<uint4 *>(stg + TC_EPI_WARPS * 32 * TC_STG_LD);
+  float4 *cwh = reinterpret_cast<float4 *>(cbits + TC_EPI_WARPS * 64);
+  uint64_t *full = reinterpret_cast<uint64_t *>(cwh + TC_EPI_WARPS * 64);
   uint64_t *empty = full + TC_STAGES;
-  uint64_t *done = empty + TC_STAGES;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
-  int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
-  uint32_t *colbits = reinterpret_cast<uint32_t *>(abort_flag + 1);  // [TC_BN][words]
-  float2 *colh = reinterpret_cast<float2 *>(
-      (reinterpret_cast<uintptr_t>(colbits + TC_BN * 9) + 7) & ~uintptr_t(7));  // [TC_BN]
-  float2 *colw = colh + TC_BN;                                                  // [TC_BN]
+  uint64_t *tfull = empty + TC_STAGES;  // [2]
+  uint64_t *tempty = tfull + 2;         // [2]
+  uint64_t *drain = tempty + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // once any CTA has timed out, the remaining ones do no work
-  if (tid == 0) *reinterpret_cast<volatile int *>(tmem_slot + 1) =
-      (ep.status && (*reinterpret_cast<volatile int32_t *>(ep.status) & VMCK_DEV_TIMEOUT)) ? 1 : 0;
+  if (tid == 0)
+    *abort_flag =
+        (ep.status && (*reinterpret_cast<volatile int32_t *>(ep.status) & VMCK_DEV_TIMEOUT)) ? 1 : 0;
   __syncthreads();
-  if (*reinterpret_cast<volatile int *>(tmem_slot + 1)) return;
-  __syncthreads();
-  int64_t I, J;
-  tc_tri_tile(blockIdx.x, I, J);
-  const int64_t r0 = I * TC_BM, c0 = J * TC_BN;
-
-  if (warp == 0) {
+  if (*abort_flag) return;  // an earlier CTA timed out: do no work
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(TC_TMEM_COLS)
@@ -248,151 +280,217 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(done, 1);
-    *abort_flag = 0;
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], TC_EPI_WARPS);
+    }
+    mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapL)) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapR)) : "memory");
-  }
-  // stage the column-side epilogue inputs while the pipeline runs
-  for (int e = tid; e < TC_BN * ep.words; e += TC_THREADS) {
-    const int c = e / ep.words, w = e % ep.words;
-    colbits[c * 9 + w] = (c0 + c < ep.n) ? ep.bits[(c0 + c) * ep.words + w] : 0u;
-  }
-  for (int c = tid; c < TC_BN; c += TC_THREADS) {
-    colh[c] = (c0 + c < ep.n) ? ep.h[c0 + c] : make_float2(0.0f, 0.0f);
-    colw[c] = (c0 + c < ep.n) ? ep.w[c0 + c] : make_float2(0.0f, 0.0f);
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  // ---------------- producer + MMA issuer: one thread drives the ring
-  if (tid == 0) {
-    const uint32_t idesc = umma_idesc_bf16(TC_BM, TC_BN);
-    const int pre = num_kb < TC_STAGES ? num_kb : TC_STAGES;
-    bool ok = true;
-    int issued = 0;
-    for (int kb = 0; kb < pre; ++kb) {
-      mbar_expect_tx(&full[kb], 2 * SLAB);
-      tma_load_2d(slabA + kb * SLAB, &mapL, &full[kb], kb * TC_BK, (int)r0);
-      tma_load_2d(slabB + kb * SLAB, &mapR, &full[kb], kb * TC_BK, (int)c0);
-      ++issued;
+  auto fail = [&]() {
+    if (ep.status) atomicOr(ep.status, VMCK_DEV_TIMEOUT);
+    *abort_flag = 1;
+  };
+
+  if (warp == 0) {
+    // ---------------- TMA producer
+    if (lane == 0) {
+      int64_t it = 0;
+      for (int64_t tile = blockIdx.x; tile < n_tiles && !*abort_flag; tile += gridDim.x) {
+        int64_t I, J;
+        tc_tri_tile(tile, I, J);
+        for (int kb = 0; kb < num_kb; ++kb, ++it) {
+          const int s = (int)(it % TC_STAGES);
+          if (it >= TC_STAGES && !mbar_wait(&empty[s], (uint32_t)(((it / TC_STAGES) - 1) & 1))) {
+            fail();
+            break;
+          }
+          if (*abort_flag) break;
+          mbar_expect_tx(&full[s], 2 * SLAB);
+          tma_load_2d(slabA + s * SLAB, &mapL, &full[s], kb * TC_BK, (int)(I * TC_BM));
+          tma_load_2d(slabB + s * SLAB, &mapR, &full[s], kb * TC_BK, (int)(J * TC_BN));
+        }
+      }
+      // every copy issued must land before the CTA may exit: wait for the last
+      // TC_STAGES fills (bounded)
+      const int64_t first = it > TC_STAGES ? it - TC_STAGES : 0;
+      for (int64_t q = first; q < it; ++q)
+        mbar_wait(&full[q % TC_STAGES], (uint32_t)((q / TC_STAGES) & 1));
     }
-    for (int kb = 0; kb < num_kb && ok; ++kb) {
-      const int s = kb % TC_STAGES;
-      const uint32_t ph = (kb / TC_STAGES) & 1;
-      if (!mbar_wait(&full[s], ph)) {
-        ok = false;
-        break;
-      }
-      tc_fence_after();
-      const uint32_t a0 = smem_u32(slabA + s * SLAB), b0 = smem_u32(slabB + s * SLAB);
-      // K-blocks rotate over TC_ACC accumulators: the tensor core's FP32
-      // accumulation error grows with the number of accumulate steps, so each
-      // accumulator takes a quarter of them and the epilogue sums the four.
-      const uint32_t dacc = tmem_base + (uint32_t)((kb % TC_ACC) * TC_BN);
-#pragma unroll
-      for (int k = 0; k < TC_BK / TC_UMMA_K; ++k) {
-        const uint32_t off = k * TC_UMMA_K * 2;  // bytes along the swizzled row
-        umma_bf16(dacc, umma_desc_sw128(a0 + off), umma_desc_sw128(b0 + off), idesc,
-                  (kb >= TC_ACC || k > 0) ? 1u : 0u);
-      }
-      umma_commit(&empty[s]);
-      const int nk = kb + TC_STAGES;
-      if (nk < num_kb) {
-        // the slab is refilled once the MMAs that read it have completed
-        if (!mbar_wait(&empty[s], ph)) {
-          ok = false;
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = umma_idesc_bf16(TC_BM, TC_BN);
+      int64_t it = 0, tcount = 0;
+      bool issued_any = false;
+      for (int64_t tile = blockIdx.x; tile < n_tiles && !*abort_flag; tile += gridDim.x, ++tcount) {
+        const int b = (int)(tcount & 1);
+        if (tcount >= 2 && !mbar_wait(&tempty[b], (uint32_t)(((tcount >> 1) - 1) & 1))) {
+          fail();
           break;
         }
-        mbar_expect_tx(&full[s], 2 * SLAB);
-        tma_load_2d(slabA + s * SLAB, &mapL, &full[s], nk * TC_BK, (int)r0);
-        tma_load_2d(slabB + s * SLAB, &mapR, &full[s], nk * TC_BK, (int)c0);
-        ++issued;
+        tc_fence_after();
+        bool ok = true;
+        for (int kb = 0; kb < num_kb; ++kb, ++it) {
+          const int s = (int)(it % TC_STAGES);
+          if (!mbar_wait(&full[s], (uint32_t)((it / TC_STAGES) & 1))) {
+            fail();
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const int region = kb_hi ? (kb < kb_hi ? 0 : 1) : (kb & 1);
+          const bool first = kb_hi ? (kb == 0 || kb == kb_hi) : (kb < 2);
+          const uint32_t dacc = tmem_base + (uint32_t)(b * 2 * TC_BN + region * TC_BN);
+          const uint32_t a0 = smem_u32(slabA + s * SLAB), b0 = smem_u32(slabB + s * SLAB);
+#pragma unroll
+          for (int k = 0; k < TC_BK / TC_UMMA_K; ++k) {
+            const uint32_t off = k * TC_UMMA_K * 2;  // bytes along the swizzled row
+            umma_bf16(dacc, umma_desc_sw128(a0 + off), umma_desc_sw128(b0 + off), idesc,
+                      (first && k == 0) ? 0u : 1u);
+          }
+          umma_commit(&empty[s]);
+          issued_any = true;
+        }
+        if (!ok) break;
+        umma_commit(&tfull[b]);
+      }
+      // wait for every MMA issued to complete before the tensor memory is freed
+      if (issued_any) {
+        umma_commit(drain);
+        mbar_wait(drain, 0);
       }
     }
-    if (ok) {
-      umma_commit(done);
-    } else {
-      // wind down: let every TMA copy this CTA issued land before exiting
-      *abort_flag = 1;
-      if (ep.status) atomicOr(ep.status, VMCK_DEV_TIMEOUT);
-      for (int q = 0; q < issued; ++q) {
-        const int s = q % TC_STAGES;
-        mbar_wait(&full[s], (q / TC_STAGES) & 1);
-      }
-      mbar_wait(&empty[(num_kb - 1) % TC_STAGES], ((num_kb - 1) / TC_STAGES) & 1);
-    }
-  }
-  __syncwarp();
-  // ---------------- epilogue: all four warps
-  bool have = true;
-  if (!mbar_wait(done, 0)) have = false;
-  __syncthreads();
-  if (*abort_flag) have = false;
-  if (!have) {
-    if (tid == 0 && ep.status) atomicOr(ep.status, VMCK_DEV_TIMEOUT);
   } else {
-    tc_fence_after();
-    const int r = warp * 32 + lane;  // TMEM lane == tile row
-    const int64_t srow = r0 + r;
-    uint32_t rb[9];
-    float2 hrow = make_float2(0.0f, 0.0f), wrow = hrow;
-    if (srow < ep.n) {
-      for (int w = 0; w < ep.words; ++w) rb[w] = ep.bits[srow * ep.words + w];
-      hrow = ep.h[srow];
-      wrow = ep.w[srow];
-    }
+    // ---------------- epilogue: warp e = warp - 2 reads TMEM lane quarter (warp & 3),
+    // columns [64 * (e >> 2), +64)
+    const int e = warp - 2, quarter = warp & 3, half = e >> 2;
+    const int r = quarter * 32 + lane;  // tile row of this thread
+    float2 *st = stg + e * 32 * TC_STG_LD;
+    uint4 *wb = cbits + e * 64;
+    float4 *wwh = cwh + e * 64;
     const df32 shift = df_from(ep.diag_shift);
     const df32 s0sq = {ep.s0sq->x, ep.s0sq->y};
-    const df32 wr_s0 = df_add(df32{wrow.x, wrow.y}, s0sq);
-    const uint32_t lane_addr = tmem_base + (static_cast<uint32_t>(warp * 32) << 16);
-    const int nacc = num_kb < TC_ACC ? num_kb : TC_ACC;
-#pragma unroll 1
-    for (int q = 0; q < TC_BN / 32; ++q) {
-      df32 acc[32];
-      {
-        float part[32];
-        tmem_ld_32cols(lane_addr + q * 32, part);
+    const bool two = kb_hi ? (num_kb > kb_hi) : (num_kb > 1);
+    const bool narrow = ep.words <= 4;  // sign bits of a column fit one uint4
+    int64_t tcount = 0;
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++tcount) {
+      const int b = (int)(tcount & 1);
+      int64_t I, J;
+      tc_tri_tile(tile, I, J);
+      const int64_t r0 = I * TC_BM, c0 = J * TC_BN;
+      // column-side inputs of this warp's 64 columns (independent of the MMAs)
+      __syncwarp();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) acc[j] = {part[j], 0.0f};
+      for (int u = 0; u < 2; ++u) {
+        const int cc = lane + 32 * u;
+        const int64_t scol = c0 + half * 64 + cc;
+        uint4 bw = make_uint4(0u, 0u, 0u, 0u);
+        float4 v4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (scol < ep.n) {
+          if (narrow) {
+            const uint32_t *bp = ep.bits + scol * ep.words;
+            bw.x = bp[0];
+            if (ep.words > 1) bw.y = bp[1];
+            if (ep.words > 2) bw.z = bp[2];
+            if (ep.words > 3) bw.w = bp[3];
+          }
+          const float2 cw = ep.w[scol], ch = ep.h[scol];
+          v4 = make_float4(cw.x, cw.y, ch.x, ch.y);
+        }
+        wb[cc] = bw;
+        wwh[cc] = v4;
       }
-      for (int r = 1; r < nacc; ++r) {
-        float part[32];
-        tmem_ld_32cols(lane_addr + r * TC_BN + q * 32, part);
+      const int64_t srow = r0 + r;
+      uint32_t rb[9];
+      float2 hrow = make_float2(0.0f, 0.0f), wrow = hrow;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) acc[j] = df_add(acc[j], part[j]);
-      }
+      for (int w = 0; w < 9; ++w) rb[w] = 0u;
       if (srow < ep.n) {
-        double *o64 = ep.T64 ? ep.T64 + srow * ep.n : nullptr;
-        float *o32 = ep.T32 + srow * ep.n;
+#pragma unroll
+        for (int w = 0; w < 9; ++w)
+          if (w < ep.words) rb[w] = ep.bits[srow * ep.words + w];
+        hrow = ep.h[srow];
+        wrow = ep.w[srow];
+      }
+      const df32 wr_s0 = df_add(df32{wrow.x, wrow.y}, s0sq);
+      const df32 nh_row = {-hrow.x, -hrow.y};
+      __syncwarp();
+      if (!mbar_wait(&tfull[b], (uint32_t)((tcount >> 1) & 1))) {
+        fail();
+        break;
+      }
+      if (*abort_flag) break;
+      tc_fence_after();
+      const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) +
+                             (uint32_t)(b * 2 * TC_BN + half * 64);
+#pragma unroll 1
+      for (int ch = 0; ch < 64 / TC_CHUNK; ++ch) {
+        float a0[TC_CHUNK], a1[TC_CHUNK];
+        tmem_ld_16cols(taddr + ch * TC_CHUNK, a0);
+        if (two) tmem_ld_16cols(taddr + TC_BN + ch * TC_CHUNK, a1);
+        tmem_wait_ld();
+        if (ch == 64 / TC_CHUNK - 1) {
+          // all of this warp's reads of buffer b are done: release it to the MMA warp
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[b]);
+        }
+#pragma unroll
+        for (int j = 0; j < TC_CHUNK; ++j) {
+          const int cl = ch * TC_CHUNK + j;  // column within the warp's 64
+          int diff = 0;
+          if (narrow) {
+            const uint4 bw = wb[cl];
+            diff = __popc(rb[0] ^ bw.x) + __popc(rb[1] ^ bw.y) + __popc(rb[2] ^ bw.z) +
+                   __popc(rb[3] ^ bw.w);
+          } else {
+            const int64_t scol = c0 + half * 64 + cl;
+            if (scol < ep.n) {
+#pragma unroll
+              for (int w = 0; w < 9; ++w)
+                if (w < ep.words) diff += __popc(rb[w] ^ __ldg(ep.bits + scol * ep.words + w));
+            }
+          }
+          const int B = ep.N - 2 * diff;
+          const float4 cv = wwh[cl];
+          const df32 acc = two ? df_two_sum(a0[j], a1[j]) : df32{a0[j], 0.0f};
+          const df32 a = df_add(df_add(wr_s0, df32{cv.x, cv.y}), acc);
+          df32 v = df_mul(a, (float)(1 + B));
+          v = df_add(v, (float)B);
+          v = df_add(v, df_add(nh_row, df32{-cv.z, -cv.w}));
+          v = df_mul(v, ep.inv_n);
+          if (c0 + half * 64 + cl == srow) v = df_add(v, shift);
+          st[lane * TC_STG_LD + j] = make_float2(v.hi, v.lo);
+        }
+        __syncwarp();
+        // coalesced write-out: half-warps take rows, lanes 16 consecutive columns
+        const int cb = half * 64 + ch * TC_CHUNK;
 #pragma unroll 4
-        for (int j = 0; j < 32; ++j) {
-          const int c = q * 32 + j;
-          const int64_t scol = c0 + c;
-          if (scol < ep.n && scol <= srow) {
-            int diff = 0;
-            for (int w = 0; w < ep.words; ++w) diff += __popc(rb[w] ^ colbits[c * 9 + w]);
-            const int B = ep.N - 2 * diff;
-            df32 a = df_add(df_add(wr_s0, df32{colw[c].x, colw[c].y}), acc[j]);
-            df32 v = df_mul(a, (float)(1 + B));
-            v = df_add(v, (float)B);
-            v = df_add(v, df32{-hrow.x, -hrow.y});
-            v = df_add(v, df32{-colh[c].x, -colh[c].y});
-            v = df_mul(v, ep.inv_n);
-            if (scol == srow) v = df_add(v, shift);
-            if (o64) o64[scol] = df_to_double(v);
-            o32[scol] = v.hi + v.lo;
+        for (int q = 0; q < 16; ++q) {
+          const int rr = 2 * q + (lane >> 4), cc = lane & 15;
+          const int64_t orow = r0 + quarter * 32 + rr, ocol = c0 + cb + cc;
+          if (orow < ep.n && ocol <= orow) {
+            const float2 v = st[rr * TC_STG_LD + cc];
+            ep.T32[orow * ep.n + ocol] = v.x + v.y;
+            if (ep.T64) ep.T64[orow * ep.n + ocol] = df_to_double(df32{v.x, v.y});
           }
         }
+        __syncwarp();
       }
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
+    tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(TC_TMEM_COLS)
                  : "memory");
@@ -434,10 +532,8 @@ static int make_map(CUtensorMap *map, const void *base, int64_t rows, int64_t Kp
   return VMCK_OK;
 }
 
-static int64_t tc_kp(int M, bool split) {
-  const int64_t k = split ? 4 * (int64_t)M : M;
-  return (k + TC_BK - 1) / TC_BK * TC_BK;
-}
+static int tc_mp(int M) { return (M + TC_BK - 1) / TC_BK * TC_BK; }
+static int64_t tc_kp(int M, bool split) { return (split ? 4 : 1) * (int64_t)tc_mp(M); }
 
 int64_t gram_tc_workspace_doubles(int M, int64_t n) {
   // two bf16 panels of n x Kp (split layout, the larger one), plus alignment
@@ -445,8 +541,9 @@ int64_t gram_tc_workspace_doubles(int M, int64_t n) {
 }
 
 static size_t tc_smem_bytes() {
-  return 1024 /*align*/ + 2 * TC_STAGES * TC_BM * TC_BK * 2 + 8 * (2 * TC_STAGES + 1) + 16 +
-         TC_BN * 9 * 4 + 8 + 2 * TC_BN * 8 + 256 /*margin*/;
+  return 1024 /*align*/ + 2 * TC_STAGES * TC_BM * TC_BK * 2 +
+         TC_EPI_WARPS * 32 * TC_STG_LD * 8 + TC_EPI_WARPS * 64 * (16 + 16) +
+         8 * (2 * TC_STAGES + 5) + 16 + 256 /*margin*/;
 }
 
 int gram_tc_launch(vmck_ctx *ctx, cudaStream_t st, const float *tanh_theta, const uint32_t *bits,
@@ -466,7 +563,8 @@ int gram_tc_launch(vmck_ctx *ctx, cudaStream_t st, const float *tanh_theta, cons
   __nv_bfloat16 *L = reinterpret_cast<__nv_bfloat16 *>(
       (reinterpret_cast<uintptr_t>(ws) + 1023) & ~uintptr_t(1023));
   __nv_bfloat16 *R = L + n * Kp;  // n * Kp * 2 bytes: a multiple of 128, so 16-byte aligned
-  tc_split_kernel<<<ceil_div(n * Kp, 256), 256, 0, st>>>(tanh_theta, n, M, (int)Kp, split, L, R);
+  tc_split_kernel<<<ceil_div(n * Kp, 256), 256, 0, st>>>(tanh_theta, n, M, tc_mp(M), (int)Kp,
+                                                          split, L, R);
   int rc = check_launch("gram_tc split");
   if (rc) return rc;
   CUtensorMap mL, mR;
@@ -475,10 +573,14 @@ int gram_tc_launch(vmck_ctx *ctx, cudaStream_t st, const float *tanh_theta, cons
   const size_t smem = tc_smem_bytes();
   VMCK_CUDA(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
-  const int64_t nt = (n + TC_BM - 1) / TC_BM;
+  const int64_t nt = (n + TC_BM - 1) / TC_BM, tiles = nt * (nt + 1) / 2;
   TcEpilogue ep{bits, words, N, n, h, w, s0sq, (float)inv_n, diag_shift, T64, T32, status};
-  gram_tc_kernel<<<(unsigned)(nt * (nt + 1) / 2), TC_THREADS, smem, st>>>(mL, mR,
-                                                                          (int)(Kp / TC_BK), ep);
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
+  const int kb_hi = split ? tc_mp(M) / TC_BK : 0;
+  gram_tc_kernel<<<grid, TC_THREADS, smem, st>>>(mL, mR, (int)(Kp / TC_BK), kb_hi, tiles, ep);
   return check_launch("gram_tc");
 }
 

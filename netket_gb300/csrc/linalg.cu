@@ -564,20 +564,30 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_fwd_kernel(const float *__r
     if (K >= nb) break;
     const int64_t k0 = (int64_t)K * TB;
     const int mk = (int)((n - k0) < TB ? (n - k0) : TB);
+    // this thread's share of Y_K for the final product, loaded before any wait
+    const int yc = tid & (TB - 1), yh = tid >> 7;
+    float ys[32];
+    {
+      const float *Y = Yinv + (int64_t)K * TB * TB;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) ys[i] = __ldg(Y + (32 * yh + i) * TB + yc);
+    }
     float acc[8] = {};
     bool alive = true;
     for (int J = 0; J < K && alive; ++J) {
+      float4 u[8];  // U_JK does not depend on y: load it before waiting for y_J
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int c = 8 * warp + q;
+        u[q] = (c < mk) ? __ldg(reinterpret_cast<const float4 *>(U + (k0 + c) * n + (int64_t)J * TB) + lane)
+                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
       alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status);
       if (!alive) break;
       const float4 yj = __ldcg(reinterpret_cast<const float4 *>(y + (int64_t)J * TB) + lane);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int c = 8 * warp + q;
-        if (c < mk) {
-          const float4 u = __ldg(reinterpret_cast<const float4 *>(U + (k0 + c) * n + (int64_t)J * TB) + lane);
-          acc[q] = __fmaf_rn(u.x, yj.x, __fmaf_rn(u.y, yj.y, __fmaf_rn(u.z, yj.z, __fmaf_rn(u.w, yj.w, acc[q]))));
-        }
-      }
+      for (int q = 0; q < 8; ++q)
+        acc[q] = __fmaf_rn(u[q].x, yj.x, __fmaf_rn(u[q].y, yj.y, __fmaf_rn(u[q].z, yj.z, __fmaf_rn(u[q].w, yj.w, acc[q]))));
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -587,12 +597,10 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_fwd_kernel(const float *__r
     }
     __syncthreads();
     {  // y_K[c] = sum_c' Y_K(c, c') z[c'], thread (h, c): c' in [32h, 32h + 32)
-      const int c = tid & (TB - 1), h = tid >> 7;
-      const float *Y = Yinv + (int64_t)K * TB * TB;
       float sacc = 0.0f;
-#pragma unroll 8
-      for (int i = 0; i < 32; ++i) sacc = __fmaf_rn(Y[(32 * h + i) * TB + c], z[32 * h + i], sacc);
-      part[h][c] = sacc;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) sacc = __fmaf_rn(ys[i], z[32 * yh + i], sacc);
+      part[yh][yc] = sacc;
     }
     __syncthreads();
     if (tid < mk) {
@@ -627,35 +635,43 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_bwd_kernel(const float *__r
     const int64_t k0 = (int64_t)K * TB;
     const int mk = (int)((n - k0) < TB ? (n - k0) : TB);
     const bool full = (4 * lane + 3) < mk;
+    // this warp's columns of Y_K for the final product, loaded before any wait
+    float4 ycol[8];
+    {
+      const float *Y = Yinv + (int64_t)K * TB * TB;
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        ycol[q] = __ldg(reinterpret_cast<const float4 *>(Y + (int64_t)(8 * warp + q) * TB) + lane);
+    }
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
     bool alive = true;
     for (int J = nb - 1; J > K && alive; --J) {
-      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status);
-      if (!alive) break;
       const int64_t j0 = (int64_t)J * TB;
       const int mj = (int)((n - j0) < TB ? (n - j0) : TB);
-      float xs[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) xs[q] = (8 * warp + q < mj) ? __ldcg(x + j0 + 8 * warp + q) : 0.0f;
+      float4 u[8];  // U_KJ does not depend on x: load it before waiting for x_J
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int cj = 8 * warp + q;
-        if (cj < mj) {
-          const float xj = xs[q];
-          const float *col = U + (j0 + cj) * n + k0;
-          if (full) {
-            const float4 u = __ldg(reinterpret_cast<const float4 *>(col) + lane);
-            a0 = __fmaf_rn(u.x, xj, a0);
-            a1 = __fmaf_rn(u.y, xj, a1);
-            a2 = __fmaf_rn(u.z, xj, a2);
-            a3 = __fmaf_rn(u.w, xj, a3);
-          } else {
-            const int rr = 4 * lane;
-            if (rr < mk) a0 = __fmaf_rn(col[rr], xj, a0);
-            if (rr + 1 < mk) a1 = __fmaf_rn(col[rr + 1], xj, a1);
-            if (rr + 2 < mk) a2 = __fmaf_rn(col[rr + 2], xj, a2);
-          }
+        const float *col = U + (j0 + cj) * n + k0;
+        if (cj >= mj) {
+          u[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else if (full) {
+          u[q] = __ldg(reinterpret_cast<const float4 *>(col) + lane);
+        } else {
+          const int rr = 4 * lane;
+          u[q] = make_float4(rr < mk ? col[rr] : 0.0f, rr + 1 < mk ? col[rr + 1] : 0.0f,
+                             rr + 2 < mk ? col[rr + 2] : 0.0f, 0.0f);
         }
+      }
+      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status);
+      if (!alive) break;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float xj = (8 * warp + q < mj) ? __ldcg(x + j0 + 8 * warp + q) : 0.0f;
+        a0 = __fmaf_rn(u[q].x, xj, a0);
+        a1 = __fmaf_rn(u[q].y, xj, a1);
+        a2 = __fmaf_rn(u[q].z, xj, a2);
+        a3 = __fmaf_rn(u[q].w, xj, a3);
       }
     }
     part[warp][4 * lane] = a0;
@@ -671,16 +687,11 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_bwd_kernel(const float *__r
     }
     __syncthreads();
     {  // x_K[c] = sum_c' Y_K(c', c) w[c'] (column c of Y_K is contiguous): warp per 8 c
-      const float *Y = Yinv + (int64_t)K * TB * TB;
       const float4 w4 = reinterpret_cast<const float4 *>(wv)[lane];
-      float4 yc[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        yc[q] = __ldg(reinterpret_cast<const float4 *>(Y + (int64_t)(8 * warp + q) * TB) + lane);
       float v[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        v[q] = warp_sum(yc[q].x * w4.x + yc[q].y * w4.y + yc[q].z * w4.z + yc[q].w * w4.w);
+        v[q] = warp_sum(ycol[q].x * w4.x + ycol[q].y * w4.y + ycol[q].z * w4.z + ycol[q].w * w4.w);
       if (lane == 0) {
 #pragma unroll
         for (int q = 0; q < 8; ++q)

@@ -10,11 +10,13 @@ Two ways to form T:
     ``O(s).O(s') = (t_s.t_s')(1 + x_s.x_s') + x_s.x_s'`` (t = tanh theta) turns
     the (n x n x P) contraction into (n x n x M), and O is never stored.  For an
     FP32 t the contraction is shifted by the column mean and the shift is added
-    back in double-float (no cancellation); ``gram_mode=1`` (default) contracts
-    in FP32 on the CUDA cores, ``2`` / ``3`` on the tensor cores (tcgen05) with t
-    rounded to hi + lo BF16 pairs / one BF16.  At n = 16,384 and diag_shift
-    1e-4 an entrywise T error of ~1e-6 already has a spectral norm close to the
-    shift, so only mode 1 keeps T positive definite there (see the design notes);
+    back in double-float (no cancellation); ``gram_mode=2`` (default) contracts
+    on the tensor cores (tcgen05) with t rounded to hi + lo BF16 pairs (all four
+    products, so T is the Gram matrix of a 16-bit-mantissa Jacobian; the large
+    hi * hi part accumulates apart from the small cross terms), ``3`` with one
+    BF16, ``1`` in FP32 on the CUDA cores.  At n = 16,384 and diag_shift 1e-4 the
+    minSR update of mode 2 is within 1.2e-4 (relative) of the all-FP64 one,
+    mode 1 within 2.5e-4, mode 3 within 2.4e-2;
   * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
     and a cuBLAS SYRK.
 Solvers (``solve=``):
@@ -55,7 +57,7 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     s = 1.0 / math.sqrt(n)
     mode = None
     if gram == "structured":
-        mode = gram_mode if gram_mode is not None else (0 if t.dtype == torch.float64 else 1)
+        mode = gram_mode if gram_mode is not None else (0 if t.dtype == torch.float64 else 2)
     obar = K.column_means(t, x, N, M)
     dv = K.center_scale(e, mean_dev, 2.0 * s)
     status = _status()
