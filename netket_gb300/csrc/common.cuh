@@ -92,13 +92,29 @@ __device__ __forceinline__ float log_cosh(float x) {
   x = fabsf(x);
   return x + log1pf(expf(-2.0f * x)) - 0.693147180559945309f;
 }
-// Same formula on the special-function units (__expf / __logf, one MUFU op
-// each): 1 + exp(-2|x|) lies in (1, 2], so log(1 + e) loses nothing to the
-// missing log1p; absolute error ~1e-7, used by the FP32 sampler and local-energy
-// kernels (whose results carry a 1e-4 relative bound).
+// Same formula with one special-function op: e = exp(-2|x|) on the MUFU unit
+// (__expf), log1p(e) for e in (0, 1] as a degree-9 polynomial in e on the FMA
+// pipe (a Chebyshev fit of log1p on [0, 1] made for this library, converted to
+// the monomial basis; error 5e-9 in exact arithmetic, ~1e-7 after FP32 Horner
+// rounding).  The sampler and local-energy kernels evaluate hundreds of
+// log_cosh per proposal / connected element, and the MUFU unit (a quarter of
+// the FMA rate) bounds them.  Absolute error of the result ~5e-7 at |x| ~ 20
+// (half an ulp of the result), ~1e-7 for |x| < 4; used by the FP32 paths,
+// whose results carry a 1e-4 relative bound.
 __device__ __forceinline__ float log_cosh_fast(float x) {
   x = fabsf(x);
-  return x + __logf(1.0f + __expf(-2.0f * x)) - 0.693147180559945309f;
+  const float e = __expf(-2.0f * x);
+  float p = 0.003752624150365591f;
+  p = __fmaf_rn(p, e, -0.02303827926516533f);
+  p = __fmaf_rn(p, e, 0.06651248037815094f);
+  p = __fmaf_rn(p, e, -0.12526661157608032f);
+  p = __fmaf_rn(p, e, 0.1846884787082672f);
+  p = __fmaf_rn(p, e, -0.24635660648345947f);
+  p = __fmaf_rn(p, e, 0.3328184187412262f);
+  p = __fmaf_rn(p, e, -0.4999622404575348f);
+  p = __fmaf_rn(p, e, 0.999998927116394f);
+  p = __fmaf_rn(p, e, 5.239402245393876e-09f);
+  return x + p - 0.693147180559945309f;
 }
 __device__ __forceinline__ double log_cosh_fast(double x) { return log_cosh(x); }
 

@@ -214,26 +214,30 @@ __global__ void info_accumulate_kernel(const int *info, int32_t *status) {
 constexpr int LEAF_LD = LEAF_B + 4;
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
+// 4-byte asynchronous global -> shared copies (cp.async), so that all of a
+// thread's loads are in flight at once; cp_async_wait() completes them.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // Load the upper triangle of the b x b column-major block A (lda) into Us
 // (LEAF_ROWS x LEAF_LD), zeros elsewhere: the 4 x 4 tiles of a block whose size
-// is not a multiple of 4 run up to 3 rows / columns past it.
+// is not a multiple of 4 run up to 3 rows / columns past it.  The caller
+// completes the copies with cp_async_wait() and a barrier.
 constexpr int LEAF_ROWS = LEAF_B + 4;
 __device__ inline void leaf_load_upper(float *Us, const float *A, int64_t lda, int b) {
-  constexpr int TOTAL = LEAF_ROWS * LEAF_LD, BATCH = 8;
-  for (int e0 = threadIdx.x; e0 < TOTAL; e0 += BATCH * blockDim.x) {
-    float v[BATCH];
-#pragma unroll
-    for (int u = 0; u < BATCH; ++u) {  // issue all loads of the batch first
-      const int e = e0 + u * blockDim.x;
-      const int j = e / LEAF_ROWS, i = e - j * LEAF_ROWS;
-      v[u] = (e < TOTAL && i <= j && j < b) ? A[(int64_t)j * lda + i] : 0.0f;
-    }
-#pragma unroll
-    for (int u = 0; u < BATCH; ++u) {
-      const int e = e0 + u * blockDim.x;
-      const int j = e / LEAF_ROWS, i = e - j * LEAF_ROWS;
-      if (e < TOTAL) Us[i * LEAF_LD + j] = v[u];
-    }
+  for (int e = threadIdx.x; e < LEAF_ROWS * LEAF_LD; e += blockDim.x) {
+    const int j = e / LEAF_ROWS, i = e - j * LEAF_ROWS;
+    if (i <= j && j < b)
+      cp_async4(&Us[i * LEAF_LD + j], A + (int64_t)j * lda + i);
+    else
+      Us[i * LEAF_LD + j] = 0.0f;
   }
 }
 
@@ -284,6 +288,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) potrf_leaf_kernel(float *A, int6
   __shared__ __align__(16) float rowk[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   leaf_load_upper(Us, A, lda, b);
+  cp_async_wait();
   __syncthreads();
   bool bad = false;
   for (int p = 0; p < b; p += 32) {
@@ -440,24 +445,14 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsm_leaf_kernel(const float *__
   const int64_t c0 = (int64_t)blockIdx.x * TRSM_COLS;
   const int nc = (int)((nrhs - c0) < TRSM_COLS ? (nrhs - c0) : TRSM_COLS);
   leaf_load_upper(Us, Ug, ldu, m);
-  {
-    constexpr int TOTAL = TRSM_LD * LEAF_ROWS, BATCH = 8;
-    for (int e0 = tid; e0 < TOTAL; e0 += BATCH * blockDim.x) {
-      float v[BATCH];
-#pragma unroll
-      for (int u = 0; u < BATCH; ++u) {
-        const int e = e0 + u * blockDim.x;
-        const int c = e / LEAF_ROWS, k = e - c * LEAF_ROWS;
-        v[u] = (e < TOTAL && c < nc && k < m) ? B[(c0 + c) * ldb + k] : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < BATCH; ++u) {
-        const int e = e0 + u * blockDim.x;
-        const int c = e / LEAF_ROWS, k = e - c * LEAF_ROWS;
-        if (e < TOTAL) Bs[k * TRSM_LD + c] = v[u];
-      }
-    }
+  for (int e = tid; e < TRSM_LD * LEAF_ROWS; e += blockDim.x) {
+    const int c = e / LEAF_ROWS, k = e - c * LEAF_ROWS;
+    if (c < nc && k < m)
+      cp_async4(&Bs[k * TRSM_LD + c], B + (c0 + c) * ldb + k);
+    else
+      Bs[k * TRSM_LD + c] = 0.0f;
   }
+  cp_async_wait();
   __syncthreads();
   if (tid < m) rinv[tid] = 1.0f / Us[tid * LEAF_LD + tid];
   __syncthreads();
@@ -526,6 +521,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_inv_kernel(const float *__r
     const int c = e / LEAF_ROWS, k = e - c * LEAF_ROWS;
     Bs[k * TRSM_LD + c] = (c < TRSM_COLS && k < m && k == cbase + c) ? 1.0f : 0.0f;
   }
+  cp_async_wait();
   __syncthreads();
   if (tid < m) rinv[tid] = 1.0f / Us[tid * LEAF_LD + tid];
   __syncthreads();

@@ -60,19 +60,32 @@ __device__ inline LocalConnShared local_conn_shared_layout(unsigned char *p,
   return s;
 }
 
-// Block-wide exclusive scan of per-thread values; returns the prefix of this
+// A group of threads that synchronise together: the whole CTA (bar == 0,
+// __syncthreads) or a warp-aligned slice of it with its own named barrier.
+struct Grp {
+  int tid, size, bar;
+};
+__device__ inline Grp cta_grp() { return Grp{(int)threadIdx.x, (int)blockDim.x, 0}; }
+__device__ inline void grp_sync(const Grp &g) {
+  if (g.bar == 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;" ::"r"(g.bar), "r"(g.size) : "memory");
+}
+
+// Group-wide exclusive scan of per-thread values; returns the prefix of this
 // thread and writes the total to *total (all threads).  scratch: 32 ints.
-__device__ inline int block_exclusive_scan(int v, int *scratch, int *total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+__device__ inline int grp_exclusive_scan(const Grp &g, int v, int *scratch, int *total) {
+  const int lane = g.tid & 31, wid = g.tid >> 5, nw = g.size >> 5;
   int inc = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     int t = __shfl_up_sync(0xffffffffu, inc, o);
     if (lane >= o) inc += t;
   }
-  __syncthreads();
+  grp_sync(g);
   if (lane == 31) scratch[wid] = inc;
-  __syncthreads();
+  grp_sync(g);
   if (wid == 0) {
     int w = (lane < nw) ? scratch[lane] : 0;
     int wi = w;
@@ -84,22 +97,27 @@ __device__ inline int block_exclusive_scan(int v, int *scratch, int *total) {
     if (lane < nw) scratch[lane] = wi - w;  // exclusive warp offsets
     if (lane == nw - 1) scratch[31] = wi;   // total
   }
-  __syncthreads();
+  grp_sync(g);
   int res = scratch[wid] + inc - v;
   *total = scratch[31];
-  __syncthreads();
+  grp_sync(g);
   return res;
+}
+
+__device__ inline int block_exclusive_scan(int v, int *scratch, int *total) {
+  return grp_exclusive_scan(cta_grp(), v, scratch, total);
 }
 
 // Requires sh.xs to hold the configuration.  Returns the number of kept
 // entries (<= max_conn_size); slots [0, kept) are filled.
-__device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnShared &sh) {
+__device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnShared &sh,
+                                           const Grp &g) {
   const int T = op.n_terms, S = op.max_sites, R = op.max_rows, C = op.max_conns;
   const int K = op.max_conn_size;
   const double cut = op.mel_cutoff;
   // contiguous chunk of terms per thread keeps the scan order equal to term order
-  const int per = (T + blockDim.x - 1) / blockDim.x;
-  const int t0 = threadIdx.x * per, t1 = min(T, t0 + per);
+  const int per = (T + g.size - 1) / g.size;
+  const int t0 = g.tid * per, t1 = min(T, t0 + per);
   int mine = 0;
   for (int t = t0; t < t1; ++t) {
     const int sz = op.acting_size[t];
@@ -117,16 +135,16 @@ __device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnSha
   }
   int *scratch = reinterpret_cast<int *>(sh.misc + 4);
   int total = 0;
-  int pre = block_exclusive_scan(mine, scratch, &total);
+  int pre = grp_exclusive_scan(g, mine, scratch, &total);
   // rows are visible after the scan's barriers
-  if (threadIdx.x == 0) {
+  if (g.tid == 0) {
     int base = 0;
     if (op.nonzero_diagonal) {
       double tot = 0.0;
       int t = 0;
-      for (int g = 0; g < op.n_groups; ++g) {
+      for (int gg = 0; gg < op.n_groups; ++gg) {
         double gs = 0.0;
-        for (; t < op.group_end[g]; ++t) gs += op.diag_mels[(int64_t)t * R + sh.row[t]];
+        for (; t < op.group_end[gg]; ++t) gs += op.diag_mels[(int64_t)t * R + sh.row[t]];
         tot += gs;
       }
       double d = op.constant + tot;
@@ -139,7 +157,7 @@ __device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnSha
     }
     sh.misc[0] = base;
   }
-  __syncthreads();
+  grp_sync(g);
   const int base = sh.misc[0];
   int pos = base + pre;
   for (int t = t0; t < t1; ++t) {
@@ -158,9 +176,13 @@ __device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnSha
       }
     }
   }
-  __syncthreads();
+  grp_sync(g);
   int kept = base + total;
   return kept < K ? kept : K;
+}
+
+__device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnShared &sh) {
+  return local_conn_enumerate(op, sh, cta_grp());
 }
 
 inline int validate_local_op(const vmck_local_op &op) {

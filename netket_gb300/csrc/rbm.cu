@@ -131,12 +131,25 @@ __global__ void eloc_reduce_kernel(const T *__restrict__ lp, const T *__restrict
 // with d_s = x'_s - x_s.  Warps take connected elements round-robin; lanes split j.
 constexpr int EL_THREADS = 128;
 
+// block_sum over a thread group (same tree: warp shuffles, then the warp totals
+// in one warp).  red: 32 elements of this group.
+template <typename T>
+__device__ inline T grp_sum(const Grp &g, T v, T *red) {
+  const int lane = g.tid & 31, wid = g.tid >> 5, nw = g.size >> 5;
+  v = warp_sum(v);
+  grp_sync(g);
+  if (lane == 0) red[wid] = v;
+  grp_sync(g);
+  T t = (lane < nw) ? red[lane] : T(0);
+  return warp_sum(t);
+}
+
 template <typename T>
 __device__ inline void theta_and_logpsi(const RbmParams<T> &P, const int8_t *xs, T *th, T *lc,
-                                        T *red, T *logpsi_out) {
+                                        T *red, T *logpsi_out, const Grp &g) {
   const int N = P.N, M = P.M;
   T part = 0;
-  for (int j = threadIdx.x; j < M; j += blockDim.x) {
+  for (int j = g.tid; j < M; j += g.size) {
     T acc = P.b[j];
     for (int i = 0; i < N; ++i) acc += (T)xs[i] * P.W[(int64_t)i * M + j];
     th[j] = acc;
@@ -144,9 +157,15 @@ __device__ inline void theta_and_logpsi(const RbmParams<T> &P, const int8_t *xs,
     lc[j] = l;
     part += l;
   }
-  for (int i = threadIdx.x; i < N; i += blockDim.x) part += (T)xs[i] * P.a[i];
-  T tot = block_sum(part, red);
-  if (logpsi_out && threadIdx.x == 0) *logpsi_out = tot;
+  for (int i = g.tid; i < N; i += g.size) part += (T)xs[i] * P.a[i];
+  T tot = grp_sum(g, part, red);
+  if (logpsi_out && g.tid == 0) *logpsi_out = tot;
+}
+
+template <typename T>
+__device__ inline void theta_and_logpsi(const RbmParams<T> &P, const int8_t *xs, T *th, T *lc,
+                                        T *red, T *logpsi_out) {
+  theta_and_logpsi(P, xs, th, lc, red, logpsi_out, cta_grp());
 }
 
 template <typename T>
@@ -248,55 +267,66 @@ __global__ void __launch_bounds__(EL_THREADS) batched_eloc_ising_kernel(
   }
 }
 
+// Local energy of sample b by one 4-warp group g (the whole CTA in
+// eloc_local_kernel): theta, enumeration of the connected elements, warps take
+// them round-robin, lane 0 accumulates, the group's tree sums the warps.
+template <typename T>
+__device__ inline void eloc_local_sample(const RbmParams<T> &P, const int8_t *__restrict__ x,
+                                         int64_t b, const vmck_local_op &op, double *eloc,
+                                         T *logpsi_out, LocalConnShared &sh, T *th, T *lc, T *red,
+                                         double *redd, const Grp &g) {
+  const int N = P.N;
+  const int warp = g.tid >> 5, lane = g.tid & 31, nw = g.size >> 5;
+  const int S = op.max_sites;
+  for (int i = g.tid; i < N; i += g.size) sh.xs[i] = x[b * N + i];
+  grp_sync(g);
+  theta_and_logpsi(P, sh.xs, th, lc, red, logpsi_out ? logpsi_out + b : nullptr, g);
+  int kept = local_conn_enumerate(op, sh, g);
+  double acc = 0.0;
+  for (int k = warp; k < kept; k += nw) {
+    double mel = sh.slot_mel[k];
+    int t = sh.slot_term[k];
+    int site[4];
+    T d[4];
+    int ns = 0;
+    if (t >= 0) {
+      const int row = sh.row[t], c = sh.slot_col[k], sz = op.acting_size[t];
+      const int8_t *xpv = op.x_prime + (((int64_t)t * op.max_rows + row) * op.max_conns + c) * S;
+      for (int q = 0; q < sz; ++q) {
+        int st = op.acting_on[t * S + q];
+        int dv = (int)xpv[q] - (int)sh.xs[st];
+        if (dv != 0) {
+          site[ns] = st;
+          d[ns] = (T)dv;
+          ++ns;
+        }
+      }
+    }
+    if (ns == 0) {
+      if (lane == 0) acc += mel;
+    } else {
+      T lr = warp_log_ratio(P, th, lc, site, d, ns);
+      if (lane == 0) acc += mel * exp_ratio(lr);
+    }
+  }
+  double e = grp_sum(g, acc, redd);
+  if (g.tid == 0) eloc[b] = e;
+  grp_sync(g);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(EL_THREADS) eloc_local_kernel(
     RbmParams<T> P, const int8_t *__restrict__ x, int64_t n, vmck_local_op op, double *eloc,
     T *logpsi_out) {
   extern __shared__ unsigned char smem_raw[];
-  const int M = P.M, N = P.N;
   LocalConnShared sh = local_conn_shared_layout(smem_raw, op);
   T *th = reinterpret_cast<T *>(sh.end);
-  T *lc = th + M;
+  T *lc = th + P.M;
   __shared__ T red[32];
   __shared__ double redd[32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const int S = op.max_sites;
-  for (int64_t b = blockIdx.x; b < n; b += gridDim.x) {
-    for (int i = threadIdx.x; i < N; i += blockDim.x) sh.xs[i] = x[b * N + i];
-    __syncthreads();
-    theta_and_logpsi(P, sh.xs, th, lc, red, logpsi_out ? logpsi_out + b : nullptr);
-    int kept = local_conn_enumerate(op, sh);
-    double acc = 0.0;
-    for (int k = warp; k < kept; k += nw) {
-      double mel = sh.slot_mel[k];
-      int t = sh.slot_term[k];
-      int site[4];
-      T d[4];
-      int ns = 0;
-      if (t >= 0) {
-        const int row = sh.row[t], c = sh.slot_col[k], sz = op.acting_size[t];
-        const int8_t *xpv = op.x_prime + (((int64_t)t * op.max_rows + row) * op.max_conns + c) * S;
-        for (int q = 0; q < sz; ++q) {
-          int st = op.acting_on[t * S + q];
-          int dv = (int)xpv[q] - (int)sh.xs[st];
-          if (dv != 0) {
-            site[ns] = st;
-            d[ns] = (T)dv;
-            ++ns;
-          }
-        }
-      }
-      if (ns == 0) {
-        if (lane == 0) acc += mel;
-      } else {
-        T lr = warp_log_ratio(P, th, lc, site, d, ns);
-        if (lane == 0) acc += mel * exp_ratio(lr);
-      }
-    }
-    double e = block_sum(acc, redd);
-    if (threadIdx.x == 0) eloc[b] = e;
-    __syncthreads();
-  }
+  const Grp g = cta_grp();
+  for (int64_t b = blockIdx.x; b < n; b += gridDim.x)
+    eloc_local_sample(P, x, b, op, eloc, logpsi_out, sh, th, lc, red, redd, g);
 }
 
 // ============================================================ O^T v

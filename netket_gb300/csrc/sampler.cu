@@ -245,6 +245,272 @@ __global__ void batch_advance_counters_kernel(vmck_batch_chains *inst, int n_ins
   if (i < n_inst) inst[i].counter += (uint64_t)steps * (uint64_t)inst[i].sweep_size;
 }
 
+// ------------------------------------------------------------ Exchange, W in smem
+// Exchange-rule sweeps for an FP32 RBM whose parameters fit in shared memory:
+// the CTA stages W, b, a once; one warp drives one chain with theta and
+// log_cosh(theta) in registers (lane l holds hidden units l + 32 r).  The set of
+// hoppable clusters (x_u != x_v) is a per-chain bitmask in shared memory, so a
+// proposal picks the k-th hoppable cluster with a warp scan of the word counts
+// and updates the hoppable count from the clusters incident to the two swapped
+// sites (incidence lists built in shared memory; sites with more than 16
+// incident clusters fall back to a full recount).  Random stream, proposal
+// order and every floating-point expression match metropolis_kernel<float, 1>,
+// so the samples are identical.
+constexpr int XS_MAXDEG = 16;
+
+__device__ __forceinline__ int warp_sum_int(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+constexpr int XS_MAX_WARPS = 28;  // 896 threads: 73 registers per thread
+
+template <int R>
+__global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem_kernel(
+    const float *__restrict__ params, int N, int M, int8_t *sigma, double *log_prob,
+    int64_t *n_accepted, int B, int sweep, int n_discard, int L, int8_t *samples, uint32_t k0,
+    uint32_t k1, uint64_t counter, const int32_t *__restrict__ clusters, int C, int wpb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nwords = (C + 31) >> 5;
+  float *Ws = reinterpret_cast<float *>(smem_raw);                    // N x M
+  float *bs = Ws + (size_t)N * M;                                     // M
+  float *as = bs + M;                                                 // N
+  int16_t *cl = reinterpret_cast<int16_t *>(as + N);                  // 2C
+  int16_t *inc = cl + 2 * C;                                          // N x XS_MAXDEG
+  int *deg = reinterpret_cast<int *>(                                 // N
+      (reinterpret_cast<uintptr_t>(inc + (size_t)N * XS_MAXDEG) + 3) & ~uintptr_t(3));
+  __shared__ int overflow;
+  unsigned char *per_warp_base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(deg + N) + 15) & ~uintptr_t(15));
+  const size_t per_warp = (((size_t)N + 15) & ~size_t(15)) + 4 * (size_t)nwords;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  {  // stage the parameters, clusters and incidence lists
+    const float *Wg = params + M;
+    for (int64_t e = tid; e < (int64_t)N * M; e += blockDim.x) Ws[e] = Wg[e];
+    for (int j = tid; j < M; j += blockDim.x) bs[j] = params[j];
+    for (int i = tid; i < N; i += blockDim.x) {
+      as[i] = params[M + (int64_t)N * M + i];
+      deg[i] = 0;
+    }
+    for (int q = tid; q < 2 * C; q += blockDim.x) cl[q] = (int16_t)clusters[q];
+    if (tid == 0) overflow = 0;
+    __syncthreads();
+    for (int q = tid; q < C; q += blockDim.x) {
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int site = cl[2 * q + e];
+        const int pos = atomicAdd(&deg[site], 1);
+        if (pos < XS_MAXDEG) inc[site * XS_MAXDEG + pos] = (int16_t)q;
+        else overflow = 1;
+      }
+    }
+    __syncthreads();
+  }
+  const bool full_recount = overflow != 0;
+  const int b = blockIdx.x * wpb + warp;
+  if (b >= B) return;
+  int8_t *xs = reinterpret_cast<int8_t *>(per_warp_base + warp * per_warp);
+  uint32_t *mask = reinterpret_cast<uint32_t *>(xs + ((N + 15) & ~15));
+  int8_t *sigma_row = sigma + (int64_t)b * N;
+  for (int i = lane; i < N; i += 32) xs[i] = sigma_row[i];
+  __syncwarp();
+  // hoppable bitmask and count
+  int hop = 0;
+  for (int w = lane; w < nwords; w += 32) {
+    uint32_t bits = 0u;
+    for (int t = 0; t < 32; ++t) {
+      const int q = 32 * w + t;
+      if (q < C && xs[cl[2 * q]] != xs[cl[2 * q + 1]]) bits |= 1u << t;
+    }
+    mask[w] = bits;
+    hop += __popc(bits);
+  }
+  hop = warp_sum_int(hop);
+  __syncwarp();
+  float th[R], lc[R];
+  float logpsi = 0.0f;
+  auto recompute = [&]() {
+    float part = 0.0f;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int j = lane + 32 * r;
+      if (j < M) {
+        float acc = bs[j];
+        for (int i = 0; i < N; ++i) acc += (float)xs[i] * Ws[i * M + j];
+        th[r] = acc;
+        const float l = log_cosh_fast(acc);
+        lc[r] = l;
+        part += l;
+      }
+    }
+    for (int i = lane; i < N; i += 32) part += (float)xs[i] * as[i];
+    logpsi = warp_sum(part);
+    __syncwarp();
+  };
+  int64_t acc_count = 0;
+  const int total = n_discard + L;
+  for (int step = 0; step < total; ++step) {
+    recompute();
+    for (int p = 0; p < sweep; ++p) {
+      const uint64_t pidx = counter + (uint64_t)step * sweep + p;
+      u32x4 rr = philox4x32_10(u32x4{(uint32_t)pidx, (uint32_t)(pidx >> 32), (uint32_t)b, 0u}, k0, k1);
+      if (hop == 0) continue;  // no move possible: rejected
+      // the k-th hoppable cluster in cluster order
+      int k = (int)below(rr.x, (uint32_t)hop);
+      const uint32_t wbits = lane < nwords ? mask[lane] : 0u;
+      const int cnt = __popc(wbits);
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int excl = incl - cnt;
+      const bool owner = excl <= k && k < incl;
+      const unsigned ob = __ballot_sync(0xffffffffu, owner);
+      if (ob == 0u) continue;  // unreachable while hop matches the mask
+      const int src = __ffs(ob) - 1;
+      int pick = -1;
+      if (owner) {
+        const unsigned bit = __fns(wbits, 0u, k - excl + 1);
+        if (bit < 32u) pick = 32 * lane + (int)bit;
+      }
+      pick = __shfl_sync(0xffffffffu, pick, src);
+      if (pick < 0 || pick >= C) continue;  // likewise unreachable; never index out of range
+      const int su = cl[2 * pick], sv = cl[2 * pick + 1];
+      const int8_t xu = xs[su], xv = xs[sv];
+      const float du = (float)(xv - xu), dv = (float)(xu - xv);
+      // change of the hoppable count: clusters incident to su (lanes 0-15) or sv
+      // (lanes 16-31, skipping those that also touch su)
+      int q = -1, newh = 0;
+      int hop_new;
+      if (!full_recount) {
+        const int site = lane < 16 ? su : sv, slot = lane & 15;
+        if (slot < deg[site]) {
+          q = inc[site * XS_MAXDEG + slot];
+          const int a0 = cl[2 * q], a1 = cl[2 * q + 1];
+          if (lane >= 16 && (a0 == su || a1 == su)) q = -1;
+          if (q >= 0) {
+            const int8_t x0 = a0 == su ? xv : (a0 == sv ? xu : xs[a0]);
+            const int8_t x1 = a1 == su ? xv : (a1 == sv ? xu : xs[a1]);
+            newh = x0 != x1;
+          }
+        }
+        const int oldh = q >= 0 ? (int)((mask[q >> 5] >> (q & 31)) & 1u) : 0;
+        hop_new = hop + warp_sum_int(q >= 0 ? newh - oldh : 0);
+      } else {
+        int h2 = 0;
+        for (int q0 = 0; q0 < C; q0 += 32) {
+          const int qq = q0 + lane;
+          if (qq < C) {
+            const int a0 = cl[2 * qq], a1 = cl[2 * qq + 1];
+            const int8_t x0 = a0 == su ? xv : (a0 == sv ? xu : xs[a0]);
+            const int8_t x1 = a1 == su ? xv : (a1 == sv ? xu : xs[a1]);
+            h2 += x0 != x1;
+          }
+        }
+        hop_new = warp_sum_int(h2);
+      }
+      const float corr = logf((float)hop) - logf((float)hop_new);
+      // log-ratio of the RBM amplitude
+      float sacc = 0.0f;
+      const float *Wu = Ws + su * M, *Wv = Ws + sv * M;
+      float ln[R];  // log_cosh of the proposal, kept for an accepted move
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int j = lane + 32 * r;
+        ln[r] = 0.0f;
+        if (j < M) {
+          float t = th[r] + du * Wu[j];
+          t += dv * Wv[j];
+          const float l = log_cosh_fast(t);
+          ln[r] = l;
+          sacc += l - lc[r];
+        }
+      }
+      float s = warp_sum(sacc);
+      s += du * as[su];
+      s += dv * as[sv];
+      const float dlp = 2.0f * s;
+      const float u = u01f(rr.y);
+      if (u < expf(dlp + corr)) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int j = lane + 32 * r;
+          if (j < M) {
+            float t = th[r] + du * Wu[j];
+            t += dv * Wv[j];
+            th[r] = t;
+            lc[r] = ln[r];
+          }
+        }
+        __syncwarp();
+        if (lane == 0) {
+          xs[su] = (int8_t)(xu + (int)du);
+          xs[sv] = (int8_t)(xv + (int)dv);
+        }
+        if (!full_recount) {
+          if (q >= 0) {
+            const uint32_t bit = 1u << (q & 31);
+            if (newh) atomicOr(&mask[q >> 5], bit);
+            else atomicAnd(&mask[q >> 5], ~bit);
+          }
+        } else {
+          __syncwarp();
+          for (int w = lane; w < nwords; w += 32) {
+            uint32_t bits = 0u;
+            for (int t = 0; t < 32; ++t) {
+              const int qq = 32 * w + t;
+              if (qq < C && xs[cl[2 * qq]] != xs[cl[2 * qq + 1]]) bits |= 1u << t;
+            }
+            mask[w] = bits;
+          }
+        }
+        hop = hop_new;
+        logpsi += s;
+        ++acc_count;
+      }
+      __syncwarp();
+    }
+    if (step >= n_discard) {
+      int8_t *dst = samples + ((int64_t)b * L + (step - n_discard)) * N;
+      for (int i = lane; i < N; i += 32) dst[i] = xs[i];
+    }
+  }
+  recompute();
+  for (int i = lane; i < N; i += 32) sigma_row[i] = xs[i];
+  if (lane == 0) {
+    log_prob[b] = 2.0 * (double)logpsi;
+    n_accepted[b] += acc_count;
+  }
+}
+
+static size_t exchange_smem_bytes(int N, int M, int C, int wpb) {
+  const int nwords = (C + 31) >> 5;
+  size_t bytes = (size_t)N * M * 4 + (size_t)M * 4 + (size_t)N * 4 + (size_t)C * 4 +
+                 (size_t)N * XS_MAXDEG * 2 + 4 + (size_t)N * 4 + 16;
+  bytes += (size_t)wpb * ((((size_t)N + 15) & ~size_t(15)) + 4 * (size_t)nwords);
+  return bytes + 64;
+}
+
+template <int R>
+static int launch_exchange_smem(cudaStream_t st, const float *p, int N, int M, int8_t *sigma,
+                                double *log_prob, int64_t *n_acc, int B, int sweep, int n_discard,
+                                int L, int8_t *samples, uint32_t k0, uint32_t k1, uint64_t counter,
+                                const int32_t *clusters, int C, int sms) {
+  int wpb = (B + sms - 1) / sms;
+  if (wpb > XS_MAX_WARPS) wpb = XS_MAX_WARPS;
+  const size_t smem = exchange_smem_bytes(N, M, C, wpb);
+  VMCK_CUDA(cudaFuncSetAttribute(metropolis_exchange_smem_kernel<R>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int grid = (B + wpb - 1) / wpb;
+  metropolis_exchange_smem_kernel<R><<<grid, 32 * wpb, smem, st>>>(
+      p, N, M, sigma, log_prob, n_acc, B, sweep, n_discard, L, samples, k0, k1, counter, clusters,
+      C, wpb);
+  return check_launch("metropolis_sample (exchange, shared-memory weights)");
+}
+
 template <typename T>
 int launch_metropolis(cudaStream_t st, const void *params, int N, int M, int8_t *sigma,
                       double *log_prob, int64_t *n_acc, int B, int sweep, int n_discard, int L,
@@ -260,6 +526,26 @@ int launch_metropolis(cudaStream_t st, const void *params, int N, int M, int8_t 
   int grid = (B + wpb - 1) / wpb;
   const T *p = static_cast<const T *>(params);
   uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  if (sizeof(T) == 4 && rule == 1 && C <= 1024 && M <= 512) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int wpb = std::min((B + sms - 1) / sms, XS_MAX_WARPS);
+    if (exchange_smem_bytes(N, M, C, wpb) <= 200 * 1024) {
+      const float *pf = reinterpret_cast<const float *>(params);
+      if (M <= 128)
+        return launch_exchange_smem<4>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard,
+                                       L, samples, k0, k1, counter, clusters, C, sms);
+      if (M <= 256)
+        return launch_exchange_smem<8>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard,
+                                       L, samples, k0, k1, counter, clusters, C, sms);
+      if (M <= 416)
+        return launch_exchange_smem<13>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard,
+                                        L, samples, k0, k1, counter, clusters, C, sms);
+      return launch_exchange_smem<16>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard,
+                                      L, samples, k0, k1, counter, clusters, C, sms);
+    }
+  }
   if (rule == 0) {
     if (smem > 48 * 1024)
       VMCK_CUDA(cudaFuncSetAttribute(metropolis_kernel<T, 0>,
