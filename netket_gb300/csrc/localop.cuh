@@ -109,9 +109,11 @@ __device__ inline int block_exclusive_scan(int v, int *scratch, int *total) {
 }
 
 // Requires sh.xs to hold the configuration.  Returns the number of kept
-// entries (<= max_conn_size); slots [0, kept) are filled.
+// entries (<= max_conn_size); slots [0, kept) are filled.  seq_diag: sum the
+// diagonal sequentially in NetKet's order on one thread (bit-exact parity
+// path); otherwise warp 0 sums it with a shuffle tree (FP32 consumers).
 __device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnShared &sh,
-                                           const Grp &g) {
+                                           const Grp &g, bool seq_diag = true) {
   const int T = op.n_terms, S = op.max_sites, R = op.max_rows, C = op.max_conns;
   const int K = op.max_conn_size;
   const double cut = op.mel_cutoff;
@@ -137,15 +139,24 @@ __device__ inline int local_conn_enumerate(const vmck_local_op &op, LocalConnSha
   int total = 0;
   int pre = grp_exclusive_scan(g, mine, scratch, &total);
   // rows are visible after the scan's barriers
+  double dtree = 0.0;
+  if (!seq_diag && op.nonzero_diagonal && g.tid < 32) {
+    for (int t = g.tid; t < T; t += 32) dtree += op.diag_mels[(int64_t)t * R + sh.row[t]];
+    dtree = warp_sum(dtree);
+  }
   if (g.tid == 0) {
     int base = 0;
     if (op.nonzero_diagonal) {
       double tot = 0.0;
-      int t = 0;
-      for (int gg = 0; gg < op.n_groups; ++gg) {
-        double gs = 0.0;
-        for (; t < op.group_end[gg]; ++t) gs += op.diag_mels[(int64_t)t * R + sh.row[t]];
-        tot += gs;
+      if (seq_diag) {
+        int t = 0;
+        for (int gg = 0; gg < op.n_groups; ++gg) {
+          double gs = 0.0;
+          for (; t < op.group_end[gg]; ++t) gs += op.diag_mels[(int64_t)t * R + sh.row[t]];
+          tot += gs;
+        }
+      } else {
+        tot = dtree;
       }
       double d = op.constant + tot;
       if (fabs(d) > cut) {

@@ -168,6 +168,33 @@ __device__ inline void theta_and_logpsi(const RbmParams<T> &P, const int8_t *xs,
   theta_and_logpsi(P, xs, th, lc, red, logpsi_out, cta_grp());
 }
 
+// Log-ratio for NS sites with the W row pointers and the changes held in
+// registers; a site with d = 0 adds an exact zero, so the result equals
+// warp_log_ratio over the changed sites only.
+template <typename T, int NS>
+__device__ inline T warp_log_ratio_n(const RbmParams<T> &P, const T *th, const T *lc,
+                                     const int (&site)[4], const T (&d)[4]) {
+  const int lane = threadIdx.x & 31, M = P.M;
+  const T *w[NS];
+  T dd[NS];
+#pragma unroll
+  for (int q = 0; q < NS; ++q) {
+    w[q] = P.W + (int64_t)site[q] * M;
+    dd[q] = d[q];
+  }
+  T s = 0;
+  for (int j = lane; j < M; j += 32) {
+    T t = th[j];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) t += dd[q] * w[q][j];
+    s += log_cosh_fast(t) - lc[j];
+  }
+  s = warp_sum(s);
+#pragma unroll
+  for (int q = 0; q < NS; ++q) s += dd[q] * P.a[site[q]];
+  return s;
+}
+
 template <typename T>
 __device__ inline T warp_log_ratio(const RbmParams<T> &P, const T *th, const T *lc,
                                    const int *site, const T *d, int ns) {
@@ -281,31 +308,38 @@ __device__ inline void eloc_local_sample(const RbmParams<T> &P, const int8_t *__
   for (int i = g.tid; i < N; i += g.size) sh.xs[i] = x[b * N + i];
   grp_sync(g);
   theta_and_logpsi(P, sh.xs, th, lc, red, logpsi_out ? logpsi_out + b : nullptr, g);
-  int kept = local_conn_enumerate(op, sh, g);
+  int kept = local_conn_enumerate(op, sh, g, sizeof(T) == 8);
   double acc = 0.0;
   for (int k = warp; k < kept; k += nw) {
     double mel = sh.slot_mel[k];
     int t = sh.slot_term[k];
-    int site[4];
-    T d[4];
-    int ns = 0;
+    // sites of the term in slots 0..sz-1 (unchanged sites get d = 0)
+    int site[4] = {0, 0, 0, 0};
+    T d[4] = {0, 0, 0, 0};
+    int ns = 0, sz = 0;
     if (t >= 0) {
-      const int row = sh.row[t], c = sh.slot_col[k], sz = op.acting_size[t];
+      const int row = sh.row[t], c = sh.slot_col[k];
+      sz = op.acting_size[t];
       const int8_t *xpv = op.x_prime + (((int64_t)t * op.max_rows + row) * op.max_conns + c) * S;
-      for (int q = 0; q < sz; ++q) {
-        int st = op.acting_on[t * S + q];
-        int dv = (int)xpv[q] - (int)sh.xs[st];
-        if (dv != 0) {
-          site[ns] = st;
-          d[ns] = (T)dv;
-          ++ns;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (q < sz) {
+          const int st = op.acting_on[t * S + q];
+          const int dv = (int)xpv[q] - (int)sh.xs[st];
+          site[q] = st;
+          d[q] = (T)dv;
+          ns += dv != 0;
         }
       }
     }
     if (ns == 0) {
       if (lane == 0) acc += mel;
     } else {
-      T lr = warp_log_ratio(P, th, lc, site, d, ns);
+      T lr;
+      if (sz <= 1) lr = warp_log_ratio_n<T, 1>(P, th, lc, site, d);
+      else if (sz == 2) lr = warp_log_ratio_n<T, 2>(P, th, lc, site, d);
+      else if (sz == 3) lr = warp_log_ratio_n<T, 3>(P, th, lc, site, d);
+      else lr = warp_log_ratio_n<T, 4>(P, th, lc, site, d);
       if (lane == 0) acc += mel * exp_ratio(lr);
     }
   }
