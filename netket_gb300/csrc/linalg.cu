@@ -33,6 +33,7 @@ struct vmck_ctx {
   // look-ahead Cholesky: a second stream / cuBLAS handle for the trailing
   // updates and a pool of events (two per panel), created on first use
   cudaStream_t side = nullptr;
+  cudaStream_t chain = nullptr;  // highest priority: the factorisation's critical path
   cublasHandle_t blas2 = nullptr;
   cudaEvent_t *events = nullptr;
   int n_events = 0;
@@ -790,7 +791,10 @@ static int chol_rec(RecChol &R, float *A, int64_t lda, int64_t n) {
 // updated by panel q) orders the caller's update of that row by panel q+1.
 static int chol_lookahead_setup(vmck_ctx *c, int panels) {
   if (!c->side) {
+    int lo = 0, hi = 0;
+    VMCK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     VMCK_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    VMCK_CUDA(cudaStreamCreateWithPriority(&c->chain, cudaStreamNonBlocking, hi));
     VMCK_BLAS(cublasCreate(&c->blas2));
   }
   const int need = 2 * panels + 2;
@@ -812,16 +816,40 @@ static int chol_lookahead_setup(vmck_ctx *c, int panels) {
   return VMCK_OK;
 }
 
+static int chol_blocked_on(RecChol &R, float *A, int64_t lda, int64_t n);
+
+// The chain runs on the context's highest-priority stream so that its short,
+// latency-bound kernels are scheduled ahead of the side stream's GEMM blocks;
+// the caller's stream waits for both at the end.
 static int chol_blocked(RecChol &R, float *A, int64_t lda, int64_t n) {
-  const float mone = -1.0f, one = 1.0f;
   vmck_ctx *c = R.c;
   const int panels = (int)((n + PANEL_W - 1) / PANEL_W);
   int rc = chol_lookahead_setup(c, panels);
   if (rc) return rc;
-  cudaEvent_t *F = c->events, *U = c->events + panels;
+  cudaStream_t caller = R.st;
   cudaEvent_t start = c->events[2 * panels], done = c->events[2 * panels + 1];
-  VMCK_CUDA(cudaEventRecord(start, R.st));
+  VMCK_CUDA(cudaEventRecord(start, caller));
+  VMCK_CUDA(cudaStreamWaitEvent(c->chain, start, 0));
   VMCK_CUDA(cudaStreamWaitEvent(c->side, start, 0));
+  VMCK_BLAS(cublasSetStream(c->blas, c->chain));
+  R.st = c->chain;
+  rc = chol_blocked_on(R, A, lda, n);
+  R.st = caller;
+  cublasSetStream(c->blas, caller);
+  if (rc) return rc;
+  VMCK_CUDA(cudaEventRecord(done, c->chain));
+  VMCK_CUDA(cudaStreamWaitEvent(caller, done, 0));
+  VMCK_CUDA(cudaEventRecord(done, c->side));
+  VMCK_CUDA(cudaStreamWaitEvent(caller, done, 0));
+  return VMCK_OK;
+}
+
+static int chol_blocked_on(RecChol &R, float *A, int64_t lda, int64_t n) {
+  const float mone = -1.0f, one = 1.0f;
+  vmck_ctx *c = R.c;
+  const int panels = (int)((n + PANEL_W - 1) / PANEL_W);
+  int rc = VMCK_OK;
+  cudaEvent_t *F = c->events, *U = c->events + panels;
   for (int q = 0; q < panels; ++q) {
     const int64_t k0 = q * PANEL_W, k1 = std::min<int64_t>(n, k0 + PANEL_W), w = k1 - k0;
     const int64_t m = n - k1;
@@ -854,8 +882,6 @@ static int chol_blocked(RecChol &R, float *A, int64_t lda, int64_t n) {
                             A + k3 + (k3 + c0) * lda, (int)lda));
     }
   }
-  VMCK_CUDA(cudaEventRecord(done, c->side));
-  VMCK_CUDA(cudaStreamWaitEvent(R.st, done, 0));
   return VMCK_OK;
 }
 
@@ -1018,6 +1044,7 @@ extern "C" int vmck_ctx_destroy(vmck_ctx *c) {
   free(c->events);
   if (c->blas2) cublasDestroy(c->blas2);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->chain) cudaStreamDestroy(c->chain);
   if (c->params) cusolverDnDestroyParams(c->params);
   if (c->solver) cusolverDnDestroy(c->solver);
   if (c->blas) cublasDestroy(c->blas);
