@@ -230,15 +230,25 @@ def run_ours(args):
     gram_ms = phases.get("gram")
     n = vs.n_samples
     flops = float(n) * (n + 1) * 400  # lower triangle of t t^T (n x n x M), 2 flop per FMA
+    # tcgen05 mode 2: hi*hi, hi*lo, lo*hi, lo*lo over K = 400 padded to 448
+    executed = float(n) * (n + 1) * 4 * 448
+    # DRAM bytes per launch from the n = 8,192 ncu capture (profiles/gram_tc_kernel_n8192.md),
+    # scaled by the number of T entries
+    traffic = args.gram_traffic if args.gram_traffic is not None else \
+        (73.9e6 + 346.2e6) * (n / 8192.0) ** 2
     roof = None
     if gram_ms:
         peaks = load_peaks()
         achieved = flops / (gram_ms * 1e-3) / 1e12
-        roof = {"kernel": "structured Gram T = O_L O_L^T (vmck_rbm_gram)", "bound": "tensor",
-                "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": round(achieved / peaks["bf16_tflops"], 5), "traffic": args.gram_traffic,
-                "peak_source": peaks["source"], "algorithmic_flops_per_launch": flops,
-                "launch_ms": round(gram_ms, 4)}
+        roof = {"kernel": "structured Gram T = O_L O_L^T (gram_tc_kernel, tcgen05)",
+                "bound": "tensor", "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"],
+                "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 5),
+                "traffic": traffic, "peak_source": peaks["source"],
+                "algorithmic_flops_per_launch": flops,
+                "executed_tensor_tflops": round(executed / (gram_ms * 1e-3) / 1e12, 3),
+                "launch_ms": round(gram_ms, 4),
+                "note": "Gram phase time (shift, g vector, operand split, kernel); the step's "
+                        "largest phase is the Cholesky solve (profiles/)"}
     cpu = None
     if not args.no_cpu_baseline:
         cpu = run_cpu_baseline(n_samples=args.cpu_samples)
