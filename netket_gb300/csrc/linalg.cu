@@ -275,6 +275,29 @@ __device__ __forceinline__ void panel_forward(const float *Us, const float *rinv
   }
 }
 
+// Inverse of the upper-triangular 32 x 32 diagonal block at (p, p) of Us (rows
+// / columns past pw are treated as the identity), by one warp: lane l computes
+// column l of X = U_pp^-1 by back substitution, all rows held in registers
+// (fully unrolled, so the indices are compile-time).  Writes X row-major
+// (X[i * 32 + l], zeros below the diagonal) to dst.  rinv[p + i] = 1 / u_ii.
+__device__ inline void invert_diag32(const float *Us, const float *rinv, int p, int pw,
+                                     float *dst) {
+  const int lane = threadIdx.x & 31;
+  float x[32];
+#pragma unroll
+  for (int i = 31; i >= 0; --i) {
+    float sacc = (i == lane) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int k = i + 1; k < 32; ++k) {
+      const float u = (i < pw && k < pw) ? Us[(p + i) * LEAF_LD + p + k] : 0.0f;
+      sacc = __fmaf_rn(-u, x[k], sacc);
+    }
+    x[i] = (i < pw) ? sacc * rinv[p + i] : sacc;
+  }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dst[i * 32 + lane] = (i <= lane) ? x[i] : 0.0f;
+}
+
 // Right-looking upper Cholesky of one b x b diagonal block (b <= 128) of a
 // column-major matrix.  Per 32-row panel: (a) warp 0 factors the 32 x 32
 // diagonal block in registers (lane l holds column l; the unused part of a short
@@ -283,7 +306,7 @@ __device__ __forceinline__ void panel_forward(const float *Us, const float *rinv
 // sets VMCK_DEV_NOT_SPD and is replaced by 1; the caller falls back on the
 // status word.
 __global__ void __launch_bounds__(LEAF_THREADS) potrf_leaf_kernel(float *A, int64_t lda, int b,
-                                                                  int32_t *status) {
+                                                                  int32_t *status, float *dinv) {
   extern __shared__ __align__(16) float Us[];
   __shared__ float rinv[LEAF_B];
   __shared__ __align__(16) float rowk[32];
@@ -379,6 +402,11 @@ __global__ void __launch_bounds__(LEAF_THREADS) potrf_leaf_kernel(float *A, int6
     __syncthreads();
   }
   if (__syncthreads_or(bad) && tid == 0 && status) atomicOr(status, VMCK_DEV_NOT_SPD);
+  // inverses of the 32 x 32 diagonal blocks for trsm_leaf_kernel (warp w: block w)
+  if (dinv && warp < (b + 31) / 32) {
+    const int p = 32 * warp, pw = (b - p) < 32 ? (b - p) : 32;
+    invert_diag32(Us, rinv, p, pw, dinv + warp * 1024);
+  }
   leaf_store_upper(Us, A, lda, b);
 }
 
@@ -391,12 +419,41 @@ constexpr int TRSM_COLS = 64;
 constexpr int TRSM_LD = TRSM_COLS + 4;
 
 // Forward substitution Us^T X = Bs in place for an m x m upper Us (m <= 128) and a
-// 64-column Bs[k * TRSM_LD + c] in shared memory; rinv[i] = 1 / u_ii.
-__device__ void leaf_trsm_core(const float *Us, float *Bs, const float *rinv, int m) {
+// 64-column Bs[k * TRSM_LD + c] in shared memory; rinv[i] = 1 / u_ii.  With Dinv
+// (the row-major inverses of the 32 x 32 diagonal blocks, 1024 floats each) the
+// panel step is a 32 x 32 x 64 product X_p = Dinv_p^T B_p instead of a 32-step
+// substitution.
+__device__ void leaf_trsm_core(const float *Us, float *Bs, const float *rinv, int m,
+                               const float *Dinv = nullptr) {
   const int tid = threadIdx.x, warp = tid >> 5;
   for (int p = 0; p < m; p += 32) {
     const int pw = (m - p) < 32 ? (m - p) : 32;
-    if (warp < 8) {  // (a) 256 threads: column c = tid >> 2, quarter q = tid & 3
+    if (Dinv) {  // (a') 128 threads: 4 x 4 tiles of X_p (rows i0.., columns c0..)
+      const float *D = Dinv + (p >> 5) * 1024;
+      float acc[4][4] = {};
+      const int i0 = 4 * (tid >> 4), cc0 = 4 * (tid & 15);
+      if (tid < 128) {
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+          const float4 dv = *reinterpret_cast<const float4 *>(&D[k * 32 + i0]);
+          const float4 bv = *reinterpret_cast<const float4 *>(&Bs[(p + k) * TRSM_LD + cc0]);
+          const float av[4] = {dv.x, dv.y, dv.z, dv.w}, xv[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int y = 0; y < 4; ++y) acc[u][y] = __fmaf_rn(av[u], xv[y], acc[u][y]);
+        }
+      }
+      __syncthreads();
+      if (tid < 128) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (i0 + u < pw) {
+#pragma unroll
+            for (int y = 0; y < 4; ++y) Bs[(p + i0 + u) * TRSM_LD + cc0 + y] = acc[u][y];
+          }
+      }
+    } else if (warp < 8) {  // (a) 256 threads: column c = tid >> 2, quarter q = tid & 3
       const int c = tid >> 2, q = tid & 3;
       float v[8];
 #pragma unroll
@@ -437,10 +494,12 @@ __device__ void leaf_trsm_core(const float *Us, float *Bs, const float *rinv, in
 
 __global__ void __launch_bounds__(LEAF_THREADS) trsm_leaf_kernel(const float *__restrict__ Ug,
                                                                  int64_t ldu, int m, float *B,
-                                                                 int64_t ldb, int64_t nrhs) {
+                                                                 int64_t ldb, int64_t nrhs,
+                                                                 const float *__restrict__ dinv) {
   extern __shared__ __align__(16) float sm[];
   float *Us = sm;                         // LEAF_ROWS x LEAF_LD
   float *Bs = sm + LEAF_ROWS * LEAF_LD;   // LEAF_ROWS x TRSM_LD
+  float *Ds = Bs + LEAF_ROWS * TRSM_LD;   // 4 x 1024 (diagonal-block inverses)
   __shared__ float rinv[LEAF_B];
   const int tid = threadIdx.x;
   const int64_t c0 = (int64_t)blockIdx.x * TRSM_COLS;
@@ -453,11 +512,13 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsm_leaf_kernel(const float *__
     else
       Bs[k * TRSM_LD + c] = 0.0f;
   }
+  if (dinv)
+    for (int e = tid; e < 4 * 1024; e += blockDim.x) cp_async4(&Ds[e], dinv + e);
   cp_async_wait();
   __syncthreads();
   if (tid < m) rinv[tid] = 1.0f / Us[tid * LEAF_LD + tid];
   __syncthreads();
-  leaf_trsm_core(Us, Bs, rinv, m);
+  leaf_trsm_core(Us, Bs, rinv, m, dinv ? Ds : nullptr);
   for (int e = tid; e < TRSM_COLS * m; e += blockDim.x) {
     const int c = e / m, k = e - c * m;
     if (c < nc) B[(c0 + c) * ldb + k] = Bs[k * TRSM_LD + c];
@@ -702,7 +763,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_bwd_kernel(const float *__r
 }
 
 constexpr size_t LEAF_SMEM = (size_t)LEAF_ROWS * LEAF_LD * sizeof(float);
-constexpr size_t TRSM_SMEM = (size_t)LEAF_ROWS * (LEAF_LD + TRSM_LD) * sizeof(float);
+constexpr size_t TRSM_SMEM = ((size_t)LEAF_ROWS * (LEAF_LD + TRSM_LD) + 4 * 1024) * sizeof(float);
 
 static int num_sms() {
   int dev = 0, sms = 148;
@@ -718,7 +779,18 @@ struct RecChol {
   size_t dsize, hsize;
   int64_t leaf;
   bool own_leaf;
+  const float *A0 = nullptr;  // the matrix being factored (leaves sit on its diagonal)
+  int64_t lda0 = 0;
+  float *dinv = nullptr;      // per 128-row leaf: four 32 x 32 diagonal-block inverses
 };
+
+// Inverse store of the leaf whose diagonal block starts at U (a multiple of 128
+// rows down the diagonal of R.A0), or nullptr.
+static float *leaf_dinv(const RecChol &R, const float *U) {
+  if (!R.dinv || !R.A0) return nullptr;
+  const int64_t k0 = (U - R.A0) / (R.lda0 + 1);
+  return R.dinv + (k0 / LEAF_B) * 4096;
+}
 
 // C (n x n, upper) -= A^T A with A (k x n)
 static int syrk_rec(RecChol &R, float *C, int64_t ldc, int64_t n, const float *A, int64_t lda,
@@ -743,7 +815,7 @@ static int trsm_rec(RecChol &R, const float *U, int64_t ldu, int64_t m, float *B
   const float mone = -1.0f, one = 1.0f;
   if (m <= R.leaf && R.own_leaf) {
     trsm_leaf_kernel<<<(unsigned)((nrhs + TRSM_COLS - 1) / TRSM_COLS), LEAF_THREADS, TRSM_SMEM,
-                       R.st>>>(U, ldu, (int)m, B, ldb, nrhs);
+                       R.st>>>(U, ldu, (int)m, B, ldb, nrhs, leaf_dinv(R, U));
     return check_launch("trsm leaf");
   }
   if (m <= R.leaf) {
@@ -763,7 +835,7 @@ static int chol_rec(RecChol &R, float *A, int64_t lda, int64_t n) {
   if (n <= R.leaf) {
     if (R.own_leaf) {
       potrf_leaf_kernel<<<1, LEAF_THREADS, LEAF_SMEM, R.st>>>(
-          A, lda, (int)n, R.status);
+          A, lda, (int)n, R.status, leaf_dinv(R, A));
       return check_launch("cholesky leaf");
     }
     VMCK_SOLVER(cusolverDnXpotrf(R.c->solver, R.c->params, CUBLAS_FILL_MODE_UPPER, n, CUDA_R_32F,
@@ -1120,7 +1192,8 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
   const size_t yinv_off = (ws_off + (size_t)nt * n * 8 + 255) & ~size_t(255);
   const size_t y32_off = (yinv_off + (own_trsv ? (size_t)nb * TB * TB * 4 : 0) + 255) & ~size_t(255);
   const size_t sync_off = (y32_off + (own_trsv ? (size_t)n * 4 : 0) + 255) & ~size_t(255);
-  const size_t need = sync_off + (own_trsv ? (size_t)(2 * nb + 4) * 4 : 0);
+  const size_t dinv_off = (sync_off + (own_trsv ? (size_t)(2 * nb + 4) * 4 : 0) + 255) & ~size_t(255);
+  const size_t need = dinv_off + (factor_mode == 3 ? (size_t)nb * 4096 * 4 : 0);
   if ((rc = grow(&c->aux, &c->aux_bytes, need, st))) return rc;
   char *aux = static_cast<char *>(c->aux);
   double *r = static_cast<double *>(c->aux);
@@ -1149,6 +1222,9 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
       VMCK_BLAS(cublasSetEmulationSpecialValuesSupport(c->blas,
                                                         CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE));
       RecChol R{c, st, status, dsize, hsize, LEAF_B, true};
+      R.A0 = A32;
+      R.lda0 = n;
+      R.dinv = reinterpret_cast<float *>(aux + dinv_off);
       rc = chol_blocked(R, A32, n, n);
       cublasSetEmulationSpecialValuesSupport(c->blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_DEFAULT);
     }
