@@ -14,9 +14,11 @@ Two ways to form T:
     on the tensor cores (tcgen05) with t rounded to hi + lo BF16 pairs (all four
     products, so T is the Gram matrix of a 16-bit-mantissa Jacobian; the large
     hi * hi part accumulates apart from the small cross terms), ``3`` with one
-    BF16, ``1`` in FP32 on the CUDA cores.  At n = 16,384 and diag_shift 1e-4 the
-    minSR update of mode 2 is within 1.2e-4 (relative) of the all-FP64 one,
-    mode 1 within 2.5e-4, mode 3 within 2.4e-2;
+    BF16, ``1`` in FP32 on the CUDA cores.  At n = 16,384, M = 400 and
+    diag_shift 1e-4 the minSR update of mode 2 is within 1.2e-4 (relative) of
+    the all-FP64 one, mode 1 within 2.5e-4, mode 3 within 2.4e-2.  With M = 2048
+    (16 x 16, alpha 8) mode 2's T is no longer positive definite, so the default
+    is mode 2 only for M <= ``TC_GRAM_MAX_M`` and mode 1 above;
   * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
     and a cuBLAS SYRK.
 Solvers (``solve=``):
@@ -43,6 +45,9 @@ def _status():
     return torch.zeros(1, dtype=torch.int32, device=nat.device())
 
 
+TC_GRAM_MAX_M = 512
+
+
 def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram_mode=None,
                  solve="cholesky", refine_iters=3, refine_tol=1e-10, rtol=1e-14,
                  rtol_smooth=1e-14, jac_dtype=None, check=True, phase_timer=None):
@@ -57,7 +62,14 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     s = 1.0 / math.sqrt(n)
     mode = None
     if gram == "structured":
-        mode = gram_mode if gram_mode is not None else (0 if t.dtype == torch.float64 else 2)
+        if gram_mode is not None:
+            mode = gram_mode
+        elif t.dtype == torch.float64:
+            mode = 0
+        else:
+            # the tensor cores' FP32 accumulation over K = M of the hi * hi term keeps T
+            # positive definite at M = 400 (diag_shift 1e-4) but not at M = 2048
+            mode = 2 if M <= TC_GRAM_MAX_M else 1
     obar = K.column_means(t, x, N, M)
     dv = K.center_scale(e, mean_dev, 2.0 * s)
     status = _status()
