@@ -245,6 +245,12 @@ int vmck_stats_f64_noalloc(vmck_stream s, const double *data, int32_t n_chains,
  *   out[bias_j] = sum_s t_sj v_s, out[kernel_ij] = sum_s x_si t_sj v_s,
  *   out[visible_i] = sum_s x_si v_s,  t = tanh(theta) (n, M) in dtype.
  * v (n,) and out (P,) are FP64.  workspace: vmck_ot_v_workspace_size() doubles. */
+/* out = O v (n,) for the RBM Jacobian O (n, P) without materialising it: the
+ * JVP behind QGTOnTheFly's mat-vec (netket/optimizer/qgt/qgt_onthefly_logic.py:
+ * 43-56):  out[s] = t_s . (v_bias + x_s^T V) + x_s . v_visible, V = v_kernel
+ * (N x M).  v (P,) and out (n,) FP64; FP64 accumulation. */
+int vmck_rbm_o_v(vmck_stream s, int32_t dtype, const void *tanh_theta, const int8_t *x,
+                 int32_t N, int32_t M, int64_t n, const double *v, double *out);
 int64_t vmck_ot_v_workspace_size(int32_t N, int32_t M, int64_t n);
 int vmck_rbm_ot_v(vmck_stream s, int32_t dtype, const void *tanh_theta,
                   const int8_t *x, int32_t N, int32_t M, int64_t n, const double *v,

@@ -75,6 +75,7 @@ _SIGNATURES = {
     "vmck_stats_workspace_size": ([c_i32, c_i32], c_i64),
     "vmck_stats_f64": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp, c_i64], c_i32),
     "vmck_stats_f64_noalloc": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_vp], c_i32),
+    "vmck_rbm_o_v": ([c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_vp], c_i32),
     "vmck_ot_v_workspace_size": ([c_i32, c_i32, c_i64], c_i64),
     "vmck_rbm_ot_v": ([c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_i64],
                       c_i32),

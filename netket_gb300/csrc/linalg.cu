@@ -194,7 +194,17 @@ __global__ void sgd_kernel(double *p, const double *u, int64_t P, double lr, flo
 constexpr int64_t CHOL_LEAF = 1024;
 constexpr int LEAF_B = 128;        // potrf_leaf_kernel block
 constexpr int LEAF_THREADS = 512;
-constexpr int64_t PANEL_W = 512;   // blocked factorization panel
+constexpr int64_t PANEL_W_DEFAULT = 512;  // blocked factorization panel
+// Panel width of the blocked Cholesky: VMCK_CHOL_PANEL (a multiple of 128,
+// 128 - 2048) overrides the default, read once per process.
+static int64_t chol_panel_width() {
+  static const int64_t w = [] {
+    const char *e = getenv("VMCK_CHOL_PANEL");
+    const long v = e ? strtol(e, nullptr, 10) : 0;
+    return (v >= 128 && v <= 2048 && v % 128 == 0) ? (int64_t)v : PANEL_W_DEFAULT;
+  }();
+  return w;
+}
 constexpr int64_t STRIP_W = 2048;  // trailing-update GEMM strip width
 
 static int64_t half_split(int64_t n) {
@@ -895,6 +905,7 @@ static int chol_blocked_on(RecChol &R, float *A, int64_t lda, int64_t n);
 // the caller's stream waits for both at the end.
 static int chol_blocked(RecChol &R, float *A, int64_t lda, int64_t n) {
   vmck_ctx *c = R.c;
+  const int64_t PANEL_W = chol_panel_width();
   const int panels = (int)((n + PANEL_W - 1) / PANEL_W);
   int rc = chol_lookahead_setup(c, panels);
   if (rc) return rc;
@@ -919,6 +930,7 @@ static int chol_blocked(RecChol &R, float *A, int64_t lda, int64_t n) {
 static int chol_blocked_on(RecChol &R, float *A, int64_t lda, int64_t n) {
   const float mone = -1.0f, one = 1.0f;
   vmck_ctx *c = R.c;
+  const int64_t PANEL_W = chol_panel_width();
   const int panels = (int)((n + PANEL_W - 1) / PANEL_W);
   int rc = VMCK_OK;
   cudaEvent_t *F = c->events, *U = c->events + panels;

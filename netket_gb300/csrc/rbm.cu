@@ -363,6 +363,30 @@ __global__ void __launch_bounds__(EL_THREADS) eloc_local_kernel(
     eloc_local_sample(P, x, b, op, eloc, logpsi_out, sh, th, lc, red, redd, g);
 }
 
+// ============================================================ O v
+// One warp per sample: lanes take hidden units j, u_j = v_bias[j] + x_s . V[:, j]
+// (FP64, V read through L1), then t_s . u + x_s . v_visible, a shuffle tree.
+template <typename T>
+__global__ void o_v_kernel(const T *__restrict__ t, const int8_t *__restrict__ x, int N, int M,
+                           int64_t n, const double *__restrict__ v, double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= n) return;
+  const int8_t *xs = x + s * N;
+  const T *ts = t + s * M;
+  const double *V = v + M;
+  double acc = 0.0;
+  for (int j = lane; j < M; j += 32) {
+    double u = v[j];
+    for (int i = 0; i < N; ++i) u += (double)xs[i] * __ldg(V + (int64_t)i * M + j);
+    acc += (double)ts[j] * u;
+  }
+  const double *va = v + M + (int64_t)N * M;
+  for (int i = lane; i < N; i += 32) acc += (double)xs[i] * va[i];
+  acc = warp_sum(acc);
+  if (lane == 0) out[s] = acc;
+}
+
 // ============================================================ O^T v
 // grid (ceil(M/64), ceil(N/64), chunks).  Each CTA accumulates, over its chunk
 // of samples, out[kernel_ij] for a 64 x 64 (i, j) tile (plus bias_j when
@@ -520,6 +544,25 @@ int launch_eloc_local(cudaStream_t st, const void *params, int N, int M, const i
 }  // namespace vmck
 
 using namespace vmck;
+
+extern "C" int vmck_rbm_o_v(vmck_stream s, int32_t dtype, const void *tanh_theta,
+                            const int8_t *x, int32_t N, int32_t M, int64_t n, const double *v,
+                            double *out) {
+  VMCK_REQUIRE(tanh_theta && x && v && out && N > 0 && M > 0 && n >= 0, "rbm_o_v arguments");
+  if (n == 0) return VMCK_OK;
+  const unsigned grid = (unsigned)((n + 7) / 8);
+  if (dtype == VMCK_F64)
+    o_v_kernel<double><<<grid, 256, 0, as_stream(s)>>>(static_cast<const double *>(tanh_theta), x,
+                                                        N, M, n, v, out);
+  else if (dtype == VMCK_F32)
+    o_v_kernel<float><<<grid, 256, 0, as_stream(s)>>>(static_cast<const float *>(tanh_theta), x,
+                                                       N, M, n, v, out);
+  else {
+    set_last_error("rbm_o_v: dtype %d unsupported", dtype);
+    return VMCK_ERR_UNSUPPORTED;
+  }
+  return check_launch("rbm_o_v");
+}
 
 extern "C" int vmck_rbm_logpsi(vmck_stream s, int32_t dtype, const void *params, int32_t N,
                                int32_t M, const int8_t *x, int64_t n, void *logpsi,

@@ -99,6 +99,15 @@ def ot_v(tanh_t, x, N, M, v):
     return out
 
 
+def o_v(tanh_t, x, N, M, v):
+    """O v (n,) FP64 for the RBM Jacobian (the JVP of QGTOnTheFly), O never stored."""
+    n = x.shape[0]
+    out = torch.empty(n, dtype=torch.float64, device=x.device)
+    nat.check(nat.lib().vmck_rbm_o_v(nat.stream(), nat.dtype_code(tanh_t.dtype), nat.ptr(tanh_t),
+                                     nat.ptr(x), N, M, n, nat.ptr(v.contiguous()), nat.ptr(out)))
+    return out
+
+
 def column_means(tanh_t, x, N, M):
     n = x.shape[0]
     v = torch.full((n,), 1.0 / n, dtype=torch.float64, device=x.device)

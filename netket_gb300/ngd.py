@@ -141,6 +141,71 @@ def sr_update(t, x, N, M, e, mean_dev, diag_shift, *, jac_dtype=None, rtol=1e-14
     return solve_with_fallback(S.to(torch.float64), F, rtol, rtol_smooth)
 
 
+class QGTOnTheFly:
+    """``S v = O_L^T (O_L v) + diag_shift v`` without forming O or S
+    (``netket/optimizer/qgt/qgt_onthefly_logic.py:43-56``): ``O v`` by the
+    ``vmck_rbm_o_v`` JVP kernel, ``O^T w`` by ``vmck_rbm_ot_v``, both centred
+    with the column means (``O_L = (O - 1 obar^T) / sqrt(n)``)."""
+
+    def __init__(self, t, x, N, M, diag_shift):
+        self.t, self.x, self.N, self.M = t, x, N, M
+        self.n = x.shape[0]
+        self.s = 1.0 / math.sqrt(self.n)
+        self.diag_shift = diag_shift
+        self.obar = K.column_means(t, x, N, M)
+
+    def o_l(self, v):
+        """O_L v (n,)."""
+        w = K.o_v(self.t, self.x, self.N, self.M, v)
+        return (w - torch.dot(self.obar, v)) * self.s
+
+    def o_l_t(self, u):
+        """O_L^T u (P,)."""
+        raw = K.ot_v(self.t, self.x, self.N, self.M, u)
+        return K.center_update(raw, self.obar, u, self.s)
+
+    def __matmul__(self, v):
+        return self.o_l_t(self.o_l(v)) + self.diag_shift * v
+
+
+def cg(A, b, x0=None, tol=1e-5, atol=0.0, maxiter=None):
+    """Conjugate gradients with ``jax.scipy.sparse.linalg.cg``'s stopping rule
+    (``|r| <= max(tol |b|, atol)``, ``maxiter`` = 10 * size by default), the
+    solver NetKet's ``SR`` uses by default.  Returns (x, iterations)."""
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    maxiter = 10 * b.numel() if maxiter is None else maxiter
+    bound2 = max(tol * tol * float(torch.dot(b, b)), atol * atol)
+    r = b - A @ x
+    p = r.clone()
+    gamma = float(torch.dot(r, r))
+    k = 0
+    while gamma > bound2 and k < maxiter:
+        Ap = A @ p
+        alpha = gamma / float(torch.dot(p, Ap))
+        x += alpha * p
+        r -= alpha * Ap
+        gamma_new = float(torch.dot(r, r))
+        p = r + (gamma_new / gamma) * p
+        gamma = gamma_new
+        k += 1
+    return x, k
+
+
+def sr_update_onthefly(t, x, N, M, e, mean_dev, diag_shift, *, x0=None, tol=1e-5, atol=0.0,
+                       maxiter=None):
+    """SR with ``QGTOnTheFly`` and CG (NetKet's defaults for an RBM:
+    ``netket/optimizer/qgt/default.py:58-97``, ``netket/optimizer/sr.py:62-216``).
+    Returns (delta (P,), info with the CG iteration count)."""
+    n = x.shape[0]
+    S = QGTOnTheFly(t, x, N, M, diag_shift)
+    dv = K.center_scale(e, mean_dev, 2.0 * S.s)
+    F = S.o_l_t(dv)
+    delta, iters = cg(S, F, x0=x0, tol=tol, atol=atol, maxiter=maxiter)
+    info = SolveInfo(solver_fallback=False)
+    info["cg_iterations"] = iters
+    return delta, info
+
+
 def solve_with_fallback(A, b, rtol=1e-14, rtol_smooth=1e-14):
     """``cholesky_with_fallback`` for an SPD matrix whose lower triangle is set."""
     status = _status()

@@ -16,7 +16,7 @@ import torch
 
 from . import kernels as K
 from . import _native as nat
-from .ngd import solve_with_fallback, sr_update
+from .ngd import solve_with_fallback, sr_update, sr_update_onthefly
 
 
 class Sgd:
@@ -41,11 +41,24 @@ def _flat(tree_or_flat, model):
 
 
 class SR:
-    """Preconditioner ``(vstate, grad, step) -> dp`` with the dense QGT."""
+    """Preconditioner ``(vstate, grad, step) -> dp``.
 
-    def __init__(self, diag_shift=0.01, *, jac_dtype=torch.float64):
+    ``qgt="dense"`` (default here): the dense QGT solved by Cholesky with the
+    pinv_smooth fallback.  ``qgt="onthefly"``: ``QGTOnTheFly`` with conjugate
+    gradients (``solver="cg"``, ``tol``, ``maxiter``), NetKet's own default for an
+    RBM; as in NetKet (``solver_restart=False``) CG starts from the previous
+    step's solution."""
+
+    def __init__(self, diag_shift=0.01, *, jac_dtype=torch.float64, qgt="dense", solver="cholesky",
+                 tol=1e-5, maxiter=None, solver_restart=False):
+        if qgt not in ("dense", "onthefly"):
+            raise ValueError(f"qgt must be 'dense' or 'onthefly', not {qgt!r}")
         self.diag_shift = diag_shift
         self.jac_dtype = jac_dtype
+        self.qgt = qgt
+        self.solver = "cg" if qgt == "onthefly" else solver
+        self.tol, self.maxiter, self.solver_restart = tol, maxiter, solver_restart
+        self._x0 = None
         self.info = None
 
     def __call__(self, vstate, grad, step=0):
@@ -53,12 +66,19 @@ class SR:
         if c is None:
             raise RuntimeError("SR needs expect_and_grad to have run on this state")
         shift = self.diag_shift(step) if callable(self.diag_shift) else self.diag_shift
+        if self.qgt == "onthefly":
+            x0 = None if self.solver_restart else self._x0
+            dp, self.info = sr_update_onthefly(c["t"], c["x"], vstate.N, vstate.M, c["e"],
+                                               c["stats_dev"][0:1], shift, x0=x0, tol=self.tol,
+                                               maxiter=self.maxiter)
+            self._x0 = dp
+            return dp
         dp, self.info = sr_update(c["t"], c["x"], vstate.N, vstate.M, c["e"],
                                   c["stats_dev"][0:1], shift, jac_dtype=self.jac_dtype)
         return dp
 
     def __repr__(self):
-        return f"SR(diag_shift={self.diag_shift})"
+        return f"SR(diag_shift={self.diag_shift}, qgt={self.qgt!r}, solver={self.solver!r})"
 
 
 def identity_preconditioner(vstate, grad, step=0):

@@ -232,3 +232,48 @@ def test_sr_equals_minsr(nk):
     a, _ = nk.ngd.minsr_update(t, x, N, M, e, mean, 1e-3)
     b, _ = nk.ngd.sr_update(t, x, N, M, e, mean, 1e-3)
     np.testing.assert_allclose(a.cpu().numpy(), b.cpu().numpy(), atol=1e-10)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_qgt_onthefly_matvec_matches_dense(nk, dtype):
+    """QGTOnTheFly (netket/optimizer/qgt/qgt_onthefly_logic.py:43-56): O_L v by the
+    JVP kernel, O_L^T u by O^T v, S v = O_L^T O_L v + shift v, against the dense
+    centred Jacobian (FP64: 1e-11 relative)."""
+    N, n = 12, 600
+    model, flat, M, x, t, p = _problem(nk, N, 2, n, seed=7)
+    tt = t if dtype == "f64" else t.float()
+    S = nk.ngd.QGTOnTheFly(tt, x, N, M, 1e-2)
+    # the dense centred Jacobian of the same (FP32-rounded on the f32 path) t
+    O_L = nk.kernels.jacobian_dense(tt.double(), x, N, M, S.obar, S.s, torch.float64)
+    rng = np.random.default_rng(1)
+    v = torch.as_tensor(rng.normal(size=O_L.shape[1]), device="cuda")
+    u = torch.as_tensor(rng.normal(size=n), device="cuda")
+    tol = 1e-11 if dtype == "f64" else 2e-6
+    ref_ov = (O_L @ v).cpu().numpy()
+    np.testing.assert_allclose(S.o_l(v).cpu().numpy(), ref_ov, rtol=tol, atol=tol * np.abs(ref_ov).max())
+    ref_otu = (O_L.T @ u).cpu().numpy()
+    np.testing.assert_allclose(S.o_l_t(u).cpu().numpy(), ref_otu, rtol=tol,
+                               atol=tol * np.abs(ref_otu).max())
+    ref_sv = (O_L.T @ (O_L @ v) + 1e-2 * v).cpu().numpy()
+    np.testing.assert_allclose((S @ v).cpu().numpy(), ref_sv, rtol=tol, atol=tol * np.abs(ref_sv).max())
+
+
+def test_sr_onthefly_cg_matches_dense_sr(nk):
+    """SR with QGTOnTheFly + CG (NetKet's default for an RBM) converges to the
+    dense-QGT Cholesky solution: to 1e-8 with a tight tolerance, and within the
+    jax cg default (tol 1e-5) otherwise; warm start from the previous solution
+    takes fewer iterations."""
+    N, n = 16, 1008
+    model, flat, M, x, t, p = _problem(nk, N, 1, n, seed=8)
+    g = nk.graph.Chain(N)
+    H = nk.operator.Ising(nk.hilbert.Spin(0.5, N), g, h=1.0, J=1.0)
+    e = nk.kernels.local_energies_fused(H, flat, x, N, M)
+    mean = e.mean().reshape(1)
+    dense, _ = nk.ngd.sr_update(t, x, N, M, e, mean, 1e-2)
+    d = dense.cpu().numpy()
+    tight, info = nk.ngd.sr_update_onthefly(t, x, N, M, e, mean, 1e-2, tol=1e-12)
+    np.testing.assert_allclose(tight.cpu().numpy(), d, rtol=1e-8, atol=1e-8 * np.abs(d).max())
+    loose, info1 = nk.ngd.sr_update_onthefly(t, x, N, M, e, mean, 1e-2)
+    assert np.linalg.norm(loose.cpu().numpy() - d) < 1e-3 * np.linalg.norm(d)
+    warm, info2 = nk.ngd.sr_update_onthefly(t, x, N, M, e, mean, 1e-2, x0=loose)
+    assert info2["cg_iterations"] <= 1 < info1["cg_iterations"]

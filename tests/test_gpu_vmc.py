@@ -113,3 +113,21 @@ def test_vmc_sr_minsr_step_mixed_matches_fp64(nk):
     assert abs(e64 - e32) / abs(e64) < 1e-5
     d64, d32 = out["fp64"][1].cpu().numpy(), out["mixed"][1].cpu().numpy()
     assert np.linalg.norm(d64 - d32) / np.linalg.norm(d64) < 5e-2
+
+
+def test_vmc_sr_onthefly_tracks_dense_sr(nk):
+    """VMC + SR on the 1D TFIM (N = 16): the QGTOnTheFly + CG preconditioner with a
+    tight tolerance gives the same trajectory as the dense QGT for 10 steps."""
+    N = 16
+    g = nk.graph.Chain(N)
+    hi = nk.hilbert.Spin(0.5, N)
+    H = nk.operator.Ising(hi, g, h=1.0, J=1.0)
+    params = []
+    for qgt in ("dense", "onthefly"):
+        vs = nk.vqs.MCState(nk.sampler.MetropolisLocal(hi, n_chains=16), nk.models.RBM(alpha=1),
+                            n_samples=1008, n_discard_per_chain=32, seed=0, precision="fp64")
+        sr = nk.optimizer.SR(diag_shift=0.01, qgt=qgt, tol=1e-12)
+        drv = nk.driver.VMC(H, nk.optimizer.Sgd(0.01), variational_state=vs, preconditioner=sr)
+        drv.run(10)
+        params.append(vs.flat_parameters.cpu().numpy())
+    np.testing.assert_allclose(params[1], params[0], rtol=1e-7, atol=1e-9)
