@@ -20,6 +20,7 @@ from . import driver
 from . import exact
 from . import batched
 from . import serving
+from . import serialization
 
-__all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd", "batched", "serving",
+__all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd", "batched", "serving", "serialization",
            "optimizer", "vqs", "driver", "exact"]

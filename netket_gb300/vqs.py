@@ -151,6 +151,49 @@ class MCState:
         e = self.local_estimators(op)
         return Stats.from_array(K.stats_device(e, _plain_rhat()).cpu().numpy())
 
+    def expect_to_precision(self, op, *, atol=None, rtol=None, max_iter=10_000):
+        """Sample until the standard error of the mean meets ``atol`` (absolute)
+        and / or ``rtol`` (relative to |mean|); both must hold when both are given
+        (``netket/_src/vqs/expect_to_precision.py``: same arguments, checks and
+        sampling loop, later rounds without discarded sweeps).  The error is the
+        blocking estimator of ``statistics`` over all chains' accumulated local
+        estimators, where NetKet updates an online autocorrelation estimate."""
+        if atol is None and rtol is None:
+            raise ValueError("At least one of 'atol' or 'rtol' must be specified.")
+        if atol is not None and atol <= 0:
+            raise ValueError("atol must be > 0.")
+        if rtol is not None and rtol <= 0:
+            raise ValueError("rtol must be > 0.")
+
+        def not_converged(st):
+            err, scale = abs(st.error_of_mean), abs(st.mean)
+            if not math.isfinite(err):
+                return True
+            if atol is not None and err > atol:
+                return True
+            if rtol is not None:
+                rel = (0.0 if err == 0.0 else math.inf) if scale == 0.0 else err / scale
+                if rel > rtol:
+                    return True
+            return False
+
+        self.sample()
+        chunks = [self.local_estimators(op)]
+
+        def stats():
+            data = torch.cat(chunks, dim=1).contiguous()
+            return Stats.from_array(K.stats_device(data, _plain_rhat()).cpu().numpy())
+
+        st = stats()
+        it = 0
+        while not_converged(st) and it < max_iter:
+            self.sample(n_discard_per_chain=0)
+            chunks.append(self.local_estimators(op))
+            st = stats()
+            it += 1
+        self.last_precision_rounds = it
+        return st
+
     def _forward_cache(self, op):
         """Samples, tanh(theta), local energies and their device statistics."""
         x = self._flat_samples()

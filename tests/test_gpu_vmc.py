@@ -131,3 +131,57 @@ def test_vmc_sr_onthefly_tracks_dense_sr(nk):
         drv.run(10)
         params.append(vs.flat_parameters.cpu().numpy())
     np.testing.assert_allclose(params[1], params[0], rtol=1e-7, atol=1e-9)
+
+
+def test_checkpoint_resume_continues_chains_exactly(nk):
+    """to_bytes / from_bytes (flax.serialization as NetKet uses it): a state
+    restored into a fresh MCState continues parameters, chains and random stream
+    bit for bit."""
+    N = 12
+    g = nk.graph.Chain(N)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    H = nk.operator.Heisenberg(hi, g)
+
+    def make():
+        vs = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=g, n_chains=32),
+                            nk.models.RBM(alpha=1), n_samples=256, seed=3, precision="fp64")
+        drv = nk.driver.VMC(H, nk.optimizer.Sgd(0.02), variational_state=vs,
+                            preconditioner=nk.optimizer.SR(diag_shift=0.01))
+        return vs, drv
+    vs, drv = make()
+    drv.run(3)
+    blob = nk.serialization.to_bytes(vs)
+    drv.run(2)
+    ref = vs.flat_parameters.cpu().numpy().copy()
+    ref_samples = vs.sample().cpu().numpy()
+    vs2, drv2 = make()
+    nk.serialization.from_bytes(vs2, blob)
+    drv2.run(2)
+    np.testing.assert_array_equal(vs2.flat_parameters.cpu().numpy(), ref)
+    np.testing.assert_array_equal(vs2.sample().cpu().numpy(), ref_samples)
+
+
+def test_expect_to_precision_reaches_tolerance(nk):
+    """expect_to_precision (netket/_src/vqs/expect_to_precision.py): sampling rounds
+    continue until the error of the mean meets atol; the estimate is within 5
+    sigma of the exact expectation value (full sum)."""
+    N = 8
+    g = nk.graph.Chain(N)
+    hi = nk.hilbert.Spin(0.5, N)
+    H = nk.operator.Ising(hi, g, h=1.0, J=1.0)
+    model = nk.models.RBM(alpha=1, kernel_init_std=0.3, hidden_bias_init_std=0.3,
+                          visible_bias_init_std=0.3)
+    vs = nk.vqs.MCState(nk.sampler.MetropolisLocal(hi, n_chains=64), model, n_samples=512,
+                        seed=2, precision="fp64")
+    st = vs.expect_to_precision(H, atol=2e-3)
+    assert st.error_of_mean <= 2e-3 and vs.last_precision_rounds >= 1
+    # exact expectation from the full sum over the 256 configurations
+    allx = torch.as_tensor(hi.all_states(), device="cuda")
+    lp = vs.log_value(allx)
+    w = torch.exp(2 * (lp - lp.max()))
+    w = w / w.sum()
+    e = nk.kernels.local_energies_fused(H, vs.flat_parameters, allx, N, vs.M)
+    exact = float((w * e).sum())
+    assert abs(st.mean - exact) < 5 * st.error_of_mean
+    with pytest.raises(ValueError):
+        vs.expect_to_precision(H)

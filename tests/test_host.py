@@ -133,3 +133,28 @@ def test_fails_loudly_without_gpu(built_lib):
     hi = nk.hilbert.Spin(0.5, N=4)
     with pytest.raises(nk._native.VmckError):
         hi.random_state(0, 3)
+
+
+def test_state_dict_bytes_round_trip():
+    """The checkpoint byte format keeps NetKet's nested state-dict structure and
+    every array bit for bit (uint64 rng words, int8 chains, FP64 parameters)."""
+    from netket_gb300 import serialization as ser
+    rng = np.random.default_rng(0)
+    d = {"variables": {"params": {"Dense": {"bias": rng.normal(size=4),
+                                            "kernel": rng.normal(size=(3, 4))},
+                                  "visible_bias": rng.normal(size=3)}},
+         "sampler_state": {"σ": rng.choice(np.array([-1, 1], dtype=np.int8), size=(5, 3)),
+                           "rng": np.array([2**64 - 1, 12345], dtype=np.uint64),
+                           "n_steps_proc": np.int64(7), "n_accepted_proc": np.arange(5)},
+         "n_samples": np.int64(20), "n_discard_per_chain": np.int64(5)}
+    back = ser.dict_from_bytes(ser.dict_to_bytes(d))
+
+    def check(a, b):
+        if isinstance(a, dict):
+            assert set(a) == set(b)
+            for k in a:
+                check(a[k], b[k])
+        else:
+            assert np.asarray(a).dtype == np.asarray(b).dtype
+            np.testing.assert_array_equal(a, b)
+    check(d, back)
