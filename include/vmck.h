@@ -238,6 +238,33 @@ int vmck_stats_f64(vmck_stream s, const double *data, int32_t n_chains,
 int vmck_stats_f64_noalloc(vmck_stream s, const double *data, int32_t n_chains,
                            int32_t chain_length, int32_t plain_rhat, double *out5);
 
+/* ---------------------------------------------------------------- f4
+ * Streaming statistics: the update of netket.stats.OnlineStats
+ * (netket/_src/stats/online_stats/kernels.py:123-190, called from
+ * accumulator.py:160-223) on the device.  The state of n_chains chains is
+ * FP64 device arrays, row-major:
+ *   count, mean, M2          (n_chains)              per-chain Welford state
+ *   cross, m1, m2, pair      (n_chains, max_lag + 1) sums of x_t x_{t-k},
+ *                                                    x_{t-k}, x_t and pair counts
+ *   buf                      (n_chains, max_lag)     the last max_lag samples,
+ *                                                    newest last
+ * (the ACF arrays may be NULL when max_lag == 0).  data is (n_chains, n_batch)
+ * FP64.  buf_len = how many buffer entries are valid before this call
+ * (min(samples seen so far per chain, max_lag)); the caller advances it to
+ * min(buf_len + n_batch, max_lag).  decay in [0, 1] multiplies the old counts
+ * and sums first (1 = the reference's decay=None).  mean_f32 != 0 rounds the
+ * stored per-chain means to float after the merge (float32 input data). */
+#define VMCK_ONLINE_STATS_MAX_LAG 4096
+typedef struct vmck_online_stats {
+  double *count, *mean, *M2;
+  double *cross, *m1, *m2, *pair;
+  double *buf;
+} vmck_online_stats;
+int vmck_online_stats_update(vmck_stream s, const double *data, int32_t n_chains,
+                             int32_t n_batch, int32_t max_lag, int32_t buf_len,
+                             double decay, int32_t mean_f32,
+                             const vmck_online_stats *state);
+
 /* ---------------------------------------------------------------- a11 / a12 / a14
  * out = O^T v for the RBM Jacobian O (n, P) without materialising it
  * (the VJP of netket/vqs/mc/mc_state/expect_forces.py:99-106 and the

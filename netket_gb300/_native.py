@@ -48,6 +48,11 @@ class BatchIsingStruct(ctypes.Structure):
                 ("pad", c_i32)]
 
 
+class OnlineStatsStruct(ctypes.Structure):
+    """Mirror of ``vmck_online_stats``."""
+    _fields_ = [(k, c_vp) for k in ("count", "mean", "M2", "cross", "m1", "m2", "pair", "buf")]
+
+
 _SIGNATURES = {
     "vmck_abi_version": ([], c_i32),
     "vmck_error_string": ([c_i32], ctypes.c_char_p),
@@ -75,6 +80,8 @@ _SIGNATURES = {
     "vmck_stats_workspace_size": ([c_i32, c_i32], c_i64),
     "vmck_stats_f64": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp, c_i64], c_i32),
     "vmck_stats_f64_noalloc": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_vp], c_i32),
+    "vmck_online_stats_update": ([c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_dbl, c_i32,
+                                  ctypes.POINTER(OnlineStatsStruct)], c_i32),
     "vmck_rbm_o_v": ([c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_vp], c_i32),
     "vmck_ot_v_workspace_size": ([c_i32, c_i32, c_i64], c_i64),
     "vmck_rbm_ot_v": ([c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_i64],

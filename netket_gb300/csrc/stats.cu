@@ -125,9 +125,118 @@ __global__ void stats_pass2(const double *__restrict__ data, StatsLayout lay, in
   }
 }
 
+// ------------------------------------------------------------ online accumulator
+// One warp per chain (netket/_src/stats/online_stats/kernels.py:123-190).
+// Welford: the batch mean and the batch sum of squared deviations (two passes
+// over the chain's row), then the merge into (count, mean, M2) after the decay.
+// ACF: lane l owns the lags k = l, l + 32, ...; for each it walks the batch once
+// for the pairs (x_j, x_{j-k}) with j >= k and once for the pairs whose older
+// member is in the rolling buffer (j < k, k - j <= buf_len).  In every
+// iteration all lanes read the same x_j (a broadcast) and neighbouring x_{j-k}
+// (one coalesced line), so the row is read from L1 after its first touch.
+// The within-batch and cross-batch sums are formed separately and added to the
+// (decayed) accumulator as (within + cross), the reference's association.
+// Finally the buffer keeps the newest max_lag samples: a forward in-place shift
+// by n_batch in 32-wide chunks (each chunk's reads are at higher addresses than
+// every write so far) followed by the batch's tail.
+constexpr int OS_WARPS = 4;
+
+__global__ void __launch_bounds__(OS_WARPS * 32)
+    online_stats_update_kernel(const double *__restrict__ data, int C, int nb, int L,
+                               int old_len, double decay, int mean_f32, vmck_online_stats st) {
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * OS_WARPS + (threadIdx.x >> 5);
+  if (c >= C) return;
+  const double *x = data + (int64_t)c * nb;
+
+  double s = 0.0;
+  for (int j = lane; j < nb; j += 32) s += x[j];
+  const double c_mean = warp_sum(s) / nb;
+  double q = 0.0;
+  for (int j = lane; j < nb; j += 32) {
+    const double d = x[j] - c_mean;
+    q += d * d;
+  }
+  q = warp_sum(q);
+  if (lane == 0) {
+    const double cnt = st.count[c] * decay;
+    const double M2 = st.M2[c] * decay;
+    const double mu = st.mean[c];
+    const double cnt_new = cnt + nb;
+    const double safe = cnt_new > 0.0 ? cnt_new : 1.0;
+    const double delta = c_mean - mu;
+    double mu_new = mu + delta * ((double)nb / safe);
+    if (mean_f32) mu_new = (double)(float)mu_new;
+    st.mean[c] = mu_new;
+    st.M2[c] = M2 + q + delta * delta * (cnt * nb / safe);
+    st.count[c] = cnt_new;
+  }
+  if (L <= 0) return;
+
+  const int64_t arow = (int64_t)c * (L + 1);
+  double *buf = st.buf + (int64_t)c * L;
+  for (int k = lane; k <= L; k += 32) {
+    double cw = 0.0, m1w = 0.0, m2w = 0.0;
+    for (int j = k; j < nb; ++j) {
+      const double cur = x[j], lag = x[j - k];
+      cw = fma(cur, lag, cw);
+      m1w += lag;
+      m2w += cur;
+    }
+    const double nw = nb > k ? (double)(nb - k) : 0.0;
+    double cc = 0.0, m1c = 0.0, m2c = 0.0;
+    const int jlo = k - old_len > 0 ? k - old_len : 0;
+    const int jhi = k < nb ? k : nb;
+    for (int j = jlo; j < jhi; ++j) {
+      const double cur = x[j], lag = buf[L - (k - j)];
+      cc = fma(cur, lag, cc);
+      m1c += lag;
+      m2c += cur;
+    }
+    const double nc = jhi > jlo ? (double)(jhi - jlo) : 0.0;
+    st.cross[arow + k] = st.cross[arow + k] * decay + (cw + cc);
+    st.m1[arow + k] = st.m1[arow + k] * decay + (m1w + m1c);
+    st.m2[arow + k] = st.m2[arow + k] * decay + (m2w + m2c);
+    st.pair[arow + k] = st.pair[arow + k] * decay + (nw + nc);
+  }
+  __syncwarp();
+  if (nb >= L) {
+    for (int i = lane; i < L; i += 32) buf[i] = x[nb - L + i];
+  } else {
+    const int keep = L - nb;
+    for (int base = 0; base < keep; base += 32) {
+      const int i = base + lane;
+      const double v = i < keep ? buf[i + nb] : 0.0;
+      __syncwarp();
+      if (i < keep) buf[i] = v;
+      __syncwarp();
+    }
+    for (int i = lane; i < nb; i += 32) buf[keep + i] = x[i];
+  }
+}
+
 }  // namespace vmck
 
 using namespace vmck;
+
+extern "C" int vmck_online_stats_update(vmck_stream s, const double *data, int32_t n_chains,
+                                        int32_t n_batch, int32_t max_lag, int32_t buf_len,
+                                        double decay, int32_t mean_f32,
+                                        const vmck_online_stats *state) {
+  VMCK_REQUIRE(data && state && n_chains > 0 && n_batch > 0, "online_stats_update arguments");
+  VMCK_REQUIRE(max_lag >= 0 && max_lag <= VMCK_ONLINE_STATS_MAX_LAG,
+               "online_stats_update: max_lag out of range");
+  VMCK_REQUIRE(buf_len >= 0 && buf_len <= max_lag, "online_stats_update: buf_len out of range");
+  VMCK_REQUIRE(decay >= 0.0 && decay <= 1.0, "online_stats_update: decay must lie in [0, 1]");
+  VMCK_REQUIRE(state->count && state->mean && state->M2, "online_stats_update: state");
+  VMCK_REQUIRE(max_lag == 0 || (state->cross && state->m1 && state->m2 && state->pair &&
+                                state->buf),
+               "online_stats_update: ACF state");
+  const int blocks = (n_chains + OS_WARPS - 1) / OS_WARPS;
+  online_stats_update_kernel<<<blocks, OS_WARPS * 32, 0, as_stream(s)>>>(
+      data, n_chains, n_batch, max_lag, buf_len, decay, mean_f32 ? 1 : 0, *state);
+  return check_launch("online_stats_update");
+}
 
 // ------------------------------------------------------------ allocation-free variant
 // Scratch for vmck_stats_f64_noalloc: a fixed array that lives in every device's

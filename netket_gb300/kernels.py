@@ -85,6 +85,20 @@ def stats_device(data2d, plain_rhat=False):
     return out
 
 
+def online_stats_update(data2d, state, max_lag, buf_len, decay, mean_f32):
+    """Merge ``data2d`` (n_chains, n_batch) FP64 into the accumulator tensors
+    ``state`` (dict count/mean/M2/cross/m1/m2/pair/buf, FP64, on the device) in
+    place; see ``vmck_online_stats_update``."""
+    C, nb = data2d.shape
+    d = data2d.to(torch.float64).contiguous()
+    st = nat.OnlineStatsStruct(*[nat.ptr(state[k]) if state[k].numel() else None
+                                 for k in ("count", "mean", "M2", "cross", "m1", "m2", "pair",
+                                           "buf")])
+    nat.check(nat.lib().vmck_online_stats_update(nat.stream(), nat.ptr(d), C, nb, int(max_lag),
+                                                 int(buf_len), float(decay), int(mean_f32),
+                                                 ctypes.byref(st)))
+
+
 # ------------------------------------------------------------------ Jacobian products
 def ot_v(tanh_t, x, N, M, v):
     """O^T v (P,) FP64 for the RBM Jacobian, never materialising O."""

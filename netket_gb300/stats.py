@@ -34,6 +34,9 @@ class Stats:
         return {"Mean": self.mean, "Variance": self.variance, "Sigma": self.error_of_mean,
                 "R_hat": self.R_hat, "TauCorr": self.tau_corr}
 
+    def to_compound(self):
+        return "Mean", self.to_dict()
+
     def as_array(self):
         return np.array([self.mean, self.error_of_mean, self.variance, self.tau_corr, self.R_hat])
 
@@ -61,3 +64,8 @@ def statistics(data):
     if d.ndim != 2:
         raise NotImplementedError("Statistics are implemented only for ndim<=2")
     return Stats.from_array(stats_device(d, _plain_rhat()).cpu().numpy())
+
+
+from .online_stats import (  # noqa: E402  (re-exported as netket.stats does)
+    LocalEstimators, LocalEstimatorsBatch, OnlineStats, OnlineStatsBatch, StatsBatch,
+    expand_max_lag, online_statistics, online_statistics_batch, thin_acf_by_2)

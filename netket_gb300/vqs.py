@@ -20,6 +20,7 @@ import torch
 from . import _native as nat
 from . import kernels as K
 from .stats import Stats, _plain_rhat
+from .online_stats import online_statistics
 
 
 class MCState:
@@ -151,13 +152,15 @@ class MCState:
         e = self.local_estimators(op)
         return Stats.from_array(K.stats_device(e, _plain_rhat()).cpu().numpy())
 
-    def expect_to_precision(self, op, *, atol=None, rtol=None, max_iter=10_000):
+    def expect_to_precision(self, op, *, atol=None, rtol=None, max_iter=10_000, max_lag=64):
         """Sample until the standard error of the mean meets ``atol`` (absolute)
         and / or ``rtol`` (relative to |mean|); both must hold when both are given
-        (``netket/_src/vqs/expect_to_precision.py``: same arguments, checks and
-        sampling loop, later rounds without discarded sweeps).  The error is the
-        blocking estimator of ``statistics`` over all chains' accumulated local
-        estimators, where NetKet updates an online autocorrelation estimate."""
+        (``netket/_src/vqs/expect_to_precision.py:70-164``).  ``op`` is an operator
+        or a list / tuple / dict of operators; each has its own ``OnlineStats``
+        accumulator (``max_lag`` lags of online autocorrelation), fed with the
+        local estimators of every sampling round until it converges, and the
+        accumulators are returned in the structure of ``op``.  Later rounds
+        discard no sweeps, as in the reference."""
         if atol is None and rtol is None:
             raise ValueError("At least one of 'atol' or 'rtol' must be specified.")
         if atol is not None and atol <= 0:
@@ -165,34 +168,43 @@ class MCState:
         if rtol is not None and rtol <= 0:
             raise ValueError("rtol must be > 0.")
 
-        def not_converged(st):
+        if isinstance(op, dict):
+            keys, leaves = list(op), list(op.values())
+        elif isinstance(op, (list, tuple)):
+            keys, leaves = None, list(op)
+        else:
+            keys, leaves = None, [op]
+
+        def not_converged(acc):
+            st = acc.get_stats()
             err, scale = abs(st.error_of_mean), abs(st.mean)
-            if not math.isfinite(err):
-                return True
-            if atol is not None and err > atol:
+            if atol is not None and not err <= atol:
                 return True
             if rtol is not None:
                 rel = (0.0 if err == 0.0 else math.inf) if scale == 0.0 else err / scale
-                if rel > rtol:
+                if not rel <= rtol:
                     return True
             return False
 
+        def accumulate(active, accs):
+            return [online_statistics(self.local_estimators(o), a, max_lag=max_lag)
+                    if i in active else a for i, (o, a) in enumerate(zip(leaves, accs))]
+
         self.sample()
-        chunks = [self.local_estimators(op)]
-
-        def stats():
-            data = torch.cat(chunks, dim=1).contiguous()
-            return Stats.from_array(K.stats_device(data, _plain_rhat()).cpu().numpy())
-
-        st = stats()
+        accs = accumulate(set(range(len(leaves))), [None] * len(leaves))
+        active = [i for i in range(len(leaves)) if not_converged(accs[i])]
         it = 0
-        while not_converged(st) and it < max_iter:
+        while active and it < max_iter:
             self.sample(n_discard_per_chain=0)
-            chunks.append(self.local_estimators(op))
-            st = stats()
+            accs = accumulate(set(active), accs)
+            active = [i for i in active if not_converged(accs[i])]
             it += 1
         self.last_precision_rounds = it
-        return st
+        if keys is not None:
+            return dict(zip(keys, accs))
+        if isinstance(op, (list, tuple)):
+            return type(op)(accs)
+        return accs[0]
 
     def _forward_cache(self, op):
         """Samples, tanh(theta), local energies and their device statistics."""

@@ -354,6 +354,128 @@ def gen_ngd():
     np.savez_compressed(os.path.join(HERE, "ngd.npz"), **out)
 
 
+# ---------------------------------------------------------------- online stats
+class AtArray(np.ndarray):
+    """ndarray with jax's functional ``x.at[idx].add(v)``."""
+
+    @property
+    def at(self):
+        arr = self
+
+        class _Idx:
+            def __getitem__(self, idx):
+                class _Op:
+                    def add(self, v):
+                        out = np.array(arr, copy=True).view(AtArray)
+                        out[idx] += v
+                        return out
+                return _Op()
+        return _Idx()
+
+
+def lax_scan(f, init, xs):
+    carry = init
+    for x in xs:
+        carry, _ = f(carry, x)
+    return carry, None
+
+
+def lax_dynamic_slice_in_dim(a, start, size, axis=0):
+    # XLA clamps the start index so that the slice stays in bounds
+    start = int(min(max(int(start), 0), a.shape[axis] - size))
+    idx = [slice(None)] * a.ndim
+    idx[axis] = slice(start, start + size)
+    return a[tuple(idx)]
+
+
+def gen_online_stats():
+    jnp = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("_")})
+    jax = types.SimpleNamespace(
+        jit=lambda *a, **k: (lambda f: f),
+        lax=types.SimpleNamespace(scan=lax_scan, dynamic_slice_in_dim=lax_dynamic_slice_in_dim))
+    ns = {"np": np, "jnp": jnp, "jax": jax, "lax": jax.lax,
+          "partial": lambda *a, **k: (lambda f: f)}
+    load("_src/stats/online_stats/kernels.py", ["_acf_core", "_update_arrays"], ns)
+    import math
+    gns = {"np": np, "jnp": jnp, "jax": jax, "isnan": math.isnan, "sqrt": math.sqrt,
+           "_NaN": np.nan,
+           "Stats": lambda **kw: np.array([kw["mean"], kw["error_of_mean"], kw["variance"],
+                                           kw["tau_corr"], kw["R_hat"]], dtype=np.float64)}
+    getters = ["mean", "variance", "tau_corr", "tau_corr_batch", "tau_corr_acf", "acf",
+               "R_hat", "n_chains", "get_stats", "_compute_error_of_mean"]
+    load("_src/stats/online_stats/accumulator.py", getters, gns, class_name="OnlineStats")
+    props = {g: property(gns[g]) for g in getters if g not in ("get_stats",
+                                                               "_compute_error_of_mean")}
+    props["get_stats"] = gns["get_stats"]
+    props["_compute_error_of_mean"] = gns["_compute_error_of_mean"]
+    FakeOS = type("FakeOS", (), props)
+
+    def run(chunks, max_lag, decay):
+        C = chunks[0].shape[0]
+        acf_len = max_lag + 1 if max_lag > 0 else 0
+        z = lambda *s: np.zeros(s).view(AtArray)
+        st = [z(C), np.zeros(C), z(C), z(C, acf_len), z(C, acf_len), z(C, acf_len),
+              z(C, acf_len), z(C, max_lag)]
+        buf_len, n_total = 0, 0
+        for d in chunks:
+            st = list(ns["_update_arrays"](*st, decay, max_lag, buf_len, d))
+            st = [np.asarray(a).view(AtArray) for a in st]
+            buf_len = min(buf_len + d.shape[1], max_lag)
+            n_total += d.size
+        o = FakeOS()
+        (o._chain_count, o._chain_mean, o._chain_M2, o._cross_sum, o._m1_sum, o._m2_sum,
+         o._pair_count, o._chain_buf) = [np.asarray(a) for a in st]
+        o.max_lag, o._n_samples_total, o._buf_len = max_lag, n_total, buf_len
+        derived = np.array([o.mean, o.variance, o.tau_corr, o.tau_corr_batch,
+                            o.tau_corr_acf, o.R_hat, float(np.real(o.get_stats()[1]))],
+                           dtype=np.float64)
+        acf = o.acf
+        return [np.asarray(a) for a in st], buf_len, derived, (
+            np.zeros(0) if acf is None else np.asarray(acf))
+
+    rng = np.random.default_rng(2024)
+
+    def ar1(C, T, phi):
+        x = np.zeros((C, T))
+        x[:, 0] = rng.standard_normal(C)
+        for t in range(1, T):
+            x[:, t] = phi * x[:, t - 1] + math.sqrt(1 - phi ** 2) * rng.standard_normal(C)
+        return x
+
+    cases = {
+        # (chunk lengths along the chain axis, n_chains, max_lag, decay, generator)
+        "iid_oneshot": ([300], 8, 64, None, "iid"),
+        "iid_chunks": ([30] * 10, 8, 32, None, "iid"),
+        "ar1_small_batches": ([4] * 40, 16, 64, None, "ar1"),
+        "ar1_ragged": ([1, 7, 3, 64, 2, 100, 5], 6, 16, None, "ar1"),
+        "big_then_small": ([12, 6, 6, 6, 6, 6], 4, 8, None, "iid"),
+        "decay": ([50] * 6, 4, 16, 0.9, "ar1"),
+        "no_acf": ([40] * 5, 6, 0, None, "iid"),
+        "one_chain": ([200, 56], 1, 64, None, "ar1"),
+        "shifted_mean": ([5] * 20, 64, 64, None, "shift"),
+    }
+    out = {}
+    for name, (lens, C, max_lag, decay, gen) in cases.items():
+        T = sum(lens)
+        if gen == "iid":
+            data = rng.standard_normal((C, T))
+        elif gen == "ar1":
+            data = ar1(C, T, 0.8)
+        else:
+            data = -37.5 + 0.25 * rng.standard_normal((C, T))
+        chunks = np.split(data, np.cumsum(lens)[:-1], axis=1)
+        st, buf_len, derived, acf = run(chunks, max_lag, decay)
+        out[name + "__data"] = data
+        out[name + "__lens"] = np.array(lens)
+        out[name + "__cfg"] = np.array([max_lag, -1.0 if decay is None else decay])
+        for key, a in zip(["count", "mean", "M2", "cross", "m1", "m2", "pair", "buf"], st):
+            out[f"{name}__{key}"] = a
+        out[name + "__buf_len"] = np.array(buf_len)
+        out[name + "__derived"] = derived
+        out[name + "__acf"] = acf
+    np.savez_compressed(os.path.join(HERE, "online_stats.npz"), **out)
+
+
 if __name__ == "__main__":
     edges = gen_edges()
     gen_ising(edges)

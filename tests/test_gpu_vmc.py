@@ -173,8 +173,10 @@ def test_expect_to_precision_reaches_tolerance(nk):
                           visible_bias_init_std=0.3)
     vs = nk.vqs.MCState(nk.sampler.MetropolisLocal(hi, n_chains=64), model, n_samples=512,
                         seed=2, precision="fp64")
-    st = vs.expect_to_precision(H, atol=2e-3)
+    acc = vs.expect_to_precision(H, atol=2e-3)
+    st = acc.get_stats()
     assert st.error_of_mean <= 2e-3 and vs.last_precision_rounds >= 1
+    assert acc.n_samples == 512 * (vs.last_precision_rounds + 1)
     # exact expectation from the full sum over the 256 configurations
     allx = torch.as_tensor(hi.all_states(), device="cuda")
     lp = vs.log_value(allx)
@@ -185,3 +187,8 @@ def test_expect_to_precision_reaches_tolerance(nk):
     assert abs(st.mean - exact) < 5 * st.error_of_mean
     with pytest.raises(ValueError):
         vs.expect_to_precision(H)
+    # a dict of operators: one accumulator each, returned under the same keys
+    Z = nk.operator.LocalOperator(hi, [np.array([[1.0, 0.0], [0.0, -1.0]])], [[0]])
+    res = vs.expect_to_precision({"H": H, "Z": Z}, rtol=0.05, max_iter=50)
+    assert set(res) == {"H", "Z"}
+    assert res["H"].get_stats().error_of_mean <= 0.05 * abs(res["H"].mean)

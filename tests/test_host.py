@@ -1,6 +1,7 @@
 """CPU tests of the product's host side: lattice edges, operator packing, the
 C-ABI library (loads and exports every declared symbol), and loud failure
 without a GPU.  No kernel is launched here."""
+import math
 import os
 import re
 
@@ -158,3 +159,92 @@ def test_state_dict_bytes_round_trip():
             assert np.asarray(a).dtype == np.asarray(b).dtype
             np.testing.assert_array_equal(a, b)
     check(d, back)
+
+
+def _online_from_oracle(s, decay=None, device="cpu"):
+    from netket_gb300.online_stats import OnlineStats
+    d = {k: s[k] for k in ("count", "mean", "M2", "cross", "m1", "m2", "pair", "buf")}
+    d.update(max_lag=s["max_lag"], n_total=s["n_total"], buf_len=s["buf_len"],
+             decay=-1.0 if decay is None else decay)
+    return OnlineStats.from_state_dict(d, device=device)
+
+
+@pytest.mark.parametrize("name", ["iid_oneshot", "iid_chunks", "ar1_small_batches",
+                                  "ar1_ragged", "big_then_small", "decay", "no_acf",
+                                  "one_chain", "shifted_mean"])
+def test_online_stats_readouts(golden, name):
+    """OnlineStats read-outs (mean, variance, tau via Geyer / batch, R-hat, error,
+    ACF) on the accumulator state, vs the reference's own read-outs."""
+    from test_oracle_golden import acf_tolerance, online_oracle_run
+    g = golden("online_stats")
+    cfg = g[name + "__cfg"]
+    est = _online_from_oracle(online_oracle_run(g, name), None if cfg[1] < 0 else cfg[1])
+    st = est.get_stats()
+    got = np.array([est.mean, est.variance, est.tau_corr, est.tau_corr_batch, est.tau_corr_acf,
+                    est.R_hat, st.error_of_mean])
+    np.testing.assert_allclose(got, g[name + "__derived"], rtol=1e-11, atol=1e-13,
+                               equal_nan=True)
+    assert st.mean == est.mean and st.tau_corr == est.tau_corr
+    ga = g[name + "__acf"]
+    if ga.size == 0:
+        assert est.acf is None
+    else:
+        np.testing.assert_allclose(est.acf.numpy(), ga, rtol=0, atol=acf_tolerance(g, name))
+    key, d = est.to_compound()
+    assert key == "Mean" and set(d) >= {"Mean", "Variance", "Sigma", "R_hat", "TauCorr"}
+
+
+def test_online_stats_window_operations():
+    """expand_max_lag / thin_acf_by_2 (netket/_src/stats/online_stats/
+    operations.py:129-261), the reference tests' properties: old lags kept, new
+    lags zero, buffer right-aligned, Welford state untouched, even lags kept."""
+    from oracle import online_stats as oos
+    from netket_gb300.online_stats import expand_max_lag, thin_acf_by_2
+    rng = np.random.default_rng(5)
+    s = oos.new_state(4, 16)
+    for ch in np.split(rng.standard_normal((4, 200)), 4, axis=1):
+        s = oos.update(s, ch)
+    est = _online_from_oracle(s)
+    ex = expand_max_lag(est, 48)
+    assert ex.max_lag == 48 and ex._cross_sum.shape == (4, 49) and ex._chain_buf.shape == (4, 48)
+    np.testing.assert_array_equal(ex._cross_sum[:, :17].numpy(), s["cross"])
+    np.testing.assert_array_equal(ex._pair_count[:, :17].numpy(), s["pair"])
+    assert not ex._cross_sum[:, 17:].any() and not ex._pair_count[:, 17:].any()
+    np.testing.assert_array_equal(ex._chain_buf[:, 32:].numpy(), s["buf"])
+    assert not ex._chain_buf[:, :32].any()
+    np.testing.assert_array_equal(est.acf.numpy(), ex.acf[:17].numpy())
+    assert ex.mean == est.mean and ex.variance == est.variance and ex.n_samples == est.n_samples
+    with pytest.raises(ValueError, match="must be >"):
+        expand_max_lag(est, 16)
+    th = thin_acf_by_2(est)
+    assert th.max_lag == 8 and th._buf_len == s["buf_len"] // 2
+    np.testing.assert_array_equal(th._cross_sum.numpy(), s["cross"][:, ::2])
+    np.testing.assert_array_equal(th._chain_buf.numpy(), s["buf"][:, 0::2])
+    z = _online_from_oracle(oos.update(oos.new_state(4, 0), rng.standard_normal((4, 10))))
+    assert z.acf is None and math.isnan(z.tau_corr_acf)
+    ez = expand_max_lag(z, 32)
+    assert ez._cross_sum.shape == (4, 33) and ez._chain_buf.shape == (4, 32)
+
+
+def test_online_stats_batch_delta_method():
+    """OnlineStatsBatch: combinator of K channel means with the delta-method
+    error J^T Cov J, Cov the covariance of the chain means / n_chains
+    (accumulator_batch.py:31-68, 196-211)."""
+    from oracle import online_stats as oos
+    from netket_gb300.online_stats import OnlineStatsBatch
+    rng = np.random.default_rng(8)
+    data = rng.standard_normal((64, 50, 2)) + np.array([0.5, 1.0])
+    ests = []
+    for k in range(2):
+        ests.append(_online_from_oracle(oos.update(oos.new_state(64, 8), data[..., k])))
+    acc = OnlineStatsBatch(ests, lambda mu: mu[1] - mu[0] ** 2)
+    X = data.reshape(-1, 2).mean(0)
+    cm = data.mean(1)
+    cov = (cm - X).T @ (cm - X) / 64 ** 2
+    J = np.array([-2 * X[0], 1.0])
+    st = acc.get_stats()
+    np.testing.assert_allclose(st.mean, X[1] - X[0] ** 2, rtol=1e-12)
+    np.testing.assert_allclose(st.error_of_mean, np.sqrt(J @ cov @ J), rtol=1e-10)
+    vec = OnlineStatsBatch(ests, lambda mu: torch.stack([mu[0], mu[0] * mu[1]])).get_stats()
+    assert tuple(vec.mean.shape) == (2,) and tuple(vec.error_of_mean.shape) == (2,)
+    np.testing.assert_allclose(float(vec.error_of_mean[0]), np.sqrt(cov[0, 0]), rtol=1e-10)

@@ -178,3 +178,45 @@ def test_vectorised_conn_equals_loop_oracle(golden, name):
     rxp, rm = op.get_conn_padded(x)
     np.testing.assert_array_equal(xp, rxp)
     np.testing.assert_array_equal(m, rm)
+
+
+ONLINE_CASES = ["iid_oneshot", "iid_chunks", "ar1_small_batches", "ar1_ragged",
+                "big_then_small", "decay", "no_acf", "one_chain", "shifted_mean"]
+
+
+def online_oracle_run(g, name):
+    from oracle import online_stats as oos
+    data, lens, cfg = g[name + "__data"], g[name + "__lens"], g[name + "__cfg"]
+    decay = None if cfg[1] < 0 else float(cfg[1])
+    s = oos.new_state(data.shape[0], int(cfg[0]))
+    for ch in np.split(data, np.cumsum(lens)[:-1], axis=1):
+        s = oos.update(s, ch, decay)
+    return s
+
+
+def acf_tolerance(g, name):
+    """The ACF is formed from raw moment sums (sum x_t x_{t-k} - sum x_{t-k} sum
+    x_t / n), so rounding in the sums is amplified by mean^2 / variance."""
+    d = g[name + "__data"]
+    return 1e-13 * max(1.0, float(np.mean(d)) ** 2 / float(np.var(d)))
+
+
+@pytest.mark.parametrize("name", ONLINE_CASES)
+def test_online_stats_oracle(golden, name):
+    """Oracle restatement of OnlineStats vs the reference's own _update_arrays /
+    _acf_core and read-outs, executed on the same chunks."""
+    from oracle import online_stats as oos
+    g = golden("online_stats")
+    s = online_oracle_run(g, name)
+    for k in ("count", "mean", "M2", "cross", "m1", "m2", "pair", "buf"):
+        ref = g[f"{name}__{k}"]
+        scale = max(1.0, float(np.abs(ref).max())) if ref.size else 1.0
+        np.testing.assert_allclose(s[k], ref, rtol=0, atol=1e-14 * scale, err_msg=k)
+    assert s["buf_len"] == int(g[name + "__buf_len"])
+    np.testing.assert_allclose(oos.derived(s), g[name + "__derived"], rtol=1e-11,
+                               atol=1e-13, equal_nan=True)
+    a, ga = oos.acf(s), g[name + "__acf"]
+    if ga.size == 0:
+        assert a is None
+    else:
+        np.testing.assert_allclose(a, ga, rtol=0, atol=acf_tolerance(g, name))
