@@ -38,6 +38,7 @@ extern "C" {
 #define VMCK_DEV_NOT_SPD 2     /* Cholesky info != 0 */
 #define VMCK_DEV_NO_CONVERGE 4 /* iterative refinement did not reach tolerance */
 #define VMCK_DEV_TIMEOUT 8     /* a bounded device-side wait ran out (kernel wound down) */
+#define VMCK_DEV_INTERNAL 16   /* a kernel's internal consistency check failed (work skipped) */
 
 /* element types */
 #define VMCK_F64 0
@@ -159,6 +160,27 @@ int vmck_metropolis_sample(vmck_stream s, int32_t dtype, const void *params, int
                            int32_t n_discard, int32_t chain_length, int8_t *samples,
                            uint64_t seed, uint64_t counter, int32_t rule,
                            const int32_t *clusters, int32_t n_clusters);
+
+/* ---------------------------------------------------------------- f3
+ * MetropolisSampler with the Hamiltonian rule (netket/sampler/metropolis.py:
+ * 686-735, rules/hamiltonian.py:99-213) for the RBM: every proposal picks one of
+ * the n(x) entries of x's operator row uniformly,
+ *   n(x) = [diagonal slot] + sum_t #{stored off-diagonal columns of term t's
+ *          row with |mel| > mel_cutoff},
+ * the diagonal slot proposing x itself, and corrects the acceptance by
+ * log n(x) - log n(x').  diag_rule: 0 = no diagonal slot, 1 = a slot whenever
+ * the operator has a diagonal (LocalOperator n_conn, _local_operator/jax.py:
+ * 107-112), 2 = a slot only where |diagonal element| > mel_cutoff (IsingJax
+ * n_conn, _ising/jax.py:168-175; pass Ising as its LocalOperator tables).
+ * Arguments, samples, random stream and bookkeeping as vmck_metropolis_sample.
+ * status (device int32) gets VMCK_DEV_INTERNAL if a chain's counts ever
+ * disagree with its row (not expected; the proposal is skipped). */
+int vmck_metropolis_hamiltonian(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                                int32_t M, const vmck_local_op *op, int32_t diag_rule,
+                                int8_t *sigma, double *log_prob, int64_t *n_accepted, int32_t B,
+                                int32_t sweep_size, int32_t n_discard, int32_t chain_length,
+                                int8_t *samples, uint64_t seed, uint64_t counter,
+                                int32_t *status);
 
 /* ---------------------------------------------------------------- batched (C3)
  * Many independent problems of uneven size in one persistent launch.  Each

@@ -13,7 +13,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libvmck.so")
 
 F64, F32, BF16 = 0, 1, 2
-DEV_NONFINITE, DEV_NOT_SPD, DEV_NO_CONVERGE, DEV_TIMEOUT = 1, 2, 4, 8
+DEV_NONFINITE, DEV_NOT_SPD, DEV_NO_CONVERGE, DEV_TIMEOUT, DEV_INTERNAL = 1, 2, 4, 8, 16
 
 c_i32, c_i64, c_u64, c_dbl, c_vp = (ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64,
                                     ctypes.c_double, ctypes.c_void_p)
@@ -73,6 +73,9 @@ _SIGNATURES = {
                              ctypes.POINTER(LocalOpStruct), c_vp, c_vp], c_i32),
     "vmck_metropolis_sample": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32,
                                 c_i32, c_i32, c_vp, c_u64, c_u64, c_i32, c_vp, c_i32], c_i32),
+    "vmck_metropolis_hamiltonian": ([c_vp, c_i32, c_vp, c_i32, c_i32, ctypes.POINTER(LocalOpStruct),
+                                     c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp,
+                                     c_u64, c_u64, c_vp], c_i32),
     "vmck_batched_metropolis_local": ([c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32,
                                        c_i32, c_i32, c_i32, c_i32], c_i32),
     "vmck_batched_eloc_ising": ([c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32, c_i32,

@@ -24,6 +24,13 @@ class Spin:
                 raise ValueError(f"total_sz={total_sz} is incompatible with N={self.N}")
         self.total_sz = total_sz
 
+    def __eq__(self, other):
+        return (isinstance(other, Spin) and self.N == other.N and
+                self.total_sz == other.total_sz)
+
+    def __hash__(self):
+        return hash(("Spin", self.N, self.total_sz))
+
     @property
     def size(self):
         return self.N

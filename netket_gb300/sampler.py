@@ -1,6 +1,7 @@
 """Metropolis samplers (``netket.sampler``): ``MetropolisSampler`` with the
-``LocalRule`` / ``ExchangeRule`` transition rules and the ``MetropolisLocal`` /
-``MetropolisExchange`` constructors.
+``LocalRule`` / ``ExchangeRule`` / ``HamiltonianRule`` transition rules and the
+``MetropolisLocal`` / ``MetropolisExchange`` / ``MetropolisHamiltonian``
+constructors.
 
 The whole chain (discarded plus kept sweeps) runs in ONE launch of
 ``vmck_metropolis_sample``: a warp per chain, the RBM pre-activations kept
@@ -9,6 +10,7 @@ in shared memory and updated per proposal.  Samples come back shaped
 The random stream is Philox4x32-10, keyed by the sampler seed, with a
 proposal counter carried in the sampler state.
 """
+import ctypes
 from dataclasses import dataclass
 
 import numpy as np
@@ -58,6 +60,40 @@ class ExchangeRule(MetropolisRule):
         return f"ExchangeRule(# of clusters: {len(self.clusters)})"
 
 
+class HamiltonianRule(MetropolisRule):
+    """Move to one of the entries of x's operator row, chosen uniformly, with
+    the correction log n(x) - log n(x') (``netket/sampler/rules/hamiltonian.py:
+    99-235``).  The operator is an ``Ising`` (its diagonal slot counts only where
+    the diagonal element is nonzero, as IsingJax's ``n_conn``) or a
+    ``LocalOperator`` (the slot counts whenever the operator has a diagonal,
+    as LocalOperator's ``n_conn``; the numba rule draws among the same
+    entries).  The reference's jax rule draws among the nonzero entries but
+    normalises by ``n_conn``: where a LocalOperator's diagonal element is
+    exactly zero that selects no entry and proposes an all-zero row; here the
+    zero diagonal entry proposes x itself, as the numba rule does."""
+    code = 2
+
+    def __init__(self, operator):
+        from .operator import Ising, LocalOperator
+        if isinstance(operator, Ising):
+            self._local = operator.to_local_operator()
+            self.diag_rule = 2
+        elif isinstance(operator, LocalOperator):
+            self._local = operator
+            self.diag_rule = 1 if operator._pack()["nonzero_diag"] else 0
+        else:
+            raise TypeError("Argument to HamiltonianRule must be a valid operator, "
+                            f"but operator is a {type(operator)}.")
+        self.operator = operator
+        self.status = None
+
+    def device_op(self):
+        return self._local.device_struct()
+
+    def __repr__(self):
+        return f"HamiltonianRule(operator={self.operator})"
+
+
 @dataclass
 class MetropolisSamplerState:
     """Chain state (``netket/sampler/metropolis.py:42-95``)."""
@@ -87,6 +123,10 @@ class MetropolisSampler:
                  reset_chains=False, dtype=torch.int8):
         if not isinstance(rule, MetropolisRule):
             raise TypeError("rule must be a MetropolisRule")
+        if isinstance(rule, HamiltonianRule) and rule.operator.hilbert != hilbert:
+            raise ValueError(f"The hilbert space of the sampler ({hilbert}) and the hilbert "
+                             f"space of the operator ({rule.operator.hilbert}) for "
+                             "HamiltonianRule must be the same.")
         if n_chains is None:
             n_chains = n_chains_per_rank if n_chains_per_rank is not None else 16
         self.hilbert = hilbert
@@ -134,6 +174,18 @@ class MetropolisSampler:
         B = self.n_chains
         L = int(chain_length)
         samples = torch.empty((B, L, N), dtype=torch.int8, device=state.σ.device)
+        if self.rule.code == 2:
+            st = self.rule.device_op()
+            if self.rule.status is None or self.rule.status.device != state.σ.device:
+                self.rule.status = torch.zeros(1, dtype=torch.int32, device=state.σ.device)
+            nat.check(nat.lib().vmck_metropolis_hamiltonian(
+                nat.stream(), nat.dtype_code(params.dtype), nat.ptr(params.contiguous()), N, M,
+                ctypes.byref(st), self.rule.diag_rule, nat.ptr(state.σ), nat.ptr(state.log_prob),
+                nat.ptr(state.n_accepted_proc), B, self.sweep_size, int(n_discard), L,
+                nat.ptr(samples), state.seed, state.counter, nat.ptr(self.rule.status)))
+            state.counter += (int(n_discard) + L) * self.sweep_size
+            state.n_steps_proc += (int(n_discard) + L) * self.sweep_size * B
+            return samples, state
         cl, C = self.rule.device_clusters()
         nat.check(nat.lib().vmck_metropolis_sample(
             nat.stream(), nat.dtype_code(params.dtype), nat.ptr(params.contiguous()), N, M,
@@ -156,3 +208,10 @@ def MetropolisLocal(hilbert, **kwargs):
 def MetropolisExchange(hilbert, *, clusters=None, graph=None, d_max=1, **kwargs):
     return MetropolisSampler(hilbert, ExchangeRule(clusters=clusters, graph=graph, d_max=d_max),
                              **kwargs)
+
+
+def MetropolisHamiltonian(hilbert, hamiltonian, **kwargs):
+    """Moves along the nonzero off-diagonal entries of ``hamiltonian``
+    (``netket/sampler/metropolis.py:686-735``); preserves the operator's
+    symmetries (Sz for Heisenberg)."""
+    return MetropolisSampler(hilbert, HamiltonianRule(hamiltonian), **kwargs)

@@ -10,6 +10,12 @@ samples shaped (n_chains, chain_length, N).  Rules:
 * Exchange (``netket/sampler/rules/exchange.py:143-218``): choose uniformly among
   clusters (i, j) with s_i != s_j, swap, ``corr = log #hoppable(s) - log #hoppable(s')``.
 
+* Hamiltonian (``netket/sampler/rules/hamiltonian.py:84-127``, the numba form):
+  choose uniformly among the entries of x's flattened operator row (the
+  diagonal entry first whenever the operator has a diagonal; with
+  ``diag_rule=2`` only where it is above the cutoff, IsingJax's ``n_conn``,
+  ``operator/_ising/jax.py:168-175``), ``corr = log n(x) - log n(x')``.
+
 The random stream is numpy's, so parity with the CUDA sampler (and with NetKet,
 whose JAX threefry stream cannot run here) is distributional only, as in
 NetKet's own tests (``test/sampler/test_sampler.py:400-458``).
@@ -23,8 +29,39 @@ def _hoppable(x, clusters):
     return x[:, clusters[:, 0]] != x[:, clusters[:, 1]]
 
 
+def hamiltonian_row(op, x, diag_rule=1):
+    """Candidate states of each row of x (list of (k, N) arrays), numba order."""
+    P = op.pack()
+    rows = []
+    for xs, ms in op.get_conn_flattened_numba_order(x):
+        if P["nonzero_diagonal"] and (diag_rule == 0 or
+                                      (diag_rule == 2 and not abs(ms[0]) > op.mel_cutoff)):
+            xs = xs[1:]
+        rows.append(xs)
+    return rows
+
+
+def hamiltonian_propose(op, x, u, diag_rule=1):
+    """Proposal and log-correction for uniforms u (``_choose``, hamiltonian.py:
+    118-127, then ``- log n_conn(x')``)."""
+    x = np.asarray(x, dtype=np.int8)
+    rows = hamiltonian_row(op, x, diag_rule)
+    prop = x.copy()
+    corr = np.zeros(len(x))
+    for b, xs in enumerate(rows):
+        n = len(xs)
+        if n == 0:
+            corr[b] = np.nan
+            continue
+        prop[b] = xs[int(np.floor(u[b] * n))]
+        corr[b] = np.log(n)
+    n_new = np.array([len(r) for r in hamiltonian_row(op, prop, diag_rule)], dtype=np.float64)
+    with np.errstate(divide="ignore"):
+        return prop, corr - np.log(n_new)
+
+
 def sample_chain(params, x, rng, chain_length, sweep_size=None, rule="local",
-                 clusters=None, n_discard=0):
+                 clusters=None, n_discard=0, operator=None, diag_rule=1):
     x = np.array(x, dtype=np.int8)
     B, N = x.shape
     sweep_size = N if sweep_size is None else sweep_size
@@ -39,6 +76,8 @@ def sample_chain(params, x, rng, chain_length, sweep_size=None, rule="local",
                 i = rng.integers(0, N, size=B)
                 xp[rows, i] = -xp[rows, i]
                 corr = 0.0
+            elif rule == "hamiltonian":
+                xp, corr = hamiltonian_propose(operator, x, rng.random(B), diag_rule)
             else:
                 mask = _hoppable(x, clusters)
                 cnt = mask.sum(axis=1)

@@ -18,6 +18,10 @@ Covered:
                  and Ising-as-LocalOperator
   logcosh.npz    log_cosh (nn/activation.py:78-84)
   stats.npz      _statistics (stats/mc_stats_old.py:88-196)
+  online_stats.npz  OnlineStats update (_src/stats/online_stats/kernels.py:23-190) and
+                 read-outs (accumulator.py:240-447) over chunk sequences
+  hamiltonian_rule.npz  HamiltonianRuleNumba proposal (sampler/rules/hamiltonian.py:
+                 84-127: get_conn_flattened, _choose, n_conn) and IsingJax n_conn
   ngd.npz        _prepare_input + _compute_srt_update + _compute_sr_update
                  (_src/ngd/sr_srt_common.py:45-101, _src/ngd/srt.py:22-96,
                  _src/ngd/sr.py:23-80) with cholesky / pinv_smooth /
@@ -224,6 +228,83 @@ def _store_localop(ns, out, name, N, ops, aon, rng, oop):
         K += k
         nz = nz or bool(p["nonzero_diagonal"])
     out[name + "__max_conn_jax"] = np.array(K + (1 if nz else 0))
+
+
+# ---------------------------------------------------------------- Hamiltonian rule
+def gen_hamiltonian_rule(edges):
+    """HamiltonianRuleNumba.transition (sampler/rules/hamiltonian.py:84-127):
+    get_conn_flattened, _choose with given uniforms, n_conn of the proposals
+    (_discrete_operator.py:173-200); and IsingJax's n_conn (_ising/jax.py:168-175)."""
+    from oracle import operator as oop
+    import math
+    ns = {"np": np, "numba": numba_stub, "sparse": scipy.sparse, "math": math}
+    load("operator/_local_operator/compile_helpers.py",
+         ["pack_internals", "_append_matrix", "_append_matrix_sparse",
+          "_number_to_state", "max_nonzero_per_row"], ns)
+    load("operator/_local_operator/numba.py", ["_get_conn_flattened_kernel"], ns,
+         class_name="LocalOperatorNumba")
+    load("sampler/rules/hamiltonian.py", ["_choose"], ns)
+    load("operator/_discrete_operator.py", ["_n_conn_from_sections"], ns,
+         class_name="DiscreteOperator")
+    rng = np.random.default_rng(777)
+    out = {}
+
+    def flattened(packed, x_ids):
+        sections = np.zeros(x_ids.shape[0], dtype=np.int64)
+        xp, mels = ns["_get_conn_flattened_kernel"](
+            x_ids, sections, packed["basis"], np.array(0.0), packed["diag_mels"],
+            packed["n_conns"], packed["mels"], packed["x_prime"], packed["acting_on"],
+            packed["acting_size"], packed["nonzero_diagonal"], False)
+        return xp, sections
+
+    def heis_terms(N, e, J):
+        sz = np.array([[1.0, 0.0], [0.0, -1.0]])
+        sx = np.array([[0.0, 1.0], [1.0, 0.0]])
+        sy = np.array([[0.0, -1j], [1j, 0.0]])
+        m = (np.kron(sz, sz) - np.kron(sx, sx) - np.real(np.kron(sy, sy))) * J
+        return {tuple(sorted((int(i), int(j)))): m.real for i, j in e}
+
+    cases = {
+        "heis_chain10": (10, heis_terms(10, [(i, (i + 1) % 10) for i in range(10)], 1.0)),
+        "ising_local_chain5": (5, None),
+    }
+    for name, (N, d) in cases.items():
+        if d is None:
+            e = edges["chain5"][:, :2]
+            d = {(i,): -0.7 * oop.SIGMAX for i in range(5)}
+            for i, j in e:
+                d[(int(i), int(j))] = 1.3 * np.kron(oop.SIGMAZ, oop.SIGMAZ)
+        packed = ns["pack_internals"](FakeHilbert(N), d, np.float64(0.0), np.float64, 1e-10)
+        n = 64
+        x_ids = rng.integers(0, 2, size=(n, N)).astype(np.int8)
+        u = rng.random(n)
+        vp, sections = flattened(packed, x_ids)
+        prop = np.empty_like(x_ids)
+        corr = np.zeros(n)
+        ns["_choose"](vp, sections, u, prop, corr)
+        _, sec2 = flattened(packed, prop)
+        corr = corr - np.log(ns["_n_conn_from_sections"](sec2.copy()))
+        out[name + "__x_ids"] = x_ids
+        out[name + "__u"] = u
+        out[name + "__proposed_ids"] = prop
+        out[name + "__corr"] = corr
+        out[name + "__aon"] = np.array([list(a) + [-1] * (2 - len(a)) for a in d])
+        out[name + "__ops"] = np.array([np.pad(m, ((0, 4 - m.shape[0]), (0, 4 - m.shape[1])))
+                                        for m in d.values()])
+        out[name + "__sizes"] = np.array([len(a) for a in d])
+        out[name + "__N"] = np.array(N)
+    # IsingJax n_conn on +-1 states: h = 0.7, J = 1.3 and J = 0 (diagonal never counted)
+    class StaticZero:
+        pass
+    ins = {"jnp": np, "jax": types.SimpleNamespace(jit=lambda f: f), "StaticZero": StaticZero}
+    load("operator/_ising/jax.py", ["_ising_n_conn_jax"], ins)
+    # open 7-site chain: 6 bonds, so J * sum(+-1) is zero for 3 domain walls
+    e = np.array([(i, i + 1) for i in range(6)])
+    x = rng.integers(0, 2, size=(200, 7)).astype(np.int8)
+    out["ising_nconn__x_ids"] = x
+    out["ising_nconn__edges"] = e
+    out["ising_nconn__n"] = ins["_ising_n_conn_jax"](x, e, 0.7, 1.3)
+    np.savez_compressed(os.path.join(HERE, "hamiltonian_rule.npz"), **out)
 
 
 # ---------------------------------------------------------------- log_cosh
@@ -482,6 +563,8 @@ if __name__ == "__main__":
     gen_localop(edges)
     gen_logcosh()
     gen_stats()
+    gen_online_stats()
+    gen_hamiltonian_rule(edges)
     gen_ngd()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

@@ -122,3 +122,120 @@ def test_local_sampler_fp32_matches_fp64_marginals(nk):
         s = s.reshape(-1, N).to(torch.float64)
         corr.append((s[:, :-1] * s[:, 1:]).mean(0).cpu().numpy())
     assert np.all(np.abs(corr[0] - corr[1]) < 0.03)
+
+
+# ------------------------------------------------------------------ Hamiltonian rule
+def _plaquette_op(nk, hi, N):
+    """ZZ bonds, 4-site XXXX and 3-site XZX terms and single-site X terms:
+    proposals change 1 to 4 sites at once."""
+    sx = np.array([[0.0, 1.0], [1.0, 0.0]])
+    sz = np.array([[1.0, 0.0], [0.0, -1.0]])
+    ops, aon = [], []
+    for i in range(N):
+        ops.append(0.8 * np.kron(sz, sz))
+        aon.append([i, (i + 1) % N])
+    for i in range(0, N, 2):
+        ops.append(-0.6 * np.kron(np.kron(sx, sx), np.kron(sx, sx)))
+        aon.append(sorted([i, (i + 1) % N, (i + 2) % N, (i + 3) % N]))
+    ops.append(-0.4 * np.kron(np.kron(sx, sz), sx))
+    aon.append([0, 1, 2])
+    for i in range(N):  # single flips make the chain ergodic on all 2^N states
+        ops.append(-0.5 * sx)
+        aon.append([i])
+    return nk.operator.LocalOperator(hi, ops, aon)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("std,independent", [(0.1, False), (0.5, True)])
+def test_hamiltonian_rule_heisenberg_distribution(nk, dtype, std, independent):
+    """Heisenberg (diagonal slot always counted): stays in the Sz = 0 sector and
+    samples |psi|^2 there."""
+    N = 8
+    model = _model(nk, std)
+    flat = model.init_flat(9, N)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    H = nk.operator.Heisenberg(hi, nk.graph.Chain(N))
+    make = lambda nc: nk.sampler.MetropolisHamiltonian(hi, H, n_chains=nc)
+    assert make(1).rule.diag_rule == 1
+    assert _chi2_pvalues(nk, make, model, flat, N, 0, dtype, independent=independent) > 0.01
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_hamiltonian_rule_ising_distribution(nk, dtype):
+    """Ising on an open chain (diagonal slot only where J sum s_i s_j != 0)."""
+    N = 7
+    model = _model(nk, 0.5)
+    flat = model.init_flat(10, N)
+    hi = nk.hilbert.Spin(0.5, N)
+    H = nk.operator.Ising(hi, nk.graph.Chain(N, pbc=False), h=0.9, J=1.1)
+    make = lambda nc: nk.sampler.MetropolisHamiltonian(hi, H, n_chains=nc)
+    assert make(1).rule.diag_rule == 2
+    assert _chi2_pvalues(nk, make, model, flat, N, None, dtype, independent=True) > 0.01
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_hamiltonian_rule_multisite_distribution(nk, dtype):
+    """4-site and 3-site off-diagonal terms.  Parameters N(0, 0.25^2) from a
+    fixed numpy seed: every one of the 256 states expects >= 0.2 of the 10,240
+    samples and none more than 620 (with std 0.5 one state holds 81 % of |psi|^2
+    and no sampler, the oracle's included, equilibrates between the modes in 30
+    sweeps)."""
+    N = 8
+    model = _model(nk, 0.5)
+    M = model.n_hidden(N)
+    flat = torch.as_tensor(np.random.default_rng(11).normal(0, 0.25, M + N * M + N),
+                           device="cuda")
+    hi = nk.hilbert.Spin(0.5, N)
+    H = _plaquette_op(nk, hi, N)
+    make = lambda nc: nk.sampler.MetropolisHamiltonian(hi, H, n_chains=nc)
+    assert _chi2_pvalues(nk, make, model, flat, N, None, dtype, independent=True) > 0.01
+
+
+def test_hamiltonian_rule_matches_oracle_acceptance(nk):
+    """Mean acceptance per proposal agrees with the oracle's numba-form rule
+    run on the same initial states (both are exact Metropolis chains, so their
+    stationary acceptance rates agree within sampling error)."""
+    from gpu_common import oracle_local
+    from oracle import sampler as osamp
+    N = 8
+    model = _model(nk, 0.4)
+    flat = model.init_flat(12, N)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    H = nk.operator.Heisenberg(hi, nk.graph.Chain(N, max_neighbor_order=2), J=[1.0, 0.5])
+    sampler = nk.sampler.MetropolisHamiltonian(hi, H, n_chains=2048)
+    st = sampler.init_state(model, flat, seed=4)
+    _, st = sampler.sample(model, flat, state=st, chain_length=1, n_discard=20)
+    st = sampler.reset(model, flat, st)
+    x0 = st.σ.clone()
+    _, st = sampler.sample(model, flat, state=st, chain_length=5)
+    acc_gpu = st.acceptance
+    rng = np.random.default_rng(0)
+    p = oracle_params(flat, N, model.n_hidden(N))
+    _, _, _, nacc = osamp.sample_chain(p, x0[:512].cpu().numpy(), rng, 5, rule="hamiltonian",
+                                       operator=oracle_local(H), diag_rule=1)
+    acc_or = nacc.sum() / (512 * 5 * N)
+    sd = np.sqrt(acc_or * (1 - acc_or) / (512 * 5 * N)) * 4  # correlated proposals: x4
+    assert abs(acc_gpu - acc_or) < max(4 * sd, 0.01), (acc_gpu, acc_or)
+
+
+def test_hamiltonian_rule_bookkeeping(nk):
+    N = 16
+    model = nk.models.RBM(alpha=2)
+    flat = model.init_flat(3, N)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    H = nk.operator.Heisenberg(hi, nk.graph.Chain(N))
+    sampler = nk.sampler.MetropolisHamiltonian(hi, H, n_chains=256)
+    s1 = sampler.init_state(model, flat, seed=5)
+    a, s1 = sampler.sample(model, flat, state=s1, chain_length=6, n_discard=4)
+    s2 = sampler.init_state(model, flat, seed=5)
+    b, s2 = sampler.sample(model, flat, state=s2, chain_length=6, n_discard=4)
+    assert torch.equal(a, b)
+    assert torch.all(a.to(torch.int32).sum(-1) == 0), "Sz must be conserved"
+    assert torch.equal(a[:, -1], s1.σ)
+    torch.testing.assert_close(s1.log_prob, 2 * model.apply(flat, s1.σ), rtol=1e-12, atol=1e-12)
+    assert int(sampler.rule.status.item()) == 0
+    assert 0.05 < s1.acceptance <= 1.0
+    with pytest.raises(ValueError, match="hilbert"):
+        nk.sampler.MetropolisHamiltonian(nk.hilbert.Spin(0.5, N), H, n_chains=4)
+    with pytest.raises(TypeError):
+        nk.sampler.MetropolisHamiltonian(hi, "not an operator")

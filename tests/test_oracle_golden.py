@@ -220,3 +220,33 @@ def test_online_stats_oracle(golden, name):
         assert a is None
     else:
         np.testing.assert_allclose(a, ga, rtol=0, atol=acf_tolerance(g, name))
+
+
+@pytest.mark.parametrize("name", ["heis_chain10", "ising_local_chain5"])
+def test_hamiltonian_rule_proposal(golden, name):
+    """Oracle Hamiltonian-rule proposal vs the reference's numba transition
+    (get_conn_flattened, _choose, n_conn) on the same states and uniforms."""
+    from oracle import hilbert as oh_
+    from oracle import sampler as osamp
+    g = golden("hamiltonian_rule")
+    N = int(g[name + "__N"])
+    ops = [m[:2 ** s, :2 ** s] for m, s in zip(g[name + "__ops"], g[name + "__sizes"])]
+    aon = [list(a[:s]) for a, s in zip(g[name + "__aon"], g[name + "__sizes"])]
+    op = oop.LocalOperator(N, ops, aon)
+    x = oh_.local_indices_to_states(g[name + "__x_ids"])
+    prop, corr = osamp.hamiltonian_propose(op, x, g[name + "__u"], diag_rule=1)
+    np.testing.assert_array_equal(prop, oh_.local_indices_to_states(g[name + "__proposed_ids"]))
+    np.testing.assert_allclose(corr, g[name + "__corr"], rtol=0, atol=1e-15)
+
+
+def test_hamiltonian_rule_ising_count(golden):
+    """diag_rule 2 on Ising's LocalOperator tables counts IsingJax's n_conn:
+    N flips plus the diagonal only where J * sum(+-1) != 0."""
+    from oracle import hilbert as oh_
+    from oracle import sampler as osamp
+    g = golden("hamiltonian_rule")
+    x = oh_.local_indices_to_states(g["ising_nconn__x_ids"])
+    op = oop.ising_as_local_operator(7, g["ising_nconn__edges"], 0.7, 1.3)
+    n = [len(r) for r in osamp.hamiltonian_row(op, x, diag_rule=2)]
+    np.testing.assert_array_equal(n, g["ising_nconn__n"])
+    assert set(g["ising_nconn__n"]) == {7, 8}
