@@ -106,6 +106,38 @@ typedef struct {
   const int8_t *x_prime;    /* [T][R][C][S] new spin values (+1/-1) */
 } vmck_local_op;
 
+/* ---------------------------------------------------------------- f3b
+ * PauliStrings on spin-1/2 states (netket/operator/_pauli_strings/jax.py), as
+ * bitmasks.  Slot f (one per distinct flip set, in PauliStringsJax's order:
+ * by the number of strings sharing the flip set, then first appearance) maps x
+ * to x with the sites of flip_mask[f] flipped, with
+ *   mel_f(x) = sum_{s = string_offset[f]}^{string_offset[f+1]-1}
+ *              weight[s] * (-1)^popcount(z_mask[s] & down(x)),
+ * down(x) bit i set where x_i = -1.  A string's weight already carries the
+ * (-i)^(#Y) factor; only real weights are supported (an even number of Y per
+ * string).  z_mask holds the sites a string reads with Z or Y.  Words are
+ * 32-bit, bit i of word w is site 32 w + i.  All pointers are device pointers. */
+typedef struct {
+  int32_t n_sites;               /* N */
+  int32_t n_words;               /* W = (N + 31) / 32 */
+  int32_t n_flips;               /* F: slots (max_conn_size) */
+  int32_t n_strings;             /* strings after dropping |weight| <= cutoff */
+  double cutoff;                 /* drop a slot where |mel| <= cutoff */
+  const uint32_t *flip_mask;     /* [F][W] */
+  const int32_t *flip_offset;    /* [F+1] CSR into flip_site */
+  const int32_t *flip_site;      /* flipped sites of each slot, ascending */
+  const int32_t *string_offset;  /* [F+1] CSR into z_mask / weight */
+  const uint32_t *z_mask;        /* [n_strings][W] */
+  const double *weight;          /* [n_strings] */
+} vmck_pauli_strings;
+
+/* PauliStringsJax.get_conn_padded (jax.py:240-269, 342-355): xp (n, F, N),
+ * mels (n, F) with dropped slots holding (x, 0.0); n_conn (nullable, int32
+ * (n,)) = the number of nonzero slots (PauliStringsJax.n_conn, jax.py:256-269,
+ * 331-340). */
+int vmck_get_conn_pauli(vmck_stream s, const vmck_pauli_strings *op, const int8_t *x,
+                        int64_t n, int8_t *xp, double *mels, int32_t *n_conn);
+
 /* LocalOperatorJax.get_conn_padded (netket/operator/_local_operator/jax.py:
  * 74-201, 256-288): candidates [diagonal] + per term, per stored column; those
  * with |mel| > mel_cutoff are compacted to the front; the rest of the K slots
@@ -141,6 +173,12 @@ int vmck_rbm_eloc_ising(vmck_stream s, int32_t dtype, const void *params, int32_
                         void *logpsi_out);
 int vmck_rbm_eloc_local(vmck_stream s, int32_t dtype, const void *params, int32_t N,
                         int32_t M, const int8_t *x, int64_t n, const vmck_local_op *op,
+                        double *eloc, void *logpsi_out);
+/* The same for PauliStrings: slot f's log-ratio flips the sites of
+ * flip_site[flip_offset[f] : flip_offset[f+1]]; slots with an empty flip set
+ * add their mel directly. */
+int vmck_rbm_eloc_pauli(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                        int32_t M, const int8_t *x, int64_t n, const vmck_pauli_strings *op,
                         double *eloc, void *logpsi_out);
 
 /* ---------------------------------------------------------------- a2 - a4

@@ -34,6 +34,14 @@ class LocalOpStruct(ctypes.Structure):
     ]
 
 
+class PauliStringsStruct(ctypes.Structure):
+    """Mirror of ``vmck_pauli_strings``."""
+    _fields_ = [("n_sites", c_i32), ("n_words", c_i32), ("n_flips", c_i32), ("n_strings", c_i32),
+                ("cutoff", c_dbl), ("flip_mask", c_vp), ("flip_offset", c_vp),
+                ("flip_site", c_vp), ("string_offset", c_vp), ("z_mask", c_vp),
+                ("weight", c_vp)]
+
+
 class BatchChainsStruct(ctypes.Structure):
     """Mirror of ``vmck_batch_chains``."""
     _fields_ = [("params", c_vp), ("sigma", c_vp), ("log_prob", c_vp), ("n_accepted", c_vp),
@@ -65,6 +73,10 @@ _SIGNATURES = {
                              c_vp, c_vp], c_i32),
     "vmck_get_conn_local": ([c_vp, ctypes.POINTER(LocalOpStruct), c_vp, c_i64, c_vp, c_vp, c_vp],
                             c_i32),
+    "vmck_get_conn_pauli": ([c_vp, ctypes.POINTER(PauliStringsStruct), c_vp, c_i64, c_vp, c_vp,
+                             c_vp], c_i32),
+    "vmck_rbm_eloc_pauli": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64,
+                             ctypes.POINTER(PauliStringsStruct), c_vp, c_vp], c_i32),
     "vmck_rbm_logpsi": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp], c_i32),
     "vmck_eloc_from_logpsi": ([c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp], c_i32),
     "vmck_rbm_eloc_ising": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64, c_vp, c_i32, c_dbl,

@@ -8,6 +8,7 @@
 
 #include "common.cuh"
 #include "localop.cuh"
+#include "pauli.cuh"
 
 namespace vmck {
 
@@ -363,6 +364,65 @@ __global__ void __launch_bounds__(EL_THREADS) eloc_local_kernel(
     eloc_local_sample(P, x, b, op, eloc, logpsi_out, sh, th, lc, red, redd, g);
 }
 
+// Local energy for PauliStrings, one CTA per sample (grid-stride): theta and
+// log_cosh(theta) in shared memory, the down-spin bitmask, then warps take
+// slots round-robin.  Lanes split the slot's strings for its matrix element
+// (a warp tree sum) and the hidden units for the log-ratio of flipping the
+// slot's sites F: sum_j [log_cosh(theta_j - 2 sum_{i in F} x_i W_ij) -
+// log_cosh(theta_j)] - 2 sum_{i in F} x_i a_i.
+template <typename T>
+__global__ void __launch_bounds__(EL_THREADS) eloc_pauli_kernel(
+    RbmParams<T> P, const int8_t *__restrict__ x, int64_t n, vmck_pauli_strings op,
+    double *eloc, T *logpsi_out) {
+  extern __shared__ unsigned char smem_raw[];
+  const int N = P.N, M = P.M;
+  T *th = reinterpret_cast<T *>(smem_raw);
+  T *lc = th + M;
+  uint32_t *down = reinterpret_cast<uint32_t *>(lc + M);
+  int8_t *xs = reinterpret_cast<int8_t *>(down + op.n_words);
+  __shared__ T red[32];
+  __shared__ double redd[32];
+  const Grp g = cta_grp();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int64_t b = blockIdx.x; b < n; b += gridDim.x) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) xs[i] = x[b * N + i];
+    __syncthreads();
+    pauli_down_mask(xs, N, op.n_words, down, threadIdx.x, blockDim.x);
+    theta_and_logpsi(P, xs, th, lc, red, logpsi_out ? logpsi_out + b : nullptr, g);
+    double acc = 0.0;
+    for (int f = warp; f < op.n_flips; f += nw) {
+      double m = 0.0;
+      for (int s = op.string_offset[f] + lane; s < op.string_offset[f + 1]; s += 32)
+        m += op.weight[s] * pauli_sign(op, s, down);
+      m = warp_sum(m);
+      if (!(fabs(m) > op.cutoff)) continue;
+      const int q0 = op.flip_offset[f], q1 = op.flip_offset[f + 1];
+      if (q0 == q1) {
+        if (lane == 0) acc += m;
+        continue;
+      }
+      T sl = 0;
+      for (int j = lane; j < M; j += 32) {
+        T t = th[j];
+        for (int q = q0; q < q1; ++q) {
+          const int i = op.flip_site[q];
+          t += (T)(-2 * xs[i]) * P.W[(int64_t)i * M + j];
+        }
+        sl += log_cosh_fast(t) - lc[j];
+      }
+      sl = warp_sum(sl);
+      for (int q = q0; q < q1; ++q) {
+        const int i = op.flip_site[q];
+        sl += (T)(-2 * xs[i]) * P.a[i];
+      }
+      if (lane == 0) acc += m * exp_ratio(sl);
+    }
+    const double e = grp_sum(g, acc, redd);
+    if (threadIdx.x == 0) eloc[b] = e;
+    __syncthreads();
+  }
+}
+
 // ============================================================ O v
 // One warp per sample: lanes take hidden units j, u_j = v_bias[j] + x_s . V[:, j]
 // (FP64, V read through L1), then t_s . u + x_s . v_visible, a shuffle tree.
@@ -541,9 +601,40 @@ int launch_eloc_local(cudaStream_t st, const void *params, int N, int M, const i
   return check_launch("rbm_eloc_local");
 }
 
+template <typename T>
+int launch_eloc_pauli(cudaStream_t st, const void *params, int N, int M, const int8_t *x,
+                      int64_t n, const vmck_pauli_strings &op, double *eloc, void *lp) {
+  RbmParams<T> P = rbm_view<T>(params, N, M);
+  const size_t smem = 2 * sizeof(T) * (size_t)M + 4 * (size_t)op.n_words + N + 16;
+  VMCK_REQUIRE(smem <= 200 * 1024, "M too large for the fused local-energy kernel");
+  if (smem > 48 * 1024)
+    VMCK_CUDA(cudaFuncSetAttribute(eloc_pauli_kernel<T>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int64_t grid = std::min<int64_t>(n, (int64_t)num_sms() * 32);
+  eloc_pauli_kernel<T><<<(unsigned)grid, EL_THREADS, smem, st>>>(P, x, n, op, eloc,
+                                                                 static_cast<T *>(lp));
+  return check_launch("rbm_eloc_pauli");
+}
+
 }  // namespace vmck
 
 using namespace vmck;
+
+extern "C" int vmck_rbm_eloc_pauli(vmck_stream s, int32_t dtype, const void *params, int32_t N,
+                                   int32_t M, const int8_t *x, int64_t n,
+                                   const vmck_pauli_strings *op, double *eloc, void *logpsi_out) {
+  VMCK_REQUIRE(params && x && op && eloc && N > 0 && M > 0 && n >= 0, "rbm_eloc_pauli arguments");
+  int rc = validate_pauli(*op);
+  if (rc) return rc;
+  VMCK_REQUIRE(op->n_sites == N, "rbm_eloc_pauli: operator size differs from N");
+  if (n == 0) return VMCK_OK;
+  if (dtype == VMCK_F64)
+    return launch_eloc_pauli<double>(as_stream(s), params, N, M, x, n, *op, eloc, logpsi_out);
+  if (dtype == VMCK_F32)
+    return launch_eloc_pauli<float>(as_stream(s), params, N, M, x, n, *op, eloc, logpsi_out);
+  set_last_error("rbm_eloc_pauli: dtype %d unsupported", dtype);
+  return VMCK_ERR_UNSUPPORTED;
+}
 
 extern "C" int vmck_rbm_o_v(vmck_stream s, int32_t dtype, const void *tanh_theta,
                             const int8_t *x, int32_t N, int32_t M, int64_t n, const double *v,

@@ -33,10 +33,15 @@ def rbm_forward(params_c, x, N, M, want_theta=False, want_tanh=False):
 # ------------------------------------------------------------------ local energies
 def local_energies_fused(op, params_c, x, N, M):
     """E_loc (n,) FP64 via the fused log-ratio kernel (no connected states stored)."""
-    from .operator import Ising, LocalOperator
+    from .operator import Ising, LocalOperator, PauliStrings
     n = x.shape[0]
     e = torch.empty(n, dtype=torch.float64, device=x.device)
     dt = nat.dtype_code(params_c.dtype)
+    if isinstance(op, PauliStrings):
+        st = op.device_struct()
+        nat.check(nat.lib().vmck_rbm_eloc_pauli(nat.stream(), dt, nat.ptr(params_c), N, M,
+                                                nat.ptr(x), n, ctypes.byref(st), nat.ptr(e), None))
+        return e
     if isinstance(op, Ising):
         ed = op._edges_dev()
         nat.check(nat.lib().vmck_rbm_eloc_ising(nat.stream(), dt, nat.ptr(params_c), N, M,

@@ -1,5 +1,5 @@
 """Hamiltonians of the hot path: ``Ising``, ``LocalOperator``, ``Heisenberg``,
-``GraphOperator`` (``netket.operator`` for spin-1/2).
+``GraphOperator``, ``PauliStrings`` (``netket.operator`` for spin-1/2).
 
 ``get_conn_padded(x)`` follows NetKet's JAX operators (``IsingJax``,
 ``LocalOperatorJax``): for x (..., N) it returns x' (..., K, N) int8 and
@@ -315,6 +315,125 @@ class LocalOperator(DiscreteOperator):
     def __repr__(self):
         return (f"LocalOperator(dim={self.hilbert.size}, #acting_on={len(self._terms)} "
                 f"locations, constant={self.constant})")
+
+
+class PauliStrings(DiscreteOperator):
+    """Sum of weighted Pauli strings (``netket/operator/_pauli_strings``), e.g.
+    ``PauliStrings(hi, ["XXI", "ZZI"], [0.5, 1.0])``; character k of a string
+    acts on site k.  Strings that flip the same sites share one connected
+    element, ordered as PauliStringsJax orders them
+    (``_pauli_strings/jax.py:137-238``).  Real matrix elements only: every
+    string needs an even number of Y (a real weight times (-i)^#Y)."""
+
+    def __init__(self, hilbert, operators=None, weights=None, *, cutoff=1.0e-10, dtype=None):
+        super().__init__(hilbert)
+        if operators is None:
+            operators = []
+        if isinstance(operators, str):
+            operators = [operators]
+        operators = [str(o) for o in operators]
+        if weights is None:
+            weights = [1.0] * len(operators)
+        elif np.isscalar(weights):
+            weights = [weights] * len(operators)
+        weights = list(weights)
+        if len(weights) != len(operators):
+            raise ValueError("weights and operators must have the same length")
+        for o in operators:
+            if len(o) != hilbert.size or any(ch not in "XYZI" for ch in o):
+                raise ValueError(f"invalid Pauli string {o!r} for {hilbert.size} sites")
+        if any(np.iscomplexobj(np.asarray(w)) and np.imag(w) != 0 for w in weights):
+            raise TypeError("PauliStrings: complex weights are not supported on this path")
+        if any(o.count("Y") % 2 for o in operators):
+            raise TypeError("PauliStrings: a string with an odd number of Y has imaginary "
+                            "matrix elements, not supported on this path")
+        self.operators = operators
+        self.weights = [float(np.real(w)) for w in weights]
+        self.cutoff = float(cutoff)
+        self._tables = None
+        self._dev = {}
+
+    def _pack(self):
+        if self._tables is not None:
+            return self._tables
+        N = self.hilbert.size
+        W = (N + 31) // 32
+        acting = {}
+        for op, w in zip(self.operators, self.weights):
+            if abs(w) <= self.cutoff:
+                continue
+            flip = tuple(i for i, ch in enumerate(op) if ch in "XY")
+            wt = w * (-1.0) ** (op.count("Y") // 2)  # (-i)^#Y for an even #Y
+            z = [i for i, ch in enumerate(op) if ch in "ZY"]
+            acting.setdefault(flip, []).append((wt, z))
+        by_count = {}
+        for flip, rest in acting.items():
+            by_count.setdefault(len(rest), []).append((flip, rest))
+        slots = [item for k in sorted(by_count) for item in by_count[k]]
+
+        def mask(sites):
+            m = np.zeros(W, dtype=np.uint32)
+            for i in sites:
+                m[i // 32] |= np.uint32(1 << (i % 32))
+            return m
+
+        F = len(slots)
+        flip_mask = np.zeros((max(F, 1), W), dtype=np.uint32)
+        flip_offset, flip_site, string_offset, z_mask, weight = [0], [], [0], [], []
+        for f, (flip, rest) in enumerate(slots):
+            flip_mask[f] = mask(flip)
+            flip_site.extend(flip)
+            flip_offset.append(len(flip_site))
+            for wt, z in rest:
+                z_mask.append(mask(z))
+                weight.append(wt)
+            string_offset.append(len(weight))
+        self._tables = dict(
+            N=N, W=W, F=F, S=len(weight), flip_mask=flip_mask,
+            flip_offset=np.array(flip_offset, dtype=np.int32),
+            flip_site=np.array(flip_site + [0], dtype=np.int32),
+            string_offset=np.array(string_offset, dtype=np.int32),
+            z_mask=np.array(z_mask, dtype=np.uint32).reshape(-1, W) if z_mask else
+            np.zeros((1, W), dtype=np.uint32),
+            weight=np.array(weight + [0.0], dtype=np.float64))
+        return self._tables
+
+    @property
+    def max_conn_size(self):
+        return self._pack()["F"]
+
+    def device_struct(self):
+        d = torch.cuda.current_device()
+        if d not in self._dev:
+            tb = self._pack()
+            dev = nat.device()
+            keep = {}
+            for k in ("flip_mask", "z_mask"):
+                keep[k] = torch.as_tensor(tb[k].view(np.int32), device=dev).contiguous()
+            for k in ("flip_offset", "flip_site", "string_offset", "weight"):
+                keep[k] = torch.as_tensor(tb[k], device=dev).contiguous()
+            st = nat.PauliStringsStruct(
+                n_sites=tb["N"], n_words=tb["W"], n_flips=tb["F"], n_strings=tb["S"],
+                cutoff=self.cutoff, flip_mask=keep["flip_mask"].data_ptr(),
+                flip_offset=keep["flip_offset"].data_ptr(), flip_site=keep["flip_site"].data_ptr(),
+                string_offset=keep["string_offset"].data_ptr(), z_mask=keep["z_mask"].data_ptr(),
+                weight=keep["weight"].data_ptr())
+            self._dev[d] = (st, keep)
+        return self._dev[d][0]
+
+    def _conn(self, x):
+        n, N = x.shape
+        st = self.device_struct()
+        F = st.n_flips
+        xp = torch.empty((n, F, N), dtype=torch.int8, device=x.device)
+        mels = torch.empty((n, F), dtype=torch.float64, device=x.device)
+        nc = torch.empty((n,), dtype=torch.int32, device=x.device)
+        nat.check(nat.lib().vmck_get_conn_pauli(nat.stream(), ctypes.byref(st), nat.ptr(x), n,
+                                                nat.ptr(xp), nat.ptr(mels), nat.ptr(nc)))
+        return xp, mels, nc
+
+    def __repr__(self):
+        return f"PauliStrings(hilbert={self.hilbert}, n_strings={len(self.operators)})"
 
 
 def GraphOperator(hilbert, graph, site_ops=(), bond_ops=(), bond_ops_colors=()):

@@ -323,3 +323,53 @@ def to_sparse_from_conn(get_conn, states):
                 cols.append(j)
                 vals.append(mels[i, k])
     return sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+
+
+# ---------------------------------------------------------------- PauliStrings
+def pauli_pack(operators, weights, cutoff=0.0):
+    """Flip sets of a list of Pauli strings (``netket/operator/_pauli_strings/
+    jax.py:50-105`` grouping, ``137-238`` ordering).
+
+    Each string flips the sites holding X or Y and reads the sign of the sites
+    holding Z or Y; a Y contributes a factor -i, absorbed into the weight.
+    Strings with the same flip set form one connected element.  Elements are
+    ordered by how many strings share them (ascending), then by first
+    appearance.  Returns a list of (flip_sites tuple, [(weight, z_sites)])."""
+    acting = {}
+    for op, w in zip(operators, weights):
+        if abs(w) <= cutoff:
+            continue
+        flip = tuple(sorted(i for i, ch in enumerate(op) if ch in "XY"))
+        ny = sum(ch == "Y" for ch in op)
+        wt = complex(w) * (-1j) ** ny
+        if wt.imag == 0:
+            wt = wt.real
+        z = sorted(i for i, ch in enumerate(op) if ch in "ZY")
+        acting.setdefault(flip, []).append((wt, z))
+    by_count = {}
+    for flip, rest in acting.items():
+        by_count.setdefault(len(rest), []).append((flip, rest))
+    return [item for k in sorted(by_count) for item in by_count[k]]
+
+
+def pauli_get_conn_padded(x, operators, weights, cutoff=1e-10):
+    """PauliStringsJax.get_conn_padded on +-1 states: one slot per flip set,
+    mel = sum_s w_s prod_{z in s} (-1)^[x_z = -1]; slots with |mel| <= cutoff
+    hold (x, 0) (``jax.py:240-269``).  Also returns n_conn (nonzero slots)."""
+    groups = pauli_pack(operators, weights)
+    x = np.asarray(x, dtype=np.int8)
+    n, N = x.shape
+    F = len(groups)
+    xp = np.repeat(x[:, None, :], F, axis=1)
+    mels = np.zeros((n, F))
+    for f, (flip, rest) in enumerate(groups):
+        m = np.zeros(n)
+        for w, z in rest:
+            sgn = np.prod(np.where(x[:, z] < 0, -1.0, 1.0), axis=1) if z else np.ones(n)
+            m = m + w * sgn
+        keep = np.abs(m) > cutoff
+        mels[:, f] = np.where(keep, m, 0.0)
+        if flip:
+            sub = xp[:, f]
+            sub[np.ix_(keep, list(flip))] = -sub[np.ix_(keep, list(flip))]
+    return xp, mels, (np.abs(mels) > 0).sum(axis=1)

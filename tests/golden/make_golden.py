@@ -307,6 +307,85 @@ def gen_hamiltonian_rule(edges):
     np.savez_compressed(os.path.join(HERE, "hamiltonian_rule.npz"), **out)
 
 
+# ---------------------------------------------------------------- PauliStrings
+class _DropKeyword(ast.NodeTransformer):
+    """Remove a keyword argument numpy does not take (``promote_integers``)."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def visit_Call(self, node):
+        self.generic_visit(node)
+        node.keywords = [k for k in node.keywords if k.arg != self.name]
+        return node
+
+
+def gen_pauli_strings():
+    """PauliStringsJax.get_conn_padded / n_conn (operator/_pauli_strings/jax.py:
+    50-355) in its default "index" mode, on spin states."""
+    import functools
+    path = os.path.join(NK, "operator/_pauli_strings/jax.py")
+    tree = ast.parse(open(path).read(), filename=path)
+    names = ["_ising_conn_states_jax", "pack_internals", "sites_to_mask", "_check_mode",
+             "pack_internals_jax", "_pauli_strings_mels_jax", "_pauli_strings_kernel_jax",
+             "_pauli_strings_n_conn_jax"]
+    nodes = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in names]
+    assert {n.name for n in nodes} == set(names)
+    for n in nodes:
+        n.decorator_list = []
+    mod = _DropKeyword("promote_integers").visit(ast.Module(body=nodes, type_ignores=[]))
+    ast.fix_missing_locations(mod)
+    jnp = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("_")})
+    jnp.bool_ = np.bool_
+    jax = types.SimpleNamespace(lax=types.SimpleNamespace(select=np.where), jit=lambda f: f)
+    ns = {"np": np, "jnp": jnp, "jax": jax, "partial": functools.partial,
+          "_available_modes": ["index", "mask"]}
+    exec(compile(mod, path, "exec"), ns)
+
+    rng = np.random.default_rng(31)
+    out = {}
+    N = 10
+    ring = [(i, (i + 1) % N) for i in range(N)]
+
+    def pstr(ch):
+        s = ["I"] * N
+        for site, c in ch:
+            s[site] = c
+        return "".join(s)
+
+    cases = {
+        # TFIM written as strings: the ZZ strings share the empty flip set
+        "tfim": ([pstr([(i, "X")]) for i in range(N)] +
+                 [pstr([(i, "Z"), (j, "Z")]) for i, j in ring],
+                 [-0.8] * N + [1.1] * N),
+        # XX + YY + ZZ Heisenberg bonds: XX and YY share a flip set, so its
+        # element is zero on aligned pairs (dropped by the cutoff)
+        "heisenberg_xyz": ([pstr([(i, c), (j, c)]) for i, j in ring for c in "XYZ"],
+                           [0.5, 0.5, 1.0] * N),
+        # mixed strings: Y pairs, Z checks on flipped sites, long strings, a
+        # repeated flip set with different weights, identity
+        "mixed": (["XYIIIIIIYZ", "ZZZZZIIIII", "IIXXXXIIII", "YIYIIIIIIX", "XXXXXXXXXX",
+                   "IIXXXXIIII", "IIIIIIIIII", "ZIIIIIIIIZ", "IXZYYZXIII", "YYYYIIIIII"],
+                  [0.3, -1.25, 0.75, 0.5, -0.1, 0.25, 2.0, -0.6, 0.4, 1.5]),
+    }
+    for name, (ops, w) in cases.items():
+        ops_a = np.array(ops)
+        w_a = np.array(w, dtype=np.float64)
+        flips, z_data = ns["pack_internals_jax"](ops_a, w_a, weight_dtype=np.float64,
+                                                 mode="index")
+        x_ids = rng.integers(0, 2, size=(40, N)).astype(np.int8)
+        xp_ids, mels, _ = ns["_pauli_strings_kernel_jax"](flips, z_data, x_ids, cutoff=1e-10)
+        nconn = ns["_pauli_strings_n_conn_jax"](flips, z_data, x_ids, cutoff=1e-10)
+        out[name + "__ops"] = ops_a
+        out[name + "__weights"] = w_a
+        out[name + "__x_ids"] = x_ids
+        out[name + "__xp_ids"] = np.asarray(xp_ids, dtype=np.int8)
+        out[name + "__mels"] = np.real(np.asarray(mels)).astype(np.float64)
+        out[name + "__n_conn"] = np.asarray(nconn)
+        out[name + "__flips"] = np.asarray(flips, dtype=np.int8)
+    np.savez_compressed(os.path.join(HERE, "pauli_strings.npz"), **out)
+
+
 # ---------------------------------------------------------------- log_cosh
 def gen_logcosh():
     ns = {"jnp": np}

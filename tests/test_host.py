@@ -248,3 +248,34 @@ def test_online_stats_batch_delta_method():
     vec = OnlineStatsBatch(ests, lambda mu: torch.stack([mu[0], mu[0] * mu[1]])).get_stats()
     assert tuple(vec.mean.shape) == (2,) and tuple(vec.error_of_mean.shape) == (2,)
     np.testing.assert_allclose(float(vec.error_of_mean[0]), np.sqrt(cov[0, 0]), rtol=1e-10)
+
+
+def test_pauli_strings_pack_matches_oracle(golden):
+    """Host packer of PauliStrings: slot order, flip sites, string weights with
+    the (-i)^#Y factor and Z-check sites equal the oracle's grouping (which is
+    pinned to the reference's pack_internals_jax)."""
+    from oracle import operator as oop_
+    import netket_gb300 as nk
+    g = golden("pauli_strings")
+    for name in ("tfim", "heisenberg_xyz", "mixed"):
+        ops, w = list(g[name + "__ops"]), g[name + "__weights"]
+        N = len(ops[0])
+        tb = nk.operator.PauliStrings(nk.hilbert.Spin(0.5, N), ops, w)._pack()
+        ref = oop_.pauli_pack(ops, w)
+        assert tb["F"] == len(ref)
+        for f, (flip, rest) in enumerate(ref):
+            sites = tb["flip_site"][tb["flip_offset"][f]:tb["flip_offset"][f + 1]]
+            assert tuple(sites) == flip
+            bits = [i for i in range(N) if (tb["flip_mask"][f, i // 32] >> (i % 32)) & 1]
+            assert tuple(bits) == flip
+            s0, s1 = tb["string_offset"][f], tb["string_offset"][f + 1]
+            assert s1 - s0 == len(rest)
+            for k, (wt, z) in enumerate(rest):
+                assert tb["weight"][s0 + k] == wt
+                zs = [i for i in range(N) if (tb["z_mask"][s0 + k, i // 32] >> (i % 32)) & 1]
+                assert zs == z
+    hi = nk.hilbert.Spin(0.5, 3)
+    with pytest.raises(TypeError):
+        nk.operator.PauliStrings(hi, ["YII"], [1.0])
+    with pytest.raises(ValueError):
+        nk.operator.PauliStrings(hi, ["XQI"], [1.0])

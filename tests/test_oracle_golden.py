@@ -250,3 +250,16 @@ def test_hamiltonian_rule_ising_count(golden):
     n = [len(r) for r in osamp.hamiltonian_row(op, x, diag_rule=2)]
     np.testing.assert_array_equal(n, g["ising_nconn__n"])
     assert set(g["ising_nconn__n"]) == {7, 8}
+
+
+@pytest.mark.parametrize("name", ["tfim", "heisenberg_xyz", "mixed"])
+def test_pauli_strings_conn(golden, name):
+    """Oracle PauliStrings get_conn_padded / n_conn vs the reference's own
+    pack_internals_jax + _pauli_strings_kernel_jax (index mode)."""
+    from oracle import hilbert as oh_
+    g = golden("pauli_strings")
+    x = oh_.local_indices_to_states(g[name + "__x_ids"])
+    xp, mels, nc = oop.pauli_get_conn_padded(x, list(g[name + "__ops"]), g[name + "__weights"])
+    np.testing.assert_array_equal(xp, oh_.local_indices_to_states(g[name + "__xp_ids"]))
+    np.testing.assert_array_equal(mels, g[name + "__mels"])
+    np.testing.assert_array_equal(nc, g[name + "__n_conn"])
