@@ -220,6 +220,17 @@ int vmck_metropolis_hamiltonian(vmck_stream s, int32_t dtype, const void *params
                                 int8_t *samples, uint64_t seed, uint64_t counter,
                                 int32_t *status);
 
+/* The Hamiltonian rule for PauliStrings: n(x) = the number of slots with
+ * |mel| > cutoff (PauliStringsJax.n_conn, _pauli_strings/jax.py:256-269); a
+ * kept slot with an empty flip set proposes x itself.  Otherwise as
+ * vmck_metropolis_hamiltonian. */
+int vmck_metropolis_hamiltonian_pauli(vmck_stream s, int32_t dtype, const void *params,
+                                      int32_t N, int32_t M, const vmck_pauli_strings *op,
+                                      int8_t *sigma, double *log_prob, int64_t *n_accepted,
+                                      int32_t B, int32_t sweep_size, int32_t n_discard,
+                                      int32_t chain_length, int8_t *samples, uint64_t seed,
+                                      uint64_t counter, int32_t *status);
+
 /* ---------------------------------------------------------------- batched (C3)
  * Many independent problems of uneven size in one persistent launch.  Each
  * instance's chains run exactly as vmck_metropolis_sample would run them

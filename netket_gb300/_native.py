@@ -88,6 +88,10 @@ _SIGNATURES = {
     "vmck_metropolis_hamiltonian": ([c_vp, c_i32, c_vp, c_i32, c_i32, ctypes.POINTER(LocalOpStruct),
                                      c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_vp,
                                      c_u64, c_u64, c_vp], c_i32),
+    "vmck_metropolis_hamiltonian_pauli": ([c_vp, c_i32, c_vp, c_i32, c_i32,
+                                           ctypes.POINTER(PauliStringsStruct), c_vp, c_vp, c_vp,
+                                           c_i32, c_i32, c_i32, c_i32, c_vp, c_u64, c_u64, c_vp],
+                                          c_i32),
     "vmck_batched_metropolis_local": ([c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32,
                                        c_i32, c_i32, c_i32, c_i32], c_i32),
     "vmck_batched_eloc_ising": ([c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32, c_i32,

@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "localop.cuh"
+#include "pauli.cuh"
 
 namespace vmck {
 
@@ -72,6 +73,55 @@ __device__ int ham_count(const vmck_local_op &op, const int8_t *xs, uint8_t *cnt
   return tot + slot;
 }
 
+// theta = b + x W and log_cosh(theta) from scratch into th / lc (th, lc may be
+// null for the final log-amplitude only); returns logpsi(x).
+template <typename T>
+__device__ T chain_theta(const T *__restrict__ params, int N, int M, const int8_t *xs, T *th,
+                         T *lc) {
+  const int lane = threadIdx.x & 31;
+  const T *bvec = params, *W = params + M, *a = params + M + (int64_t)N * M;
+  T part = 0;
+  for (int j = lane; j < M; j += 32) {
+    T acc = bvec[j];
+    for (int i = 0; i < N; ++i) acc += (T)xs[i] * W[(int64_t)i * M + j];
+    const T l = log_cosh_fast(acc);
+    if (th) {
+      th[j] = acc;
+      lc[j] = l;
+    }
+    part += l;
+  }
+  for (int i = lane; i < N; i += 32) part += (T)xs[i] * a[i];
+  const T r = warp_sum(part);
+  __syncwarp();
+  return r;
+}
+
+// Index of the entry holding the k-th unit of the counts cnt[0..n) (warp scan
+// in chunks of 32); *kk = its offset inside that entry.  -1 if k >= sum(cnt).
+__device__ inline int warp_pick_kth(const uint8_t *cnt, int n, int k, int *kk) {
+  const int lane = threadIdx.x & 31;
+  for (int t0 = 0; t0 < n; t0 += 32) {
+    const int t = t0 + lane;
+    const int v = t < n ? cnt[t] : 0;
+    int inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    const int chunk = __shfl_sync(0xffffffffu, inc, 31);
+    if (k < chunk) {
+      const unsigned m = __ballot_sync(0xffffffffu, inc > k);
+      const int l = __ffs(m) - 1;
+      *kk = k - (__shfl_sync(0xffffffffu, inc, l) - __shfl_sync(0xffffffffu, v, l));
+      return t0 + l;
+    }
+    k -= chunk;
+  }
+  return -1;
+}
+
 template <typename T>
 __device__ void run_chain_ham(const T *__restrict__ params, int N, int M, const vmck_local_op &op,
                               int diag_rule, int8_t *sigma_row, double *log_prob_b,
@@ -79,7 +129,7 @@ __device__ void run_chain_ham(const T *__restrict__ params, int N, int M, const 
                               int8_t *samples_chain, uint32_t k0, uint32_t k1, uint64_t counter,
                               HamSmem<T> c, int *err) {
   const int lane = threadIdx.x & 31;
-  const T *bvec = params, *W = params + M, *a = params + M + (int64_t)N * M;
+  const T *W = params + M, *a = params + M + (int64_t)N * M;
   const int S = op.max_sites;
   for (int i = lane; i < N; i += 32) c.xs[i] = sigma_row[i];
   __syncwarp();
@@ -90,20 +140,7 @@ __device__ void run_chain_ham(const T *__restrict__ params, int N, int M, const 
   const int total = n_discard + L;
   for (int step = 0; step < total; ++step) {
     // theta, log_cosh(theta) recomputed exactly once per sweep
-    {
-      T part = 0;
-      for (int j = lane; j < M; j += 32) {
-        T acc = bvec[j];
-        for (int i = 0; i < N; ++i) acc += (T)c.xs[i] * W[(int64_t)i * M + j];
-        c.th[j] = acc;
-        T l = log_cosh_fast(acc);
-        c.lc[j] = l;
-        part += l;
-      }
-      for (int i = lane; i < N; i += 32) part += (T)c.xs[i] * a[i];
-      logpsi = warp_sum(part);
-      __syncwarp();
-    }
+    logpsi = chain_theta(params, N, M, c.xs, c.th, c.lc);
     for (int p = 0; p < sweep; ++p) {
       const uint64_t pidx = counter + (uint64_t)step * sweep + p;
       u32x4 r = philox4x32_10(u32x4{(uint32_t)pidx, (uint32_t)(pidx >> 32), (uint32_t)b, 0u}, k0, k1);
@@ -117,26 +154,8 @@ __device__ void run_chain_ham(const T *__restrict__ params, int N, int M, const 
         --k;
       }
       // term holding the k-th kept entry: warp scan over the counts
-      int t_sel = -1, kk = 0;
-      for (int t0 = 0; t0 < op.n_terms && t_sel < 0; t0 += 32) {
-        const int t = t0 + lane;
-        const int v = t < op.n_terms ? c.cnt_cur[t] : 0;
-        int inc = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, inc, o);
-          if (lane >= o) inc += y;
-        }
-        const int chunk = __shfl_sync(0xffffffffu, inc, 31);
-        if (k < chunk) {
-          const unsigned m = __ballot_sync(0xffffffffu, inc > k);
-          const int l = __ffs(m) - 1;
-          t_sel = t0 + l;
-          kk = k - (__shfl_sync(0xffffffffu, inc, l) - __shfl_sync(0xffffffffu, v, l));
-        } else {
-          k -= chunk;
-        }
-      }
+      int kk = 0;
+      const int t_sel = warp_pick_kth(c.cnt_cur, op.n_terms, k, &kk);
       if (t_sel < 0) {  // counts inconsistent with n_cur: flag it, never index out of range
         if (lane == 0) atomicOr(err, VMCK_DEV_INTERNAL);
         continue;
@@ -236,14 +255,7 @@ __device__ void run_chain_ham(const T *__restrict__ params, int N, int M, const 
     }
   }
   // final log-amplitude from scratch
-  T part = 0;
-  for (int j = lane; j < M; j += 32) {
-    T acc = bvec[j];
-    for (int i = 0; i < N; ++i) acc += (T)c.xs[i] * W[(int64_t)i * M + j];
-    part += log_cosh_fast(acc);
-  }
-  for (int i = lane; i < N; i += 32) part += (T)c.xs[i] * a[i];
-  logpsi = warp_sum(part);
+  logpsi = chain_theta<T>(params, N, M, c.xs, nullptr, nullptr);
   for (int i = lane; i < N; i += 32) sigma_row[i] = c.xs[i];
   if (lane == 0) {
     *log_prob_b = 2.0 * (double)logpsi;
@@ -303,9 +315,221 @@ static int launch_ham(cudaStream_t st, const void *params, int N, int M, const v
   return check_launch("metropolis_hamiltonian");
 }
 
+// ------------------------------------------------------------ PauliStrings
+// The same rule for PauliStrings (PauliStringsJax.n_conn = the number of slots
+// with |mel| > cutoff, _pauli_strings/jax.py:256-269, which is also the set the
+// jax rule draws from).  Per chain: the keep flag of every slot at x (keep_cur)
+// and the down-spin mask of x; a proposal takes the k-th kept slot, flips its
+// sites, recounts the slots at x' with down(x') = down(x) ^ flip_mask, and
+// forms the RBM log-ratio of the flipped sites.  A kept slot with an empty flip
+// set proposes x itself (always accepted).
+template <typename T>
+struct PauliChainSmem {
+  T *th, *lc, *tn, *ln;
+  int8_t *xs;
+  uint32_t *down, *down_new;
+  uint8_t *keep_cur, *keep_new;
+};
+
+__device__ int pauli_count(const vmck_pauli_strings &op, const uint32_t *down, uint8_t *keep) {
+  const int lane = threadIdx.x & 31;
+  int tot = 0;
+  for (int f = lane; f < op.n_flips; f += 32) {
+    const int k = fabs(pauli_mel(op, f, down)) > op.cutoff;
+    keep[f] = (uint8_t)k;
+    tot += k;
+  }
+  tot = warp_sum(tot);
+  __syncwarp();
+  return tot;
+}
+
+template <typename T>
+__device__ void run_chain_ham_pauli(const T *__restrict__ params, int N, int M,
+                                    const vmck_pauli_strings &op, int8_t *sigma_row,
+                                    double *log_prob_b, int64_t *n_accepted_b, int b, int sweep,
+                                    int n_discard, int L, int8_t *samples_chain, uint32_t k0,
+                                    uint32_t k1, uint64_t counter, PauliChainSmem<T> c,
+                                    int *err) {
+  const int lane = threadIdx.x & 31;
+  const T *W = params + M, *a = params + M + (int64_t)N * M;
+  const int Wd = op.n_words;
+  for (int i = lane; i < N; i += 32) c.xs[i] = sigma_row[i];
+  __syncwarp();
+  pauli_down_mask(c.xs, N, Wd, c.down, lane, 32);
+  __syncwarp();
+  int n_cur = pauli_count(op, c.down, c.keep_cur);
+  T logpsi = 0;
+  int64_t acc_count = 0;
+  const int total = n_discard + L;
+  for (int step = 0; step < total; ++step) {
+    logpsi = chain_theta(params, N, M, c.xs, c.th, c.lc);
+    for (int p = 0; p < sweep; ++p) {
+      const uint64_t pidx = counter + (uint64_t)step * sweep + p;
+      u32x4 r = philox4x32_10(u32x4{(uint32_t)pidx, (uint32_t)(pidx >> 32), (uint32_t)b, 0u}, k0, k1);
+      if (n_cur <= 0) continue;
+      int kk = 0;
+      const int f = warp_pick_kth(c.keep_cur, op.n_flips, (int)below(r.x, (uint32_t)n_cur), &kk);
+      if (f < 0) {
+        if (lane == 0) atomicOr(err, VMCK_DEV_INTERNAL);
+        continue;
+      }
+      const int q0 = op.flip_offset[f], q1 = op.flip_offset[f + 1];
+      if (q0 == q1) {  // x' = x
+        ++acc_count;
+        continue;
+      }
+      for (int w = lane; w < Wd; w += 32) c.down_new[w] = c.down[w] ^ op.flip_mask[(int64_t)f * Wd + w];
+      __syncwarp();
+      const int n_new = pauli_count(op, c.down_new, c.keep_new);
+      T s = 0;
+      for (int j = lane; j < M; j += 32) {
+        T t = c.th[j];
+        for (int q = q0; q < q1; ++q) {
+          const int i = op.flip_site[q];
+          t += (T)(-2 * c.xs[i]) * W[(int64_t)i * M + j];
+        }
+        const T l = log_cosh_fast(t);
+        c.tn[j] = t;
+        c.ln[j] = l;
+        s += l - c.lc[j];
+      }
+      s = warp_sum(s);
+      for (int q = q0; q < q1; ++q) {
+        const int i = op.flip_site[q];
+        s += (T)(-2 * c.xs[i]) * a[i];
+      }
+      const T corr = log((T)n_cur) - log((T)n_new);
+      bool accept;
+      if (sizeof(T) == 8) {
+        accept = u01d(r.y, r.z) < exp((double)(2 * s + corr));
+      } else {
+        accept = u01f(r.y) < expf((float)(2 * s + corr));
+      }
+      if (accept) {
+        for (int j = lane; j < M; j += 32) {
+          c.th[j] = c.tn[j];
+          c.lc[j] = c.ln[j];
+        }
+        __syncwarp();
+        for (int q = q0 + lane; q < q1; q += 32) {
+          const int i = op.flip_site[q];
+          c.xs[i] = (int8_t)(-c.xs[i]);
+        }
+        uint8_t *tk = c.keep_cur;
+        c.keep_cur = c.keep_new;
+        c.keep_new = tk;
+        uint32_t *td = c.down;
+        c.down = c.down_new;
+        c.down_new = td;
+        n_cur = n_new;
+        logpsi += s;
+        ++acc_count;
+      }
+      __syncwarp();
+    }
+    if (step >= n_discard) {
+      int8_t *dst = samples_chain + (int64_t)(step - n_discard) * N;
+      for (int i = lane; i < N; i += 32) dst[i] = c.xs[i];
+    }
+  }
+  logpsi = chain_theta<T>(params, N, M, c.xs, nullptr, nullptr);
+  for (int i = lane; i < N; i += 32) sigma_row[i] = c.xs[i];
+  if (lane == 0) {
+    *log_prob_b = 2.0 * (double)logpsi;
+    *n_accepted_b += acc_count;
+  }
+}
+
+__host__ __device__ inline size_t pauli_chain_bytes(int N, int M, int Wd, int F, size_t tsize) {
+  return ((4 * (size_t)M * tsize + 15) & ~size_t(15)) + ((N + 15) & ~15) +
+         2 * ((4 * (size_t)Wd + 15) & ~size_t(15)) + 2 * (((size_t)F + 15) & ~size_t(15));
+}
+
+template <typename T>
+__global__ void metropolis_hamiltonian_pauli_kernel(const T *__restrict__ params, int N, int M,
+                                                    vmck_pauli_strings op, int8_t *sigma,
+                                                    double *log_prob, int64_t *n_accepted, int B,
+                                                    int sweep, int n_discard, int L,
+                                                    int8_t *samples, uint32_t k0, uint32_t k1,
+                                                    uint64_t counter, int wpb, int *err) {
+  extern __shared__ unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5;
+  const int b = blockIdx.x * wpb + warp;
+  if (b >= B) return;
+  unsigned char *p =
+      smem_raw + warp * pauli_chain_bytes(N, M, op.n_words, op.n_flips, sizeof(T));
+  PauliChainSmem<T> c;
+  c.th = reinterpret_cast<T *>(p);
+  c.lc = c.th + M;
+  c.tn = c.lc + M;
+  c.ln = c.tn + M;
+  p += (4 * (size_t)M * sizeof(T) + 15) & ~size_t(15);
+  c.xs = reinterpret_cast<int8_t *>(p);
+  p += (N + 15) & ~15;
+  c.down = reinterpret_cast<uint32_t *>(p);
+  p += (4 * (size_t)op.n_words + 15) & ~size_t(15);
+  c.down_new = reinterpret_cast<uint32_t *>(p);
+  p += (4 * (size_t)op.n_words + 15) & ~size_t(15);
+  c.keep_cur = p;
+  c.keep_new = p + ((op.n_flips + 15) & ~15);
+  run_chain_ham_pauli<T>(params, N, M, op, sigma + (int64_t)b * N, log_prob + b, n_accepted + b,
+                         b, sweep, n_discard, L, samples + (int64_t)b * L * N, k0, k1, counter, c,
+                         err);
+}
+
+template <typename T>
+static int launch_ham_pauli(cudaStream_t st, const void *params, int N, int M,
+                            const vmck_pauli_strings &op, int8_t *sigma, double *log_prob,
+                            int64_t *n_acc, int B, int sweep, int n_discard, int L,
+                            int8_t *samples, uint64_t seed, uint64_t counter, int *err) {
+  const size_t per_warp = pauli_chain_bytes(N, M, op.n_words, op.n_flips, sizeof(T));
+  const size_t budget = 200 * 1024;
+  VMCK_REQUIRE(per_warp <= budget, "metropolis_hamiltonian_pauli: M or the slot count too large");
+  const int wpb = (int)std::min<size_t>(4, budget / per_warp);
+  const size_t smem = wpb * per_warp;
+  if (smem > 48 * 1024)
+    VMCK_CUDA(cudaFuncSetAttribute(metropolis_hamiltonian_pauli_kernel<T>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int grid = (B + wpb - 1) / wpb;
+  metropolis_hamiltonian_pauli_kernel<T><<<grid, 32 * wpb, smem, st>>>(
+      static_cast<const T *>(params), N, M, op, sigma, log_prob, n_acc, B, sweep, n_discard, L,
+      samples, (uint32_t)seed, (uint32_t)(seed >> 32), counter, wpb, err);
+  return check_launch("metropolis_hamiltonian_pauli");
+}
+
 }  // namespace vmck
 
 using namespace vmck;
+
+extern "C" int vmck_metropolis_hamiltonian_pauli(vmck_stream s, int32_t dtype, const void *params,
+                                                 int32_t N, int32_t M,
+                                                 const vmck_pauli_strings *op, int8_t *sigma,
+                                                 double *log_prob, int64_t *n_accepted, int32_t B,
+                                                 int32_t sweep_size, int32_t n_discard,
+                                                 int32_t chain_length, int8_t *samples,
+                                                 uint64_t seed, uint64_t counter,
+                                                 int32_t *status) {
+  VMCK_REQUIRE(params && op && sigma && log_prob && n_accepted && status && N > 0 && M > 0 &&
+                   B > 0,
+               "metropolis_hamiltonian_pauli arguments");
+  VMCK_REQUIRE(sweep_size >= 0 && n_discard >= 0 && chain_length >= 0, "metropolis lengths");
+  VMCK_REQUIRE(chain_length == 0 || samples, "samples buffer");
+  int rc = validate_pauli(*op);
+  if (rc) return rc;
+  VMCK_REQUIRE(op->n_sites == N, "metropolis_hamiltonian_pauli: operator size differs from N");
+  cudaStream_t st = as_stream(s);
+  if (dtype == VMCK_F64)
+    return launch_ham_pauli<double>(st, params, N, M, *op, sigma, log_prob, n_accepted, B,
+                                    sweep_size, n_discard, chain_length, samples, seed, counter,
+                                    status);
+  if (dtype == VMCK_F32)
+    return launch_ham_pauli<float>(st, params, N, M, *op, sigma, log_prob, n_accepted, B,
+                                   sweep_size, n_discard, chain_length, samples, seed, counter,
+                                   status);
+  set_last_error("metropolis_hamiltonian_pauli: dtype %d unsupported", dtype);
+  return VMCK_ERR_UNSUPPORTED;
+}
 
 extern "C" int vmck_metropolis_hamiltonian(vmck_stream s, int32_t dtype, const void *params,
                                            int32_t N, int32_t M, const vmck_local_op *op,

@@ -70,12 +70,17 @@ class HamiltonianRule(MetropolisRule):
     entries).  The reference's jax rule draws among the nonzero entries but
     normalises by ``n_conn``: where a LocalOperator's diagonal element is
     exactly zero that selects no entry and proposes an all-zero row; here the
-    zero diagonal entry proposes x itself, as the numba rule does."""
+    zero diagonal entry proposes x itself, as the numba rule does.  For
+    ``PauliStrings`` n(x) is the number of slots with a nonzero matrix element
+    (PauliStringsJax's ``n_conn``)."""
     code = 2
 
     def __init__(self, operator):
-        from .operator import Ising, LocalOperator
-        if isinstance(operator, Ising):
+        from .operator import Ising, LocalOperator, PauliStrings
+        self._pauli = isinstance(operator, PauliStrings)
+        if self._pauli:
+            self._local, self.diag_rule = operator, None
+        elif isinstance(operator, Ising):
             self._local = operator.to_local_operator()
             self.diag_rule = 2
         elif isinstance(operator, LocalOperator):
@@ -178,6 +183,15 @@ class MetropolisSampler:
             st = self.rule.device_op()
             if self.rule.status is None or self.rule.status.device != state.σ.device:
                 self.rule.status = torch.zeros(1, dtype=torch.int32, device=state.σ.device)
+            if self.rule._pauli:
+                nat.check(nat.lib().vmck_metropolis_hamiltonian_pauli(
+                    nat.stream(), nat.dtype_code(params.dtype), nat.ptr(params.contiguous()), N,
+                    M, ctypes.byref(st), nat.ptr(state.σ), nat.ptr(state.log_prob),
+                    nat.ptr(state.n_accepted_proc), B, self.sweep_size, int(n_discard), L,
+                    nat.ptr(samples), state.seed, state.counter, nat.ptr(self.rule.status)))
+                state.counter += (int(n_discard) + L) * self.sweep_size
+                state.n_steps_proc += (int(n_discard) + L) * self.sweep_size * B
+                return samples, state
             nat.check(nat.lib().vmck_metropolis_hamiltonian(
                 nat.stream(), nat.dtype_code(params.dtype), nat.ptr(params.contiguous()), N, M,
                 ctypes.byref(st), self.rule.diag_rule, nat.ptr(state.σ), nat.ptr(state.log_prob),

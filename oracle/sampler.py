@@ -99,3 +99,20 @@ def sample_chain(params, x, rng, chain_length, sweep_size=None, rule="local",
         if step >= n_discard:
             out[:, step - n_discard] = x
     return out, x, lp, n_acc
+
+
+def pauli_hamiltonian_propose(operators, weights, x, u, cutoff=1e-10):
+    """Hamiltonian rule for PauliStrings (the jax rule, ``hamiltonian.py:
+    153-213``, whose draw set equals ``n_conn`` for PauliStrings): uniform over
+    the nonzero slots of x's padded row, ``corr = log n(x) - log n(x')``."""
+    from .operator import pauli_get_conn_padded
+    x = np.asarray(x, dtype=np.int8)
+    xp, mels, n = pauli_get_conn_padded(x, operators, weights, cutoff)
+    prop = x.copy()
+    for b in range(len(x)):
+        nz = np.flatnonzero(mels[b])
+        if len(nz):
+            prop[b] = xp[b, nz[int(np.floor(u[b] * len(nz)))]]
+    _, _, n2 = pauli_get_conn_padded(prop, operators, weights, cutoff)
+    with np.errstate(divide="ignore"):
+        return prop, np.log(n.astype(np.float64)) - np.log(n2.astype(np.float64))

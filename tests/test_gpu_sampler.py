@@ -239,3 +239,75 @@ def test_hamiltonian_rule_bookkeeping(nk):
         nk.sampler.MetropolisHamiltonian(nk.hilbert.Spin(0.5, N), H, n_chains=4)
     with pytest.raises(TypeError):
         nk.sampler.MetropolisHamiltonian(hi, "not an operator")
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_hamiltonian_rule_pauli_distribution(nk, dtype):
+    """PauliStrings operator: XX+YY exchange (zero on aligned pairs, so n(x)
+    varies), ZZ, a 4-site XXXX string and single X strings."""
+    N = 8
+    hi = nk.hilbert.Spin(0.5, N)
+    ops, w = [], []
+    for i in range(N):
+        j = (i + 1) % N
+        for c, wc in (("X", 0.5), ("Y", 0.5), ("Z", 1.0)):
+            s = ["I"] * N
+            s[i] = s[j] = c
+            ops.append("".join(s))
+            w.append(wc)
+        s = ["I"] * N
+        s[i] = "X"
+        ops.append("".join(s))
+        w.append(-0.3)
+    ops.append("XXXXIIII")
+    w.append(0.4)
+    H = nk.operator.PauliStrings(hi, ops, w)
+    model = _model(nk, 0.5)
+    M = model.n_hidden(N)
+    flat = torch.as_tensor(np.random.default_rng(11).normal(0, 0.25, M + N * M + N),
+                           device="cuda")
+    make = lambda nc: nk.sampler.MetropolisHamiltonian(hi, H, n_chains=nc)
+    assert _chi2_pvalues(nk, make, model, flat, N, None, dtype, independent=True) > 0.01
+    s = make(64)
+    st = s.init_state(model, flat.to(dtype), seed=1)
+    _, st = s.sample(model, flat.to(dtype), state=st, chain_length=3)
+    assert int(s.rule.status.item()) == 0
+
+
+def test_hamiltonian_rule_pauli_sz_conserving(nk):
+    """XX + YY + ZZ strings conserve Sz: chains started at Sz = 0 stay there,
+    and the acceptance agrees with the oracle's rule."""
+    from oracle import sampler as osamp
+    N = 10
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    ops, w = [], []
+    for i in range(N):
+        for c, wc in (("X", 1.0), ("Y", 1.0), ("Z", 1.0)):
+            s = ["I"] * N
+            s[i] = s[(i + 1) % N] = c
+            ops.append("".join(s))
+            w.append(wc)
+    H = nk.operator.PauliStrings(hi, ops, w)
+    model = _model(nk, 0.3)
+    flat = model.init_flat(2, N)
+    sampler = nk.sampler.MetropolisHamiltonian(hi, H, n_chains=1024)
+    st = sampler.init_state(model, flat, seed=3)
+    a, st = sampler.sample(model, flat, state=st, chain_length=4, n_discard=10)
+    assert torch.all(a.to(torch.int32).sum(-1) == 0)
+    torch.testing.assert_close(st.log_prob, 2 * model.apply(flat, st.σ), rtol=1e-12, atol=1e-12)
+    st = sampler.reset(model, flat, st)
+    x0 = st.σ[:512].cpu().numpy().copy()
+    _, st = sampler.sample(model, flat, state=st, chain_length=4)
+    p = oracle_params(flat, N, model.n_hidden(N))
+    rng = np.random.default_rng(5)
+    x, acc = x0, 0
+    lp = 2 * orbm.logpsi(p, x)
+    for _ in range(4 * N):
+        xp, corr = osamp.pauli_hamiltonian_propose(ops, w, x, rng.random(len(x)))
+        lpp = 2 * orbm.logpsi(p, xp)
+        ok = rng.random(len(x)) < np.exp(lpp - lp + corr)
+        x = np.where(ok[:, None], xp, x)
+        lp = np.where(ok, lpp, lp)
+        acc += ok.sum()
+    acc_or = acc / (512 * 4 * N)
+    assert abs(st.acceptance - acc_or) < 0.03, (st.acceptance, acc_or)
