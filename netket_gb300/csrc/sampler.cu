@@ -266,6 +266,21 @@ __device__ __forceinline__ int warp_sum_int(int v) {
 
 constexpr int XS_MAX_WARPS = 28;  // 896 threads: 73 registers per thread
 
+// Position of the n-th (0-based) set bit of v, which has more than n set bits:
+// a bisection on popcounts of the low half, quarter, ... of what is left.
+__device__ __forceinline__ int nth_set_bit(uint32_t v, int n) {
+  int pos = 0, c = __popc(v & 0xFFFFu);
+  if (n >= c) { n -= c; pos += 16; v >>= 16; }
+  c = __popc(v & 0xFFu);
+  if (n >= c) { n -= c; pos += 8; v >>= 8; }
+  c = __popc(v & 0xFu);
+  if (n >= c) { n -= c; pos += 4; v >>= 4; }
+  c = __popc(v & 0x3u);
+  if (n >= c) { n -= c; pos += 2; v >>= 2; }
+  if (n >= (int)(v & 1u)) pos += 1;
+  return pos;
+}
+
 template <int R>
 __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem_kernel(
     const float *__restrict__ params, int N, int M, int8_t *sigma, double *log_prob,
@@ -276,7 +291,8 @@ __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem
   float *Ws = reinterpret_cast<float *>(smem_raw);                    // N x M
   float *bs = Ws + (size_t)N * M;                                     // M
   float *as = bs + M;                                                 // N
-  int16_t *cl = reinterpret_cast<int16_t *>(as + N);                  // 2C
+  float *logtab = as + N;                                             // C + 1
+  int16_t *cl = reinterpret_cast<int16_t *>(logtab + C + 1);          // 2C
   int16_t *inc = cl + 2 * C;                                          // N x XS_MAXDEG
   int *deg = reinterpret_cast<int *>(                                 // N
       (reinterpret_cast<uintptr_t>(inc + (size_t)N * XS_MAXDEG) + 3) & ~uintptr_t(3));
@@ -293,6 +309,7 @@ __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem
       as[i] = params[M + (int64_t)N * M + i];
       deg[i] = 0;
     }
+    for (int k = tid; k <= C; k += blockDim.x) logtab[k] = logf((float)k);
     for (int q = tid; q < 2 * C; q += blockDim.x) cl[q] = (int16_t)clusters[q];
     if (tid == 0) overflow = 0;
     __syncthreads();
@@ -372,10 +389,7 @@ __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem
       if (ob == 0u) continue;  // unreachable while hop matches the mask
       const int src = __ffs(ob) - 1;
       int pick = -1;
-      if (owner) {
-        const unsigned bit = __fns(wbits, 0u, k - excl + 1);
-        if (bit < 32u) pick = 32 * lane + (int)bit;
-      }
+      if (owner) pick = 32 * lane + nth_set_bit(wbits, k - excl);
       pick = __shfl_sync(0xffffffffu, pick, src);
       if (pick < 0 || pick >= C) continue;  // likewise unreachable; never index out of range
       const int su = cl[2 * pick], sv = cl[2 * pick + 1];
@@ -412,7 +426,7 @@ __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem
         }
         hop_new = warp_sum_int(h2);
       }
-      const float corr = logf((float)hop) - logf((float)hop_new);
+      const float corr = logtab[hop] - logtab[hop_new];
       // log-ratio of the RBM amplitude
       float sacc = 0.0f;
       const float *Wu = Ws + su * M, *Wv = Ws + sv * M;
@@ -488,8 +502,8 @@ __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem
 
 static size_t exchange_smem_bytes(int N, int M, int C, int wpb) {
   const int nwords = (C + 31) >> 5;
-  size_t bytes = (size_t)N * M * 4 + (size_t)M * 4 + (size_t)N * 4 + (size_t)C * 4 +
-                 (size_t)N * XS_MAXDEG * 2 + 4 + (size_t)N * 4 + 16;
+  size_t bytes = (size_t)N * M * 4 + (size_t)M * 4 + (size_t)N * 4 + (size_t)(C + 1) * 4 +
+                 (size_t)C * 4 + (size_t)N * XS_MAXDEG * 2 + 4 + (size_t)N * 4 + 16;
   bytes += (size_t)wpb * ((((size_t)N + 15) & ~size_t(15)) + 4 * (size_t)nwords);
   return bytes + 64;
 }
