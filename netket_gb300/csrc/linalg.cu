@@ -123,14 +123,52 @@ __global__ void solve_check_kernel(const int *info, const T *x, const T *b, int6
   }
 }
 
-__global__ void d2f_kernel(const double *in, float *out, int64_t n) {
+// Kernels of the refinement loop take `done` (nullable): once the residual check
+// has set it, they return at entry, so the remaining iterations cost only their
+// launches.
+__device__ __forceinline__ bool refine_done(const int *done) {
+  return done && *reinterpret_cast<const volatile int *>(done) != 0;
+}
+
+__global__ void d2f_kernel(const double *in, float *out, int64_t n, const int *done = nullptr) {
+  if (refine_done(done)) return;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) out[i] = (float)in[i];
 }
 
-__global__ void axpy_f2d_kernel(double *x, const float *d, int64_t n) {
+__global__ void axpy_f2d_kernel(double *x, const float *d, int64_t n, const int *done) {
+  if (refine_done(done)) return;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) x[i] += (double)d[i];
+}
+
+// *done = 1 when ||r|| <= tol ||b|| (FP64 sums of squares, one block).
+__global__ void __launch_bounds__(256) refine_converged_kernel(const double *__restrict__ r,
+                                                               const double *__restrict__ b,
+                                                               int64_t n, double tol, int *done) {
+  if (refine_done(done)) return;
+  __shared__ double red[2][8];
+  double sr = 0.0, sb = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    sr += r[i] * r[i];
+    sb += b[i] * b[i];
+  }
+  sr = warp_sum(sr);
+  sb = warp_sum(sb);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][w] = sr;
+    red[1][w] = sb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tr = 0.0, tb = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      tr += red[0][k];
+      tb += red[1][k];
+    }
+    if (sqrt(tr) <= tol * sqrt(tb)) *done = 1;  // false for NaN: the loop goes on
+  }
 }
 
 __global__ void refine_check_kernel(const double *nr, const double *nb, const int *info,
@@ -618,7 +656,9 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_fwd_kernel(const float *__r
                                                                 const float *__restrict__ Yinv,
                                                                 const float *__restrict__ r,
                                                                 float *y, TrsvSync sy,
-                                                                unsigned epoch, int32_t *status) {
+                                                                unsigned epoch, int32_t *status,
+                                                                const int *done) {
+  if (refine_done(done)) return;  // before any ticket: every CTA leaves
   __shared__ float z[TB];
   __shared__ float part[4][TB];
   __shared__ int K_s;
@@ -688,7 +728,9 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_bwd_kernel(const float *__r
                                                                 const float *__restrict__ Yinv,
                                                                 const float *__restrict__ yv,
                                                                 float *x, TrsvSync sy,
-                                                                unsigned epoch, int32_t *status) {
+                                                                unsigned epoch, int32_t *status,
+                                                                const int *done) {
+  if (refine_done(done)) return;
   __shared__ __align__(16) float wv[TB];
   __shared__ float part[16][TB];
   __shared__ int K_s;
@@ -1023,7 +1065,9 @@ __device__ __forceinline__ df32 df_fma(df32 acc, df32 a, df32 x) {
 __global__ void __launch_bounds__(256) symv_lower_partial_kernel(const double *__restrict__ A,
                                                                  int64_t n,
                                                                  const double *__restrict__ x,
-                                                                 double *__restrict__ ws) {
+                                                                 double *__restrict__ ws,
+                                                                 const int *done) {
+  if (refine_done(done)) return;
   __shared__ float ahi[SY_T * SY_LD], alo[SY_T * SY_LD];
   __shared__ df32 xr[SY_T], xc[SY_T];
   __shared__ df32 part[4][SY_T];  // [row half 0, row half 1, col half 0, col half 1]
@@ -1082,7 +1126,9 @@ __global__ void __launch_bounds__(256) symv_lower_partial_kernel(const double *_
 }
 
 __global__ void symv_residual_reduce_kernel(const double *__restrict__ ws, int64_t n, int nt,
-                                            const double *__restrict__ b, double *__restrict__ r) {
+                                            const double *__restrict__ b, double *__restrict__ r,
+                                            const int *done) {
+  if (refine_done(done)) return;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double s = 0.0;
@@ -1091,12 +1137,12 @@ __global__ void symv_residual_reduce_kernel(const double *__restrict__ ws, int64
 }
 
 static int symv_residual(cudaStream_t st, const double *A, int64_t n, const double *x,
-                         const double *b, double *r, double *ws) {
+                         const double *b, double *r, double *ws, const int *done) {
   const int64_t nt = (n + SY_T - 1) / SY_T;
-  symv_lower_partial_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, st>>>(A, n, x, ws);
+  symv_lower_partial_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, st>>>(A, n, x, ws, done);
   int rc = check_launch("symv partial");
   if (rc) return rc;
-  symv_residual_reduce_kernel<<<ceil_div(n, 256), 256, 0, st>>>(ws, n, (int)nt, b, r);
+  symv_residual_reduce_kernel<<<ceil_div(n, 256), 256, 0, st>>>(ws, n, (int)nt, b, r, done);
   return check_launch("symv reduce");
 }
 
@@ -1212,6 +1258,7 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
   float *r32 = reinterpret_cast<float *>(r + n);
   double *norms = reinterpret_cast<double *>(
       (reinterpret_cast<uintptr_t>(r32 + n) + 15) & ~uintptr_t(15));
+  int *done = reinterpret_cast<int *>(norms + 2);  // inside the 64-byte slack after r32
   double *sws = reinterpret_cast<double *>(aux + ws_off);
   float *yinv = reinterpret_cast<float *>(aux + yinv_off);
   float *y32 = reinterpret_cast<float *>(aux + y32_off);
@@ -1264,32 +1311,38 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
     if ((rc = check_launch("refined solve info"))) return rc;
   }
   VMCK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
+  VMCK_CUDA(cudaMemsetAsync(done, 0, sizeof(int), st));
   const int blocks = ceil_div(n, 256);
+  // Iteration it > 0 first forms r = b - A x and stops the loop (on the device)
+  // once ||r|| <= tol ||b||; the kernels after that return at entry.
   for (int it = 0; it < max_iter; ++it) {
     if (it == 0) {
       VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-    } else if ((rc = symv_residual(st, A64, n, x, b, r, sws))) {
-      return rc;
+    } else {
+      if ((rc = symv_residual(st, A64, n, x, b, r, sws, done))) return rc;
+      refine_converged_kernel<<<1, 256, 0, st>>>(r, b, n, tol, done);
+      if ((rc = check_launch("refined solve convergence"))) return rc;
     }
-    d2f_kernel<<<blocks, 256, 0, st>>>(r, r32, n);
+    d2f_kernel<<<blocks, 256, 0, st>>>(r, r32, n, done);
     if ((rc = check_launch("refined solve cast"))) return rc;
     if (own_trsv) {
       const unsigned grid = (unsigned)std::min<int64_t>(nb, 2 * (int64_t)num_sms());
       VMCK_CUDA(cudaMemsetAsync(sync + 2 * nb, 0, 2 * sizeof(unsigned), st));  // tickets
       trsv_fwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(A32, n, yinv, r32, y32, sync_f,
-                                                     (unsigned)(it + 1), status);
+                                                     (unsigned)(it + 1), status, done);
       if ((rc = check_launch("refined solve forward"))) return rc;
       trsv_bwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(A32, n, yinv, y32, r32, sync_b,
-                                                     (unsigned)(it + 1), status);
+                                                     (unsigned)(it + 1), status, done);
       if ((rc = check_launch("refined solve backward"))) return rc;
     } else {
       VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, CUDA_R_32F,
                                    A32, n, CUDA_R_32F, r32, n, c->d_info));
     }
-    axpy_f2d_kernel<<<blocks, 256, 0, st>>>(x, r32, n);
+    axpy_f2d_kernel<<<blocks, 256, 0, st>>>(x, r32, n, done);
     if ((rc = check_launch("refined solve update"))) return rc;
   }
-  if ((rc = symv_residual(st, A64, n, x, b, r, sws))) return rc;
+  // the final residual (skipped when the loop stopped early: r already belongs to x)
+  if ((rc = symv_residual(st, A64, n, x, b, r, sws, done))) return rc;
   VMCK_BLAS(cublasSetPointerMode(c->blas, CUBLAS_POINTER_MODE_DEVICE));
   cublasStatus_t s1 = cublasDnrm2(c->blas, (int)n, r, 1, norms);
   cublasStatus_t s2 = cublasDnrm2(c->blas, (int)n, b, 1, norms + 1);
