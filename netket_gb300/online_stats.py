@@ -301,6 +301,20 @@ def _torch_dtype(dt):
         np.dtype(dt), torch.float64)
 
 
+def not_converged(stats, atol, rtol):
+    """True while ``stats.error_of_mean`` misses ``atol`` (absolute) or ``rtol``
+    (relative to |mean|); a NaN error never converges
+    (``netket/_src/vqs/expect_to_precision.py:38-45``)."""
+    err, scale = abs(stats.error_of_mean), abs(stats.mean)
+    if atol is not None and not err <= atol:
+        return True
+    if rtol is not None:
+        rel = (0.0 if err == 0.0 else math.inf) if scale == 0.0 else err / scale
+        if not rel <= rtol:
+            return True
+    return False
+
+
 def online_statistics(data, old_estimator=None, *, decay=None, max_lag=64):
     """Merge ``data`` into ``old_estimator`` (a new accumulator when None)
     (operations.py:51-126).  A ``LocalEstimatorsBatch`` goes to

@@ -1,6 +1,6 @@
-"""Continuous-batching VMC server: ``expect`` / ``expect_and_grad`` requests over
-a mix of Hamiltonians, state resident on the device, admission by HBM budget,
-p50 / p99 latency.
+"""Continuous-batching VMC server: ``expect`` / ``expect_and_grad`` requests and
+expect-to-tolerance requests over a mix of Hamiltonians, state resident on the
+device, admission by HBM budget, p50 / p99 latency.
 
 * A *session* is a variational state (RBM parameters + Metropolis chains) that
   stays on the device between requests; a request names its session and the
@@ -15,6 +15,13 @@ p50 / p99 latency.
 * Completion is detected by polling CUDA events, so requests that arrive while
   others are in flight are admitted as soon as a slot and memory free up --
   the device is never drained between requests.
+* A request with ``atol`` / ``rtol`` is served as ``MCState.expect_to_precision``
+  (``netket/_src/vqs/expect_to_precision.py:70-164``): sampling rounds (the
+  first with the discarded sweeps, later ones without) whose local energies
+  are merged into an ``OnlineStats`` accumulator on the request's slot, until
+  its error of the mean meets the tolerance or ``max_rounds`` is reached.  The
+  request keeps its slot between rounds; the accumulator is read only after a
+  round's event has completed, so the other slots keep running meanwhile.
 * Every request's work is a fixed sequence of deterministic kernels on its own
   data, so its result is the same alone and in any mix.
 """
@@ -34,6 +41,7 @@ from .hilbert import Spin
 from .models import RBM
 from .operator import Heisenberg, Ising
 from .sampler import MetropolisExchange, MetropolisLocal
+from .online_stats import not_converged, online_statistics
 from .stats import Stats
 from .vqs import MCState
 
@@ -61,6 +69,13 @@ class Request:
     session: str = field(compare=False)
     spec: ProblemSpec = field(compare=False)
     want_grad: bool = field(compare=False, default=True)
+    atol: float = field(compare=False, default=None)
+    rtol: float = field(compare=False, default=None)
+    max_rounds: int = field(compare=False, default=64)
+
+    @property
+    def to_tolerance(self):
+        return self.atol is not None or self.rtol is not None
 
 
 @dataclass
@@ -73,6 +88,7 @@ class Result:
     start: float
     finish: float
     n_samples: int = 0
+    rounds: int = 1
 
     @property
     def latency_ms(self):
@@ -106,9 +122,10 @@ class Session:
 
 
 class _InFlight:
-    def __init__(self, req, slot, start, event, host_stats, host_grad, nbytes):
+    def __init__(self, req, slot, start, event, host_stats, host_grad, nbytes, acc=None):
         self.req, self.slot, self.start, self.event = req, slot, start, event
         self.host_stats, self.host_grad, self.nbytes = host_stats, host_grad, nbytes
+        self.acc, self.rounds = acc, 1
 
 
 class Server:
@@ -132,10 +149,31 @@ class Server:
         return self.sessions[name]
 
     # ------------------------------------------------------------ one request
+    def _round(self, req, slot, acc, first):
+        """One sampling round of an expect-to-tolerance request: local energies
+        merged into the accumulator on the slot's stream."""
+        sess = self.sessions[req.session]
+        vs, op = sess.vs, sess.H
+        strm = self.slots[slot]
+        strm.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(strm), nat.use_ctx(100 + slot):
+            if first:
+                vs.sample()
+            else:
+                vs.sample(n_discard_per_chain=0)
+            acc = online_statistics(vs.local_estimators(op), acc, max_lag=64)
+            ev = torch.cuda.Event()
+            ev.record(strm)
+        return acc, ev
+
     def _launch(self, req, slot):
         sess = self.session(req.session, req.spec)
         sess.busy = True
         nbytes = sess.footprint()
+        if req.to_tolerance:
+            acc, ev = self._round(req, slot, None, True)
+            self.in_use += nbytes
+            return _InFlight(req, slot, time.perf_counter(), ev, None, None, nbytes, acc)
         vs, op = sess.vs, sess.H
         strm = self.slots[slot]
         strm.wait_stream(torch.cuda.current_stream())
@@ -180,17 +218,31 @@ class Server:
 
     def _retire(self):
         done = [f for f in self.inflight if f.event.query()]
+        finished = 0
         for f in done:
+            req = f.req
+            if req.to_tolerance:
+                with torch.cuda.stream(self.slots[f.slot]):
+                    st = f.acc.get_stats()  # the round's event has completed: no wait
+                if not_converged(st, req.atol, req.rtol) and f.rounds < req.max_rounds:
+                    f.acc, f.event = self._round(req, f.slot, f.acc, False)
+                    f.rounds += 1
+                    continue
             self.inflight.remove(f)
             now = time.perf_counter()
             self.free_slots.append(f.slot)
             self.in_use -= f.nbytes
-            self.sessions[f.req.session].busy = False
+            self.sessions[req.session].busy = False
+            finished += 1
+            if req.to_tolerance:
+                self.results.append(Result(req.rid, req.session, st, None, req.arrival, f.start,
+                                           now, f.acc.n_samples, f.rounds))
+                continue
             grad = f.host_grad.numpy().copy() if f.host_grad is not None else None
-            self.results.append(Result(f.req.rid, f.req.session,
+            self.results.append(Result(req.rid, req.session,
                                        Stats.from_array(f.host_stats.numpy()), grad,
-                                       f.req.arrival, f.start, now, f.req.spec.n_samples))
-        return len(done)
+                                       req.arrival, f.start, now, req.spec.n_samples))
+        return finished
 
     def serve(self, requests, t0=None):
         """Run a request stream whose ``arrival`` times are seconds after t0."""

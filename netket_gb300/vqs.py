@@ -20,7 +20,7 @@ import torch
 from . import _native as nat
 from . import kernels as K
 from .stats import Stats, _plain_rhat
-from .online_stats import online_statistics
+from .online_stats import not_converged, online_statistics
 
 
 class MCState:
@@ -175,16 +175,8 @@ class MCState:
         else:
             keys, leaves = None, [op]
 
-        def not_converged(acc):
-            st = acc.get_stats()
-            err, scale = abs(st.error_of_mean), abs(st.mean)
-            if atol is not None and not err <= atol:
-                return True
-            if rtol is not None:
-                rel = (0.0 if err == 0.0 else math.inf) if scale == 0.0 else err / scale
-                if not rel <= rtol:
-                    return True
-            return False
+        def unconverged(acc):
+            return not_converged(acc.get_stats(), atol, rtol)
 
         def accumulate(active, accs):
             return [online_statistics(self.local_estimators(o), a, max_lag=max_lag)
@@ -192,12 +184,12 @@ class MCState:
 
         self.sample()
         accs = accumulate(set(range(len(leaves))), [None] * len(leaves))
-        active = [i for i in range(len(leaves)) if not_converged(accs[i])]
+        active = [i for i in range(len(leaves)) if unconverged(accs[i])]
         it = 0
         while active and it < max_iter:
             self.sample(n_discard_per_chain=0)
             accs = accumulate(set(active), accs)
-            active = [i for i in active if not_converged(accs[i])]
+            active = [i for i in active if unconverged(accs[i])]
             it += 1
         self.last_precision_rounds = it
         if keys is not None:

@@ -60,3 +60,37 @@ def test_budget_limits_concurrency(nk):
     assert len(res) == 5 and srv.peak_inflight == 1
     summ = nk.serving.latency_summary(res, 1.0)
     assert summ["p99_ms"] >= summ["p50_ms"] > 0
+
+
+def test_expect_to_tolerance_request(nk):
+    """An rtol request is served as MCState.expect_to_precision: the same rounds
+    and the same accumulator as on an identically built state, bit for bit,
+    alone and in a mix with gradient requests on other sessions.  (TFIM N = 16
+    with near-uniform initial weights: E_loc variance ~16 around ~-16, so
+    rtol = 2e-3 takes tens of 1,024-sample rounds.)"""
+    S = nk.serving.ProblemSpec
+    spec = S("tfim", 16, h=1.0, alpha=1, n_samples=1024, seed=11)
+    rtol = 2e-3
+
+    def tol_request(rid, arrival=0.0):
+        return nk.serving.Request(arrival, rid, "tol", spec, want_grad=False, rtol=rtol,
+                                  max_rounds=500)
+
+    alone = nk.serving.Server(n_slots=4).serve([tol_request(0)])[0]
+    sess = nk.serving.Session(spec)
+    acc = sess.vs.expect_to_precision(sess.H, rtol=rtol, max_iter=499)
+    ref = acc.get_stats()
+    assert alone.rounds == sess.vs.last_precision_rounds + 1 >= 2
+    np.testing.assert_array_equal(alone.stats.as_array(), ref.as_array())
+    assert alone.stats.error_of_mean <= rtol * abs(alone.stats.mean)
+    assert alone.n_samples == acc.n_samples
+
+    others = _specs(nk)[:4]
+    reqs = nk.serving.poisson_stream(others, rate_hz=2000.0, seed=3,
+                                     sessions=["a", "b", "c", "d"])
+    reqs.append(tol_request(len(reqs), arrival=reqs[1].arrival))
+    srv = nk.serving.Server(hbm_budget_bytes=4 << 30, n_slots=4)
+    mix = {r.rid: r for r in srv.serve(reqs)}
+    assert srv.peak_inflight > 1
+    np.testing.assert_array_equal(mix[len(reqs) - 1].stats.as_array(), alone.stats.as_array())
+    assert mix[len(reqs) - 1].rounds == alone.rounds
