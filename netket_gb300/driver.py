@@ -137,7 +137,10 @@ class VMC(AbstractVariationalDriver):
 
 
 class VMC_SR(AbstractVariationalDriver):
-    """Natural-gradient VMC: minSR (``use_ntk=True``) or SR.
+    """Natural-gradient VMC: minSR (``use_ntk=True``) or SR, optionally SPRING
+    (``momentum``, ``proj_reg``; ``netket/_src/driver/vmc_sr.py:146-176``).
+    ``diag_shift``, ``proj_reg`` and ``momentum`` may be schedules
+    ``step -> value``.
 
     ``use_ntk=None`` picks minSR when n_parameters > n_samples
     (``vmc_sr.py:356-357``).  ``gram``/``solve``/``gram_mode`` select the
@@ -148,8 +151,9 @@ class VMC_SR(AbstractVariationalDriver):
                  gram="structured", gram_mode=None, solve=None, refine_iters=3,
                  refine_tol=1e-10, jac_dtype=None, proj_reg=None, momentum=None):
         super().__init__(variational_state, optimizer)
-        if proj_reg is not None or momentum is not None:
-            raise NotImplementedError("proj_reg / momentum are not supported")
+        self.proj_reg = proj_reg
+        self.momentum = momentum
+        self._old_updates = None
         self._ham = hamiltonian
         self.diag_shift = diag_shift
         if use_ntk is None:
@@ -176,13 +180,21 @@ class VMC_SR(AbstractVariationalDriver):
         c = st._forward_cache(self._ham)
         if ph:
             ph.mark("local_energy")
-        shift = self.diag_shift(self.step_count) if callable(self.diag_shift) else self.diag_shift
+        step = self.step_count
+        shift = self.diag_shift(step) if callable(self.diag_shift) else self.diag_shift
+        proj_reg = self.proj_reg(step) if callable(self.proj_reg) else self.proj_reg
+        mom = self.momentum(step) if callable(self.momentum) else self.momentum
+        if mom is not None and self._old_updates is None:
+            self._old_updates = torch.zeros(st.n_parameters, dtype=torch.float64,
+                                            device=c["e"].device)
+        old = self._old_updates if mom is not None else None
         if self.use_ntk:
             dp, self.info = minsr_update(c["t"], c["x"], st.N, st.M, c["e"], c["stats_dev"][0:1],
                                          shift, gram=self.gram, gram_mode=self.gram_mode,
                                          solve=self.solve, refine_iters=self.refine_iters,
                                          refine_tol=self.refine_tol, jac_dtype=self.jac_dtype,
-                                         check=False, phase_timer=ph)
+                                         check=False, phase_timer=ph, proj_reg=proj_reg,
+                                         momentum=mom, old_updates=old)
             # one host read per step: energy statistics and solver status together
             host = torch.cat([c["stats_dev"], self.info["status_dev"].to(torch.float64)]).cpu()
             status = int(host[5].item())
@@ -192,8 +204,15 @@ class VMC_SR(AbstractVariationalDriver):
             if status & (DEV_NOT_SPD | DEV_NONFINITE):
                 dp = minsr_fallback(self.info)
             stats = Stats.from_array(host[:5].numpy())
+            if mom is not None:
+                dp = dp + mom * old  # SPRING (netket/_src/ngd/srt.py:79-82)
         else:
+            if proj_reg is not None:
+                raise ValueError("proj_reg not implemented for SR")
             dp, self.info = sr_update(c["t"], c["x"], st.N, st.M, c["e"], c["stats_dev"][0:1],
-                                      shift, jac_dtype=self.jac_dtype)
+                                      shift, jac_dtype=self.jac_dtype, momentum=mom,
+                                      old_updates=old)
             stats = Stats.from_array(c["stats_dev"].cpu().numpy())
+        if mom is not None:
+            self._old_updates = dp
         return stats, dp

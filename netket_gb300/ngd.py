@@ -48,15 +48,27 @@ def _status():
 TC_GRAM_MAX_M = 512
 
 
+def _o_l_v(t, x, N, M, obar, s, v):
+    """O_L v = (O v - (obar . v) 1) / sqrt(n) by the JVP kernel."""
+    return (K.o_v(t, x, N, M, v) - torch.dot(obar, v)) * s
+
+
 def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram_mode=None,
                  solve="cholesky", refine_iters=3, refine_tol=1e-10, rtol=1e-14,
-                 rtol_smooth=1e-14, jac_dtype=None, check=True, phase_timer=None):
+                 rtol_smooth=1e-14, jac_dtype=None, check=True, phase_timer=None,
+                 proj_reg=None, momentum=None, old_updates=None):
     """Returns (delta (P,) FP64, info).  ``t`` = tanh(theta) (n, M) in the compute
     dtype, ``e`` = local energies (n,) FP64, ``mean_dev`` = their mean (device).
 
     With ``check=False`` the device status is not read here: ``info["status_dev"]``
     holds it and ``minsr_fallback(info)`` recomputes delta with pinv_smooth if the
-    caller finds a failed factorisation (one host read per step)."""
+    caller finds a failed factorisation (one host read per step).
+
+    SPRING (``netket/_src/ngd/srt.py:34-35, 63-66``): ``proj_reg`` adds
+    ``proj_reg / n`` to every entry of T; ``momentum`` with ``old_updates``
+    subtracts ``momentum O_L old`` from dv.  The caller adds ``momentum old`` to
+    the returned delta (after any fallback) and keeps the sum as the next
+    ``old_updates``."""
     ph = phase_timer
     n = x.shape[0]
     s = 1.0 / math.sqrt(n)
@@ -72,11 +84,19 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
             mode = 2 if M <= TC_GRAM_MAX_M else 1
     obar = K.column_means(t, x, N, M)
     dv = K.center_scale(e, mean_dev, 2.0 * s)
+    if momentum is not None and old_updates is not None:
+        # SPRING (netket/_src/ngd/srt.py:34-35): dv -= momentum O_L old
+        dv = dv - momentum * _o_l_v(t, x, N, M, obar, s, old_updates)
     status = _status()
     info = SolveInfo(solver_fallback=False)
     if gram == "structured":
         T64, T32 = K.gram_structured(t, x, N, M, obar, diag_shift, mode,
                                      want_f32=(solve == "refined" or mode >= 2), status=status)
+        if proj_reg is not None:
+            # T + proj_reg / n 1 1^T (netket/_src/ngd/srt.py:63-66)
+            T64.add_(proj_reg / n)
+            if T32 is not None:
+                T32.add_(proj_reg / n)
         if ph:
             ph.mark("gram")
         if solve == "refined":
@@ -89,6 +109,8 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
         jd = jac_dtype or t.dtype
         O_L = K.jacobian_dense(t, x, N, M, obar, s, jd)
         T = K.gram_dense(O_L, diag_shift)
+        if proj_reg is not None:
+            T.add_(proj_reg / n)
         del O_L
         if ph:
             ph.mark("gram")
@@ -127,14 +149,17 @@ def minsr_fallback(info):
 
 
 def sr_update(t, x, N, M, e, mean_dev, diag_shift, *, jac_dtype=None, rtol=1e-14,
-              rtol_smooth=1e-14):
-    """SR with the dense QGT: (O_L^T O_L + lambda I) delta = O_L^T dv."""
+              rtol_smooth=1e-14, momentum=None, old_updates=None):
+    """SR with the dense QGT: (O_L^T O_L + lambda I) delta = O_L^T dv; with
+    ``momentum``, ``F += diag_shift momentum old`` (netket/_src/ngd/sr.py:43-47)."""
     n = x.shape[0]
     s = 1.0 / math.sqrt(n)
     obar = K.column_means(t, x, N, M)
     dv = K.center_scale(e, mean_dev, 2.0 * s)
     raw = K.ot_v(t, x, N, M, dv)
     F = K.center_update(raw, obar, dv, s)
+    if momentum is not None and old_updates is not None:
+        F = F + (diag_shift * momentum) * old_updates
     jd = jac_dtype or torch.float64
     O_L = K.jacobian_dense(t, x, N, M, obar, s, jd)
     S = K.gram_dense(O_L, diag_shift, transpose=True)

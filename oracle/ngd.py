@@ -4,9 +4,10 @@
 * ``prepare_input``: ``netket/_src/ngd/sr_srt_common.py:45-101``
   (``O_L = O_c / sqrt(n)``, ``dv = 2 (E - mean E) / sqrt(n)``, real mode).
 * ``srt_update`` (minSR): ``netket/_src/ngd/srt.py:22-96``
-  (``T = O_L O_L^T + lambda I [+ proj_reg/n 11^T]``, ``delta = O_L^T T^-1 dv``).
+  (``T = O_L O_L^T + lambda I [+ proj_reg/n 11^T]``, ``delta = O_L^T T^-1 dv``,
+  SPRING momentum).
 * ``sr_update``: ``netket/_src/ngd/sr.py:23-80``
-  (``(O_L^T O_L + lambda I) delta = O_L^T dv``).
+  (``(O_L^T O_L + lambda I) delta = O_L^T dv``, momentum).
 * ``cholesky``, ``pinv_smooth``, ``cholesky_with_fallback``:
   ``netket/optimizer/solver/solvers.py:33-139, 242-340`` and
   ``netket/_src/solvers/nan_fallback.py:22-45``.
@@ -59,23 +60,42 @@ def cholesky_with_fallback(A, b, rtol=1e-14, rtol_smooth=1e-14):
     return x, {"solver_fallback": False}
 
 
-def srt_update(O_c, eloc, diag_shift, solver=cholesky_with_fallback, proj_reg=None):
-    """minSR update from the centred Jacobian ``O_c`` (n, P)."""
+def srt_update(O_c, eloc, diag_shift, solver=cholesky_with_fallback, proj_reg=None,
+               momentum=None, old_updates=None):
+    """minSR update from the centred Jacobian ``O_c`` (n, P).  With ``momentum``
+    (SPRING, ``srt.py:34-35, 79-82``): ``dv -= momentum O_L old`` and the update
+    gains ``momentum old``; returns (update, info) or, with momentum,
+    (update, info, new old_updates = update)."""
     O_L, dv = prepare_input(O_c, eloc)
+    if momentum is not None:
+        old = np.zeros(O_L.shape[1]) if old_updates is None else np.asarray(old_updates)
+        dv = dv - momentum * (O_L @ old)
     T = O_L @ O_L.T
     T = T + diag_shift * np.eye(T.shape[0])
     if proj_reg is not None:
         T = T + proj_reg / T.shape[0]
     aux, info = solver(T, dv)
-    return O_L.T @ aux, info
+    upd = O_L.T @ aux
+    if momentum is None:
+        return upd, info
+    upd = upd + momentum * old
+    return upd, info, upd
 
 
-def sr_update(O_c, eloc, diag_shift, solver=cholesky_with_fallback):
+def sr_update(O_c, eloc, diag_shift, solver=cholesky_with_fallback, momentum=None,
+              old_updates=None):
+    """SR update; with ``momentum``: ``F += diag_shift momentum old``
+    (``sr.py:43-47``) and the new old_updates is the update."""
     O_L, dv = prepare_input(O_c, eloc)
     F = O_L.T @ dv
+    if momentum is not None:
+        old = np.zeros(O_L.shape[1]) if old_updates is None else np.asarray(old_updates)
+        F = F + diag_shift * momentum * old
     S = O_L.T @ O_L + diag_shift * np.eye(O_L.shape[1])
     x, info = solver(S, F)
-    return x, info
+    if momentum is None:
+        return x, info
+    return x, info, x
 
 
 def sgd(flat_params, update, lr):

@@ -22,6 +22,7 @@ Covered:
                  read-outs (accumulator.py:240-447) over chunk sequences
   hamiltonian_rule.npz  HamiltonianRuleNumba proposal (sampler/rules/hamiltonian.py:
                  84-127: get_conn_flattened, _choose, n_conn) and IsingJax n_conn
+  spring.npz     the same updates with SPRING momentum / proj_reg
   ngd.npz        _prepare_input + _compute_srt_update + _compute_sr_update
                  (_src/ngd/sr_srt_common.py:45-101, _src/ngd/srt.py:22-96,
                  _src/ngd/sr.py:23-80) with cholesky / pinv_smooth /
@@ -431,7 +432,8 @@ def gen_stats():
 
 
 # ---------------------------------------------------------------- NGD
-def gen_ngd():
+def _ngd_namespace():
+    """The reference's NGD update functions and solvers on numpy stand-ins."""
     jnp = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("_")})
     # XLA's factorisations return NaN instead of raising; mirror that
     def cho_factor(A, lower=False):
@@ -472,7 +474,11 @@ def gen_ngd():
             return lambda A_, b_, x0=None: pinv(A_, b_, **kw)
         return pinv(A, b, **kw)
     ns["pinv_smooth"] = pinv_kw
+    return ns
 
+
+def gen_ngd():
+    ns = _ngd_namespace()
     rng = np.random.default_rng(2024)
     out = {}
     for name, n, P, shift in [("minsr", 48, 120, 1e-4), ("sr", 96, 40, 1e-2),
@@ -512,6 +518,37 @@ def gen_ngd():
     xs, _ = ns["pinv_smooth"](S, b[:10])
     out["pinv_singular__A"], out["pinv_singular__b"], out["pinv_singular__x"] = S, b[:10], xs
     np.savez_compressed(os.path.join(HERE, "ngd.npz"), **out)
+
+
+# ---------------------------------------------------------------- SPRING
+def gen_spring():
+    """_compute_srt_update / _compute_sr_update with momentum, old_updates and
+    proj_reg (_src/ngd/srt.py:22-96, _src/ngd/sr.py:23-80): SPRING."""
+    ns = _ngd_namespace()
+    rng = np.random.default_rng(77)
+    out = {}
+    cases = [("srt_momentum", "srt", 48, 120, 1e-4, None, 0.8),
+             ("srt_proj", "srt", 48, 120, 1e-4, 0.5, None),
+             ("srt_both", "srt", 40, 96, 1e-3, 1.0, 0.9),
+             ("sr_momentum", "sr", 96, 40, 1e-2, None, 0.8)]
+    for name, kind, n, P, shift, proj, mom in cases:
+        O = rng.normal(size=(n, P))
+        O = O - O.mean(axis=0)
+        e = rng.normal(-3, 1, size=n)
+        old = rng.normal(scale=0.1, size=P)
+        O_L, dv = ns["_prepare_input"](O, e, mode="real", scaling_factor=1.0 / n)
+        f = ns["_compute_srt_update"] if kind == "srt" else ns["_compute_sr_update"]
+        upd, new_old, info = f(O_L, np.array(dv), diag_shift=shift,
+                               solver_fn=ns["cholesky_with_fallback"], mode="real",
+                               proj_reg=proj, momentum=mom,
+                               old_updates=None if mom is None else old,
+                               params_structure=None)
+        out[name + "__O"], out[name + "__e"], out[name + "__old"] = O, e, old
+        out[name + "__cfg"] = np.array([shift, -1.0 if proj is None else proj,
+                                        -1.0 if mom is None else mom])
+        out[name + "__update"] = np.asarray(upd)
+        out[name + "__new_old"] = (np.zeros(0) if new_old is None else np.asarray(new_old))
+    np.savez_compressed(os.path.join(HERE, "spring.npz"), **out)
 
 
 # ---------------------------------------------------------------- online stats
@@ -645,6 +682,7 @@ if __name__ == "__main__":
     gen_online_stats()
     gen_hamiltonian_rule(edges)
     gen_ngd()
+    gen_spring()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")

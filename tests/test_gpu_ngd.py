@@ -277,3 +277,71 @@ def test_sr_onthefly_cg_matches_dense_sr(nk):
     assert np.linalg.norm(loose.cpu().numpy() - d) < 1e-3 * np.linalg.norm(d)
     warm, info2 = nk.ngd.sr_update_onthefly(t, x, N, M, e, mean, 1e-2, x0=loose)
     assert info2["cg_iterations"] <= 1 < info1["cg_iterations"]
+
+
+def test_spring_minsr_and_sr_match_oracle(nk):
+    """SPRING (netket/_src/ngd/srt.py:34-35, 63-66, 79-82; sr.py:43-47) against
+    the oracle, which is pinned to the reference's own update functions."""
+    N, n = 12, 256
+    model, flat, M, x, t, p = _problem(nk, N, 2, n, seed=9)
+    H = nk.operator.Heisenberg(nk.hilbert.Spin(0.5, N), nk.graph.Chain(N))
+    e = nk.kernels.local_energies_fused(H, flat, x, N, M)
+    mean = e.mean().reshape(1)
+    P = M + N * M + N
+    old = torch.as_tensor(np.random.default_rng(3).normal(scale=0.05, size=P), device="cuda")
+    O = orbm.jacobian(p, x.cpu().numpy(), center=True)
+    ec = e.cpu().numpy()
+    for proj in (None, 0.5):
+        dp, _ = nk.ngd.minsr_update(t, x, N, M, e, mean, 1e-3, proj_reg=proj, momentum=0.8,
+                                    old_updates=old)
+        dp = dp + 0.8 * old
+        ref, _, _ = ongd.srt_update(O, ec, 1e-3, proj_reg=proj, momentum=0.8,
+                                    old_updates=old.cpu().numpy())
+        np.testing.assert_allclose(dp.cpu().numpy(), ref, rtol=1e-8, atol=1e-8 * np.abs(ref).max())
+    dps, _ = nk.ngd.sr_update(t, x, N, M, e, mean, 1e-2, momentum=0.8, old_updates=old)
+    refs, _, _ = ongd.sr_update(O, ec, 1e-2, momentum=0.8, old_updates=old.cpu().numpy())
+    np.testing.assert_allclose(dps.cpu().numpy(), refs, rtol=1e-8, atol=1e-8 * np.abs(refs).max())
+    # proj_reg only lifts the all-ones direction of the centred T, which the
+    # centred dv does not touch: the update is unchanged
+    a, _ = nk.ngd.minsr_update(t, x, N, M, e, mean, 1e-3)
+    b, _ = nk.ngd.minsr_update(t, x, N, M, e, mean, 1e-3, proj_reg=2.0)
+    np.testing.assert_allclose(b.cpu().numpy(), a.cpu().numpy(), rtol=1e-7,
+                               atol=1e-9 * float(a.abs().max()))
+
+
+def test_vmc_sr_spring_driver(nk):
+    """VMC_SR(momentum=...): the first step equals the plain step bit for bit
+    (old_updates starts at zero), later steps differ, old_updates is the last
+    update; adding proj_reg changes only rounding (the centred minSR system does
+    not see it); proj_reg is refused for SR as in the reference."""
+    N = 10
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    H = nk.operator.Heisenberg(hi, nk.graph.Chain(N))
+
+    def make(**kw):
+        vs = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=nk.graph.Chain(N),
+                                                          n_chains=64),
+                            nk.models.RBM(alpha=2), n_samples=256, seed=5, precision="fp64")
+        return vs, nk.driver.VMC_SR(H, nk.optimizer.Sgd(0.02), diag_shift=1e-3,
+                                    variational_state=vs, use_ntk=True, **kw)
+
+    vs_a, drv_a = make()
+    vs_b, drv_b = make(momentum=lambda step: 0.8)
+    drv_a.advance(1)
+    drv_b.advance(1)
+    assert torch.equal(vs_a.flat_parameters, vs_b.flat_parameters)
+    drv_a.advance(1)
+    drv_b.advance(1)
+    assert not torch.equal(vs_a.flat_parameters, vs_b.flat_parameters)
+    assert torch.equal(drv_b._old_updates, drv_b._dp)
+    vs_p, drv_p = make(momentum=0.8, proj_reg=0.1)
+    drv_p.advance(2)
+    np.testing.assert_allclose(vs_p.flat_parameters.cpu().numpy(),
+                               vs_b.flat_parameters.cpu().numpy(), rtol=1e-6, atol=1e-9)
+    vs_s = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=nk.graph.Chain(N),
+                                                        n_chains=64),
+                          nk.models.RBM(alpha=1), n_samples=512, seed=5, precision="fp64")
+    drv_s = nk.driver.VMC_SR(H, nk.optimizer.Sgd(0.02), diag_shift=1e-3, variational_state=vs_s,
+                             use_ntk=False, proj_reg=0.1)
+    with pytest.raises(ValueError, match="proj_reg"):
+        drv_s.advance(1)

@@ -263,3 +263,21 @@ def test_pauli_strings_conn(golden, name):
     np.testing.assert_array_equal(xp, oh_.local_indices_to_states(g[name + "__xp_ids"]))
     np.testing.assert_array_equal(mels, g[name + "__mels"])
     np.testing.assert_array_equal(nc, g[name + "__n_conn"])
+
+
+@pytest.mark.parametrize("name", ["srt_momentum", "srt_proj", "srt_both", "sr_momentum"])
+def test_spring_updates(golden, name):
+    """Oracle SR / minSR with SPRING momentum and proj_reg vs the reference's own
+    _compute_srt_update / _compute_sr_update."""
+    g = golden("spring")
+    shift, proj, mom = g[name + "__cfg"]
+    proj = None if proj < 0 else float(proj)
+    mom = None if mom < 0 else float(mom)
+    f = ongd.srt_update if name.startswith("srt") else ongd.sr_update
+    kw = {"proj_reg": proj} if name.startswith("srt") else {}
+    if mom is not None:
+        kw.update(momentum=mom, old_updates=g[name + "__old"])
+    res = f(g[name + "__O"], g[name + "__e"], float(shift), **kw)
+    np.testing.assert_allclose(res[0], g[name + "__update"], rtol=1e-10, atol=1e-12)
+    if mom is not None:
+        np.testing.assert_allclose(res[2], g[name + "__new_old"], rtol=1e-10, atol=1e-12)
