@@ -139,8 +139,6 @@ class MetropolisSampler:
         self.n_chains = int(n_chains)
         self.sweep_size = hilbert.size if sweep_size is None else int(sweep_size)
         self.reset_chains = bool(reset_chains)
-        if self.reset_chains:
-            raise NotImplementedError("reset_chains=True is not supported")
         self.dtype = dtype
 
     @property
@@ -156,9 +154,14 @@ class MetropolisSampler:
 
     def reset(self, machine, params, state):
         """Recompute log_prob for the current parameters and zero the counters
-        (``netket/sampler/metropolis.py:382-414``)."""
+        (``netket/sampler/metropolis.py:382-414``).  With ``reset_chains`` the
+        chains first restart from fresh random states, drawn from the Philox
+        stream (seed, 2 + proposal counter): a new stream at every reset."""
         N = self.hilbert.size
         M = machine.sizes_from_flat(params.numel(), N)
+        if self.reset_chains:
+            state.σ = self.hilbert.random_state(state.seed, self.n_chains,
+                                                stream_id=2 + state.counter)
         from .kernels import rbm_forward
         lp, _, _ = rbm_forward(params, state.σ, N, M)
         state.log_prob = 2.0 * lp.to(torch.float64)

@@ -311,3 +311,27 @@ def test_hamiltonian_rule_pauli_sz_conserving(nk):
         acc += ok.sum()
     acc_or = acc / (512 * 4 * N)
     assert abs(st.acceptance - acc_or) < 0.03, (st.acceptance, acc_or)
+
+
+def test_reset_chains(nk):
+    """reset_chains=True (netket/sampler/metropolis.py:382-414): every reset
+    restarts the chains from fresh random states (a new Philox stream per
+    reset) and recomputes log_prob; without it the chains continue."""
+    N = 12
+    hi = nk.hilbert.Spin(0.5, N)
+    model = nk.models.RBM(alpha=1)
+    flat = model.init_flat(2, N)
+    s = nk.sampler.MetropolisLocal(hi, n_chains=64, reset_chains=True)
+    st = s.init_state(model, flat, seed=9)
+    a, st = s.sample(model, flat, state=st, chain_length=3)
+    c0 = st.counter
+    st = s.reset(model, flat, st)
+    assert torch.equal(st.σ, hi.random_state(st.seed, 64, stream_id=2 + c0))
+    assert not torch.equal(st.σ, a[:, -1])
+    torch.testing.assert_close(st.log_prob, 2 * model.apply(flat, st.σ), rtol=1e-12, atol=1e-12)
+    b, st = s.sample(model, flat, state=st, chain_length=3)
+    assert not torch.equal(s.reset(model, flat, st).σ, b[:, -1])
+    s2 = nk.sampler.MetropolisLocal(hi, n_chains=64)
+    st2 = s2.init_state(model, flat, seed=9)
+    c, st2 = s2.sample(model, flat, state=st2, chain_length=3)
+    assert torch.equal(s2.reset(model, flat, st2).σ, c[:, -1])
