@@ -279,3 +279,54 @@ def test_pauli_strings_pack_matches_oracle(golden):
         nk.operator.PauliStrings(hi, ["YII"], [1.0])
     with pytest.raises(ValueError):
         nk.operator.PauliStrings(hi, ["XQI"], [1.0])
+
+
+def _header_prototypes():
+    """{name: (return kind, [argument kinds])} parsed from include/vmck.h."""
+    hdr = open(os.path.join(ROOT, "include", "vmck.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
+    protos = {}
+    for ret, name, args in re.findall(
+            r"\b(int64_t|int|const\s+char\s*\*)\s*(vmck_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", hdr):
+        kinds = []
+        for a in args.split(","):
+            a = a.strip()
+            if not a or a == "void":
+                continue
+            if "*" in a or a.startswith("vmck_stream"):
+                kinds.append("ptr")
+            elif re.match(r"(const\s+)?uint64_t\b", a):
+                kinds.append("u64")
+            elif re.match(r"(const\s+)?int64_t\b", a):
+                kinds.append("i64")
+            elif re.match(r"(const\s+)?(int32_t|int)\b", a):
+                kinds.append("i32")
+            elif re.match(r"(const\s+)?double\b", a):
+                kinds.append("f64")
+            else:
+                raise AssertionError(f"{name}: unclassified argument {a!r}")
+        rk = {"int": "i32", "int64_t": "i64"}.get(ret, "str")
+        protos[name] = (rk, kinds)
+    return protos
+
+
+def test_ctypes_signatures_match_header():
+    """Every ctypes binding has the header prototype's argument count, kinds
+    (pointer / int32 / int64 / uint64 / double) and return type."""
+    import ctypes
+    from netket_gb300 import _native
+
+    def kind(t):
+        if t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "_type_") and \
+                isinstance(getattr(t, "_type_"), type):
+            return "ptr"
+        return {ctypes.c_int32: "i32", ctypes.c_int64: "i64", ctypes.c_uint64: "u64",
+                ctypes.c_double: "f64"}[t]
+
+    protos = _header_prototypes()
+    assert set(protos) == set(_native.declared_symbols())
+    for name, (args, res) in _native._SIGNATURES.items():
+        rk, kinds = protos[name]
+        assert [kind(a) for a in args] == kinds, name
+        exp_res = {"i32": ctypes.c_int32, "i64": ctypes.c_int64, "str": ctypes.c_char_p}[rk]
+        assert res is exp_res, name
