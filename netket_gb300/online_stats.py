@@ -379,8 +379,8 @@ class StatsBatch:
 
 
 def _delta_method_stats(f, X, Cov):
-    """Var[f_i(X)] ~ J_i^T Cov J_i with J = df/dX by forward-mode AD
-    (accumulator_batch.py:31-68)."""
+    """Var[f_i(X)] ~ J_i^T Cov J_i with J = df/dX (accumulator_batch.py:31-68;
+    the reference differentiates forward, here reverse: the same Jacobian)."""
     X = torch.as_tensor(X, dtype=torch.float64)
     mean = f(X)
     scalar = torch.as_tensor(mean).ndim == 0
@@ -388,7 +388,7 @@ def _delta_method_stats(f, X, Cov):
         if scalar:
             return Stats(mean=float(mean), error_of_mean=math.nan)
         return StatsBatch(mean, torch.full_like(torch.as_tensor(mean), math.nan))
-    J = torch.func.jacfwd(f)(X)
+    J = torch.autograd.functional.jacobian(f, X)  # (*out_shape, K)
     var = torch.einsum("...k,kl,...l->...", J, Cov, J)
     err = torch.sqrt(torch.clamp(var, min=0.0))
     if scalar:
