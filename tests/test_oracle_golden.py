@@ -281,3 +281,36 @@ def test_spring_updates(golden, name):
     np.testing.assert_allclose(res[0], g[name + "__update"], rtol=1e-10, atol=1e-12)
     if mom is not None:
         np.testing.assert_allclose(res[2], g[name + "__new_old"], rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("ham", ["ising", "heisenberg"])
+def test_full_sum_gradient_equals_finite_differences(ham):
+    """The gradient formula 2 Re<(O - <O>) (E_loc - E)> (netket/vqs/mc/common.py:
+    103-118) equals central finite differences of the exact energy <psi|H|psi>/
+    <psi|psi> (the reference's own check, test/variational/test_variational.py:
+    362-414), here on the oracle for a 6-site RBM."""
+    from oracle import exact as oex
+    N = 6
+    rng = np.random.default_rng(17)
+    p = orbm.init_params(rng, N, alpha=2, std=0.3)
+    flat0 = orbm.ravel(p)
+    M = len(p["bias"])
+    edges = np.array([(i, (i + 1) % N) for i in range(N)])
+    if ham == "ising":
+        conn = lambda s: oop.ising_get_conn_padded(s, edges, 0.8, 1.1)
+        tsz = None
+    else:
+        op = oop.heisenberg(N, og.Graph([(int(i), int(j), 0) for i, j in edges], N), 1.0, None)
+        conn = op.get_conn_padded
+        tsz = 0
+    E, G = oex.full_sum_energy_and_grad(p, conn, N, tsz)
+    h = 1e-5
+    fd = np.empty_like(flat0)
+    for k in range(flat0.size):
+        f = flat0.copy()
+        f[k] += h
+        Ep, _ = oex.full_sum_energy_and_grad(orbm.unravel(f, N, M), conn, N, tsz)
+        f[k] -= 2 * h
+        Em, _ = oex.full_sum_energy_and_grad(orbm.unravel(f, N, M), conn, N, tsz)
+        fd[k] = (Ep - Em) / (2 * h)
+    np.testing.assert_allclose(G, fd, rtol=1e-6, atol=1e-8)
