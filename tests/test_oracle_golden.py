@@ -314,3 +314,13 @@ def test_full_sum_gradient_equals_finite_differences(ham):
         Em, _ = oex.full_sum_energy_and_grad(orbm.unravel(f, N, M), conn, N, tsz)
         fd[k] = (Ep - Em) / (2 * h)
     np.testing.assert_allclose(G, fd, rtol=1e-6, atol=1e-8)
+
+
+@pytest.mark.parametrize("N,h,J", [(8, 1.0, 1.0), (10, 0.5, 1.0), (12, 1.7, -0.8)])
+def test_ed_matches_free_fermion_tfim(N, h, J):
+    """Lanczos ground energy of the oracle's sparse TFIM (get_conn -> sparse H)
+    equals the Jordan-Wigner closed form on the ring (even parity sector, even N)."""
+    from oracle import exact as oex
+    edges = np.array([(i, (i + 1) % N) for i in range(N)])
+    E0 = oex.lanczos_ed(lambda s: oop.ising_get_conn_padded(s, edges, h, J), N)[0]
+    np.testing.assert_allclose(E0, oex.tfim_ground_energy(N, J, h), rtol=1e-10)
