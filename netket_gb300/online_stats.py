@@ -302,15 +302,16 @@ def _torch_dtype(dt):
 
 
 def not_converged(stats, atol, rtol):
-    """True while ``stats.error_of_mean`` misses ``atol`` (absolute) or ``rtol``
-    (relative to |mean|); a NaN error never converges
-    (``netket/_src/vqs/expect_to_precision.py:38-45``)."""
+    """True while ``stats.error_of_mean`` exceeds ``atol`` (absolute) or ``rtol``
+    (relative to |mean|; a zero mean gives 0 or inf), as
+    ``_check_not_converged`` (``netket/_src/vqs/expect_to_precision.py:27-45``):
+    the comparisons are ``>``, so a NaN error stops the sampling."""
     err, scale = abs(stats.error_of_mean), abs(stats.mean)
-    if atol is not None and not err <= atol:
+    if atol is not None and err > atol:
         return True
     if rtol is not None:
         rel = (0.0 if err == 0.0 else math.inf) if scale == 0.0 else err / scale
-        if not rel <= rtol:
+        if rel > rtol:
             return True
     return False
 

@@ -330,3 +330,20 @@ def test_ctypes_signatures_match_header():
         assert [kind(a) for a in args] == kinds, name
         exp_res = {"i32": ctypes.c_int32, "i64": ctypes.c_int64, "str": ctypes.c_char_p}[rk]
         assert res is exp_res, name
+
+
+def test_expect_to_precision_stopping_rule():
+    """``not_converged`` is _check_not_converged of expect_to_precision.py:27-45:
+    absolute and relative tests with '>', 0 / inf relative error at zero mean,
+    NaN errors stop."""
+    from netket_gb300.online_stats import not_converged
+    from netket_gb300.stats import Stats
+    nan = float("nan")
+    assert not_converged(Stats(mean=1.0, error_of_mean=0.2), 0.1, None)
+    assert not not_converged(Stats(mean=1.0, error_of_mean=0.1), 0.1, None)
+    assert not_converged(Stats(mean=2.0, error_of_mean=0.1), None, 0.01)
+    assert not not_converged(Stats(mean=-20.0, error_of_mean=0.1), None, 0.01)
+    assert not_converged(Stats(mean=-20.0, error_of_mean=0.1), 0.05, 0.01)  # both must hold
+    assert not_converged(Stats(mean=0.0, error_of_mean=1e-9), None, 0.5)    # inf relative
+    assert not not_converged(Stats(mean=0.0, error_of_mean=0.0), None, 0.5)
+    assert not not_converged(Stats(mean=1.0, error_of_mean=nan), 0.1, 0.1)
