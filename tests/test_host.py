@@ -333,7 +333,7 @@ def test_ctypes_signatures_match_header():
 
 
 def test_expect_to_precision_stopping_rule():
-    """``not_converged`` is _check_not_converged of expect_to_precision.py:27-45:
+    """``not_converged`` is _check_not_converged of expect_to_precision.py:26-41:
     absolute and relative tests with '>', 0 / inf relative error at zero mean,
     NaN errors stop."""
     from netket_gb300.online_stats import not_converged
