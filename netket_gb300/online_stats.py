@@ -303,9 +303,9 @@ def _torch_dtype(dt):
 
 def not_converged(stats, atol, rtol):
     """True while ``stats.error_of_mean`` exceeds ``atol`` (absolute) or ``rtol``
-    (relative to |mean|; a zero mean gives 0 or inf), as
-    ``_check_not_converged`` / ``_rel_err`` (``netket/_src/vqs/expect_to_precision.py:26-41``):
-    the comparisons are ``>``, so a NaN error stops the sampling."""
+    (relative to |mean|; a zero mean gives 0 or inf), as ``_check_not_converged``
+    and ``_rel_err`` (``netket/_src/vqs/expect_to_precision.py:26-41``): the
+    comparisons are ``>``, so a NaN error stops the sampling."""
     err, scale = abs(stats.error_of_mean), abs(stats.mean)
     if atol is not None and err > atol:
         return True
