@@ -347,3 +347,46 @@ def test_expect_to_precision_stopping_rule():
     assert not_converged(Stats(mean=0.0, error_of_mean=1e-9), None, 0.5)    # inf relative
     assert not not_converged(Stats(mean=0.0, error_of_mean=0.0), None, 0.5)
     assert not not_converged(Stats(mean=1.0, error_of_mean=nan), 0.1, 0.1)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "vmck.h"
+
+/* A C caller of the ABI (what a cgo / C FFI binding would compile): entry
+   points that need no GPU -- version, error strings, argument checks. */
+int main(void) {
+  if (vmck_abi_version() != VMCK_ABI_VERSION) return 10;
+  if (strcmp(vmck_error_string(VMCK_ERR_ARG), "invalid argument") != 0) return 11;
+  if (vmck_get_conn_ising(NULL, NULL, 4, 8, NULL, 0, 1.0, 1.0, 0, NULL, NULL, NULL)
+      != VMCK_ERR_ARG) return 12;
+  if (vmck_online_stats_update(NULL, NULL, 4, 2, 8, 0, 1.0, 0, NULL) != VMCK_ERR_ARG) return 13;
+  vmck_pauli_strings ps;
+  memset(&ps, 0, sizeof ps);
+  if (vmck_get_conn_pauli(NULL, &ps, NULL, 1, NULL, NULL, NULL) != VMCK_ERR_ARG) return 14;
+  if (vmck_stats_workspace_size(16, 63) != 3 * 16 + 16 * 63) return 15;
+  printf("%s\n", vmck_last_error());
+  return 0;
+}
+"""
+
+
+def test_c_caller_compiles_and_links(built_lib, tmp_path):
+    """include/vmck.h is valid C99 and libvmck.so is callable from C."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(built_lib)
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-pedantic", str(src),
+                        "-I", os.path.join(ROOT, "include"), "-L", libdir, "-lvmck",
+                        "-Wl,-rpath," + libdir, "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert r.stdout.strip()  # the last argument error's message
