@@ -347,8 +347,22 @@ class PauliStrings(DiscreteOperator):
         if any(o.count("Y") % 2 for o in operators):
             raise TypeError("PauliStrings: a string with an odd number of Y has imaginary "
                             "matrix elements, not supported on this path")
-        self.operators = operators
-        self.weights = [float(np.real(w)) for w in weights]
+        ops = np.asarray(operators, dtype=str)
+        w = np.asarray([float(np.real(v)) for v in weights], dtype=np.float64)
+        if len(ops):
+            # the constructor's reduction (_pauli_strings/base.py:61-137, 564-599):
+            # duplicates summed in sorted string order, near-zero weights dropped
+            uniq, inv = np.unique(ops, return_inverse=True)
+            if len(uniq) != len(ops):
+                w = np.array([np.sum(w[inv == i]) for i in range(len(uniq))])
+                ops = uniq
+            keep = ~np.isclose(w, 0)
+            if np.any(keep):
+                ops, w = ops[keep], w[keep]
+            else:
+                ops, w = np.array(["I" * hilbert.size]), np.zeros(1)
+        self.operators = [str(o) for o in ops]
+        self.weights = [float(v) for v in w]
         self.cutoff = float(cutoff)
         self._tables = None
         self._dev = {}

@@ -326,6 +326,26 @@ def to_sparse_from_conn(get_conn, states):
 
 
 # ---------------------------------------------------------------- PauliStrings
+def pauli_canonicalize(operators, weights):
+    """The constructor's reduction (``_pauli_strings/base.py:61-137`` ->
+    ``_reduce_pauli_string`` / ``_remove_zero_weights``, ``:564-599``): with
+    duplicate strings, the distinct strings in sorted order with summed
+    weights; then weights ``isclose`` to 0 are dropped, and an operator left
+    empty keeps one identity string of weight 0."""
+    ops = np.asarray(list(operators), dtype=str)
+    w = np.asarray(weights, dtype=np.float64)
+    if len(ops) == 0:
+        return ops, w
+    uniq, inv = np.unique(ops, return_inverse=True)
+    if len(uniq) != len(ops):
+        w = np.array([np.sum(w[inv == i]) for i in range(len(uniq))])
+        ops = uniq
+    keep = ~np.isclose(w, 0)
+    if np.any(keep):
+        return ops[keep], w[keep]
+    return np.array(["I" * len(ops[0])]), np.zeros(1)
+
+
 def pauli_pack(operators, weights, cutoff=0.0):
     """Flip sets of a list of Pauli strings (``netket/operator/_pauli_strings/
     jax.py:50-105`` grouping, ``137-238`` ordering).
@@ -355,8 +375,9 @@ def pauli_pack(operators, weights, cutoff=0.0):
 def pauli_get_conn_padded(x, operators, weights, cutoff=1e-10):
     """PauliStringsJax.get_conn_padded on +-1 states: one slot per flip set,
     mel = sum_s w_s prod_{z in s} (-1)^[x_z = -1]; slots with |mel| <= cutoff
-    hold (x, 0) (``jax.py:240-269``).  Also returns n_conn (nonzero slots)."""
-    groups = pauli_pack(operators, weights)
+    hold (x, 0) (``jax.py:240-269``), for the operator the constructor builds
+    from (operators, weights).  Also returns n_conn (nonzero slots)."""
+    groups = pauli_pack(*pauli_canonicalize(operators, weights))
     x = np.asarray(x, dtype=np.int8)
     n, N = x.shape
     F = len(groups)

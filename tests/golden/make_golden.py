@@ -342,6 +342,9 @@ def gen_pauli_strings():
     ns = {"np": np, "jnp": jnp, "jax": jax, "partial": functools.partial,
           "_available_modes": ["index", "mask"]}
     exec(compile(mod, path, "exec"), ns)
+    # the constructor's canonicalisation (canonicalize_input, _pauli_strings/base.py:
+    # 61-137): duplicate strings summed (np.unique order), near-zero weights dropped
+    load("operator/_pauli_strings/base.py", ["_reduce_pauli_string", "_remove_zero_weights"], ns)
 
     rng = np.random.default_rng(31)
     out = {}
@@ -369,9 +372,13 @@ def gen_pauli_strings():
                    "IIXXXXIIII", "IIIIIIIIII", "ZIIIIIIIIZ", "IXZYYZXIII", "YYYYIIIIII"],
                   [0.3, -1.25, 0.75, 0.5, -0.1, 0.25, 2.0, -0.6, 0.4, 1.5]),
     }
+    cases["duplicates_and_zeros"] = (["ZZIIIIIIII", "XXIIIIIIII", "ZZIIIIIIII", "IYYIIIIIII",
+                                      "XXIIIIIIII", "IIIIIIIIXX", "IIIIZIIIIZ"],
+                                     [0.5, 1.0, 0.25, 2.0, -1.0, 1e-9, -0.75])
     for name, (ops, w) in cases.items():
-        ops_a = np.array(ops)
-        w_a = np.array(w, dtype=np.float64)
+        out[name + "__raw_ops"] = np.array(ops)
+        out[name + "__raw_weights"] = np.array(w, dtype=np.float64)
+        ops_a, w_a = ns["_reduce_pauli_string"](np.array(ops), np.array(w, dtype=np.float64))
         flips, z_data = ns["pack_internals_jax"](ops_a, w_a, weight_dtype=np.float64,
                                                  mode="index")
         x_ids = rng.integers(0, 2, size=(40, N)).astype(np.int8)

@@ -40,10 +40,11 @@ def random_strings(rng, N, n, max_len):
     return ops, w
 
 
-@pytest.mark.parametrize("name", ["tfim", "heisenberg_xyz", "mixed"])
+@pytest.mark.parametrize("name", ["tfim", "heisenberg_xyz", "mixed", "duplicates_and_zeros"])
 def test_pauli_conn_matches_reference(nk, golden, name):
+    """From the raw strings through the constructor's reduction."""
     g = golden("pauli_strings")
-    ops, w = list(g[name + "__ops"]), g[name + "__weights"]
+    ops, w = list(g[name + "__raw_ops"]), g[name + "__raw_weights"]
     N = len(ops[0])
     op = nk.operator.PauliStrings(nk.hilbert.Spin(0.5, N), ops, w)
     x = torch.as_tensor(oh.local_indices_to_states(g[name + "__x_ids"]), device="cuda")

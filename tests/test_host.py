@@ -257,11 +257,14 @@ def test_pauli_strings_pack_matches_oracle(golden):
     from oracle import operator as oop_
     import netket_gb300 as nk
     g = golden("pauli_strings")
-    for name in ("tfim", "heisenberg_xyz", "mixed"):
-        ops, w = list(g[name + "__ops"]), g[name + "__weights"]
+    for name in ("tfim", "heisenberg_xyz", "mixed", "duplicates_and_zeros"):
+        ops, w = list(g[name + "__raw_ops"]), g[name + "__raw_weights"]
         N = len(ops[0])
-        tb = nk.operator.PauliStrings(nk.hilbert.Spin(0.5, N), ops, w)._pack()
-        ref = oop_.pauli_pack(ops, w)
+        op = nk.operator.PauliStrings(nk.hilbert.Spin(0.5, N), ops, w)
+        assert op.operators == list(g[name + "__ops"])
+        np.testing.assert_array_equal(op.weights, g[name + "__weights"])
+        tb = op._pack()
+        ref = oop_.pauli_pack(g[name + "__ops"], g[name + "__weights"])
         assert tb["F"] == len(ref)
         for f, (flip, rest) in enumerate(ref):
             sites = tb["flip_site"][tb["flip_offset"][f]:tb["flip_offset"][f + 1]]

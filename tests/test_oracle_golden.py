@@ -252,14 +252,25 @@ def test_hamiltonian_rule_ising_count(golden):
     assert set(g["ising_nconn__n"]) == {7, 8}
 
 
-@pytest.mark.parametrize("name", ["tfim", "heisenberg_xyz", "mixed"])
+@pytest.mark.parametrize("name", ["tfim", "heisenberg_xyz", "mixed", "duplicates_and_zeros"])
+def test_pauli_strings_canonicalize(golden, name):
+    """The constructor's reduction of the raw strings equals the reference's
+    _reduce_pauli_string (duplicates summed, sorted, near-zero weights dropped)."""
+    g = golden("pauli_strings")
+    ops, w = oop.pauli_canonicalize(list(g[name + "__raw_ops"]), g[name + "__raw_weights"])
+    assert list(ops) == list(g[name + "__ops"])
+    np.testing.assert_array_equal(w, g[name + "__weights"])
+
+
+@pytest.mark.parametrize("name", ["tfim", "heisenberg_xyz", "mixed", "duplicates_and_zeros"])
 def test_pauli_strings_conn(golden, name):
     """Oracle PauliStrings get_conn_padded / n_conn vs the reference's own
     pack_internals_jax + _pauli_strings_kernel_jax (index mode)."""
     from oracle import hilbert as oh_
     g = golden("pauli_strings")
     x = oh_.local_indices_to_states(g[name + "__x_ids"])
-    xp, mels, nc = oop.pauli_get_conn_padded(x, list(g[name + "__ops"]), g[name + "__weights"])
+    xp, mels, nc = oop.pauli_get_conn_padded(x, list(g[name + "__raw_ops"]),
+                                             g[name + "__raw_weights"])
     np.testing.assert_array_equal(xp, oh_.local_indices_to_states(g[name + "__xp_ids"]))
     np.testing.assert_array_equal(mels, g[name + "__mels"])
     np.testing.assert_array_equal(nc, g[name + "__n_conn"])
