@@ -40,10 +40,19 @@ class ExchangeRule(MetropolisRule):
     with graph distance <= d_max, in row-major order."""
     code = 1
 
-    def __init__(self, *, clusters=None, graph=None, d_max=1):
+    def __init__(self, *, clusters=None, graph=None, d_max=1, probabilities=None):
+        if probabilities is not None:
+            probabilities = np.atleast_1d(probabilities)
+            if not np.all(probabilities > 0):
+                raise ValueError("Probabilities must be positive")
+            if not np.allclose(probabilities, probabilities.flat[0]):
+                raise NotImplementedError(
+                    "ExchangeRule: non-uniform cluster probabilities are not supported")
+        if (clusters is None) == (graph is None):
+            raise ValueError("You must either provide the list of exchange-clusters or a netket "
+                             "graph, from which clusters will be computed using the maximum "
+                             "distance d_max.")
         if clusters is None:
-            if graph is None:
-                raise ValueError("pass clusters or a graph")
             dist = np.asarray(graph.distances())
             cl = np.argwhere(dist <= d_max)
             clusters = cl[cl[:, 0] < cl[:, 1]]
@@ -222,9 +231,10 @@ def MetropolisLocal(hilbert, **kwargs):
     return MetropolisSampler(hilbert, LocalRule(), **kwargs)
 
 
-def MetropolisExchange(hilbert, *, clusters=None, graph=None, d_max=1, **kwargs):
-    return MetropolisSampler(hilbert, ExchangeRule(clusters=clusters, graph=graph, d_max=d_max),
-                             **kwargs)
+def MetropolisExchange(hilbert, *, clusters=None, graph=None, d_max=1, probabilities=None,
+                       **kwargs):
+    return MetropolisSampler(hilbert, ExchangeRule(clusters=clusters, graph=graph, d_max=d_max,
+                                                   probabilities=probabilities), **kwargs)
 
 
 def MetropolisHamiltonian(hilbert, hamiltonian, **kwargs):

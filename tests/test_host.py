@@ -393,3 +393,24 @@ def test_c_caller_compiles_and_links(built_lib, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert r.stdout.strip()  # the last argument error's message
+
+
+def test_exchange_rule_arguments():
+    """ExchangeRule (netket/sampler/rules/exchange.py:100-142, 190-205): clusters
+    from graph distances (i < j), exactly one of clusters / graph, positive
+    probabilities; uniform probabilities are the default rule, non-uniform ones
+    are refused."""
+    import netket_gb300 as nk
+    g = nk.graph.Chain(6, max_neighbor_order=2)
+    r = nk.sampler.ExchangeRule(graph=g, d_max=1)
+    assert len(r.clusters) == 12 and np.all(r.clusters[:, 0] < r.clusters[:, 1])
+    assert len(nk.sampler.ExchangeRule(graph=nk.graph.Chain(6), d_max=2).clusters) == 12
+    assert len(nk.sampler.ExchangeRule(graph=g, probabilities=[2.0, 2.0]).clusters) == 12
+    with pytest.raises(ValueError):
+        nk.sampler.ExchangeRule()
+    with pytest.raises(ValueError):
+        nk.sampler.ExchangeRule(graph=g, clusters=[(0, 1)])
+    with pytest.raises(ValueError, match="positive"):
+        nk.sampler.ExchangeRule(graph=g, probabilities=[1.0, -1.0])
+    with pytest.raises(NotImplementedError):
+        nk.sampler.ExchangeRule(graph=g, probabilities=[1.0, 0.5])
