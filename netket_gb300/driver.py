@@ -149,7 +149,29 @@ class VMC_SR(AbstractVariationalDriver):
 
     def __init__(self, hamiltonian, optimizer, *, diag_shift, variational_state, use_ntk=None,
                  gram="structured", gram_mode=None, solve=None, refine_iters=3,
-                 refine_tol=1e-10, jac_dtype=None, proj_reg=None, momentum=None):
+                 refine_tol=1e-10, jac_dtype=None, proj_reg=None, momentum=None,
+                 linear_solver=None, chunk_size_bwd=None, mode=None, on_the_fly=None):
+        # linear_solver: NetKet's cholesky_with_fallback (default), cholesky (no
+        # fallback) or pinv_smooth (netket/optimizer/solver/solvers.py); chunk_size_bwd
+        # has no effect (nothing is chunked: the Jacobian is never materialised);
+        # on_the_fly selects NetKet's srt_onthefly / srt, which here are one path.
+        from .optimizer import solver as _solvers
+        if linear_solver is None or linear_solver is _solvers.cholesky_with_fallback:
+            self._solver = "fallback"
+        elif linear_solver is _solvers.cholesky:
+            self._solver = "cholesky"
+        elif linear_solver is _solvers.pinv_smooth:
+            self._solver = "pinv_smooth"
+        else:
+            raise NotImplementedError("VMC_SR: linear_solver must be one of "
+                                      "optimizer.solver.cholesky_with_fallback / cholesky / "
+                                      "pinv_smooth")
+        if mode not in (None, "real"):
+            raise NotImplementedError(f"VMC_SR: mode={mode!r}; the RBM path is real")
+        if on_the_fly and use_ntk is False:
+            raise NotImplementedError("on_the_fly SR (use_ntk=False) is not implemented")
+        self.chunk_size_bwd = chunk_size_bwd
+        self.on_the_fly = on_the_fly
         super().__init__(variational_state, optimizer)
         self.proj_reg = proj_reg
         self.momentum = momentum
@@ -201,14 +223,19 @@ class VMC_SR(AbstractVariationalDriver):
             self.info["status"] = status
             if status & DEV_TIMEOUT:
                 raise VmckError("a device-side wait timed out in the minSR step")
-            if status & (DEV_NOT_SPD | DEV_NONFINITE):
+            failed = bool(status & (DEV_NOT_SPD | DEV_NONFINITE))
+            if self._solver == "pinv_smooth" or (self._solver == "fallback" and failed):
                 dp = minsr_fallback(self.info)
+            elif self._solver == "cholesky" and failed:
+                dp = torch.full_like(dp, float("nan"))  # a failed cho_factor gives NaN
             stats = Stats.from_array(host[:5].numpy())
             if mom is not None:
                 dp = dp + mom * old  # SPRING (netket/_src/ngd/srt.py:79-82)
         else:
             if proj_reg is not None:
                 raise ValueError("proj_reg not implemented for SR")
+            if self._solver != "fallback":
+                raise NotImplementedError("VMC_SR(use_ntk=False) uses cholesky_with_fallback")
             dp, self.info = sr_update(c["t"], c["x"], st.N, st.M, c["e"], c["stats_dev"][0:1],
                                       shift, jac_dtype=self.jac_dtype, momentum=mom,
                                       old_updates=old)

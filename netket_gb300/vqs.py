@@ -26,7 +26,19 @@ from .online_stats import not_converged, online_statistics
 class MCState:
     def __init__(self, sampler, model, *, n_samples=None, n_samples_per_rank=None,
                  chain_length=None, n_discard_per_chain=None, seed=None, sampler_seed=None,
-                 variables=None, precision=None, local_estimator="fused"):
+                 variables=None, precision=None, local_estimator="fused", chunk_size=None,
+                 init_fun=None, apply_fun=None, mutable=False, training_kwargs=None):
+        # NetKet's remaining MCState arguments (netket/vqs/mc/mc_state/state.py:180-196):
+        # chunk_size only bounds memory in NetKet and every kernel here streams its
+        # samples, so it is kept and has no effect; the model is the RBM, so custom
+        # init / apply functions and mutable collections are refused.
+        if init_fun is not None or apply_fun is not None:
+            raise NotImplementedError("MCState: custom init_fun / apply_fun are not supported; "
+                                      "the model is the RBM")
+        if mutable not in (False, None) or training_kwargs:
+            raise NotImplementedError("MCState: mutable collections / training_kwargs are not "
+                                      "supported")
+        self.chunk_size = chunk_size
         nat.require_cuda()
         self.sampler = sampler
         self.model = model

@@ -192,3 +192,29 @@ def test_expect_to_precision_reaches_tolerance(nk):
     res = vs.expect_to_precision({"H": H, "Z": Z}, rtol=0.05, max_iter=50)
     assert set(res) == {"H", "Z"}
     assert res["H"].get_stats().error_of_mean <= 0.05 * abs(res["H"].mean)
+
+
+def test_vmc_sr_linear_solver_choices(nk):
+    """VMC_SR(linear_solver=cholesky / pinv_smooth) and the accepted NetKet
+    arguments (MCState chunk_size, chunk_size_bwd, on_the_fly): the plain
+    Cholesky step equals the default step bit for bit on an SPD system, the
+    pinv_smooth step agrees to 1e-8."""
+    N = 8
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    H = nk.operator.Heisenberg(hi, nk.graph.Chain(N))
+
+    def step(**kw):
+        vs = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=nk.graph.Chain(N),
+                                                          n_chains=64),
+                            nk.models.RBM(alpha=1), n_samples=256, seed=4, precision="fp64",
+                            chunk_size=32)
+        drv = nk.driver.VMC_SR(H, nk.optimizer.Sgd(0.02), diag_shift=1e-2, variational_state=vs,
+                               use_ntk=True, chunk_size_bwd=16, on_the_fly=True, **kw)
+        drv.advance(1)
+        return vs.flat_parameters.clone()
+
+    a = step()
+    b = step(linear_solver=nk.optimizer.solver.cholesky)
+    c = step(linear_solver=nk.optimizer.solver.pinv_smooth)
+    assert torch.equal(a, b)
+    torch.testing.assert_close(c, a, rtol=1e-8, atol=1e-10)

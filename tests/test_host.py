@@ -414,3 +414,25 @@ def test_exchange_rule_arguments():
         nk.sampler.ExchangeRule(graph=g, probabilities=[1.0, -1.0])
     with pytest.raises(NotImplementedError):
         nk.sampler.ExchangeRule(graph=g, probabilities=[1.0, 0.5])
+
+
+def test_driver_and_state_arguments_refused_before_the_device():
+    """NetKet's MCState / VMC_SR arguments outside this path are refused with a
+    clear error (checked before any device work)."""
+    import netket_gb300 as nk
+    hi = nk.hilbert.Spin(0.5, 4)
+    sa = nk.sampler.MetropolisLocal(hi, n_chains=4)
+    with pytest.raises(NotImplementedError, match="init_fun"):
+        nk.vqs.MCState(sa, nk.models.RBM(), init_fun=lambda *a: None)
+    with pytest.raises(NotImplementedError, match="mutable"):
+        nk.vqs.MCState(sa, nk.models.RBM(), mutable=True)
+    H = nk.operator.Ising(hi, nk.graph.Chain(4), h=1.0)
+    opt = nk.optimizer.Sgd(0.01)
+    with pytest.raises(NotImplementedError, match="linear_solver"):
+        nk.driver.VMC_SR(H, opt, diag_shift=0.01, variational_state=None,
+                         linear_solver=lambda A, b: (b, None))
+    with pytest.raises(NotImplementedError, match="mode"):
+        nk.driver.VMC_SR(H, opt, diag_shift=0.01, variational_state=None, mode="complex")
+    with pytest.raises(NotImplementedError, match="on_the_fly"):
+        nk.driver.VMC_SR(H, opt, diag_shift=0.01, variational_state=None, use_ntk=False,
+                         on_the_fly=True)
