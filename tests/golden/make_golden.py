@@ -22,6 +22,8 @@ Covered:
                  read-outs (accumulator.py:240-447) over chunk sequences
   hamiltonian_rule.npz  HamiltonianRuleNumba proposal (sampler/rules/hamiltonian.py:
                  84-127: get_conn_flattened, _choose, n_conn) and IsingJax n_conn
+  hamiltonian_rule_pauli.npz  HamiltonianRuleJax.transition (sampler/rules/
+                 hamiltonian.py:166-213) over the reference's PauliStrings kernel
   spring.npz     the same updates with SPRING momentum / proj_reg
   ngd.npz        _prepare_input + _compute_srt_update + _compute_sr_update
                  (_src/ngd/sr_srt_common.py:45-101, _src/ngd/srt.py:22-96,
@@ -394,6 +396,67 @@ def gen_pauli_strings():
     np.savez_compressed(os.path.join(HERE, "pauli_strings.npz"), **out)
 
 
+def gen_hamiltonian_rule_pauli():
+    """HamiltonianRuleJax.transition (sampler/rules/hamiltonian.py:166-213) over a
+    PauliStringsJax operator, the operator's get_conn_padded / n_conn being the
+    reference's own PauliStrings kernel functions; jax.random.randint is replaced
+    by floor(u * maxval) for given uniforms u."""
+    import functools
+    path = os.path.join(NK, "operator/_pauli_strings/jax.py")
+    tree = ast.parse(open(path).read(), filename=path)
+    names = ["_ising_conn_states_jax", "pack_internals", "sites_to_mask", "_check_mode",
+             "pack_internals_jax", "_pauli_strings_mels_jax", "_pauli_strings_kernel_jax",
+             "_pauli_strings_n_conn_jax"]
+    nodes = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in names]
+    for n in nodes:
+        n.decorator_list = []
+    mod = _DropKeyword("promote_integers").visit(ast.Module(body=nodes, type_ignores=[]))
+    ast.fix_missing_locations(mod)
+    jnp = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("_")})
+    jnp.bool_ = np.bool_
+    jax = types.SimpleNamespace(
+        lax=types.SimpleNamespace(select=np.where), jit=lambda f: f,
+        random=types.SimpleNamespace(
+            randint=lambda key, shape, minval, maxval: np.floor(key * maxval).astype(np.int64)))
+    ns = {"np": np, "jnp": jnp, "jax": jax, "partial": functools.partial,
+          "_available_modes": ["index", "mask"]}
+    exec(compile(mod, path, "exec"), ns)
+    load("sampler/rules/hamiltonian.py", ["transition"], ns, class_name="HamiltonianRuleJax")
+
+    N = 8
+    ring = [(i, (i + 1) % N) for i in range(N)]
+
+    def pstr(ch):
+        s = ["I"] * N
+        for site, c in ch:
+            s[site] = c
+        return "".join(s)
+
+    ops = [pstr([(i, c), (j, c)]) for i, j in ring for c in "XYZ"] + [pstr([(0, "X")]),
+                                                                      "XXXXIIII"]
+    w = [0.5, 0.5, 1.0] * N + [-0.3, 0.4]
+    flips, z_data = ns["pack_internals_jax"](np.array(ops), np.array(w), weight_dtype=np.float64,
+                                             mode="index")
+
+    class Op:
+        def get_conn_padded(self, x):
+            xp_ids, mels, _ = ns["_pauli_strings_kernel_jax"](flips, z_data, (1 - x) // 2,
+                                                              cutoff=1e-10)
+            return (1 - 2 * np.asarray(xp_ids)).astype(np.int8), np.real(mels)
+
+        def n_conn(self, x):
+            return ns["_pauli_strings_n_conn_jax"](flips, z_data, (1 - x) // 2, cutoff=1e-10)
+
+    rule = types.SimpleNamespace(operator=Op())
+    rng = np.random.default_rng(55)
+    x = (1 - 2 * rng.integers(0, 2, size=(64, N))).astype(np.int8)
+    u = rng.random(64)
+    prop, corr = ns["transition"](rule, None, None, None, None, u, x)
+    np.savez_compressed(os.path.join(HERE, "hamiltonian_rule_pauli.npz"), ops=np.array(ops),
+                        weights=np.array(w), x=x, u=u, proposed=np.asarray(prop, dtype=np.int8),
+                        corr=np.asarray(corr, dtype=np.float64))
+
+
 # ---------------------------------------------------------------- log_cosh
 def gen_logcosh():
     ns = {"jnp": np}
@@ -688,6 +751,7 @@ if __name__ == "__main__":
     gen_stats()
     gen_online_stats()
     gen_hamiltonian_rule(edges)
+    gen_hamiltonian_rule_pauli()
     gen_ngd()
     gen_spring()
     for f in sorted(os.listdir(HERE)):

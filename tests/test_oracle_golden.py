@@ -335,3 +335,14 @@ def test_ed_matches_free_fermion_tfim(N, h, J):
     edges = np.array([(i, (i + 1) % N) for i in range(N)])
     E0 = oex.lanczos_ed(lambda s: oop.ising_get_conn_padded(s, edges, h, J), N)[0]
     np.testing.assert_allclose(E0, oex.tfim_ground_energy(N, J, h), rtol=1e-10)
+
+
+def test_hamiltonian_rule_pauli_proposal(golden):
+    """Oracle PauliStrings Hamiltonian-rule proposal vs the reference's own
+    HamiltonianRuleJax.transition over its PauliStrings kernel, with the same
+    uniforms (rand_i = floor(u n_conn))."""
+    from oracle import sampler as osamp
+    g = golden("hamiltonian_rule_pauli")
+    prop, corr = osamp.pauli_hamiltonian_propose(list(g["ops"]), g["weights"], g["x"], g["u"])
+    np.testing.assert_array_equal(prop, g["proposed"])
+    np.testing.assert_allclose(corr, g["corr"], rtol=0, atol=1e-14)
