@@ -122,6 +122,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The largest value over all ranks (``dist`` is ``torch.distributed`` or
+    None): replicas are timed together, so the job takes as long as its slowest
+    rank."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, ms_max):
+    """Whole-job steps/s of ``world`` replicas whose slowest takes ms_max per step."""
+    return world * 1000.0 / ms_max
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -166,11 +182,8 @@ def run_ours(args):
     phases = drv.phase_timer.summary()
     drv.phase_timer = None
     ms = start.elapsed_time(stop) / args.steps
-    t_tot = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(t_tot, op=dist.ReduceOp.MAX)
-    ms_max = float(t_tot.item())
-    value = world * 1000.0 / ms_max
+    ms_max = max_over_ranks(ms, dist, "cuda")
+    value = replica_throughput(world, ms_max)
     energy = st.mean / 100
 
     # ---------------- end to end through the public API, host buffers
@@ -194,10 +207,7 @@ def run_ours(args):
     e1.record()
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    t_e2e = torch.tensor([e2e_ms], device="cuda")
-    if dist:
-        dist.all_reduce(t_e2e, op=dist.ReduceOp.MAX)
-    e2e_value = world * 1000.0 / float(t_e2e.item())
+    e2e_value = replica_throughput(world, max_over_ranks(e2e_ms, dist, "cuda"))
 
     # ---------------- the plain FP32 GPU path (reference algorithm on the GPU)
     plain = None

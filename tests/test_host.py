@@ -436,3 +436,41 @@ def test_driver_and_state_arguments_refused_before_the_device():
     with pytest.raises(NotImplementedError, match="on_the_fly"):
         nk.driver.VMC_SR(H, opt, diag_shift=0.01, variational_state=None, use_ntk=False,
                          on_the_fly=True)
+
+
+def _replica_rank(rank, world, port, q):
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        ms = [12.5, 20.0][rank]  # the second replica is the slow one
+        ms_max = bench.max_over_ranks(ms, dist, "cpu")
+        q.put((rank, ms_max, bench.replica_throughput(world, ms_max)))
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_timing_two_ranks_gloo():
+    """bench.py's N > 1 path (replicas only): every rank sees the slowest
+    replica's time, and the whole-job throughput is world x 1000 / that time;
+    2 ranks on the gloo backend."""
+    import socket
+    import torch.multiprocessing as mp
+    import bench
+    with socket.socket() as sck:
+        sck.bind(("127.0.0.1", 0))
+        port = sck.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_replica_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in range(2))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [r[1] for r in res] == [20.0, 20.0]
+    assert all(abs(r[2] - 2 * 1000.0 / 20.0) < 1e-12 for r in res)
+    assert bench.max_over_ranks(7.25) == 7.25 and bench.replica_throughput(1, 25.0) == 40.0
