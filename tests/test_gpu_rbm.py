@@ -1,5 +1,5 @@
 """RBM log-amplitudes and local energies on the GPU against the FP64 oracle.
-Tolerances: FP64 kernels 1e-10 relative (the benchmark spec's bound for FP64 paths);
+Tolerances: FP64 kernels 1e-10 relative (the accuracy stated for FP64 paths);
 FP32 kernels 2e-5 relative on log-amplitudes and 1e-4 on local energies."""
 import numpy as np
 import pytest
