@@ -367,6 +367,60 @@ class PauliStrings(DiscreteOperator):
         self._tables = None
         self._dev = {}
 
+    # ------------------------------------------------------------ algebra
+    # (netket/operator/_pauli_strings/base.py:373-470): + concatenates and reduces
+    # as the constructor does; a scalar adds the identity string; * scales the
+    # weights (no reduction); operator products are not supported here.
+    def _scaled(self, c):
+        new = object.__new__(PauliStrings)
+        DiscreteOperator.__init__(new, self.hilbert)
+        new.operators = list(self.operators)
+        new.weights = [w * float(c) for w in self.weights]
+        new.cutoff = self.cutoff
+        new._tables, new._dev = None, {}
+        return new
+
+    def __add__(self, other):
+        if isinstance(other, PauliStrings):
+            if other.hilbert != self.hilbert:
+                raise ValueError(f"Can only add identical hilbert spaces (got A+B, "
+                                 f"A={self.hilbert}, B={other.hilbert})")
+            return PauliStrings(self.hilbert, self.operators + other.operators,
+                                self.weights + other.weights,
+                                cutoff=min(self.cutoff, other.cutoff))
+        if np.isscalar(other):
+            if other == 0:
+                return self._scaled(1.0)
+            return self + PauliStrings(self.hilbert, "I" * self.hilbert.size, float(other),
+                                       cutoff=self.cutoff)
+        return NotImplemented
+
+    def __radd__(self, other):
+        if np.isscalar(other):
+            return self.__add__(other)
+        return NotImplemented
+
+    def __mul__(self, other):
+        if isinstance(other, DiscreteOperator):
+            raise TypeError("To multiply operators use the matrix multiplication operator @; "
+                            "it is not supported for PauliStrings on this path.")
+        if np.isscalar(other):
+            if np.iscomplexobj(np.asarray(other)) and np.imag(other) != 0:
+                raise TypeError("PauliStrings: complex weights are not supported on this path")
+            return self._scaled(float(np.real(other)))
+        return NotImplemented
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return self._scaled(-1.0)
+
+    def __sub__(self, other):
+        return self + (-other)
+
+    def __rsub__(self, other):
+        return other + (-self)
+
     def _pack(self):
         if self._tables is not None:
             return self._tables

@@ -474,3 +474,30 @@ def test_replica_timing_two_ranks_gloo():
     assert [r[1] for r in res] == [20.0, 20.0]
     assert all(abs(r[2] - 2 * 1000.0 / 20.0) < 1e-12 for r in res)
     assert bench.max_over_ranks(7.25) == 7.25 and bench.replica_throughput(1, 25.0) == 40.0
+
+
+def test_pauli_strings_algebra():
+    """PauliStrings +, -, scalar + and * (netket/operator/_pauli_strings/base.py:
+    373-470): sums concatenate and reduce like the constructor, scalars add the
+    identity string, * scales the weights; the tables equal the oracle's."""
+    from oracle import operator as oop_
+    import netket_gb300 as nk
+    hi = nk.hilbert.Spin(0.5, 4)
+    A = nk.operator.PauliStrings(hi, ["XXII", "ZZII"], [0.5, 1.0])
+    B = nk.operator.PauliStrings(hi, ["ZZII", "IYYI"], [0.25, 2.0])
+    C = A + B
+    ops, w = oop_.pauli_canonicalize(["XXII", "ZZII", "ZZII", "IYYI"], [0.5, 1.0, 0.25, 2.0])
+    assert C.operators == list(ops) and C.weights == list(w)
+    D = 2.0 * A - B
+    ops, w = oop_.pauli_canonicalize(["XXII", "ZZII", "ZZII", "IYYI"], [1.0, 2.0, -0.25, -2.0])
+    assert D.operators == list(ops) and np.allclose(D.weights, w)
+    E = A + 3.0
+    assert "IIII" in E.operators and E.weights[E.operators.index("IIII")] == 3.0
+    assert (A * 0.5).weights == [0.25, 0.5] and (A * 0.5).operators == A.operators
+    assert (-A).weights == [-0.5, -1.0]
+    tb, ref = D._pack(), oop_.pauli_pack(*oop_.pauli_canonicalize(D.operators, D.weights))
+    assert tb["F"] == len(ref)
+    with pytest.raises(TypeError):
+        A * B
+    with pytest.raises(ValueError):
+        A + nk.operator.PauliStrings(nk.hilbert.Spin(0.5, 4, total_sz=0), ["XXII"], [1.0])
