@@ -184,6 +184,44 @@ class LocalOperator(DiscreteOperator):
     def n_operators(self):
         return len(self._terms)
 
+    def to_pauli_strings(self):
+        """The same operator as ``PauliStrings`` (``netket/operator/_local_operator/
+        convert.py:157-209``): every term projected on the Pauli basis of its
+        sites (``itertools.product("IXYZ")`` order, first character on the
+        term's first site), weight ``Tr(P A) / 2^k``, the constant as the
+        identity string, then the PauliStrings constructor's reduction.  The
+        terms are real symmetric, so the strings with an odd number of Y carry
+        only rounding and are dropped (the reference drops them in the same
+        reduction)."""
+        import itertools
+        N = self.hilbert.size
+        basis = {"I": np.eye(2), "X": np.array([[0.0, 1.0], [1.0, 0.0]]),
+                 "Y": np.array([[0.0, -1.0j], [1.0j, 0.0]]),
+                 "Z": np.array([[1.0, 0.0], [0.0, -1.0]])}
+        strings, weights = [], []
+        for aon, m in self._terms.items():
+            k = len(aon)
+            for chars in itertools.product("IXYZ", repeat=k):
+                P = basis[chars[0]]
+                for c in chars[1:]:
+                    P = np.kron(P, basis[c])
+                w = np.trace(P @ m) / 2 ** k
+                if w == 0:
+                    continue
+                if chars.count("Y") % 2:
+                    if not np.isclose(w, 0):
+                        raise TypeError("to_pauli_strings: the operator is not real")
+                    continue
+                s = ["I"] * N
+                for site, c in zip(aon, chars):
+                    s[site] = c
+                strings.append("".join(s))
+                weights.append(float(np.real(w)))
+        if abs(self.constant) > 1e-13:
+            strings.append("I" * N)
+            weights.append(self.constant)
+        return PauliStrings(self.hilbert, strings, weights)
+
     def copy(self):
         new = LocalOperator(self.hilbert, constant=self.constant, mel_cutoff=self.mel_cutoff)
         new._terms = {k: v.copy() for k, v in self._terms.items()}

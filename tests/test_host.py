@@ -501,3 +501,59 @@ def test_pauli_strings_algebra():
         A * B
     with pytest.raises(ValueError):
         A + nk.operator.PauliStrings(nk.hilbert.Spin(0.5, 4, total_sz=0), ["XXII"], [1.0])
+
+
+def _dense_from_local(N, terms, constant):
+    """Dense H from (sites, matrix) terms; basis index = sum idx(x_i) 2^(N-1-i),
+    idx(+1) = 0; a term's row index takes its first site as the leading bit."""
+    dim = 2 ** N
+    H = constant * np.eye(dim)
+    for aon, m in terms:
+        k = len(aon)
+        for col in range(dim):
+            bits = [(col >> (N - 1 - i)) & 1 for i in range(N)]
+            c = sum(bits[s] << (k - 1 - q) for q, s in enumerate(aon))
+            for r in range(2 ** k):
+                if m[r, c] == 0:
+                    continue
+                nb = list(bits)
+                for q, s in enumerate(aon):
+                    nb[s] = (r >> (k - 1 - q)) & 1
+                row = sum(b << (N - 1 - i) for i, b in enumerate(nb))
+                H[row, col] += m[r, c]
+    return H
+
+
+def _dense_from_pauli(N, strings, weights):
+    basis = {"I": np.eye(2), "X": np.array([[0.0, 1.0], [1.0, 0.0]]),
+             "Y": np.array([[0.0, -1.0j], [1.0j, 0.0]]), "Z": np.diag([1.0, -1.0])}
+    H = np.zeros((2 ** N, 2 ** N), dtype=complex)
+    for s, w in zip(strings, weights):
+        P = basis[s[0]]
+        for c in s[1:]:
+            P = np.kron(P, basis[c])
+        H += w * P
+    return H
+
+
+def test_local_operator_to_pauli_strings():
+    """LocalOperator.to_pauli_strings (netket/operator/_local_operator/convert.py:
+    157-209) represents the same matrix: Heisenberg with the sign rule, Ising,
+    and a 3-site term with a constant."""
+    import netket_gb300 as nk
+    N = 4
+    hi = nk.hilbert.Spin(0.5, N)
+    g = nk.graph.Chain(N)
+    sx = np.array([[0.0, 1.0], [1.0, 0.0]])
+    sz = np.diag([1.0, -1.0])
+    extra = nk.operator.LocalOperator(hi, [0.7 * np.kron(np.kron(sx, sz), sx)], [[0, 2, 3]],
+                                      constant=-1.5)
+    for op in (nk.operator.Heisenberg(hi, g), nk.operator.Ising(hi, g, h=0.6, J=1.3)
+               .to_local_operator(), extra):
+        ps = op.to_pauli_strings()
+        assert all(s.count("Y") % 2 == 0 for s in ps.operators)
+        assert ps.operators == sorted(ps.operators) or len(set(ps.operators)) == len(ps.operators)
+        H1 = _dense_from_local(N, list(op._terms.items()), op.constant)
+        H2 = _dense_from_pauli(N, ps.operators, ps.weights)
+        np.testing.assert_allclose(H2.imag, 0, atol=1e-12)
+        np.testing.assert_allclose(H2.real, H1, atol=1e-12)
