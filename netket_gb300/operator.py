@@ -10,6 +10,7 @@ on the host once (the work of
 resident on the device.
 """
 import ctypes
+import types
 
 import numpy as np
 import torch
@@ -131,6 +132,19 @@ SZSZ = np.diag([1.0, -1.0, -1.0, 1.0])
 EXCHANGE = np.array([[0, 0, 0, 0], [0, 0, 2, 0], [0, 2, 0, 0], [0, 0, 0, 0]], dtype=np.float64)
 
 
+def _embed(mat, sites, union):
+    """``mat`` on ``sites`` (sorted) as an operator on ``union`` (sorted, a
+    superset): identity on the other sites, first site the leading digit."""
+    sites = list(sites)
+    others = [u for u in union if u not in sites]
+    k, u = len(sites), len(union)
+    full = np.kron(np.asarray(mat, dtype=np.float64), np.eye(2 ** len(others)))
+    order = sites + others
+    perm = [order.index(site) for site in union]
+    t = full.reshape((2,) * (2 * u)).transpose(perm + [u + p for p in perm])
+    return t.reshape(2 ** u, 2 ** u)
+
+
 def _sort_sites(mat, sites):
     """Sort the sites of a k-local matrix, permuting its tensor factors
     (first site = most significant digit of the row index)."""
@@ -242,13 +256,46 @@ class LocalOperator(DiscreteOperator):
     __radd__ = __add__
 
     def __mul__(self, s):
+        if isinstance(s, LocalOperator):
+            return self @ s
         if not np.isscalar(s):
             return NotImplemented
         new = LocalOperator(self.hilbert, constant=self.constant * s, mel_cutoff=self.mel_cutoff)
-        new._terms = {k: v * s for k, v in self._terms.items()}
+        # a scalar at or below mel_cutoff clears the terms (local_operator/base.py:356-376)
+        new._terms = {} if abs(s) <= self.mel_cutoff else {k: v * s for k, v in self._terms.items()}
         return new
 
-    __rmul__ = __mul__
+    def __rmul__(self, s):
+        if not np.isscalar(s):
+            return NotImplemented
+        return self.__mul__(s)
+
+    def __matmul__(self, other):
+        """Operator product (``netket/operator/_local_operator/base.py:392-440``):
+        (a + sum_i A_i)(b + sum_j B_j) = b (a + sum_i A_i) + a sum_j B_j +
+        sum_ij A_i B_j, terms added in that order (equal supports merge), each
+        product on the sorted union of its two supports (at most 4 sites)."""
+        if not isinstance(other, LocalOperator):
+            return NotImplemented
+        if other.hilbert != self.hilbert:
+            raise ValueError("Can only multiply operators on identical hilbert spaces")
+        a, b = self.constant, other.constant
+        cut = min(self.mel_cutoff, other.mel_cutoff)
+        A, B = list(self._terms.items()), list(other._terms.items())
+        new = self * b
+        new.mel_cutoff = cut
+        if abs(a) > cut:
+            for k, v in B:
+                new._add(a * v, k)
+        for ka, va in A:
+            for kb, vb in B:
+                union = sorted(set(ka) | set(kb))
+                if len(union) > 4:
+                    raise NotImplementedError("terms acting on more than 4 sites are not "
+                                              "supported")
+                new._add(_embed(va, ka, union) @ _embed(vb, kb, union), union)
+        new._tables, new._dev = None, {}
+        return new
 
     def __neg__(self):
         return self * -1.0
@@ -587,3 +634,42 @@ def Heisenberg(hilbert, graph, J=1.0, sign_rule=None):
     elif sign_rule and not graph.is_bipartite():
         raise ValueError("sign_rule=True specified for a non-bipartite lattice")
     return GraphOperator(hilbert, graph, bond_ops=[J * (SZSZ - EXCHANGE if sign_rule else SZSZ + EXCHANGE)])
+
+
+# -------------------------------------------------------------------- spin
+def _spin_site(hilbert, site, mat):
+    return LocalOperator(hilbert, [np.asarray(mat, dtype=np.float64)], [[int(site)]])
+
+
+def _identity(hilbert, dtype=None):
+    """The identity (``netket/operator/spin.py:29-45``)."""
+    return LocalOperator(hilbert, constant=1.0)
+
+
+def _sigmax(hilbert, site, dtype=None):
+    """Pauli X on ``site`` (``netket/operator/spin.py:48-78``)."""
+    return _spin_site(hilbert, site, [[0.0, 1.0], [1.0, 0.0]])
+
+
+def _sigmaz(hilbert, site, dtype=None):
+    """Pauli Z on ``site``, +1 on the up state (``netket/operator/spin.py:136-166``)."""
+    return _spin_site(hilbert, site, [[1.0, 0.0], [0.0, -1.0]])
+
+
+def _sigmap(hilbert, site, dtype=None):
+    """sigma+ = (X + iY) / 2: down -> up (``netket/operator/spin.py:203-233``)."""
+    return _spin_site(hilbert, site, [[0.0, 1.0], [0.0, 0.0]])
+
+
+def _sigmam(hilbert, site, dtype=None):
+    """sigma- = (X - iY) / 2: up -> down (``netket/operator/spin.py:169-200``)."""
+    return _spin_site(hilbert, site, [[0.0, 0.0], [1.0, 0.0]])
+
+
+def _sigmay(hilbert, site, dtype=None):
+    raise TypeError("sigmay has imaginary matrix elements, not supported on this path; "
+                    "sigmay(i) @ sigmay(j) = -(sigmap(i) - sigmam(i)) @ (sigmap(j) - sigmam(j))")
+
+
+spin = types.SimpleNamespace(identity=_identity, sigmax=_sigmax, sigmay=_sigmay,
+                             sigmaz=_sigmaz, sigmap=_sigmap, sigmam=_sigmam)

@@ -557,3 +557,45 @@ def test_local_operator_to_pauli_strings():
         H2 = _dense_from_pauli(N, ps.operators, ps.weights)
         np.testing.assert_allclose(H2.imag, 0, atol=1e-12)
         np.testing.assert_allclose(H2.real, H1, atol=1e-12)
+
+
+def test_local_operator_products_and_spin_helpers():
+    """nk.operator.spin (netket/operator/spin.py) and LocalOperator @
+    (local_operator/base.py:392-440) on dense matrices; the product's term order
+    is b * A's terms, then a * B's, then the A_i B_j products."""
+    import netket_gb300 as nk
+    N = 4
+    hi = nk.hilbert.Spin(0.5, N)
+    sp = nk.operator.spin
+
+    def dense(op):
+        return _dense_from_local(N, list(op._terms.items()), op.constant)
+
+    X = np.array([[0.0, 1.0], [1.0, 0.0]])
+    Z = np.diag([1.0, -1.0])
+    Y = np.array([[0.0, -1.0j], [1.0j, 0.0]])
+
+    def on(site_mats):
+        m = np.eye(1)
+        for i in range(N):
+            m = np.kron(m, site_mats.get(i, np.eye(2)))
+        return m
+
+    np.testing.assert_array_equal(dense(sp.sigmax(hi, 1)), on({1: X}))
+    np.testing.assert_array_equal(dense(sp.sigmaz(hi, 3)), on({3: Z}))
+    np.testing.assert_array_equal(dense(sp.sigmap(hi, 0)), on({0: (X + 1j * Y).real / 2}))
+    np.testing.assert_array_equal(dense(sp.sigmam(hi, 2)), on({2: (X - 1j * Y).real / 2}))
+    np.testing.assert_array_equal(dense(sp.identity(hi)), np.eye(2 ** N))
+    with pytest.raises(TypeError):
+        sp.sigmay(hi, 0)
+    np.testing.assert_allclose(dense(sp.sigmaz(hi, 0) @ sp.sigmaz(hi, 2)), on({0: Z, 2: Z}))
+    yy = -1.0 * ((sp.sigmap(hi, 1) - sp.sigmam(hi, 1)) @ (sp.sigmap(hi, 3) - sp.sigmam(hi, 3)))
+    np.testing.assert_allclose(dense(yy), on({1: Y, 3: Y}).real, atol=1e-15)
+    A = sp.sigmax(hi, 0) + 0.5
+    B = sp.sigmaz(hi, 2) - 1.0 + 2.0 * (sp.sigmax(hi, 0) @ sp.sigmax(hi, 1))
+    np.testing.assert_allclose(dense(A @ B), dense(A) @ dense(B), atol=1e-14)
+    np.testing.assert_allclose(dense(A * B), dense(A) @ dense(B), atol=1e-14)
+    H = nk.operator.Heisenberg(hi, nk.graph.Chain(N))
+    np.testing.assert_allclose(dense(H @ H), dense(H) @ dense(H), atol=1e-12)
+    assert list((A @ B)._terms) == [(0,), (2,), (0, 1), (0, 2)]
+    assert not (sp.sigmax(hi, 0) * 0.0)._terms
