@@ -183,6 +183,7 @@ class LocalOperator(DiscreteOperator):
             raise ValueError(f"matrix shape {mat.shape} does not match sites {list(aon)}")
         m, key = _sort_sites(mat, aon)
         self._terms[key] = self._terms[key] + m if key in self._terms else m
+        self._herm = None
         self._tables = None
         self._dev = {}
 
@@ -197,6 +198,13 @@ class LocalOperator(DiscreteOperator):
     @property
     def n_operators(self):
         return len(self._terms)
+
+    @property
+    def is_hermitian(self):
+        """Every term is a symmetric (real) matrix (cached until a term is added)."""
+        if getattr(self, "_herm", None) is None:
+            self._herm = all(np.allclose(m, m.T) for m in self._terms.values())
+        return self._herm
 
     def to_pauli_strings(self):
         """The same operator as ``PauliStrings`` (``netket/operator/_local_operator/

@@ -228,7 +228,11 @@ class MCState:
 
     def expect_and_grad(self, op):
         """Energy statistics and grad = 2 Re[(1/n) O^T (E - mean E)]
-        (``netket/vqs/mc/mc_state/expect_forces.py:68-111``, ``common.py:103-118``)."""
+        (``netket/vqs/mc/mc_state/expect_forces.py:68-111``, ``common.py:103-118``),
+        the formula for a hermitian operator; NetKet switches to another one for
+        non-hermitian operators (``expect_grad.py:86-128``), not built here."""
+        if getattr(op, "is_hermitian", True) is False:
+            raise NotImplementedError("expect_and_grad of a non-hermitian operator")
         c = self._forward_cache(op)
         n = c["x"].shape[0]
         v = K.center_scale(c["e"], c["stats_dev"][0:1], 2.0 / n)

@@ -599,3 +599,20 @@ def test_local_operator_products_and_spin_helpers():
     np.testing.assert_allclose(dense(H @ H), dense(H) @ dense(H), atol=1e-12)
     assert list((A @ B)._terms) == [(0,), (2,), (0, 1), (0, 2)]
     assert not (sp.sigmax(hi, 0) * 0.0)._terms
+
+
+def test_is_hermitian():
+    """LocalOperator.is_hermitian checks its terms; the operators of the path
+    (Heisenberg, J1-J2, Ising, products of Pauli matrices) are hermitian."""
+    import netket_gb300 as nk
+    hi = nk.hilbert.Spin(0.5, 6)
+    sp = nk.operator.spin
+    g = nk.graph.Chain(6, max_neighbor_order=2)
+    assert nk.operator.Heisenberg(hi, nk.graph.Chain(6)).is_hermitian is True
+    assert nk.operator.Heisenberg(hi, g, J=[1.0, 0.5]).is_hermitian is True
+    assert nk.operator.Ising(hi, nk.graph.Chain(6), h=1.0).to_local_operator().is_hermitian
+    assert nk.operator.Ising(hi, nk.graph.Chain(6), h=1.0).is_hermitian
+    assert (sp.sigmaz(hi, 0) @ sp.sigmax(hi, 3)).is_hermitian
+    assert (sp.sigmap(hi, 1) + sp.sigmam(hi, 1)).is_hermitian
+    assert sp.sigmap(hi, 1).is_hermitian is False
+    assert nk.operator.PauliStrings(hi, ["XXIIII"], [1.0]).is_hermitian
