@@ -346,3 +346,33 @@ def test_hamiltonian_rule_pauli_proposal(golden):
     prop, corr = osamp.pauli_hamiltonian_propose(list(g["ops"]), g["weights"], g["x"], g["u"])
     np.testing.assert_array_equal(prop, g["proposed"])
     np.testing.assert_allclose(corr, g["corr"], rtol=0, atol=1e-14)
+
+
+def test_online_stats_any_chunking_equals_one_shot():
+    """For any data and any chunking the accumulated sums equal the one-shot
+    ones: the rolling lag buffer pairs samples across chunk boundaries exactly
+    (the invariance the reference's tests check for a few chunkings,
+    test/stats/test_online_stats.py:50-70, 408-423)."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from oracle import online_stats as oos
+
+    @hyp.settings(max_examples=60, deadline=None)
+    @hyp.given(C=st.integers(1, 5), T=st.integers(1, 90), L=st.integers(0, 40),
+               seed=st.integers(0, 2 ** 31 - 1), data=st.data())
+    def check(C, T, L, seed, data):
+        x = np.random.default_rng(seed).normal(size=(C, T)) * 3.0 + 1.0
+        cuts = sorted(data.draw(st.sets(st.integers(1, max(1, T - 1)), max_size=8))) if T > 1 \
+            else []
+        one = oos.update(oos.new_state(C, L), x)
+        s = oos.new_state(C, L)
+        for ch in np.split(x, cuts, axis=1):
+            if ch.shape[1]:
+                s = oos.update(s, ch)
+        for k in ("count", "cross", "m1", "m2", "pair", "buf"):
+            np.testing.assert_allclose(s[k], one[k], rtol=1e-12, atol=1e-10)
+        np.testing.assert_allclose(s["mean"], one["mean"], rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(s["M2"], one["M2"], rtol=1e-9, atol=1e-9)
+        assert s["buf_len"] == one["buf_len"] == min(T, L)
+
+    check()
