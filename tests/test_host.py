@@ -616,3 +616,51 @@ def test_is_hermitian():
     assert (sp.sigmap(hi, 1) + sp.sigmam(hi, 1)).is_hermitian
     assert sp.sigmap(hi, 1).is_hermitian is False
     assert nk.operator.PauliStrings(hi, ["XXIIII"], [1.0]).is_hermitian
+
+
+def test_operator_algebra_properties():
+    """Random real LocalOperators (terms on 1-3 of 4 sites, constants) and random
+    even-Y PauliStrings: +, -, scalar *, @ and to_pauli_strings equal the same
+    operations on the dense matrices."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    import netket_gb300 as nk
+    N = 4
+    hi = nk.hilbert.Spin(0.5, N)
+
+    def rand_local(rng, symmetric=False):
+        ops, aon = [], []
+        for _ in range(int(rng.integers(1, 4))):
+            k = int(rng.integers(1, 4))
+            sites = sorted(rng.choice(N, size=k, replace=False).tolist())
+            m = rng.normal(size=(2 ** k, 2 ** k))
+            ops.append(m + m.T if symmetric or rng.random() < 0.5 else m)
+            aon.append(sites)
+        return nk.operator.LocalOperator(hi, ops, aon, constant=float(rng.normal()))
+
+    def dense(op):
+        return _dense_from_local(N, list(op._terms.items()), op.constant)
+
+    @hyp.settings(max_examples=40, deadline=None)
+    @hyp.given(seed=st.integers(0, 2 ** 31 - 1), c=st.floats(-3, 3))
+    def check(seed, c):
+        rng = np.random.default_rng(seed)
+        A, B = rand_local(rng), rand_local(rng)
+        np.testing.assert_allclose(dense(A + B), dense(A) + dense(B), atol=1e-12)
+        np.testing.assert_allclose(dense(A - c * B), dense(A) - c * dense(B), atol=1e-12)
+        np.testing.assert_allclose(dense(A @ B), dense(A) @ dense(B), atol=1e-10)
+        S = rand_local(rng, symmetric=True)
+        assert S.is_hermitian
+        P = S.to_pauli_strings()
+        np.testing.assert_allclose(_dense_from_pauli(N, P.operators, P.weights).real,
+                                   dense(S), atol=1e-10)
+        strings = ["".join(rng.choice(list("IXZ"), size=N)) for _ in range(5)]
+        w = rng.normal(size=5)
+        P1 = nk.operator.PauliStrings(hi, strings[:3], w[:3])
+        P2 = nk.operator.PauliStrings(hi, strings[3:], w[3:])
+        D = 2.0 * P1 - P2 + c
+        ref = 2.0 * _dense_from_pauli(N, strings[:3], w[:3]) - \
+            _dense_from_pauli(N, strings[3:], w[3:]) + c * np.eye(2 ** N)
+        np.testing.assert_allclose(_dense_from_pauli(N, D.operators, D.weights), ref, atol=1e-10)
+
+    check()
