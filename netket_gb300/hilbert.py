@@ -4,8 +4,6 @@ States are int8 tensors with values +1 / -1 (NetKet's new ordering,
 ``netket/hilbert/spin.py:167-172``); local index 0 <-> +1, 1 <-> -1.
 Random states come from the CUDA kernel ``vmck_random_states``.
 """
-import itertools
-
 import numpy as np
 import torch
 
@@ -23,13 +21,6 @@ class Spin:
             if (self.N + two_sz) % 2 != 0 or abs(two_sz) > self.N:
                 raise ValueError(f"total_sz={total_sz} is incompatible with N={self.N}")
         self.total_sz = total_sz
-
-    def __eq__(self, other):
-        return (isinstance(other, Spin) and self.N == other.N and
-                self.total_sz == other.total_sz)
-
-    def __hash__(self):
-        return hash(("Spin", self.N, self.total_sz))
 
     @property
     def size(self):
@@ -84,12 +75,20 @@ class Spin:
 
     def all_states(self):
         """Every basis state (device int8), first site most significant."""
+        return torch.from_numpy(1 - 2 * self._all_local_indices()).to(nat.device())
+
+    def _all_local_indices(self):
+        """(n_states, N) int8 local indices of every basis state, in order."""
         if self.N > 26:
             raise ValueError("Hilbert space too large to enumerate")
-        idx = np.array(list(itertools.product([0, 1], repeat=self.N)), dtype=np.int8)
+        code = np.arange(2 ** self.N, dtype=np.int64)
         if self.n_down is not None:
-            idx = idx[idx.sum(axis=1) == self.n_down]
-        return torch.from_numpy(1 - 2 * idx).to(nat.device())
+            pop = np.zeros_like(code)
+            for k in range(self.N):
+                pop += (code >> k) & 1
+            code = code[pop == self.n_down]
+        shifts = np.arange(self.N - 1, -1, -1, dtype=np.int64)
+        return ((code[:, None] >> shifts) & 1).astype(np.int8)
 
     def __eq__(self, other):
         return isinstance(other, Spin) and (self.N, self.total_sz) == (other.N, other.total_sz)

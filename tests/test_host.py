@@ -664,3 +664,23 @@ def test_operator_algebra_properties():
         np.testing.assert_allclose(_dense_from_pauli(N, D.operators, D.weights), ref, atol=1e-10)
 
     check()
+
+
+def test_spin_basis_enumeration():
+    """Spin._all_local_indices lists every basis state, first site most
+    significant, filtered to the fixed number of down spins under total_sz."""
+    import itertools
+    from netket_gb300.hilbert import Spin
+    for N in range(1, 11):
+        for tsz in [None] + ([0, 1] if N % 2 == 0 else [0.5, -1.5]):
+            if tsz is not None and abs(2 * tsz) > N:
+                continue
+            h = Spin(0.5, N, total_sz=tsz)
+            ref = np.array(list(itertools.product([0, 1], repeat=N)), dtype=np.int8)
+            if h.n_down is not None:
+                ref = ref[ref.sum(axis=1) == h.n_down]
+            got = h._all_local_indices()
+            assert got.dtype == np.int8 and np.array_equal(got, ref)
+            assert len(got) == h.n_states
+    assert Spin(0.5, 4, total_sz=0) == Spin(0.5, 4, total_sz=0)
+    assert len({Spin(0.5, 4), Spin(0.5, 4), Spin(0.5, 4, total_sz=0)}) == 2
