@@ -19,9 +19,7 @@ The persistent launch shape (chains per work item, CTAs per SM) is picked by a
 small autotuner that times the candidates on the first step and caches the
 choice per size signature in ``VMCK_AUTOTUNE_CACHE`` (a JSON file).
 """
-import ctypes
 import json
-import math
 import os
 
 import numpy as np

@@ -16,7 +16,6 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .hilbert import Spin
 
 
 def _as_x(x, N):

@@ -26,7 +26,6 @@ device, admission by HBM budget, p50 / p99 latency.
   data, so its result is the same alone and in any mix.
 """
 import heapq
-import itertools
 import math
 import time
 from dataclasses import dataclass, field

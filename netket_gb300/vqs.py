@@ -14,7 +14,6 @@ Statistics and gradient accumulations are FP64 in every mode.
 """
 import math
 
-import numpy as np
 import torch
 
 from . import _native as nat

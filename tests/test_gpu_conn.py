@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import torch
 
-from gpu_common import oracle_graph, oracle_heisenberg, oracle_local
+from gpu_common import oracle_heisenberg, oracle_local
 from oracle import hilbert as oh
 from oracle import operator as oop
 

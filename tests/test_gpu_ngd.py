@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from gpu_common import oracle_heisenberg, oracle_params
+from gpu_common import oracle_params
 from oracle import ngd as ongd
 from oracle import rbm as orbm
 from oracle import stats as ost

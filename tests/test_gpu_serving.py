@@ -4,7 +4,6 @@ mix where its work overlaps with other requests' on the device; requests of
 one session keep their order; the HBM budget bounds the admitted footprint."""
 import numpy as np
 import pytest
-import torch
 
 pytestmark = pytest.mark.gpu
 
