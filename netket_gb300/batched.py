@@ -53,6 +53,57 @@ def _autotune_cache_path():
                           os.path.join(os.path.expanduser("~"), ".cache", "vmck_autotune.json"))
 
 
+_LAUNCH_KEYS = ("chains_per_item", "sampler_ctas", "samples_per_item", "eloc_ctas")
+
+
+def _load_tune_cache(path):
+    """The autotune cache as a dict; a missing or unreadable file is empty."""
+    try:
+        with open(path) as f:
+            cache = json.load(f)
+    except (OSError, ValueError):
+        return {}
+    return cache if isinstance(cache, dict) else {}
+
+
+def _cached_launch(cache, sig):
+    """The cached launch shape for ``sig`` if it names every launch parameter
+    as a positive int, else None (the signature is tuned again)."""
+    c = cache.get(sig)
+    if not isinstance(c, dict):
+        return None
+    if not all(isinstance(c.get(k), int) and c[k] > 0 for k in _LAUNCH_KEYS):
+        return None
+    return c
+
+
+def _store_tune_choice(path, sig, choice):
+    """Add ``sig -> choice`` to the cache file, re-reading it first so entries
+    other processes wrote meanwhile are kept, and replacing it atomically."""
+    try:
+        os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+        cache = _load_tune_cache(path)
+        cache[sig] = choice
+        tmp = f"{path}.{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            json.dump(cache, f, indent=1)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+
+
+def _work_lists(Ns, Ms, n_chains, n_samples, chains_per_item, samples_per_item):
+    """Flat int32 (instance, first chain) and (instance, first sample) pairs:
+    every instance's chains cut into blocks of ``chains_per_item`` and its
+    samples into blocks of ``samples_per_item``, largest instances (N * M)
+    first so the persistent CTAs end together."""
+    order = sorted(range(len(Ns)), key=lambda i: -Ns[i] * Ms[i])
+    cw = [(i, b) for i in order for b in range(0, n_chains, chains_per_item)]
+    ew = [(i, s) for i in order for s in range(0, n_samples, samples_per_item)]
+    return (np.asarray(cw, dtype=np.int32).reshape(-1),
+            np.asarray(ew, dtype=np.int32).reshape(-1))
+
+
 class BatchedTFIM:
     def __init__(self, instances, *, alpha=2, n_chains=1024, chain_length=4, n_discard=5,
                  diag_shift=1e-4, lr=0.01, seed=0, gram_mode=1, refine_iters=3,
@@ -118,17 +169,10 @@ class BatchedTFIM:
         self.ising_table = _device_table(ising)
 
     def _build_work(self):
-        cpi, spi = self.launch["chains_per_item"], self.launch["samples_per_item"]
-        order = sorted(range(self.n_inst), key=lambda i: -self.N[i] * self.M[i])
-        cw, ew = [], []
-        for i in order:
-            cw += [(i, b) for b in range(0, self.B, cpi)]
-        for i in order:
-            ew += [(i, s) for s in range(0, self.B * self.L, spi)]
-        self.chain_work = torch.as_tensor(np.asarray(cw, dtype=np.int32).reshape(-1),
-                                          device=nat.device())
-        self.eloc_work = torch.as_tensor(np.asarray(ew, dtype=np.int32).reshape(-1),
-                                         device=nat.device())
+        cw, ew = _work_lists(self.N, self.M, self.B, self.B * self.L,
+                             self.launch["chains_per_item"], self.launch["samples_per_item"])
+        self.chain_work = torch.as_tensor(cw, device=nat.device())
+        self.eloc_work = torch.as_tensor(ew, device=nat.device())
 
     # ------------------------------------------------------------ kernels
     def _sample(self):
@@ -224,12 +268,9 @@ class BatchedTFIM:
     def _autotune(self):
         sig = self._signature()
         path = _autotune_cache_path()
-        try:
-            cache = json.load(open(path))
-        except (OSError, ValueError):
-            cache = {}
-        if sig in cache:
-            return cache[sig]
+        cached = _cached_launch(_load_tune_cache(path), sig)
+        if cached is not None:
+            return cached
         sms = torch.cuda.get_device_properties(nat.device()).multi_processor_count
         best = None
         # save the chain state: tuning runs advance the chains, restore afterwards
@@ -258,10 +299,5 @@ class BatchedTFIM:
         # the tuning launches advanced the proposal counters: rebuild the tables
         self._build_tables()
         choice = dict(best[1], tuned_ms=round(best[0], 4))
-        cache[sig] = choice
-        try:
-            os.makedirs(os.path.dirname(path), exist_ok=True)
-            json.dump(cache, open(path, "w"), indent=1)
-        except OSError:
-            pass
+        _store_tune_choice(path, sig, choice)
         return choice

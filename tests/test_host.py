@@ -684,3 +684,58 @@ def test_spin_basis_enumeration():
             assert len(got) == h.n_states
     assert Spin(0.5, 4, total_sz=0) == Spin(0.5, 4, total_sz=0)
     assert len({Spin(0.5, 4), Spin(0.5, 4), Spin(0.5, 4, total_sz=0)}) == 2
+
+
+def test_batched_work_lists():
+    """Every instance's chains and samples appear in exactly one work item, in
+    blocks of the tuned size, largest instances (N * M) first, with the same
+    pairs as a direct enumeration."""
+    from netket_gb300.batched import _work_lists, tfim_instances
+    inst = tfim_instances(64, seed=5)
+    Ns = [N for N, _ in inst]
+    Ms = [2 * N for N in Ns]
+    for B, L, cpi, spi in [(1024, 4, 4, 8), (16, 3, 8, 5), (7, 1, 2, 3)]:
+        cw, ew = _work_lists(Ns, Ms, B, B * L, cpi, spi)
+        assert cw.dtype == np.int32 and ew.dtype == np.int32
+        cw, ew = cw.reshape(-1, 2), ew.reshape(-1, 2)
+        order = sorted(range(len(Ns)), key=lambda i: -Ns[i] * Ms[i])
+        ref_c = [(i, b) for i in order for b in range(0, B, cpi)]
+        ref_e = [(i, s) for i in order for s in range(0, B * L, spi)]
+        assert [tuple(r) for r in cw] == ref_c and [tuple(r) for r in ew] == ref_e
+        sizes = [Ns[i] * Ms[i] for i in cw[:, 0]]
+        assert sizes == sorted(sizes, reverse=True)
+        for i in range(len(Ns)):
+            firsts = cw[cw[:, 0] == i, 1]
+            covered = np.concatenate([np.arange(f, min(f + cpi, B)) for f in firsts])
+            assert np.array_equal(np.sort(covered), np.arange(B))
+
+
+def test_autotune_cache(tmp_path):
+    """The cache keeps other signatures' entries, is replaced atomically, and an
+    entry missing a launch parameter (or a corrupt file) is tuned again."""
+    from netket_gb300.batched import _cached_launch, _load_tune_cache, _store_tune_choice
+    path = str(tmp_path / "sub" / "tune.json")
+    assert _load_tune_cache(path) == {}
+    good = {"chains_per_item": 4, "sampler_ctas": 1216, "samples_per_item": 8,
+            "eloc_ctas": 1216, "tuned_ms": 1.5}
+    _store_tune_choice(path, "a", good)
+    _store_tune_choice(path, "b", dict(good, chains_per_item=8))
+    cache = _load_tune_cache(path)
+    assert set(cache) == {"a", "b"} and _cached_launch(cache, "a") == good
+    assert _cached_launch(cache, "b")["chains_per_item"] == 8
+    assert _cached_launch(cache, "c") is None
+    assert not [p for p in os.listdir(tmp_path / "sub") if p.endswith(".tmp")]
+    stale = dict(good)
+    del stale["eloc_ctas"]
+    assert _cached_launch({"a": stale}, "a") is None
+    assert _cached_launch({"a": dict(good, sampler_ctas=0)}, "a") is None
+    assert _cached_launch({"a": dict(good, sampler_ctas=2.5)}, "a") is None
+    assert _cached_launch({"a": "x"}, "a") is None
+    with open(path, "w") as f:
+        f.write("{not json")
+    assert _load_tune_cache(path) == {}
+    _store_tune_choice(path, "a", good)
+    assert _load_tune_cache(path) == {"a": good}
+    with open(path, "w") as f:
+        f.write("[1, 2]")
+    assert _load_tune_cache(path) == {}
