@@ -3,7 +3,7 @@ local energies, Jacobian contractions and the SR/minSR solve) as hand-written
 sm_103a CUDA kernels behind a C ABI (``include/vmck.h``, ``libvmck.so``), with a
 host API that mirrors ``netket``: ``hilbert``, ``graph``, ``operator``,
 ``models``, ``sampler``, ``vqs``, ``stats``, ``optimizer``, ``driver``,
-``exact``.
+``logging``, ``callbacks``, ``exact``.
 """
 from . import _native
 from . import graph
@@ -16,6 +16,8 @@ from . import kernels
 from . import ngd
 from . import optimizer
 from . import vqs
+from . import logging
+from . import callbacks
 from . import driver
 from . import exact
 from . import batched
@@ -23,4 +25,4 @@ from . import serving
 from . import serialization
 
 __all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd", "batched", "serving", "serialization",
-           "optimizer", "vqs", "driver", "exact"]
+           "optimizer", "vqs", "driver", "logging", "callbacks", "exact"]

@@ -1,36 +1,26 @@
 """Drivers (``netket.driver``): ``VMC`` and ``VMC_SR``.
 
 The run loop mirrors ``netket/_src/driver/abstract_variational_driver.py:349-478``
-(compute the loss and update, apply the optimiser, log, callbacks);
+(callbacks around computing the loss and update, step rejection, logging,
+applying the optimiser; ``StopRun`` ends a run normally);
 ``VMC.compute_loss_and_update`` is ``netket/driver/vmc.py:141-158`` and
 ``VMC_SR.compute_loss_and_update`` is ``netket/_src/driver/vmc_sr.py:438-510``.
 One step reads back exactly one small device buffer (the energy statistics and
-the solver status).
+the solver status); ``run`` adds the sampler's acceptance, as NetKet logs it.
 """
+import numbers
+import sys
 import time
+from pathlib import Path
 
 import torch
 
+from . import callbacks as cb
 from ._native import DEV_NONFINITE, DEV_NOT_SPD, DEV_TIMEOUT, VmckError
+from .logging import JsonLog, RuntimeLog
 from .ngd import minsr_fallback, minsr_update, sr_update
 from .optimizer import identity_preconditioner
 from .stats import Stats
-
-
-class RuntimeLog:
-    """In-memory log of the per-step quantities (``RuntimeLog``)."""
-
-    def __init__(self):
-        self.data = {}
-
-    def __call__(self, step, item):
-        for k, v in item.items():
-            self.data.setdefault(k, {"iters": [], "value": []})
-            self.data[k]["iters"].append(step)
-            self.data[k]["value"].append(v)
-
-    def __getitem__(self, k):
-        return self.data[k]
 
 
 class PhaseTimer:
@@ -83,10 +73,19 @@ class AbstractVariationalDriver:
         self.step_count = 0
         self.state.reset()
 
+    def reset_step(self):
+        self.state.reset()
+
+    def update_parameters(self, dp):
+        self.optimizer.apply(self.state, dp, self.step_count)
+
+    def _accept_step(self):
+        return True
+
     def advance(self, steps=1):
         for _ in range(steps):
             self._loss_stats, self._dp = self.compute_loss_and_update()
-            self.optimizer.apply(self.state, self._dp, self.step_count)
+            self.update_parameters(self._dp)
             self.step_count += 1
         return self._loss_stats
 
@@ -95,25 +94,99 @@ class AbstractVariationalDriver:
             self.advance(step)
             yield self.step_count
 
-    def run(self, n_iter, out=None, callback=None, timeit=False):
-        """Run ``n_iter`` steps.  ``out`` is a logger called with
-        (step, {loss_name: Stats-as-dict}); ``callback(step, log_data, driver)``
-        may return False to stop (``abstract_variational_driver.py:444-478``)."""
-        if out is None:
-            out = RuntimeLog()
-        loggers = out if isinstance(out, (list, tuple)) else [out]
-        callbacks = callback if isinstance(callback, (list, tuple)) else (
-            [callback] if callback else [])
+    def estimate(self, observables):
+        """``state.expect`` of an operator, or of each operator in a dict /
+        list / tuple, in the same structure."""
+        if isinstance(observables, dict):
+            return {k: self.estimate(v) for k, v in observables.items()}
+        if isinstance(observables, (list, tuple)):
+            return type(observables)(self.estimate(v) for v in observables)
+        return self.state.expect(observables)
+
+    def _log_additional_data(self, log_dict):
+        acc = getattr(getattr(self.state, "sampler_state", None), "acceptance", None)
+        if acc is not None:
+            log_dict["acceptance"] = acc
+        log_dict["wallclock"] = time.perf_counter()
+
+    def _default_callbacks(self, callbacks, n_iter, obs, step_size, loggers, show_progress):
+        lst = [cb.maybe_wrap_legacy_callback(c) for c in callbacks]
+        if obs is not None:
+            lst.append(cb.ObservableCallback(obs, step_size))
+        for lg in loggers:
+            lst.append(lg if isinstance(lg, cb.AbstractCallback) else cb.LegacyLoggerWrapper(lg))
+        if show_progress:
+            lst.append(cb.ProgressBarCallback(n_iter))
+        return cb.CallbackList(lst)
+
+    def run(self, n_iter, out=(), obs=None, step_size=1, show_progress=True,
+            save_params_every=50, write_every=50, callback=None, timeit=False):
+        """Run ``n_iter`` steps (``abstract_variational_driver.py:349-478``).
+
+        ``out``: a logger, an iterable of loggers, or a path prefix for a
+        ``JsonLog`` (``save_params_every`` / ``write_every`` apply to it).
+        ``obs``: operators estimated every ``step_size`` steps and logged beside
+        the loss.  ``callback``: a function ``f(step, log_data, driver)`` (a falsy
+        return stops the run) or an ``AbstractCallback``, or a list of them.
+        ``timeit``: CUDA-event times of the step's phases, printed at the end
+        and kept in ``self._timer``.  Returns the loggers."""
+        if not isinstance(n_iter, numbers.Number):
+            raise ValueError("n_iter, the first positional argument to `run`, must be a number!")
+        if isinstance(out, (str, Path)):
+            out = (JsonLog(out, "w", save_params_every, write_every),)
+        elif out is None:
+            out = ()
+        loggers = tuple(out) if isinstance(out, (list, tuple)) else (out,)
+        if callback is None:
+            callback = ()
+        elif not isinstance(callback, (list, tuple)):
+            callback = (callback,)
+        callbacks = self._default_callbacks(callback, n_iter, obs, step_size, loggers,
+                                            show_progress)
+        if timeit:
+            self.phase_timer = PhaseTimer()
         t0 = time.perf_counter()
-        for _ in range(n_iter):
-            step = self.step_count
-            stats = self.advance(1)
-            log_data = {self._loss_name: stats.to_dict()}
-            for lg in loggers:
-                lg(step, log_data)
-            if any(cb(step, log_data, self) is False for cb in callbacks):
-                break
-        self.wall_time = time.perf_counter() - t0
+        try:
+            callbacks.on_run_start(self.step_count, self)
+            for _ in range(int(n_iter)):
+                self._step_attempt = 0
+                log_data = {}
+                while True:
+                    callbacks.on_step_start(self.step_count, log_data, self)
+                    self.reset_step()
+                    callbacks.on_compute_update_start(self.step_count, log_data, self)
+                    self._loss_stats, self._dp = self.compute_loss_and_update()
+                    reject = callbacks.on_compute_update_end(self.step_count, log_data, self)
+                    if reject or not self._accept_step():
+                        self._step_attempt += 1
+                        continue
+                    break
+                if self._loss_stats is not None:
+                    log_data[self._loss_name] = self._loss_stats
+                self._log_additional_data(log_data)
+                callbacks.before_parameter_update(self.step_count, log_data, self)
+                self.update_parameters(self._dp)
+                callbacks.on_step_end(self.step_count, log_data, self)
+                self.step_count += 1
+            callbacks.on_run_end(self.step_count, self)
+        except cb.StopRun as error:
+            callbacks.on_run_end(self.step_count, self)
+            print("Stopping early because of : ", error)
+        except KeyboardInterrupt as error:
+            callbacks.on_run_error(self.step_count, error, self)
+            if hasattr(sys, "ps1"):
+                print("Stopped by user.")
+            else:
+                raise
+        except Exception as error:
+            callbacks.on_run_error(self.step_count, error, self)
+            raise
+        finally:
+            self.wall_time = time.perf_counter() - t0
+            if timeit:
+                self._timer = self.phase_timer.summary()
+                self.phase_timer = None
+                print({k: round(v, 3) for k, v in self._timer.items()})
         return loggers
 
     @property

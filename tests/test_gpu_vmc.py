@@ -77,8 +77,9 @@ def test_tfim_chain16_vmc_sr_converges(nk):
                         n_samples=1008, n_discard_per_chain=32, seed=0, precision="fp64")
     drv = nk.driver.VMC(H, nk.optimizer.Sgd(0.01), variational_state=vs,
                         preconditioner=nk.optimizer.SR(diag_shift=0.01))
-    log = drv.run(300)[0]
-    tail = np.array([d["Mean"] for d in log["Energy"]["value"][-50:]])
+    log = nk.logging.RuntimeLog()
+    drv.run(300, out=log)
+    tail = log["Energy"]["Mean"][-50:]
     assert abs(tail.mean() - E0) / abs(E0) < 1e-2
     # the state's own estimate with more samples
     st = vs.expect(H)

@@ -641,8 +641,11 @@ def test_operator_algebra_properties():
     def dense(op):
         return _dense_from_local(N, list(op._terms.items()), op.constant)
 
-    @hyp.settings(max_examples=40, deadline=None)
-    @hyp.given(seed=st.integers(0, 2 ** 31 - 1), c=st.floats(-3, 3))
+    # constants within np.isclose(., 0) of zero are dropped by the PauliStrings
+    # reduction (base.py:564-576), checked separately below
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True, database=None)
+    @hyp.given(seed=st.integers(0, 2 ** 31 - 1),
+               c=st.floats(-3, 3).filter(lambda v: v == 0 or abs(v) > 1e-6))
     def check(seed, c):
         rng = np.random.default_rng(seed)
         A, B = rand_local(rng), rand_local(rng)
@@ -664,6 +667,10 @@ def test_operator_algebra_properties():
         np.testing.assert_allclose(_dense_from_pauli(N, D.operators, D.weights), ref, atol=1e-10)
 
     check()
+    P = nk.operator.PauliStrings(hi, ["XXII", "IZZI"], [1.0, -0.5])
+    T = P + 1e-10
+    assert list(T.operators) == list(P.operators) and np.array_equal(T.weights, P.weights)
+    assert "IIII" in list((P + 1e-6).operators)
 
 
 def test_spin_basis_enumeration():
