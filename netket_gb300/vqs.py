@@ -13,6 +13,7 @@ Precision modes (``precision=``):
 Statistics and gradient accumulations are FP64 in every mode.
 """
 import math
+import warnings
 
 import torch
 
@@ -20,6 +21,38 @@ from . import _native as nat
 from . import kernels as K
 from .stats import Stats, _plain_rhat
 from .online_stats import not_converged, online_statistics
+
+
+def compute_chain_length(n_chains, n_samples):
+    """ceil(n_samples / n_chains), with the reference's warning when that
+    rounds the number of samples up (``state.py:60-80``)."""
+    if n_samples <= 0:
+        raise ValueError(f"Invalid number of samples: n_samples={n_samples}")
+    chain_length = int(math.ceil(n_samples / n_chains))
+    if chain_length * n_chains != n_samples:
+        warnings.warn(f"n_samples={n_samples} does not divide n_chains={n_chains}, increased "
+                      f"to {chain_length * n_chains}", UserWarning, stacklevel=3)
+    return chain_length
+
+
+def _derive_seed(seed):
+    """A new 64-bit seed from an old one (splitmix64 finaliser)."""
+    z = (int(seed) + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return z ^ (z >> 31)
+
+
+def log_psi_to_array(log_psi, normalize=True):
+    """exp(log psi), shifted by max(log psi) and scaled to unit L2 norm when
+    ``normalize`` (``netket/nn/utils.py:132-160``)."""
+    lp = log_psi.to(torch.float64)
+    if normalize:
+        lp = lp - lp.max()
+    psi = torch.exp(lp)
+    if normalize:
+        psi = psi / torch.linalg.vector_norm(psi)
+    return psi
 
 
 class MCState:
@@ -55,6 +88,7 @@ class MCState:
         self.local_estimator = local_estimator
         seed = 0 if seed is None else int(seed)
         sampler_seed = (seed + 1) if sampler_seed is None else int(sampler_seed)
+        self._sampler_seed = sampler_seed
         if variables is not None:
             self._flat = model.flatten(variables.get("params", variables)).to(
                 device=nat.device(), dtype=torch.float64).contiguous()
@@ -65,18 +99,72 @@ class MCState:
         self._c_version = -1
         if n_samples is None and chain_length is None:
             n_samples = 1000 if n_samples_per_rank is None else n_samples_per_rank
-        if chain_length is None:
-            chain_length = int(math.ceil(n_samples / sampler.n_chains))
-        self.chain_length = int(chain_length)
-        self.n_discard_per_chain = 5 if n_discard_per_chain is None else int(n_discard_per_chain)
-        self.sampler_state = sampler.init_state(model, self.params_c, sampler_seed)
         self._samples = None
         self._cache = None
+        if chain_length is None:
+            chain_length = compute_chain_length(sampler.n_chains, n_samples)
+        self.chain_length = chain_length
+        self.n_discard_per_chain = n_discard_per_chain
+        self.sampler_state = sampler.init_state(model, self.params_c, sampler_seed)
 
     # ---------------------------------------------------------------- parameters
     @property
     def n_samples(self):
         return self.chain_length * self.sampler.n_chains
+
+    @n_samples.setter
+    def n_samples(self, n_samples):
+        self.chain_length = compute_chain_length(self.sampler.n_chains, n_samples)
+
+    @property
+    def n_samples_per_rank(self):
+        return self.n_samples  # one device
+
+    @n_samples_per_rank.setter
+    def n_samples_per_rank(self, n):
+        self.n_samples = n
+
+    @property
+    def chain_length(self):
+        return self._chain_length
+
+    @chain_length.setter
+    def chain_length(self, chain_length):
+        """``state.py:436-441``: positive, and the samples are drawn again."""
+        if chain_length <= 0:
+            raise ValueError(f"Invalid chain length: chain_length={chain_length}")
+        self._chain_length = int(chain_length)
+        self.reset()
+
+    @property
+    def n_discard_per_chain(self):
+        return self._n_discard_per_chain
+
+    @n_discard_per_chain.setter
+    def n_discard_per_chain(self, n):
+        """``state.py:450-468``: None means 5, negative is refused."""
+        if n is not None and n < 0:
+            raise ValueError(f"Invalid number of discarded samples: n_discard_per_chain={n}")
+        self._n_discard_per_chain = 5 if n is None else int(n)
+
+    @property
+    def sampler(self):
+        return self._sampler
+
+    @sampler.setter
+    def sampler(self, sampler):
+        """A new sampler gets fresh chains from a seed derived from the state's
+        sampler seed; ``n_samples`` is kept, rounded up to the new number of
+        chains (``state.py:374-404``)."""
+        old = getattr(self, "_sampler", None)
+        self._sampler = sampler
+        if old is None:
+            return
+        n_old = self._chain_length * old.n_chains
+        self._sampler_seed = _derive_seed(self._sampler_seed)
+        self.sampler_state = sampler.init_state(self.model, self.params_c, self._sampler_seed)
+        self.n_samples = n_old
+        self.reset()
 
     @property
     def n_parameters(self):
@@ -162,6 +250,19 @@ class MCState:
     def expect(self, op):
         e = self.local_estimators(op)
         return Stats.from_array(K.stats_device(e, _plain_rhat()).cpu().numpy())
+
+    def grad(self, op):
+        """The gradient of ``expect(op)`` (``netket/vqs/base.py``: the second
+        output of ``expect_and_grad``)."""
+        return self.expect_and_grad(op)[1]
+
+    def to_array(self, normalize=True):
+        """psi on every basis state, in the order of ``hilbert.all_states()``
+        (``netket/nn/utils.py:42-160``): exp(log psi - max log psi), scaled to
+        unit norm when ``normalize``.  FP64 device tensor."""
+        x = self.hilbert.all_states()
+        lp = self.model.apply(self.params_c, x)
+        return log_psi_to_array(lp, normalize)
 
     def expect_to_precision(self, op, *, atol=None, rtol=None, max_iter=10_000, max_lag=64):
         """Sample until the standard error of the mean meets ``atol`` (absolute)

@@ -746,3 +746,72 @@ def test_autotune_cache(tmp_path):
     with open(path, "w") as f:
         f.write("[1, 2]")
     assert _load_tune_cache(path) == {}
+
+
+def test_mcstate_sample_count_setters():
+    """n_samples / chain_length / n_discard_per_chain / sampler setters follow
+    state.py:374-468 (rounding up with a warning, validation, n_samples kept
+    across a sampler change, fresh chains from a derived seed)."""
+    import warnings
+    import torch
+    from netket_gb300 import vqs
+
+    class FakeSampler:
+        def __init__(self, n_chains):
+            self.n_chains = n_chains
+            self.seeds = []
+
+        def init_state(self, model, params, seed):
+            self.seeds.append(seed)
+            return ("state", seed)
+
+    vs = vqs.MCState.__new__(vqs.MCState)
+    vs._samples = vs._cache = None
+    vs.compute_dtype = torch.float64
+    vs._flat = torch.zeros(3, dtype=torch.float64)
+    vs.model = None
+    vs._sampler_seed = 7
+    vs.sampler = FakeSampler(16)
+    vs.chain_length = 4
+    vs.n_discard_per_chain = None
+    assert vs.n_samples == 64 and vs.n_discard_per_chain == 5
+    vs._samples = "old"
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        vs.n_samples = 160
+    assert vs.chain_length == 10 and vs._samples is None
+    with pytest.warns(UserWarning, match="increased to 176"):
+        vs.n_samples = 161
+    assert vs.n_samples == 176 and vs.n_samples_per_rank == 176
+    for bad in (0, -3):
+        with pytest.raises(ValueError):
+            vs.chain_length = bad
+        with pytest.raises(ValueError):
+            vs.n_samples = bad
+    with pytest.raises(ValueError):
+        vs.n_discard_per_chain = -1
+    vs.n_discard_per_chain = 0
+    assert vs.n_discard_per_chain == 0
+    new = FakeSampler(48)
+    with pytest.warns(UserWarning):
+        vs.sampler = new          # 176 samples -> 4 chains of 48 = 192
+    assert vs.sampler is new and vs.n_samples == 192 and vs.chain_length == 4
+    assert vs.sampler_state == ("state", new.seeds[0]) and new.seeds[0] != 7
+    s1 = vs._sampler_seed
+    vs.sampler = FakeSampler(48)
+    assert vs._sampler_seed not in (7, s1) and vs.n_samples == 192
+    assert vqs._derive_seed(7) == vqs._derive_seed(7) < 2 ** 64
+
+
+def test_log_psi_to_array():
+    import torch
+    from netket_gb300.vqs import log_psi_to_array
+    rng = np.random.default_rng(2)
+    lp = rng.normal(size=64) * 30 + 500.0          # exp overflows without the shift
+    psi = log_psi_to_array(torch.as_tensor(lp)).numpy()
+    ref = np.exp(lp - lp.max())
+    np.testing.assert_allclose(psi, ref / np.linalg.norm(ref), rtol=1e-13)
+    assert abs(np.linalg.norm(psi) - 1.0) < 1e-14
+    raw = log_psi_to_array(torch.as_tensor(lp[:4] - 500.0), normalize=False).numpy()
+    np.testing.assert_allclose(raw, np.exp(lp[:4] - 500.0), rtol=1e-14)
+    assert log_psi_to_array(torch.zeros(3, dtype=torch.float32)).dtype == torch.float64
