@@ -134,24 +134,48 @@ class MetropolisSampler:
     is_exact = False
 
     def __init__(self, hilbert, rule, *, n_chains=None, n_chains_per_rank=None, sweep_size=None,
-                 reset_chains=False, dtype=torch.int8):
+                 reset_chains=False, chunk_size=None, machine_pow=2, dtype=torch.int8):
+        """Argument checks of ``netket/sampler/metropolis.py:273-325`` and
+        ``sampler/base.py:139-154`` (one device: ``n_chains_per_rank`` is
+        ``n_chains``).  ``chunk_size`` is kept and has no effect (the kernels
+        stream the chains); only ``machine_pow = 2`` (sampling |psi|^2) is
+        implemented."""
         if not isinstance(rule, MetropolisRule):
-            raise TypeError("rule must be a MetropolisRule")
+            raise TypeError(f"The second positional argument, rule, must be a MetropolisRule "
+                            f"but `type(rule)={type(rule)}`.")
+        if not isinstance(reset_chains, bool):
+            raise TypeError("reset_chains must be a boolean.")
         if isinstance(rule, HamiltonianRule) and rule.operator.hilbert != hilbert:
             raise ValueError(f"The hilbert space of the sampler ({hilbert}) and the hilbert "
                              f"space of the operator ({rule.operator.hilbert}) for "
                              "HamiltonianRule must be the same.")
+        if isinstance(machine_pow, complex):
+            raise ValueError(f"machine_pow ({machine_pow}) must be real")
+        if machine_pow < 0:
+            raise ValueError(f"machine_pow ({machine_pow}) must be positive")
+        if machine_pow != 2:
+            raise NotImplementedError("MetropolisSampler: only machine_pow=2 is implemented")
+        if n_chains is not None and n_chains_per_rank is not None:
+            raise ValueError("Cannot specify both `n_chains` and `n_chains_per_rank`")
         if n_chains is None:
             n_chains = n_chains_per_rank if n_chains_per_rank is not None else 16
+        n_chains = max(int(n_chains), 1)
+        if chunk_size is not None and n_chains > chunk_size and n_chains % chunk_size != 0:
+            raise ValueError(f"Chunk size must divide number of chains per rank, {n_chains}")
         self.hilbert = hilbert
         self.rule = rule
-        self.n_chains = int(n_chains)
+        self.n_chains = n_chains
         self.sweep_size = hilbert.size if sweep_size is None else int(sweep_size)
-        self.reset_chains = bool(reset_chains)
+        self.reset_chains = reset_chains
+        self.chunk_size = chunk_size
         self.dtype = dtype
 
     @property
     def n_batches(self):
+        return self.n_chains
+
+    @property
+    def n_chains_per_rank(self):
         return self.n_chains
 
     def init_state(self, machine, params, seed=0):

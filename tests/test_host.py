@@ -815,3 +815,29 @@ def test_log_psi_to_array():
     raw = log_psi_to_array(torch.as_tensor(lp[:4] - 500.0), normalize=False).numpy()
     np.testing.assert_allclose(raw, np.exp(lp[:4] - 500.0), rtol=1e-14)
     assert log_psi_to_array(torch.zeros(3, dtype=torch.float32)).dtype == torch.float64
+
+
+def test_sampler_constructor_checks():
+    """metropolis.py:273-325 and base.py:139-154, before any device work."""
+    import netket_gb300 as nk
+    hi = nk.hilbert.Spin(0.5, 8)
+    s = nk.sampler.MetropolisLocal(hi)
+    assert s.n_chains == 16 and s.n_chains_per_rank == 16 and s.sweep_size == 8
+    assert s.machine_pow == 2 and s.chunk_size is None and not s.is_exact
+    assert nk.sampler.MetropolisLocal(hi, n_chains_per_rank=32).n_chains == 32
+    assert nk.sampler.MetropolisLocal(hi, n_chains=64, chunk_size=16).chunk_size == 16
+    assert nk.sampler.MetropolisLocal(hi, n_chains=8, chunk_size=16).n_chains == 8
+    with pytest.raises(ValueError, match="Cannot specify both"):
+        nk.sampler.MetropolisLocal(hi, n_chains=16, n_chains_per_rank=16)
+    with pytest.raises(ValueError, match="Chunk size must divide"):
+        nk.sampler.MetropolisLocal(hi, n_chains=48, chunk_size=32)
+    with pytest.raises(TypeError, match="reset_chains"):
+        nk.sampler.MetropolisLocal(hi, reset_chains=1)
+    with pytest.raises(ValueError, match="must be real"):
+        nk.sampler.MetropolisLocal(hi, machine_pow=2j)
+    with pytest.raises(ValueError, match="must be positive"):
+        nk.sampler.MetropolisLocal(hi, machine_pow=-1)
+    with pytest.raises(NotImplementedError, match="machine_pow"):
+        nk.sampler.MetropolisLocal(hi, machine_pow=1)
+    with pytest.raises(TypeError, match="MetropolisRule"):
+        nk.sampler.MetropolisSampler(hi, "local")
