@@ -67,6 +67,19 @@ class DiscreteOperator:
         return sp.csr_matrix((m.reshape(-1)[keep], (rows[keep], cols.reshape(-1)[keep])),
                              shape=(n, n))
 
+    def __pow__(self, power):
+        """``_abstract_operator.py:157-171``: repeated ``@`` for power >= 1."""
+        if not isinstance(power, int) or power < 0:
+            return NotImplemented
+        if power == 0:
+            raise NotImplementedError(f"__pow__(0) (identity) is not implemented for "
+                                      f"{type(self).__name__}. Use the identity constructor "
+                                      "of your operator type directly.")
+        result = self
+        for _ in range(power - 1):
+            result = result @ self
+        return result
+
     def to_dense(self):
         return self.to_sparse().toarray()
 
@@ -249,18 +262,58 @@ class LocalOperator(DiscreteOperator):
         return new
 
     def __add__(self, other):
-        new = self.copy()
+        """``_local_operator/base.py:296-332``: operators on another Hilbert
+        space do not add; the sum keeps the smaller ``mel_cutoff``."""
         if isinstance(other, LocalOperator):
+            if other.hilbert != self.hilbert:
+                return NotImplemented
+            new = self.copy()
+            new.mel_cutoff = min(self.mel_cutoff, other.mel_cutoff)
             for k, v in other._terms.items():
                 new._add(v, k)
             new.constant += other.constant
-        elif np.isscalar(other):
+            return new
+        if np.isscalar(other):
+            new = self.copy()
             new.constant += float(other)
-        else:
-            return NotImplemented
-        return new
+            return new
+        return NotImplemented
 
     __radd__ = __add__
+
+    def __rsub__(self, other):
+        return other + (-self)
+
+    def __truediv__(self, other):
+        if not np.isscalar(other):
+            raise TypeError("Only division by a scalar number is supported.")
+        if other == 0:
+            raise ValueError("Dividing by 0")
+        return self.__mul__(1.0 / other)
+
+    def transpose(self, *, concrete=False):
+        """Every term's matrix transposed (``_local_operator/base.py:263-271``;
+        returned concrete whatever ``concrete`` says: there are no lazy wrappers
+        here)."""
+        new = self.copy()
+        new._terms = {k: np.ascontiguousarray(v.T) for k, v in self._terms.items()}
+        return new
+
+    def conjugate(self, *, concrete=False):
+        return self.copy()  # real matrix elements
+
+    def conj(self, *, concrete=False):
+        return self.conjugate(concrete=concrete)
+
+    @property
+    def T(self):
+        return self.transpose()
+
+    @property
+    def H(self):
+        """The adjoint: the operator itself when hermitian, else its transpose
+        (real matrix elements)."""
+        return self if self.is_hermitian else self.transpose(concrete=True)
 
     def __mul__(self, s):
         if isinstance(s, LocalOperator):
@@ -409,6 +462,36 @@ class LocalOperator(DiscreteOperator):
                 f"locations, constant={self.constant})")
 
 
+def _pauli_mul_table():
+    """(a, b) -> (c, f) with a b = f c for single-site Pauli matrices."""
+    t = {}
+    for p in "IXYZ":
+        t["I", p] = (p, 1 + 0j)
+        t[p, "I"] = (p, 1 + 0j)
+        t[p, p] = ("I", 1 + 0j)
+    for a, b, c in (("X", "Y", "Z"), ("Y", "Z", "X"), ("Z", "X", "Y")):
+        t[a, b] = (c, 1j)
+        t[b, a] = (c, -1j)
+    return t
+
+
+_PAULI_MUL = _pauli_mul_table()
+
+
+def _reduce_strings(ops, w, n_sites):
+    """The PauliStrings reduction (``_pauli_strings/base.py:564-599``):
+    duplicate strings summed in sorted string order, weights within
+    ``np.isclose(., 0)`` of zero dropped (all dropped: the identity with 0)."""
+    uniq, inv = np.unique(ops, return_inverse=True)
+    if len(uniq) != len(ops):
+        w = np.array([np.sum(w[inv == i]) for i in range(len(uniq))], dtype=w.dtype)
+        ops = uniq
+    keep = ~np.isclose(w, 0)
+    if np.any(keep):
+        return ops[keep], w[keep]
+    return np.array(["I" * n_sites]), np.zeros(1, dtype=w.dtype)
+
+
 class PauliStrings(DiscreteOperator):
     """Sum of weighted Pauli strings (``netket/operator/_pauli_strings``), e.g.
     ``PauliStrings(hi, ["XXI", "ZZI"], [0.5, 1.0])``; character k of a string
@@ -442,17 +525,7 @@ class PauliStrings(DiscreteOperator):
         ops = np.asarray(operators, dtype=str)
         w = np.asarray([float(np.real(v)) for v in weights], dtype=np.float64)
         if len(ops):
-            # the constructor's reduction (_pauli_strings/base.py:61-137, 564-599):
-            # duplicates summed in sorted string order, near-zero weights dropped
-            uniq, inv = np.unique(ops, return_inverse=True)
-            if len(uniq) != len(ops):
-                w = np.array([np.sum(w[inv == i]) for i in range(len(uniq))])
-                ops = uniq
-            keep = ~np.isclose(w, 0)
-            if np.any(keep):
-                ops, w = ops[keep], w[keep]
-            else:
-                ops, w = np.array(["I" * hilbert.size]), np.zeros(1)
+            ops, w = _reduce_strings(ops, w, hilbert.size)
         self.operators = [str(o) for o in ops]
         self.weights = [float(v) for v in w]
         self.cutoff = float(cutoff)
@@ -460,9 +533,41 @@ class PauliStrings(DiscreteOperator):
         self._dev = {}
 
     # ------------------------------------------------------------ algebra
-    # (netket/operator/_pauli_strings/base.py:373-470): + concatenates and reduces
+    # (netket/operator/_pauli_strings/base.py:330-470): + concatenates and reduces
     # as the constructor does; a scalar adds the identity string; * scales the
-    # weights (no reduction); operator products are not supported here.
+    # weights (no reduction); @ multiplies string by string.
+    def __matmul__(self, other):
+        """Product of two sums of strings (``_pauli_strings/base.py:330-371,
+        522-660``): every pair (self's string major), site by site with
+        XY = iZ, YZ = iX, ZX = iY (reversed order: -i), weight w1 w2 times the
+        phase, then the constructor's reduction.  The reference switches to
+        complex weights when some product string has an odd number of Y; the
+        result is returned here when every reduced weight is real (imaginary
+        parts that cancel included) and refused otherwise."""
+        if not isinstance(other, PauliStrings):
+            return NotImplemented
+        if other.hilbert != self.hilbert:
+            raise ValueError(f"Can only multiply identical hilbert spaces (got A@B, "
+                             f"A={self.hilbert}, B={other.hilbert})")
+        ops, ws = [], []
+        for o1, w1 in zip(self.operators, self.weights):
+            for o2, w2 in zip(other.operators, other.weights):
+                phase = 1 + 0j
+                chars = []
+                for a, b in zip(o1, o2):
+                    c, f = _PAULI_MUL[a, b]
+                    chars.append(c)
+                    phase *= f
+                ops.append("".join(chars))
+                ws.append((w1 * w2) * phase)
+        ops, w = _reduce_strings(np.asarray(ops, dtype=str), np.asarray(ws, np.complex128),
+                                 self.hilbert.size)
+        if np.any(np.imag(w) != 0):
+            raise TypeError("PauliStrings @ PauliStrings gives complex weights here; they "
+                            "are not supported on this path")
+        return PauliStrings(self.hilbert, [str(o) for o in ops], np.real(w),
+                            cutoff=min(self.cutoff, other.cutoff))
+
     def _scaled(self, c):
         new = object.__new__(PauliStrings)
         DiscreteOperator.__init__(new, self.hilbert)
@@ -494,8 +599,8 @@ class PauliStrings(DiscreteOperator):
 
     def __mul__(self, other):
         if isinstance(other, DiscreteOperator):
-            raise TypeError("To multiply operators use the matrix multiplication operator @; "
-                            "it is not supported for PauliStrings on this path.")
+            raise TypeError("To multiply operators use the matrix`@` multiplication operator "
+                            "`@` instead of the element-wise multiplication operator `*`.")
         if np.isscalar(other):
             if np.iscomplexobj(np.asarray(other)) and np.imag(other) != 0:
                 raise TypeError("PauliStrings: complex weights are not supported on this path")

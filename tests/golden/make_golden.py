@@ -743,6 +743,76 @@ def gen_online_stats():
     np.savez_compressed(os.path.join(HERE, "online_stats.npz"), **out)
 
 
+def gen_pauli_products():
+    """PauliStrings @ PauliStrings for real weights (operator/_pauli_strings/
+    base.py:330-371, 501-660): the product string and phase per pair of strings,
+    op1-major pair order, then the duplicate reduction; and the predicate that
+    makes the reference switch to complex weights (an odd number of Y in some
+    product string)."""
+    import itertools
+    ns = {"np": np, "product": itertools.product,
+          "nkjax": types.SimpleNamespace(
+              is_complex_dtype=lambda d: np.issubdtype(np.dtype(d), np.complexfloating))}
+    load("operator/_pauli_strings/base.py",
+         ["_pauli_to_num", "_num_to_pauli", "_levi_term", "_apply_pauli_op_reduction",
+          "_split_string", "_make_new_pauli_string", "_remove_zero_weights",
+          "_reduce_pauli_string", "_will_matmul_produce_complex_coefficients", "_matmul"], ns)
+    rng = np.random.default_rng(47)
+    N = 6
+
+    def real_strings(k):
+        out = []
+        while len(out) < k:
+            s = "".join(rng.choice(list("IXYZ"), size=N))
+            if s.count("Y") % 2 == 0:
+                out.append(s)
+        return out
+
+    cases = {
+        "xx_yy": (["XXIIII", "YYIIII"], [1.0, 1.0], ["XXIIII", "YYIIII"], [1.0, -1.0]),
+        "square": (["ZZIIII", "XIIIII", "IXIIII"], [0.5, -1.0, 0.25],
+                   ["ZZIIII", "XIIIII", "IXIIII"], [0.5, -1.0, 0.25]),
+        "heis_bonds": (["XXIIII", "YYIIII", "ZZIIII"], [1.0, 1.0, 1.0],
+                       ["IXXIII", "IYYIII", "IZZIII"], [1.0, 1.0, 1.0]),
+        "complex_xz": (["XIIIII"], [1.0], ["ZIIIII"], [1.0]),
+    }
+    for k in range(6):
+        na, nb = int(rng.integers(1, 6)), int(rng.integers(1, 6))
+        cases[f"random{k}"] = (real_strings(na), list(rng.normal(size=na)),
+                               real_strings(nb), list(rng.normal(size=nb)))
+
+    def strings_from(alphabet, k):
+        return ["".join(rng.choice(list(alphabet), size=N)) for _ in range(k)]
+
+    # products that stay real: X/I strings, Z/I strings, YY pairs with X/I
+    # elsewhere, and a symmetric square whose imaginary cross terms cancel
+    for k in range(3):
+        na, nb = int(rng.integers(2, 6)), int(rng.integers(2, 6))
+        cases[f"x_only{k}"] = (strings_from("IX", na), list(rng.normal(size=na)),
+                               strings_from("IX", nb), list(rng.normal(size=nb)))
+        cases[f"z_only{k}"] = (strings_from("IZ", na), list(rng.normal(size=na)),
+                               strings_from("IZ", nb), list(rng.normal(size=nb)))
+        ya = ["YY" + s[2:] for s in strings_from("IX", na)]
+        yb = ["YY" + s[2:] for s in strings_from("IX", nb)]
+        cases[f"yy_pairs{k}"] = (ya, list(rng.normal(size=na)), yb, list(rng.normal(size=nb)))
+        sq = strings_from("IXZ", na)
+        wq = list(rng.normal(size=na))
+        cases[f"square{k}"] = (sq, wq, sq, wq)
+    out = {}
+    for name, (a_ops, a_w, b_ops, b_w) in cases.items():
+        ao, aw = ns["_reduce_pauli_string"](np.array(a_ops), np.array(a_w, dtype=np.float64))
+        bo, bw = ns["_reduce_pauli_string"](np.array(b_ops), np.array(b_w, dtype=np.float64))
+        cplx = bool(ns["_will_matmul_produce_complex_coefficients"](ao, bo))
+        out[name + "__a_ops"], out[name + "__a_w"] = np.array(a_ops), np.array(a_w, np.float64)
+        out[name + "__b_ops"], out[name + "__b_w"] = np.array(b_ops), np.array(b_w, np.float64)
+        out[name + "__complex"] = np.array(cplx)
+        dtype = np.complex128 if cplx else np.float64
+        ops, w = ns["_matmul"](ao, aw.astype(dtype), bo, bw.astype(dtype), dtype=dtype)
+        out[name + "__ops"] = np.asarray(ops)
+        out[name + "__weights"] = np.asarray(w)
+    np.savez_compressed(os.path.join(HERE, "pauli_products.npz"), **out)
+
+
 if __name__ == "__main__":
     edges = gen_edges()
     gen_ising(edges)
@@ -754,6 +824,7 @@ if __name__ == "__main__":
     gen_hamiltonian_rule_pauli()
     gen_ngd()
     gen_spring()
+    gen_pauli_products()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")

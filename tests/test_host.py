@@ -841,3 +841,83 @@ def test_sampler_constructor_checks():
         nk.sampler.MetropolisLocal(hi, machine_pow=1)
     with pytest.raises(TypeError, match="MetropolisRule"):
         nk.sampler.MetropolisSampler(hi, "local")
+
+
+def test_pauli_strings_product_golden(golden):
+    """PauliStrings @ PauliStrings against the reference's own _matmul
+    (pauli_products.npz, made by tests/golden/make_golden.py): strings and
+    weights equal where the reduced product is real (imaginary cross terms that
+    cancel included), refused where a weight stays imaginary; and the product's
+    matrix is the product of the matrices."""
+    import netket_gb300 as nk
+    g = golden("pauli_products")
+    names = sorted({k.split("__")[0] for k in g})
+    N = len(str(g[names[0] + "__a_ops"][0]))
+    hi = nk.hilbert.Spin(0.5, N)
+    n_real = n_refused = 0
+    for name in names:
+        A = nk.operator.PauliStrings(hi, list(g[name + "__a_ops"]), g[name + "__a_w"])
+        B = nk.operator.PauliStrings(hi, list(g[name + "__b_ops"]), g[name + "__b_w"])
+        w_ref = g[name + "__weights"]
+        if np.any(np.imag(w_ref) != 0):
+            with pytest.raises(TypeError, match="complex"):
+                A @ B
+            n_refused += 1
+            continue
+        C = A @ B
+        assert C.operators == [str(o) for o in g[name + "__ops"]], name
+        np.testing.assert_array_equal(np.asarray(C.weights), np.real(w_ref), err_msg=name)
+        dA = _dense_from_pauli(N, A.operators, A.weights)
+        dB = _dense_from_pauli(N, B.operators, B.weights)
+        np.testing.assert_allclose(_dense_from_pauli(N, C.operators, C.weights), dA @ dB,
+                                   atol=1e-12, err_msg=name)
+        n_real += 1
+    assert n_real >= 10 and n_refused >= 5
+    P = nk.operator.PauliStrings(hi, ["XX" + "I" * (N - 2), "ZZ" + "I" * (N - 2)], [1.0, 0.5])
+    np.testing.assert_allclose(_dense_from_pauli(N, (P ** 3).operators, (P ** 3).weights),
+                               np.linalg.matrix_power(_dense_from_pauli(N, P.operators,
+                                                                        P.weights), 3),
+                               atol=1e-12)
+    with pytest.raises(TypeError, match="@"):
+        P * P
+    with pytest.raises(NotImplementedError):
+        P ** 0
+    with pytest.raises(ValueError, match="identical hilbert"):
+        P @ nk.operator.PauliStrings(nk.hilbert.Spin(0.5, N + 1), "I" * (N + 1))
+
+
+def test_local_operator_rsub_div_transpose_adjoint():
+    """LocalOperator: scalar - op, op / scalar, transpose / T, conjugate, H
+    (_local_operator/base.py:263-340, _abstract_operator.py:56-64), adding an
+    operator on another Hilbert space fails, the sum keeps the smaller
+    mel_cutoff, and ** is repeated @."""
+    import netket_gb300 as nk
+    N = 3
+    hi = nk.hilbert.Spin(0.5, N)
+    rng = np.random.default_rng(8)
+    m = rng.normal(size=(4, 4))
+    A = nk.operator.LocalOperator(hi, [m], [[0, 2]], constant=0.5)
+    dA = _dense_from_local(N, list(A._terms.items()), A.constant)
+
+    def dense(op):
+        return _dense_from_local(N, list(op._terms.items()), op.constant)
+
+    np.testing.assert_allclose(dense(2.0 - A), 2.0 * np.eye(8) - dA, atol=1e-13)
+    np.testing.assert_allclose(dense(A / 4), dA / 4, atol=1e-13)
+    np.testing.assert_allclose(dense(A.transpose()), dA.T, atol=1e-13)
+    np.testing.assert_allclose(dense(A.T), dA.T, atol=1e-13)
+    np.testing.assert_allclose(dense(A.conjugate()), dA, atol=1e-13)
+    assert not A.is_hermitian
+    np.testing.assert_allclose(dense(A.H), dA.T, atol=1e-13)
+    S = A + A.T
+    assert S.is_hermitian and S.H is S
+    np.testing.assert_allclose(dense(A ** 3), np.linalg.matrix_power(dA, 3), atol=1e-10)
+    with pytest.raises(ValueError, match="Dividing by 0"):
+        A / 0
+    with pytest.raises(TypeError, match="scalar"):
+        A / A
+    other = nk.operator.LocalOperator(nk.hilbert.Spin(0.5, N + 1), [m], [[0, 1]])
+    with pytest.raises(TypeError):
+        A + other
+    B = nk.operator.LocalOperator(hi, [m], [[1, 2]], mel_cutoff=1e-6)
+    assert (A + B).mel_cutoff == min(A.mel_cutoff, 1e-6)
