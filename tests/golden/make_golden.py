@@ -128,6 +128,50 @@ def gen_edges():
     return out
 
 
+def gen_lattice_edges():
+    """get_nn_edges (graph/_lattice_edge_logic.py:102-137) and the site
+    positions (create_site_positions, :26-48) for lattices with non-unit basis
+    vectors and several sites per cell, plus hypercubic cases run through the
+    same general code path."""
+    ns = {"np": np, "cKDTree": cKDTree, "find": find, "triu": triu}
+    load("utils/float.py", ["comparable"], ns)
+    load("graph/_lattice_edge_logic.py",
+         ["create_site_positions", "site_to_idx", "create_padded_sites",
+          "get_naive_edges", "get_nn_edges"], ns)
+    hexb = [[1.0, 0.0], [0.5, 0.75 ** 0.5]]
+    honey = [[0.5, 0.5 / 3 ** 0.5], [1.0, 1.0 / 3 ** 0.5]]
+    kag = [[0.5, 0.0], [0.25, 0.75 ** 0.5 / 2], [0.75, 0.75 ** 0.5 / 2]]
+    cases = {
+        "triangular3": (hexb, [3, 3], None, [True, True], 1),
+        "triangular4x3_nnn": (hexb, [4, 3], None, [True, True], 2),
+        "triangular4_obc": (hexb, [4, 4], None, [False, False], 2),
+        "triangular5x4_mixed": (hexb, [5, 4], None, [True, False], 3),
+        "honeycomb3": (hexb, [3, 3], honey, [True, True], 1),
+        "honeycomb4_3rd": (hexb, [4, 4], honey, [True, True], 3),
+        "honeycomb3x4_obc": (hexb, [3, 4], honey, [False, True], 2),
+        "kagome3": (hexb, [3, 3], kag, [True, True], 1),
+        "kagome4_nnn": (hexb, [4, 4], kag, [True, True], 2),
+        "rect_two_site": ([[1.0, 0.0], [0.0, 1.5]], [4, 3], [[0.0, 0.0], [0.5, 0.75]],
+                          [True, True], 3),
+        "square5_via_general": ([[1.0, 0.0], [0.0, 1.0]], [5, 5], None, [True, True], 2),
+    }
+    out = {}
+    for name, (basis, extent, offsets, pbc, order) in cases.items():
+        basis = np.asarray(basis)
+        d = basis.shape[0]
+        offs = np.zeros((1, d)) if offsets is None else np.asarray(offsets)
+        e = ns["get_nn_edges"](basis, np.asarray(extent), offs, np.array(pbc), 1e-5, order)
+        _, pos = ns["create_site_positions"](basis, np.asarray(extent), offs)
+        out[name + "__edges"] = np.array(e, dtype=np.int64).reshape(-1, 3)
+        out[name + "__basis"] = basis
+        out[name + "__extent"] = np.array(extent, dtype=np.int64)
+        out[name + "__offsets"] = offs
+        out[name + "__pbc"] = np.array(pbc)
+        out[name + "__order"] = np.array(order)
+        out[name + "__positions"] = pos
+    np.savez_compressed(os.path.join(HERE, "lattice_edges.npz"), **out)
+
+
 # ---------------------------------------------------------------- operators
 def gen_ising(edges):
     ns = {"np": np}
@@ -825,6 +869,7 @@ if __name__ == "__main__":
     gen_ngd()
     gen_spring()
     gen_pauli_products()
+    gen_lattice_edges()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")

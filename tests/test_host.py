@@ -38,7 +38,7 @@ def test_product_lattice_edges_match_reference(golden, name):
     from netket_gb300 import graph
     g = golden("edges")
     meta = g[name + "__meta"]
-    L = graph.Lattice(list(meta[:-2]), bool(meta[-2]), int(meta[-1]))
+    L = graph.Grid(list(meta[:-2]), pbc=bool(meta[-2]), max_neighbor_order=int(meta[-1]))
     np.testing.assert_array_equal(np.array(L.edges(return_color=True)).reshape(-1, 3), g[name])
 
 
@@ -921,3 +921,46 @@ def test_local_operator_rsub_div_transpose_adjoint():
         A + other
     B = nk.operator.LocalOperator(hi, [m], [[1, 2]], mel_cutoff=1e-6)
     assert (A + B).mel_cutoff == min(A.mel_cutoff, 1e-6)
+
+
+def test_general_lattices_golden(golden):
+    """Lattice with basis vectors / site offsets, Triangular, Honeycomb, Kagome:
+    edges (order and colours) and site positions equal the reference's own
+    get_nn_edges / create_site_positions (lattice_edges.npz, made by
+    tests/golden/make_golden.py), hypercubic cases included."""
+    import warnings
+    import netket_gb300 as nk
+    g = golden("lattice_edges")
+    names = sorted({k.split("__")[0] for k in g})
+    for name in names:
+        offs = g[name + "__offsets"]
+        lat = nk.graph.Lattice(g[name + "__basis"], list(g[name + "__extent"]),
+                               pbc=[bool(b) for b in g[name + "__pbc"]],
+                               site_offsets=None if not np.any(offs) and len(offs) == 1 else offs,
+                               max_neighbor_order=int(g[name + "__order"]))
+        got = np.array(lat.edges(return_color=True), dtype=np.int64).reshape(-1, 3)
+        np.testing.assert_array_equal(got, g[name + "__edges"], err_msg=name)
+        np.testing.assert_allclose(lat.positions, g[name + "__positions"], atol=1e-12,
+                                   err_msg=name)
+        assert lat.n_nodes == len(g[name + "__positions"])
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        t = nk.graph.Triangular([4, 3], max_neighbor_order=2)
+    np.testing.assert_array_equal(np.array(t.edges(return_color=True)),
+                                  g["triangular4x3_nnn__edges"])
+    h = nk.graph.Honeycomb([4, 4], max_neighbor_order=3)
+    np.testing.assert_array_equal(np.array(h.edges(return_color=True)),
+                                  g["honeycomb4_3rd__edges"])
+    k = nk.graph.Kagome([3, 3])
+    np.testing.assert_array_equal(np.array(k.edges(return_color=True)), g["kagome3__edges"])
+    assert h.n_nodes == 32 and k.n_nodes == 27
+    with pytest.warns(UserWarning, match="only 2 cells"):
+        nk.graph.Triangular([2, 3])
+    with pytest.raises(ValueError, match="pbc"):
+        nk.graph.Lattice(np.eye(2), [3, 3], pbc=[True])
+    with pytest.raises(ValueError, match="extent"):
+        nk.graph.Lattice(np.eye(2), [3, 3, 3])
+    # a Heisenberg model on the triangular lattice is an ordinary LocalOperator
+    hi = nk.hilbert.Spin(0.5, t.n_nodes)
+    H = nk.operator.Heisenberg(hi, t, J=[1.0, 0.3])
+    assert H.max_conn_size == 1 + t.n_edges
