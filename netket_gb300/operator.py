@@ -16,6 +16,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from .graph import Graph
 
 
 def _as_x(x, N):
@@ -701,17 +702,42 @@ class PauliStrings(DiscreteOperator):
         return f"PauliStrings(hilbert={self.hilbert}, n_strings={len(self.operators)})"
 
 
-def GraphOperator(hilbert, graph, site_ops=(), bond_ops=(), bond_ops_colors=()):
+def check_acting_on_subspace(acting_on_subspace, hilbert, graph):
+    """Graph node -> Hilbert site map (``netket/operator/_graph_operator.py:29-44``):
+    None is the identity, an int ``start`` maps node i to start + i, a list is
+    the map itself (one entry per node)."""
+    if acting_on_subspace is None:
+        return list(range(hilbert.size))
+    if isinstance(acting_on_subspace, (int, np.integer)) and not isinstance(acting_on_subspace,
+                                                                            bool):
+        return [int(acting_on_subspace) + i for i in range(graph.n_nodes)]
+    if isinstance(acting_on_subspace, list):
+        if len(acting_on_subspace) != graph.n_nodes:
+            raise ValueError("acting_on_subspace must be a list of length graph.n_nodes")
+        return acting_on_subspace
+    raise TypeError("acting_on_subspace must be a list or single integer")
+
+
+def _check_real_dtype(dtype, name):
+    if dtype is not None and np.issubdtype(np.dtype(dtype), np.complexfloating):
+        raise TypeError(f"{name}: complex matrix elements are not supported on this path")
+
+
+def GraphOperator(hilbert, graph, site_ops=(), bond_ops=(), bond_ops_colors=(), dtype=None, *,
+                  acting_on_subspace=None):
     """Sum of site operators on every node and bond operators on every edge
     (coloured edges select their operator), NetKet's term order
-    (``netket/operator/_graph_operator.py:103-145``)."""
+    (``netket/operator/_graph_operator.py:47-145``); node i acts on site
+    ``acting_on_subspace[i]``."""
+    _check_real_dtype(dtype, "GraphOperator")
+    sites = check_acting_on_subspace(acting_on_subspace, hilbert, graph)
     if len(site_ops) == 0 and len(bond_ops) == 0:
         raise ValueError("Must input at least site_ops or bond_ops.")
     ops, aon = [], []
     for i in range(graph.n_nodes):
         for so in site_ops:
             ops.append(so)
-            aon.append([i])
+            aon.append([sites[i]])
     if len(bond_ops_colors) > 0:
         if len(bond_ops) != len(bond_ops_colors):
             raise ValueError("The sizes of bond_ops and bond_ops_colors do not match.")
@@ -719,33 +745,43 @@ def GraphOperator(hilbert, graph, site_ops=(), bond_ops=(), bond_ops_colors=()):
             for c, bc in enumerate(bond_ops_colors):
                 if bc == color:
                     ops.append(bond_ops[c])
-                    aon.append([u, v])
-    else:
+                    aon.append([sites[u], sites[v]])
+    elif len(bond_ops) > 0:
         if len(bond_ops) != 1:
             raise ValueError("without colours exactly one bond operator is expected")
         for u, v in graph.edges():
             ops.append(bond_ops[0])
-            aon.append([u, v])
+            aon.append([sites[u], sites[v]])
     return LocalOperator(hilbert, ops, aon)
 
 
-def Heisenberg(hilbert, graph, J=1.0, sign_rule=None):
-    """``J (Sz Sz +/- 2 (S+S- + S-S+))`` per bond (``netket/operator/_heisenberg.py``);
+def Heisenberg(hilbert, graph, J=1.0, sign_rule=None, dtype=None, *, acting_on_subspace=None):
+    """``J (Sz Sz +/- 2 (S+S- + S-S+))`` per bond (``netket/operator/_heisenberg.py:31-132``);
     the minus sign applies Marshall's sign rule (default: bipartite graph for a
-    scalar J, ``False`` per colour for a J list)."""
+    scalar J, ``False`` per colour for a J list; refused on a graph, or a
+    colour's subgraph, that is not bipartite)."""
     if isinstance(J, (list, tuple)):
         if len(J) != max(graph.edge_colors) + 1:
             raise ValueError("one coupling per edge colour is expected")
         if sign_rule is None:
             sign_rule = [False] * len(J)
+        else:
+            if len(sign_rule) != len(J):
+                raise ValueError("one sign_rule entry per coupling is expected")
+            for i in range(len(J)):
+                if sign_rule[i] and not Graph(graph.edges(filter_color=i)).is_bipartite():
+                    raise ValueError("sign_rule=True specified for a non-bipartite lattice")
         bond_ops = [J[i] * (SZSZ - EXCHANGE if sign_rule[i] else SZSZ + EXCHANGE)
                     for i in range(len(J))]
-        return GraphOperator(hilbert, graph, bond_ops=bond_ops, bond_ops_colors=list(range(len(J))))
+        return GraphOperator(hilbert, graph, bond_ops=bond_ops, bond_ops_colors=list(range(len(J))),
+                             dtype=dtype, acting_on_subspace=acting_on_subspace)
     if sign_rule is None:
         sign_rule = graph.is_bipartite()
     elif sign_rule and not graph.is_bipartite():
         raise ValueError("sign_rule=True specified for a non-bipartite lattice")
-    return GraphOperator(hilbert, graph, bond_ops=[J * (SZSZ - EXCHANGE if sign_rule else SZSZ + EXCHANGE)])
+    return GraphOperator(hilbert, graph,
+                         bond_ops=[J * (SZSZ - EXCHANGE if sign_rule else SZSZ + EXCHANGE)],
+                         dtype=dtype, acting_on_subspace=acting_on_subspace)
 
 
 # -------------------------------------------------------------------- spin

@@ -964,3 +964,42 @@ def test_general_lattices_golden(golden):
     hi = nk.hilbert.Spin(0.5, t.n_nodes)
     H = nk.operator.Heisenberg(hi, t, J=[1.0, 0.3])
     assert H.max_conn_size == 1 + t.n_edges
+
+
+def test_graph_operator_subspace_and_sign_rule_checks():
+    """acting_on_subspace (_graph_operator.py:29-44): node i of a smaller graph
+    acts on site map[i]; the J-list sign rule is checked per colour subgraph
+    (_heisenberg.py:86-100); complex dtypes are refused."""
+    import netket_gb300 as nk
+    hi = nk.hilbert.Spin(0.5, 6)
+    g = nk.graph.Chain(3, pbc=False)
+    H = nk.operator.Heisenberg(hi, g, acting_on_subspace=2)
+    assert list(H._terms) == [(2, 3), (3, 4)]
+    H2 = nk.operator.Heisenberg(hi, g, acting_on_subspace=[5, 0, 3])
+    assert list(H2._terms) == [(0, 5), (0, 3)]
+    sx = np.array([[0.0, 1.0], [1.0, 0.0]])
+    G = nk.operator.GraphOperator(hi, g, site_ops=[sx], acting_on_subspace=[1, 4, 5])
+    assert sorted(G._terms) == [(1,), (4,), (5,)]
+    with pytest.raises(ValueError, match="length graph.n_nodes"):
+        nk.operator.Heisenberg(hi, g, acting_on_subspace=[0, 1])
+    with pytest.raises(TypeError, match="list or single integer"):
+        nk.operator.Heisenberg(hi, g, acting_on_subspace=(0, 1, 2))
+    with pytest.raises(TypeError, match="complex"):
+        nk.operator.Heisenberg(hi, g, dtype=np.complex128)
+    # J list with nn + nnn colours: on an even periodic square lattice both
+    # colour subgraphs are bipartite (x mod 2 colours the nnn bonds too), on an
+    # odd one neither is
+    hs = nk.hilbert.Spin(0.5, 16)
+    sq4 = nk.graph.Square(4, max_neighbor_order=2)
+    nk.operator.Heisenberg(hs, sq4, J=[1.0, 0.5], sign_rule=[True, True])
+    sq5 = nk.graph.Square(5, max_neighbor_order=2)
+    h5 = nk.hilbert.Spin(0.5, 25)
+    nk.operator.Heisenberg(h5, sq5, J=[1.0, 0.5], sign_rule=[False, False])
+    with pytest.raises(ValueError, match="non-bipartite"):
+        nk.operator.Heisenberg(h5, sq5, J=[1.0, 0.5], sign_rule=[False, True])
+    with pytest.raises(ValueError, match="one sign_rule entry"):
+        nk.operator.Heisenberg(hs, sq4, J=[1.0, 0.5], sign_rule=[True])
+    tri = nk.graph.Triangular([3, 3])
+    with pytest.raises(ValueError, match="non-bipartite"):
+        nk.operator.Heisenberg(nk.hilbert.Spin(0.5, 9), tri, sign_rule=True)
+    assert not tri.is_bipartite()
