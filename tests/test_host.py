@@ -1003,3 +1003,38 @@ def test_graph_operator_subspace_and_sign_rule_checks():
     with pytest.raises(ValueError, match="non-bipartite"):
         nk.operator.Heisenberg(nk.hilbert.Spin(0.5, 9), tri, sign_rule=True)
     assert not tri.is_bipartite()
+
+
+def test_exact_diagonalisation_wrappers():
+    """lanczos_ed (with and without matrix_free, with eigenvectors) and full_ed on
+    an operator whose matrix is a CPU TFIM from the oracle."""
+    import scipy.sparse as sp
+    from netket_gb300 import exact
+    from oracle import exact as oex
+    from oracle import operator as oop
+    N = 8
+    edges = np.array([(i, (i + 1) % N) for i in range(N)])
+
+    class CpuOp:
+        def to_sparse(self):
+            x = 1 - 2 * ((np.arange(2 ** N)[:, None] >> np.arange(N - 1, -1, -1)) & 1)
+            return sp.csr_matrix(oex.to_sparse_from_conn(
+                lambda s: oop.ising_get_conn_padded(s, edges, 1.0, 1.0), x.astype(np.int8)))
+
+        def to_dense(self):
+            return self.to_sparse().toarray()
+
+    op = CpuOp()
+    ref = np.linalg.eigvalsh(op.to_dense())
+    np.testing.assert_allclose(exact.lanczos_ed(op, k=3), ref[:3], rtol=1e-10)
+    np.testing.assert_allclose(exact.lanczos_ed(op, k=2, matrix_free=True), ref[:2], rtol=1e-10)
+    w, v = exact.lanczos_ed(op, k=2, compute_eigenvectors=True)
+    np.testing.assert_allclose(w, ref[:2], rtol=1e-10)
+    np.testing.assert_allclose(op.to_dense() @ v, v * w, atol=1e-8)
+    np.testing.assert_allclose(exact.full_ed(op), ref, rtol=1e-12, atol=1e-12)
+    w2, v2 = exact.full_ed(op, compute_eigenvectors=True)
+    np.testing.assert_allclose(w2, ref, rtol=1e-12, atol=1e-12)
+    # the example in the reference's lanczos_ed docstring (8-site Ising, h = 1)
+    np.testing.assert_allclose(exact.lanczos_ed(op, k=3), [-10.25166179, -10.05467898,
+                                                          -8.69093921], atol=1e-8)
+    assert abs(ref[0] - oex.tfim_ground_energy(N, 1.0, 1.0)) < 1e-9
