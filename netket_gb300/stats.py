@@ -14,8 +14,35 @@ from . import _native as nat
 from .kernels import stats_device
 
 
+_ALIASES = {"Mean": "mean", "Variance": "variance", "Sigma": "error_of_mean", "R": "R_hat",
+            "TauCorr": "tau_corr", "TauCorrMax": "tau_corr_max"}
+
+
+def _format_mean_error(value, err, var):
+    """"mean ± error [σ²=variance" with the mean shown to the error's first two
+    significant digits, in scientific notation for small numbers, as
+    ``netket/stats/mc_stats.py:26-74`` prints ``Stats``."""
+    if not math.isfinite(abs(value)) or not math.isfinite(err):
+        return f"{value:.2e} ± {err:.2e} [σ²={var:.1e}"
+    if err == 0.0:
+        return f"{value:.3e} [σ²={var:.1e}"
+    if abs(value) + abs(err) < 1e-2 or abs(err) <= 1e-7:
+        ref = value if value != 0 else err
+        e_val = int(math.floor(math.log10(abs(ref))))
+        digits = max(e_val - int(math.floor(math.log10(err))), 0) + 1
+        scale = 10.0 ** e_val
+        return (f"{value / scale:.{digits}f}".rjust(5) + " ± " +
+                f"{err / scale:.{digits}f}".rjust(5) + " e" + f"{ref:e}".split("e")[1] +
+                f" [σ²={var:.1e}")
+    decimals = 15 if err < 1e-15 else max(int(math.ceil(-math.log10(err))), 0) + 1
+    return f"{value:.{decimals}f} ± {err:.{decimals}f} [σ²={var:.1e}"
+
+
 class Stats:
-    """mean, error_of_mean, variance, tau_corr, R_hat (``netket/stats/mc_stats.py:85-181``)."""
+    """mean, error_of_mean, variance, tau_corr, R_hat (``netket/stats/mc_stats.py:85-181``),
+    with the reference's alias names (``Mean``, ``Sigma``, ``R``, ...)."""
+
+    tau_corr_max = float("nan")  # only the FFT autocorrelation estimator sets it
 
     def __init__(self, mean=float("nan"), error_of_mean=float("nan"), variance=float("nan"),
                  tau_corr=float("nan"), R_hat=float("nan")):
@@ -24,6 +51,27 @@ class Stats:
         self.variance = variance
         self.tau_corr = tau_corr
         self.R_hat = R_hat
+
+    def __getattr__(self, name):
+        if name in _ALIASES:
+            return getattr(self, _ALIASES[name])
+        raise AttributeError(f"'Stats' object has no attribute '{name}'")
+
+    @property
+    def shape(self):
+        return ()
+
+    def replace(self, **kw):
+        d = dict(mean=self.mean, error_of_mean=self.error_of_mean, variance=self.variance,
+                 tau_corr=self.tau_corr, R_hat=self.R_hat)
+        d.update(kw)
+        return Stats(**d)
+
+    def real(self):
+        return self.replace(mean=float(np.real(self.mean)))
+
+    def imag(self):
+        return self.replace(mean=float(np.imag(self.mean)))
 
     @classmethod
     def from_array(cls, a):
@@ -44,10 +92,8 @@ class Stats:
         return self.to_dict()[k]
 
     def __repr__(self):
-        def fmt(v):
-            return "nan" if not math.isfinite(v) else f"{v:.4g}"
-        return (f"{self.mean:.6g} ± {fmt(self.error_of_mean)} [σ²={fmt(self.variance)}, "
-                f"R̂={self.R_hat:.4f}]")
+        ext = "" if math.isnan(self.R_hat) else f", R̂={self.R_hat:.3f}"
+        return _format_mean_error(self.mean, self.error_of_mean, self.variance) + ext + "]"
 
 
 def _plain_rhat():

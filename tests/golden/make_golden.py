@@ -857,6 +857,27 @@ def gen_pauli_products():
     np.savez_compressed(os.path.join(HERE, "pauli_products.npz"), **out)
 
 
+def gen_stats_format():
+    """Stats printing: _format_main_string / _format_scientific_notation
+    (stats/mc_stats.py:26-74) on means and errors spanning the branches (large
+    and small values, tiny errors, zero error, non-finite)."""
+    import math
+    ns = {"np": np, "math": math}
+    load("stats/mc_stats.py", ["_format_main_string", "_format_scientific_notation"], ns)
+    rng = np.random.default_rng(5)
+    rows = [(-10.2516, 0.0123, 0.5), (1e-4, 2.3e-6, 1e-9), (3.0, 0.0, 0.0),
+            (float("nan"), float("nan"), float("nan")), (-43.88123, 0.00071, 1.7),
+            (0.5, 1e-8, 1e-12), (123456.7, 89.1, 3e4), (-2e-3, 4e-3, 1e-5), (1.0, 1e-16, 0.0),
+            (float("inf"), 0.1, 1.0), (-7.25, 2.5, 6.0)]
+    for _ in range(20):
+        rows.append((float(rng.normal() * 10.0 ** rng.integers(-5, 5)),
+                     float(abs(rng.normal()) * 10.0 ** rng.integers(-9, 2)),
+                     float(abs(rng.normal()))))
+    vals = np.array(rows, dtype=np.float64)
+    strs = np.array([ns["_format_main_string"](*r) for r in rows])
+    np.savez_compressed(os.path.join(HERE, "stats_format.npz"), values=vals, strings=strs)
+
+
 if __name__ == "__main__":
     edges = gen_edges()
     gen_ising(edges)
@@ -870,6 +891,7 @@ if __name__ == "__main__":
     gen_spring()
     gen_pauli_products()
     gen_lattice_edges()
+    gen_stats_format()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")

@@ -1038,3 +1038,21 @@ def test_exact_diagonalisation_wrappers():
     np.testing.assert_allclose(exact.lanczos_ed(op, k=3), [-10.25166179, -10.05467898,
                                                           -8.69093921], atol=1e-8)
     assert abs(ref[0] - oex.tfim_ground_energy(N, 1.0, 1.0)) < 1e-9
+
+
+def test_stats_printing_and_aliases(golden):
+    """Stats prints as the reference's _format_main_string (stats_format.npz,
+    made by tests/golden/make_golden.py) and answers to its alias names."""
+    from netket_gb300.stats import Stats, _format_mean_error
+    g = golden("stats_format")
+    for v, s in zip(g["values"], g["strings"]):
+        assert _format_mean_error(*v) == str(s)
+    st = Stats(-1.5, 0.02, 0.3, 1.5, 1.01)
+    assert repr(st) == _format_mean_error(-1.5, 0.02, 0.3) + ", R̂=1.010]"
+    assert repr(Stats(1.0, 0.1, 0.2)) == _format_mean_error(1.0, 0.1, 0.2) + "]"
+    assert (st.Mean, st.Sigma, st.Variance, st.R, st.TauCorr) == (-1.5, 0.02, 0.3, 1.01, 1.5)
+    assert np.isnan(st.tau_corr_max) and np.isnan(st.TauCorrMax) and st.shape == ()
+    assert st.replace(mean=2.0).mean == 2.0 and st.replace(mean=2.0).Sigma == 0.02
+    assert st.real().mean == -1.5 and st.imag().mean == 0.0
+    with pytest.raises(AttributeError):
+        st.nothing
