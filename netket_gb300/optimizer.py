@@ -3,10 +3,13 @@
 * ``Sgd(learning_rate)``: ``optax.sgd`` as NetKet wraps it
   (``netket/optimizer/__init__.py:33-60``): ``theta <- theta - lr * update``,
   applied by the ``vmck_sgd`` kernel on the FP64 master parameters.
-* ``SR(diag_shift)``: stochastic reconfiguration with the dense QGT
-  ``S = O_L^T O_L`` (``netket/optimizer/sr.py:62-216``,
-  ``netket/optimizer/qgt/qgt_jacobian_dense.py``) solved by Cholesky with the
-  pinv_smooth fallback.
+* ``SR(qgt, solver, diag_shift=)``: stochastic reconfiguration
+  (``netket/optimizer/sr.py:62-216``) with the QGT chosen as NetKet's
+  ``QGTAuto`` chooses it for an RBM (``netket/optimizer/qgt/default.py:58-97``):
+  ``QGTOnTheFly`` solved by conjugate gradients unless a dense solver is given,
+  else the dense ``S = O_L^T O_L`` (``qgt_jacobian_dense.py``) solved by
+  Cholesky with the pinv_smooth fallback.
+* ``qgt``: ``QGTAuto``, ``QGTOnTheFly``, ``QGTJacobianDense`` select the form.
 * ``solver``: the dense solvers of ``netket/optimizer/solver/solvers.py``
   (``cholesky``, ``cholesky_with_fallback``, ``pinv_smooth``) on device tensors.
 """
@@ -40,23 +43,72 @@ def _flat(tree_or_flat, model):
     return model.flatten(tree_or_flat)
 
 
+class QGTAuto:
+    """Marker: the QGT form NetKet's heuristic picks (``qgt/default.py:58-97``)."""
+
+
+class QGTOnTheFly:
+    """Marker: the matrix-free QGT, S v by a JVP and a VJP per product."""
+
+
+class QGTJacobianDense:
+    """Marker: the dense QGT S = O_L^T O_L."""
+
+
+def _qgt_kind(q):
+    if q is None or q is QGTAuto or isinstance(q, QGTAuto) or q == "auto":
+        return "auto"
+    if q is QGTOnTheFly or isinstance(q, QGTOnTheFly) or q == "onthefly":
+        return "onthefly"
+    if q is QGTJacobianDense or isinstance(q, QGTJacobianDense) or q == "dense":
+        return "dense"
+    raise ValueError(f"qgt must be QGTAuto, QGTOnTheFly or QGTJacobianDense (or 'auto', "
+                     f"'onthefly', 'dense'), not {q!r}")
+
+
+def _solver_kind(s):
+    if s is None or s == "cg":
+        return "cg"
+    if s == "cholesky" or s is solve_with_fallback:
+        return "dense"
+    if s is _cholesky or s is _pinv_smooth:
+        raise NotImplementedError("SR solves the dense QGT with cholesky_with_fallback; "
+                                  "plain cholesky / pinv_smooth are VMC_SR(linear_solver=) "
+                                  "choices")
+    raise NotImplementedError(f"SR: solver {s!r} is not supported (cg, or the dense "
+                              "optimizer.solver.cholesky_with_fallback)")
+
+
 class SR:
-    """Preconditioner ``(vstate, grad, step) -> dp``.
+    """Preconditioner ``(vstate, grad, step) -> dp``
+    (``netket/optimizer/sr.py:118-216``).
 
-    ``qgt="dense"`` (default here): the dense QGT solved by Cholesky with the
-    pinv_smooth fallback.  ``qgt="onthefly"``: ``QGTOnTheFly`` with conjugate
-    gradients (``solver="cg"``, ``tol``, ``maxiter``), NetKet's own default for an
-    RBM; as in NetKet (``solver_restart=False``) CG starts from the previous
-    step's solution."""
+    The QGT form follows ``QGTAuto`` for an RBM (three parameter leaves):
+    ``QGTOnTheFly`` with conjugate gradients (``tol``, ``maxiter``; as in NetKet
+    with ``solver_restart=False``, CG starts from the previous step's
+    solution) unless a dense solver (``optimizer.solver.cholesky_with_fallback``
+    or ``"cholesky"``) is given, in which case the dense QGT is
+    Cholesky-solved with the pinv_smooth fallback.  ``qgt=QGTJacobianDense``
+    always takes the dense form (solved the same way), ``qgt=QGTOnTheFly`` the
+    matrix-free one.  ``diag_scale`` and holomorphic SR are not implemented."""
 
-    def __init__(self, diag_shift=0.01, *, jac_dtype=torch.float64, qgt="dense", solver="cholesky",
-                 tol=1e-5, maxiter=None, solver_restart=False):
-        if qgt not in ("dense", "onthefly"):
-            raise ValueError(f"qgt must be 'dense' or 'onthefly', not {qgt!r}")
+    def __init__(self, qgt=None, solver=None, *, diag_shift=0.01, diag_scale=None,
+                 solver_restart=False, holomorphic=None, jac_dtype=torch.float64, tol=1e-5,
+                 maxiter=None):
+        if diag_scale is not None:
+            raise NotImplementedError("SR: diag_scale is not implemented")
+        if holomorphic:
+            raise NotImplementedError("SR: holomorphic SR is not implemented (real RBM path)")
+        kind, skind = _qgt_kind(qgt), _solver_kind(solver)
+        if kind == "auto":
+            kind = "dense" if skind == "dense" else "onthefly"
+        if kind == "onthefly" and skind == "dense":
+            raise ValueError("QGTOnTheFly is solved iteratively; a dense solver needs "
+                             "QGTJacobianDense")
         self.diag_shift = diag_shift
         self.jac_dtype = jac_dtype
-        self.qgt = qgt
-        self.solver = "cg" if qgt == "onthefly" else solver
+        self.qgt = kind
+        self.solver = "cg" if kind == "onthefly" else "cholesky"
         self.tol, self.maxiter, self.solver_restart = tol, maxiter, solver_restart
         self._x0 = None
         self.info = None
@@ -97,3 +149,6 @@ def _pinv_smooth(A, b, rtol=1e-14, rtol_smooth=1e-14):
 
 solver = types.SimpleNamespace(cholesky=_cholesky, cholesky_with_fallback=solve_with_fallback,
                                pinv_smooth=_pinv_smooth)
+
+qgt = types.SimpleNamespace(QGTAuto=QGTAuto, QGTOnTheFly=QGTOnTheFly,
+                            QGTJacobianDense=QGTJacobianDense)

@@ -76,7 +76,7 @@ def test_tfim_chain16_vmc_sr_converges(nk):
     vs = nk.vqs.MCState(nk.sampler.MetropolisLocal(hi, n_chains=16), nk.models.RBM(alpha=1),
                         n_samples=1008, n_discard_per_chain=32, seed=0, precision="fp64")
     drv = nk.driver.VMC(H, nk.optimizer.Sgd(0.01), variational_state=vs,
-                        preconditioner=nk.optimizer.SR(diag_shift=0.01))
+                        preconditioner=nk.optimizer.SR(qgt="dense", diag_shift=0.01))
     log = nk.logging.RuntimeLog()
     drv.run(300, out=log)
     tail = log["Energy"]["Mean"][-50:]
@@ -147,7 +147,7 @@ def test_checkpoint_resume_continues_chains_exactly(nk):
         vs = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=g, n_chains=32),
                             nk.models.RBM(alpha=1), n_samples=256, seed=3, precision="fp64")
         drv = nk.driver.VMC(H, nk.optimizer.Sgd(0.02), variational_state=vs,
-                            preconditioner=nk.optimizer.SR(diag_shift=0.01))
+                            preconditioner=nk.optimizer.SR(qgt="dense", diag_shift=0.01))
         return vs, drv
     vs, drv = make()
     drv.run(3)

@@ -1056,3 +1056,30 @@ def test_stats_printing_and_aliases(golden):
     assert st.real().mean == -1.5 and st.imag().mean == 0.0
     with pytest.raises(AttributeError):
         st.nothing
+
+
+def test_sr_qgt_selection():
+    """SR picks the QGT form as QGTAuto does for an RBM (qgt/default.py:58-97):
+    on the fly with CG unless a dense solver is given; explicit forms win."""
+    import netket_gb300 as nk
+    o = nk.optimizer
+    assert (o.SR().qgt, o.SR().solver) == ("onthefly", "cg")
+    assert o.SR(diag_shift=0.1).diag_shift == 0.1
+    assert o.SR(solver=o.solver.cholesky_with_fallback).qgt == "dense"
+    assert o.SR(o.qgt.QGTAuto, "cholesky").qgt == "dense"
+    assert o.SR(o.qgt.QGTJacobianDense).qgt == "dense"
+    assert o.SR(qgt=o.qgt.QGTJacobianDense()).solver == "cholesky"
+    assert o.SR(o.qgt.QGTOnTheFly, solver_restart=True).solver_restart
+    assert o.SR(qgt="dense").qgt == "dense" and o.SR(qgt="onthefly").qgt == "onthefly"
+    with pytest.raises(ValueError, match="dense solver"):
+        o.SR(o.qgt.QGTOnTheFly, o.solver.cholesky_with_fallback)
+    with pytest.raises(ValueError, match="qgt must be"):
+        o.SR(qgt="sparse")
+    with pytest.raises(NotImplementedError, match="diag_scale"):
+        o.SR(diag_scale=0.01)
+    with pytest.raises(NotImplementedError, match="holomorphic"):
+        o.SR(holomorphic=True)
+    with pytest.raises(NotImplementedError, match="linear_solver"):
+        o.SR(solver=o.solver.pinv_smooth)
+    with pytest.raises(NotImplementedError, match="not supported"):
+        o.SR(solver=lambda A, b: b)
