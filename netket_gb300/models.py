@@ -7,19 +7,60 @@ Parameters follow NetKet's pytree ``{"Dense": {"bias": (M,), "kernel": (N, M)},
 (row-major), visible_bias.  On the device they live in one flat buffer in that
 order, which is the layout every kernel takes.
 """
+import numpy as np
 import torch
 
 from . import _native as nat
 
 
+def _real_param_dtype(dt):
+    """torch.float64 / torch.float32 from any spelling NetKet scripts use
+    (``float``, ``np.float64``, ``"float32"``, a torch dtype); complex and
+    other types are refused."""
+    if isinstance(dt, torch.dtype):
+        if dt in (torch.float64, torch.float32):
+            return dt
+        raise NotImplementedError(f"RBM: param_dtype {dt} is not supported (float64 / float32)")
+    try:
+        npdt = np.dtype(dt)
+    except TypeError as err:
+        raise ValueError(f"RBM: param_dtype {dt!r} is not a dtype") from err
+    if npdt == np.float64:
+        return torch.float64
+    if npdt == np.float32:
+        return torch.float32
+    if np.issubdtype(npdt, np.complexfloating):
+        raise NotImplementedError("RBM: complex parameters are not supported (real RBM path)")
+    raise NotImplementedError(f"RBM: param_dtype {npdt} is not supported (float64 / float32)")
+
+
 class RBM:
+    """``alpha``, ``param_dtype`` (float64 or float32, any spelling) and the two
+    bias switches as in ``netket/models/rbm.py:33-56``; the activation is
+    log_cosh.  Parameters start Normal(0, std) per leaf (NetKet's
+    ``normal(stddev=0.01)`` initialisers); ``*_init_std`` set the three
+    standard deviations.  JAX initialiser functions, another activation and
+    ``precision`` have no meaning here and are refused."""
+
     def __init__(self, alpha=1, param_dtype=torch.float64, use_hidden_bias=True,
                  use_visible_bias=True, kernel_init_std=0.01, hidden_bias_init_std=0.01,
-                 visible_bias_init_std=0.01):
+                 visible_bias_init_std=0.01, *, activation=None, precision=None,
+                 kernel_init=None, hidden_bias_init=None, visible_bias_init=None):
         if not (use_hidden_bias and use_visible_bias):
             raise NotImplementedError("the RBM kernels take both biases")
+        if activation is not None and getattr(activation, "__name__", "") != "log_cosh":
+            raise NotImplementedError("RBM: only the log_cosh activation is implemented")
+        if precision is not None:
+            raise NotImplementedError("RBM: precision= selects JAX matmul precision; use "
+                                      "MCState(precision=...) here")
+        if any(f is not None for f in (kernel_init, hidden_bias_init, visible_bias_init)):
+            raise NotImplementedError("RBM: JAX initialiser functions are not supported; "
+                                      "use kernel_init_std / hidden_bias_init_std / "
+                                      "visible_bias_init_std")
+        if alpha <= 0:
+            raise ValueError(f"RBM: alpha must be positive, got {alpha}")
         self.alpha = alpha
-        self.param_dtype = param_dtype
+        self.param_dtype = _real_param_dtype(param_dtype)
         self.stds = (hidden_bias_init_std, kernel_init_std, visible_bias_init_std)
 
     def n_hidden(self, N):

@@ -1083,3 +1083,34 @@ def test_sr_qgt_selection():
         o.SR(solver=o.solver.pinv_smooth)
     with pytest.raises(NotImplementedError, match="not supported"):
         o.SR(solver=lambda A, b: b)
+
+
+def test_rbm_param_dtype_spellings():
+    """param_dtype as NetKet scripts write it selects the same precision
+    (float / np.float64 / "float64" -> FP64; np.float32 -> FP32); complex and
+    JAX-only arguments are refused before any device work."""
+    import torch
+    import netket_gb300 as nk
+    for dt in (float, np.float64, "float64", torch.float64, np.dtype("float64")):
+        assert nk.models.RBM(param_dtype=dt).param_dtype == torch.float64
+    for dt in (np.float32, "float32", torch.float32):
+        assert nk.models.RBM(param_dtype=dt).param_dtype == torch.float32
+    for dt in (complex, np.complex128, torch.complex64):
+        with pytest.raises(NotImplementedError):
+            nk.models.RBM(param_dtype=dt)
+    with pytest.raises(NotImplementedError):
+        nk.models.RBM(param_dtype=np.int32)
+    with pytest.raises(ValueError):
+        nk.models.RBM(param_dtype=object())
+    with pytest.raises(NotImplementedError, match="initialiser"):
+        nk.models.RBM(kernel_init=lambda *a: None)
+    with pytest.raises(NotImplementedError, match="activation"):
+        nk.models.RBM(activation=np.tanh)
+
+    def log_cosh(x):
+        return x
+    assert nk.models.RBM(activation=log_cosh).alpha == 1
+    with pytest.raises(NotImplementedError, match="precision"):
+        nk.models.RBM(precision="highest")
+    with pytest.raises(ValueError, match="alpha"):
+        nk.models.RBM(alpha=0)
