@@ -11,9 +11,21 @@ from . import _native as nat
 
 
 class Spin:
-    def __init__(self, s=0.5, N=1, total_sz=None):
+    """``netket.hilbert.Spin`` for s = 1/2 (``netket/hilbert/spin.py:110-207``):
+    ``total_sz`` fixes the number of down spins; the basis ordering is the
+    reference's default (``inverted_ordering=False``: +1 = up); unconstrained
+    spaces multiply (``Spin(0.5) ** 8``, ``a * b``) into longer chains."""
+
+    def __init__(self, s=0.5, N=1, total_sz=None, *, constraint=None, inverted_ordering=False):
         if s != 0.5:
             raise NotImplementedError("only spin-1/2 is supported")
+        if constraint is not None:
+            raise NotImplementedError("Spin: custom constraints are not supported (total_sz is)")
+        if inverted_ordering:
+            raise NotImplementedError("Spin: inverted_ordering=True (-1 = up) is not supported; "
+                                      "the kernels use the default +1 = up ordering")
+        if int(N) < 1:
+            raise ValueError(f"Spin: N must be positive, got {N}")
         self.s = 0.5
         self.N = int(N)
         if total_sz is not None:
@@ -89,6 +101,21 @@ class Spin:
             code = code[pop == self.n_down]
         shifts = np.arange(self.N - 1, -1, -1, dtype=np.int64)
         return ((code[:, None] >> shifts) & 1).astype(np.int8)
+
+    def __mul__(self, other):
+        """Spin x Spin: one longer unconstrained chain (``spin.py:201-207``)."""
+        if not isinstance(other, Spin):
+            return NotImplemented
+        if self.constrained or other.constrained:
+            raise NotImplementedError("products of constrained Spin spaces are not supported")
+        return Spin(0.5, self.N + other.N)
+
+    def __pow__(self, n):
+        if not isinstance(n, int) or n < 1:
+            return NotImplemented
+        if self.constrained:
+            raise NotImplementedError("powers of a constrained Spin space are not supported")
+        return Spin(0.5, self.N * n)
 
     def __eq__(self, other):
         return isinstance(other, Spin) and (self.N, self.total_sz) == (other.N, other.total_sz)

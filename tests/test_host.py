@@ -1114,3 +1114,23 @@ def test_rbm_param_dtype_spellings():
         nk.models.RBM(precision="highest")
     with pytest.raises(ValueError, match="alpha"):
         nk.models.RBM(alpha=0)
+
+
+def test_spin_space_products_and_arguments():
+    """Spin(s=1/2)**8 and Spin * Spin as in spin.py:201-207; constrained
+    products, custom constraints and the inverted ordering are refused."""
+    from netket_gb300.hilbert import Spin
+    assert Spin(s=1 / 2) ** 8 == Spin(0.5, 8)
+    assert Spin(0.5, 3) * Spin(0.5, 5) == Spin(0.5, 8)
+    assert Spin(0.5, 4, inverted_ordering=False).N == 4
+    for bad in (lambda: Spin(0.5, 4, total_sz=0) ** 2,
+                lambda: Spin(0.5, 4, total_sz=0) * Spin(0.5, 2),
+                lambda: Spin(0.5, 4, inverted_ordering=True),
+                lambda: Spin(0.5, 4, constraint=object()),
+                lambda: Spin(1.0, 4)):
+        with pytest.raises(NotImplementedError):
+            bad()
+    with pytest.raises(ValueError):
+        Spin(0.5, 0)
+    with pytest.raises(TypeError):
+        Spin(0.5, 2) ** 0.5
