@@ -16,6 +16,7 @@ called at ``before_parameter_update`` and a falsy return stops the run before
 that step's parameter update (``legacy_wrappers.py:16-33``).
 """
 import time
+from collections import deque
 
 import numpy as np
 
@@ -286,3 +287,24 @@ class Timeout(AbstractCallback):
     def on_step_end(self, step, log_data, driver):
         if time.time() - self._init_time >= self.timeout:
             raise StopRun(f"Timeout: training stopped after {self.timeout:.1f} seconds.")
+
+
+class ConvergenceStopping(AbstractCallback):
+    """Stops once the monitored loss statistic, averaged over the last
+    ``smoothing_window`` steps, has been at or below ``target`` for more than
+    ``patience`` consecutive steps
+    (``netket/_src/callbacks/convergence_stopping.py``)."""
+
+    def __init__(self, target, monitor="mean", *, smoothing_window=10, patience=10):
+        self.target, self.monitor = target, monitor
+        self.smoothing_window, self.patience = smoothing_window, patience
+        self._loss_window = deque([], maxlen=smoothing_window)
+        self._patience_counter = 0
+
+    def on_step_end(self, step, log_data, driver):
+        self._loss_window.append(_monitored(log_data[driver._loss_name], self.monitor))
+        smooth = float(np.mean(self._loss_window))
+        self._patience_counter = self._patience_counter + 1 if smooth <= self.target else 0
+        if self._patience_counter > self.patience:
+            raise StopRun(f"ConvergenceStopping: smoothed loss {smooth:.6g} has been below "
+                          f"target {self.target} for {self._patience_counter} steps.")

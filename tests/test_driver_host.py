@@ -335,3 +335,17 @@ def test_progress_bar_runs(capsys):
     drv.run(3)
     assert drv.step_count == 3
     assert "3/3" in capsys.readouterr().err
+
+
+def test_convergence_stopping():
+    """Losses 3, 1, 1, 1, ... smoothed over 2 steps give 3, 2, 1, 1, ...: the
+    smoothed loss is at or below the target 1.5 from step 2 on, so with
+    patience 1 the counter passes 1 at step 3 and the run stops there."""
+    losses = [3.0, 1.0, 1.0, 1.0, 1.0, 1.0]
+    drv = FakeDriver(losses=losses)
+    drv.run(6, callback=cb.ConvergenceStopping(1.5, smoothing_window=2, patience=1),
+            show_progress=False)
+    assert drv.step_count == 3
+    drv = FakeDriver(losses=[5.0] * 4)
+    drv.run(4, callback=cb.ConvergenceStopping(1.0), show_progress=False)
+    assert drv.step_count == 4
