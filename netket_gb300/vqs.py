@@ -43,6 +43,12 @@ def _derive_seed(seed):
     return z ^ (z >> 31)
 
 
+def _check_mutable(mutable):
+    if mutable not in (None, False):
+        raise NotImplementedError("mutable model collections are not supported (the RBM has "
+                                  "none)")
+
+
 def log_psi_to_array(log_psi, normalize=True):
     """exp(log psi), shifted by max(log psi) and scaled to unit L2 norm when
     ``normalize`` (``netket/nn/utils.py:132-160``)."""
@@ -319,20 +325,27 @@ class MCState:
         self._cache = dict(x=x, t=t, e=e, stats_dev=st, op=op)
         return self._cache
 
-    def expect_and_forces(self, op):
+    def expect_and_forces(self, op, *, mutable=None):
+        _check_mutable(mutable)
         c = self._forward_cache(op)
         n = c["x"].shape[0]
         v = K.center_scale(c["e"], c["stats_dev"][0:1], 1.0 / n)
         F = K.ot_v(c["t"], c["x"], self.N, self.M, v)
         return Stats.from_array(c["stats_dev"].cpu().numpy()), self.model.unflatten(F, self.N, self.M)
 
-    def expect_and_grad(self, op):
+    def expect_and_grad(self, op, *, mutable=None, use_covariance=None):
         """Energy statistics and grad = 2 Re[(1/n) O^T (E - mean E)]
-        (``netket/vqs/mc/mc_state/expect_forces.py:68-111``, ``common.py:103-118``),
-        the formula for a hermitian operator; NetKet switches to another one for
-        non-hermitian operators (``expect_grad.py:86-128``), not built here."""
-        if getattr(op, "is_hermitian", True) is False:
-            raise NotImplementedError("expect_and_grad of a non-hermitian operator")
+        (``netket/vqs/mc/mc_state/expect_forces.py:68-111``, ``common.py:103-118``):
+        the covariance formula, which NetKet uses when ``use_covariance`` is
+        True or, by default, when the operator is hermitian
+        (``expect_grad.py:42-64``).  Its other formula (``use_covariance=False``,
+        the default for a non-hermitian operator) is not built here."""
+        _check_mutable(mutable)
+        if use_covariance is None:
+            use_covariance = getattr(op, "is_hermitian", True)
+        if not use_covariance:
+            raise NotImplementedError("expect_and_grad with use_covariance=False (the "
+                                      "non-hermitian formula) is not implemented")
         c = self._forward_cache(op)
         n = c["x"].shape[0]
         v = K.center_scale(c["e"], c["stats_dev"][0:1], 2.0 / n)

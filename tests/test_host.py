@@ -1134,3 +1134,22 @@ def test_spin_space_products_and_arguments():
         Spin(0.5, 0)
     with pytest.raises(TypeError):
         Spin(0.5, 2) ** 0.5
+
+
+def test_expect_and_grad_formula_choice_refusals():
+    """expect_and_grad picks the covariance formula by use_covariance (default:
+    the operator's is_hermitian, expect_grad.py:42-64); the non-hermitian
+    formula and mutable collections are refused before any device work."""
+    import netket_gb300 as nk
+    from netket_gb300 import vqs
+    hi = nk.hilbert.Spin(0.5, 4)
+    vs = vqs.MCState.__new__(vqs.MCState)
+    sp = nk.operator.spin
+    with pytest.raises(NotImplementedError, match="use_covariance=False"):
+        vs.expect_and_grad(sp.sigmap(hi, 1))
+    with pytest.raises(NotImplementedError, match="use_covariance=False"):
+        vs.expect_and_grad(sp.sigmax(hi, 1), use_covariance=False)
+    with pytest.raises(NotImplementedError, match="mutable"):
+        vs.expect_and_grad(sp.sigmax(hi, 1), mutable=True)
+    with pytest.raises(NotImplementedError, match="mutable"):
+        vs.expect_and_forces(sp.sigmax(hi, 1), mutable="batch_stats")
