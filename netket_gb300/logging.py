@@ -112,7 +112,7 @@ class History:
         return len(self._iters)
 
     def __getitem__(self, key):
-        if isinstance(key, (int, slice)) and key not in self._series:
+        if isinstance(key, slice) or (isinstance(key, int) and key not in self._series):
             idx = range(len(self._iters))[key]
             idx = [idx] if isinstance(idx, int) else list(idx)
             h = History(main_value_name=self._main)
@@ -245,7 +245,11 @@ class RuntimeLog:
             with open(path, "w") as f:
                 json.dump(self._data, f, default=_json_default)
         else:
-            path.write(json.dumps(self._data, default=_json_default))
+            text = json.dumps(self._data, default=_json_default)
+            try:
+                path.write(text)
+            except TypeError:  # a binary stream
+                path.write(text.encode())
 
     @classmethod
     def deserialize(cls, path):

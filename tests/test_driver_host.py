@@ -349,3 +349,19 @@ def test_convergence_stopping():
     drv = FakeDriver(losses=[5.0] * 4)
     drv.run(4, callback=cb.ConvergenceStopping(1.0), show_progress=False)
     assert drv.step_count == 4
+
+
+def test_runtime_log_serialize_to_streams(tmp_path):
+    import io
+    log = nklog.RuntimeLog()
+    for k in range(3):
+        log(k, {"Energy": Stats(float(k), 0.1, 1.0, 0.0, 1.0), "x": float(2 * k)})
+    t, b = io.StringIO(), io.BytesIO()
+    log.serialize(t)
+    log.serialize(b)
+    assert json.loads(t.getvalue()) == json.loads(b.getvalue().decode())
+    assert json.loads(t.getvalue())["x"] == {"iters": [0, 1, 2], "value": [0.0, 2.0, 4.0]}
+    log.serialize(str(tmp_path / "run"))
+    back = nklog.RuntimeLog.deserialize(str(tmp_path / "run"))
+    np.testing.assert_allclose(back["Energy"]["Mean"], [0.0, 1.0, 2.0])
+    assert list(log["x"][1:].iters) == [1, 2]
