@@ -168,8 +168,16 @@ class HistoryDict(dict):
     def from_dict(cls, d):
         out = cls()
         for k, v in d.items():
-            out[k] = History(v) if isinstance(v, dict) and "iters" in v else cls.from_dict(v)
+            out[k] = cls._node(v)
         return out
+
+    @classmethod
+    def _node(cls, v):
+        if isinstance(v, dict):
+            return History(v) if "iters" in v else cls.from_dict(v)
+        if isinstance(v, list):
+            return [cls._node(x) for x in v]
+        raise ValueError(f"not a logged history: {v!r}")
 
 
 def accum_histories_in_tree(acc, tree, step):

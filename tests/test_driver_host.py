@@ -207,6 +207,10 @@ def test_observables_every_step_size_and_seen_by_loggers():
     # the observable is estimated before the update: 2 * params[0] of that step
     np.testing.assert_allclose(log["Sx"]["Mean"], [0.0, 0.0, 0.0])
     assert isinstance(log["pair"], list) and list(log["pair"][1].iters) == [0, 2, 4]
+    buf = __import__("io").StringIO()
+    log.serialize(buf)
+    back = nklog.HistoryDict.from_dict(json.loads(buf.getvalue()))
+    np.testing.assert_allclose(back["pair"][1]["Mean"], log["pair"][1]["Mean"])
     assert list(log["Energy"].iters) == [0, 1, 2, 3, 4]
     assert drv.estimate({"a": 1.0, "b": (2.0,)})["b"][0].mean == 0.0
 
