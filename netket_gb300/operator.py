@@ -89,6 +89,7 @@ class Ising(DiscreteOperator):
     """``-h sum_i X_i + J sum_<ij> Z_i Z_j`` (``netket/operator/_ising/jax.py``)."""
 
     def __init__(self, hilbert, graph, h, J=1.0, dtype=None):
+        _check_real_dtype(dtype, "Ising")
         super().__init__(hilbert)
         if hasattr(graph, "edges"):
             edges = np.asarray(graph.edges(), dtype=np.int64).reshape(-1, 2)
@@ -121,6 +122,61 @@ class Ising(DiscreteOperator):
                                                 int(self.h == 0), nat.ptr(xp), nat.ptr(mels),
                                                 nat.ptr(nc)))
         return xp, mels, nc
+
+    # algebra: NetKet sums an Ising with other operators lazily (SumOperator,
+    # netket/operator/_abstract_operator.py:117-152); here the sum is the
+    # concrete LocalOperator of the same matrix, and a scalar multiple stays an
+    # Ising (h and J scaled) so it keeps the Ising kernels.
+    def __mul__(self, s):
+        if isinstance(s, DiscreteOperator):
+            return self.to_local_operator() @ _as_local(s)
+        if not np.isscalar(s):
+            return NotImplemented
+        if np.iscomplexobj(np.asarray(s)) and np.imag(s) != 0:
+            raise TypeError("Ising: complex coefficients are not supported on this path")
+        s = float(np.real(s))
+        return Ising(self.hilbert, self.edges, self.h * s, self.J * s)
+
+    def __rmul__(self, s):
+        if not np.isscalar(s):
+            return NotImplemented
+        return self.__mul__(s)
+
+    def __truediv__(self, s):
+        if not np.isscalar(s):
+            raise TypeError("Only division by a scalar number is supported.")
+        if s == 0:
+            raise ValueError("Dividing by 0")
+        return self.__mul__(1.0 / s)
+
+    def __neg__(self):
+        return self * -1.0
+
+    def __add__(self, other):
+        if isinstance(other, (Ising, LocalOperator)) or np.isscalar(other):
+            return self.to_local_operator() + _as_local(other)
+        return NotImplemented
+
+    def __radd__(self, other):
+        if isinstance(other, (Ising, LocalOperator)) or np.isscalar(other):
+            return _as_local(other) + self.to_local_operator()
+        return NotImplemented
+
+    def __sub__(self, other):
+        return self + (-other)
+
+    def __rsub__(self, other):
+        return other + (-self)
+
+    def __matmul__(self, other):
+        if isinstance(other, (Ising, LocalOperator)):
+            return self.to_local_operator() @ _as_local(other)
+        return NotImplemented
+
+    def __rmatmul__(self, other):
+        if isinstance(other, LocalOperator):
+            return other @ self.to_local_operator()
+        return NotImplemented
 
     def to_local_operator(self):
         """``IsingBase.to_local_operator``: -h X_i terms, then J Z_i Z_j per edge."""
@@ -171,6 +227,10 @@ def _sort_sites(mat, sites):
     t = np.asarray(mat, dtype=np.float64).reshape((2,) * (2 * k))
     t = np.transpose(t, order + [k + q for q in order])
     return t.reshape(2**k, 2**k), tuple(sites[q] for q in order)
+
+
+def _as_local(op):
+    return op.to_local_operator() if isinstance(op, Ising) else op
 
 
 class LocalOperator(DiscreteOperator):

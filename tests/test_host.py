@@ -1153,3 +1153,38 @@ def test_expect_and_grad_formula_choice_refusals():
         vs.expect_and_grad(sp.sigmax(hi, 1), mutable=True)
     with pytest.raises(NotImplementedError, match="mutable"):
         vs.expect_and_forces(sp.sigmax(hi, 1), mutable="batch_stats")
+
+
+def test_ising_algebra():
+    """Ising combined with scalars and LocalOperators equals the dense-matrix
+    algebra (NetKet sums lazily; here the sum is a concrete LocalOperator), a
+    scalar multiple stays an Ising with h and J scaled."""
+    import netket_gb300 as nk
+    N = 4
+    hi = nk.hilbert.Spin(0.5, N)
+    I = nk.operator.Ising(hi, nk.graph.Chain(N), h=0.7, J=1.3)
+    Z0 = nk.operator.spin.sigmaz(hi, 0)
+    X2 = nk.operator.spin.sigmax(hi, 2)
+
+    def dense(op):
+        op = op.to_local_operator() if isinstance(op, nk.operator.Ising) else op
+        return _dense_from_local(N, list(op._terms.items()), op.constant)
+
+    dI, dZ, dX = dense(I), dense(Z0), dense(X2)
+    two = 2 * I
+    assert isinstance(two, nk.operator.Ising) and (two.h, two.J) == (1.4, 2.6)
+    np.testing.assert_allclose(dense(-I), -dI, atol=1e-13)
+    np.testing.assert_allclose(dense(I / 2), dI / 2, atol=1e-13)
+    np.testing.assert_allclose(dense(I + 0.5 * Z0), dI + 0.5 * dZ, atol=1e-13)
+    np.testing.assert_allclose(dense(Z0 + I), dZ + dI, atol=1e-13)
+    np.testing.assert_allclose(dense(1.5 - I), 1.5 * np.eye(2 ** N) - dI, atol=1e-13)
+    np.testing.assert_allclose(dense(I - X2), dI - dX, atol=1e-13)
+    np.testing.assert_allclose(dense(I + I), 2 * dI, atol=1e-13)
+    np.testing.assert_allclose(dense(I @ Z0), dI @ dZ, atol=1e-12)
+    np.testing.assert_allclose(dense(Z0 @ I), dZ @ dI, atol=1e-12)
+    np.testing.assert_allclose(dense(I ** 2), dI @ dI, atol=1e-12)
+    assert (I + Z0).is_hermitian and I.is_hermitian
+    with pytest.raises(TypeError, match="complex"):
+        nk.operator.Ising(hi, nk.graph.Chain(N), h=1.0, dtype=np.complex64)
+    with pytest.raises(TypeError, match="complex"):
+        I * 1j
