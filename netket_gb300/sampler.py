@@ -185,11 +185,14 @@ class MetropolisSampler:
         return MetropolisSamplerState(σ=σ, log_prob=lp, seed=int(seed) & (2**64 - 1), counter=0,
                                       n_accepted_proc=acc)
 
-    def reset(self, machine, params, state):
+    def reset(self, machine, params, state=None):
         """Recompute log_prob for the current parameters and zero the counters
-        (``netket/sampler/metropolis.py:382-414``).  With ``reset_chains`` the
-        chains first restart from fresh random states, drawn from the Philox
-        stream (seed, 2 + proposal counter): a new stream at every reset."""
+        (``netket/sampler/metropolis.py:382-414``); a new state when ``state`` is
+        None (``sampler/base.py:289-321``).  With ``reset_chains`` the chains
+        first restart from fresh random states, drawn from the Philox stream
+        (seed, 2 + proposal counter): a new stream at every reset."""
+        if state is None:
+            state = self.init_state(machine, params)
         N = self.hilbert.size
         M = machine.sizes_from_flat(params.numel(), N)
         if self.reset_chains:
@@ -202,14 +205,22 @@ class MetropolisSampler:
         state.n_steps_proc = 0
         return state
 
-    def sample(self, machine, params, *, state=None, chain_length=1, n_discard=0):
-        """Run ``n_discard`` discarded sweeps then ``chain_length`` kept sweeps.
-
-        ``params`` is the flat parameter vector in the compute dtype (FP64 or
-        FP32).  Returns samples (n_chains, chain_length, N) and the new state.
-        """
+    def sample(self, machine, params, *, state=None, chain_length=1, n_discard=0,
+               return_log_probabilities=False):
+        """Run ``n_discard`` discarded sweeps then ``chain_length`` kept sweeps
+        (``sampler/base.py:344-400``: without a state, a new one is initialised
+        and reset).  ``params`` is the flat parameter vector in the compute dtype
+        (FP64 or FP32).  Returns samples (n_chains, chain_length, N) and the new
+        state; with ``return_log_probabilities``, (samples, 2 Re log psi of each
+        sample, shape (n_chains, chain_length)) and the state."""
         if state is None:
-            state = self.init_state(machine, params)
+            state = self.reset(machine, params)
+        if return_log_probabilities:
+            samples, state = self.sample(machine, params, state=state,
+                                         chain_length=chain_length, n_discard=n_discard)
+            B, L, N = samples.shape
+            lp = machine.apply(params, samples.reshape(-1, N)).to(torch.float64)
+            return (samples, 2.0 * lp.reshape(B, L)), state
         N = self.hilbert.size
         M = machine.sizes_from_flat(params.numel(), N)
         B = self.n_chains
