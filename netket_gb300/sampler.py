@@ -128,6 +128,17 @@ class MetropolisSamplerState:
     def n_accepted(self):
         return int(self.n_accepted_proc.sum().item())
 
+    @property
+    def n_steps(self):
+        return self.n_steps_proc
+
+    def __repr__(self):
+        acc = ""
+        if self.n_steps > 0:
+            acc = (f"# accepted = {self.n_accepted}/{self.n_steps} "
+                   f"({self.acceptance * 100}%), ")
+        return f"MetropolisSamplerState({acc}seed = {self.seed}, counter = {self.counter})"
+
 
 class MetropolisSampler:
     machine_pow = 2

@@ -1188,3 +1188,18 @@ def test_ising_algebra():
         nk.operator.Ising(hi, nk.graph.Chain(N), h=1.0, dtype=np.complex64)
     with pytest.raises(TypeError, match="complex"):
         I * 1j
+
+
+def test_sampler_state_counters():
+    """acceptance / n_steps / n_accepted as the reference's MetropolisSamplerState
+    (metropolis.py:96-130): None before any step since the last reset."""
+    import torch
+    from netket_gb300.sampler import MetropolisSamplerState
+    st = MetropolisSamplerState(torch.zeros((4, 3), dtype=torch.int8),
+                                torch.zeros(4, dtype=torch.float64), 7, 0,
+                                torch.zeros(4, dtype=torch.int64))
+    assert st.acceptance is None and st.n_steps == 0 and "accepted" not in repr(st)
+    st.n_accepted_proc = torch.tensor([3, 1, 0, 2])
+    st.n_steps_proc = 24
+    assert st.n_accepted == 6 and st.n_steps == 24 and st.acceptance == 0.25
+    assert "# accepted = 6/24 (25.0%)" in repr(st)
