@@ -9,6 +9,7 @@ from . import _native
 from . import graph
 from . import hilbert
 from . import operator
+from . import nn
 from . import models
 from . import sampler
 from . import stats
@@ -25,4 +26,4 @@ from . import serving
 from . import serialization
 
 __all__ = ["graph", "hilbert", "operator", "models", "sampler", "stats", "kernels", "ngd", "batched", "serving", "serialization",
-           "optimizer", "vqs", "driver", "logging", "callbacks", "exact"]
+           "optimizer", "vqs", "driver", "logging", "callbacks", "exact", "nn"]

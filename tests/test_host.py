@@ -1203,3 +1203,15 @@ def test_sampler_state_counters():
     st.n_steps_proc = 24
     assert st.n_accepted == 6 and st.n_steps == 24 and st.acceptance == 0.25
     assert "# accepted = 6/24 (25.0%)" in repr(st)
+
+
+def test_nn_log_cosh(golden):
+    """nk.nn.log_cosh equals the reference's log_cosh (logcosh.npz) and is the
+    activation the RBM accepts."""
+    import torch
+    import netket_gb300 as nk
+    g = golden("logcosh")
+    np.testing.assert_allclose(nk.nn.log_cosh(g["x"]), g["y"], rtol=1e-14, atol=1e-15)
+    t = nk.nn.log_cosh(torch.as_tensor(g["x"]))
+    np.testing.assert_allclose(t.numpy(), g["y"], rtol=1e-14, atol=1e-15)
+    assert nk.models.RBM(alpha=2, activation=nk.nn.log_cosh).alpha == 2
