@@ -3,7 +3,7 @@ local energies, Jacobian contractions and the SR/minSR solve) as hand-written
 sm_103a CUDA kernels behind a C ABI (``include/vmck.h``, ``libvmck.so``), with a
 host API that mirrors ``netket``: ``hilbert``, ``graph``, ``operator``,
 ``models``, ``sampler``, ``vqs``, ``stats``, ``optimizer``, ``driver``,
-``logging``, ``callbacks``, ``exact``.
+``logging``, ``callbacks``, ``exact``, ``nn``.
 """
 from . import _native
 from . import graph
