@@ -229,6 +229,26 @@ def _sort_sites(mat, sites):
     return t.reshape(2**k, 2**k), tuple(sites[q] for q in order)
 
 
+def _real_matrix(op):
+    """A term's matrix as float64; imaginary matrix elements are refused rather
+    than dropped (the path's operators are real)."""
+    a = np.asarray(op)
+    if np.iscomplexobj(a):
+        if np.any(a.imag != 0):
+            raise TypeError("LocalOperator: complex matrix elements are not supported on this "
+                            "path (real operators only)")
+        a = a.real
+    return np.asarray(a, dtype=np.float64)
+
+
+def _real_scalar(c, name):
+    if np.iscomplexobj(np.asarray(c)):
+        if np.imag(c) != 0:
+            raise TypeError(f"LocalOperator: a complex {name} is not supported on this path")
+        c = np.real(c)
+    return float(c)
+
+
 def _as_local(op):
     return op.to_local_operator() if isinstance(op, Ising) else op
 
@@ -238,14 +258,15 @@ class LocalOperator(DiscreteOperator):
 
     def __init__(self, hilbert, operators=(), acting_on=(), constant=0.0, dtype=None,
                  mel_cutoff=1e-10):
+        _check_real_dtype(dtype, "LocalOperator")
         super().__init__(hilbert)
-        self.constant = float(constant)
+        self.constant = _real_scalar(constant, "constant")
         self.mel_cutoff = float(mel_cutoff)
         self._terms = {}
         if len(acting_on) and np.isscalar(acting_on[0]):
             operators, acting_on = [operators], [acting_on]
         for op, aon in zip(operators, acting_on):
-            self._add(np.asarray(op, dtype=np.float64), aon)
+            self._add(_real_matrix(op), aon)
         self._tables = None
         self._dev = {}
 

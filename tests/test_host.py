@@ -1215,3 +1215,24 @@ def test_nn_log_cosh(golden):
     t = nk.nn.log_cosh(torch.as_tensor(g["x"]))
     np.testing.assert_allclose(t.numpy(), g["y"], rtol=1e-14, atol=1e-15)
     assert nk.models.RBM(alpha=2, activation=nk.nn.log_cosh).alpha == 2
+
+
+def test_local_operator_refuses_imaginary_elements():
+    """A complex term (sigma^y) or complex constant raises instead of losing its
+    imaginary part; complex-typed matrices with zero imaginary part are kept."""
+    import warnings
+    import netket_gb300 as nk
+    hi = nk.hilbert.Spin(0.5, 2)
+    sy = np.array([[0, -1j], [1j, 0]])
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        with pytest.raises(TypeError, match="complex"):
+            nk.operator.LocalOperator(hi, [sy], [[0]])
+        with pytest.raises(TypeError, match="complex"):
+            nk.operator.LocalOperator(hi, constant=1j)
+        with pytest.raises(TypeError, match="complex"):
+            nk.operator.LocalOperator(hi, dtype=np.complex128)
+        op = nk.operator.LocalOperator(hi, [np.array([[0, 1], [1, 0]], dtype=complex)], [[1]],
+                                       constant=2 + 0j)
+    assert op.constant == 2.0 and op._terms[(1,)].dtype == np.float64
+    np.testing.assert_array_equal(op._terms[(1,)], [[0.0, 1.0], [1.0, 0.0]])
