@@ -89,8 +89,19 @@ class RBM:
 
     @staticmethod
     def flatten(params):
-        return torch.cat([params["Dense"]["bias"].reshape(-1), params["Dense"]["kernel"].reshape(-1),
-                          params["visible_bias"].reshape(-1)])
+        """The flat vector [bias | kernel (row-major) | visible_bias] of a
+        parameter pytree whose leaves are tensors or array-likes (NumPy arrays
+        loaded from a file, lists); complex leaves are refused."""
+        leaves = [params["Dense"]["bias"], params["Dense"]["kernel"], params["visible_bias"]]
+        out = []
+        for leaf in leaves:
+            t = leaf if isinstance(leaf, torch.Tensor) else torch.as_tensor(np.asarray(leaf))
+            if t.is_complex():
+                raise TypeError("RBM: complex parameters are not supported (real RBM path)")
+            out.append(t.reshape(-1))
+        if len({t.device for t in out}) > 1:
+            out = [t.to(out[0].device) for t in out]
+        return torch.cat(out)
 
     @staticmethod
     def sizes_from_flat(P, N):

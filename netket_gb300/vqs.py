@@ -15,6 +15,7 @@ Statistics and gradient accumulations are FP64 in every mode.
 import math
 import warnings
 
+import numpy as np
 import torch
 
 from . import _native as nat
@@ -194,7 +195,13 @@ class MCState:
 
     @flat_parameters.setter
     def flat_parameters(self, v):
-        self._flat.copy_(torch.as_tensor(v, dtype=torch.float64).to(self._flat.device).reshape(-1))
+        t = v if isinstance(v, torch.Tensor) else torch.as_tensor(np.asarray(v))
+        if t.is_complex():
+            raise TypeError("MCState: complex parameters are not supported (real RBM path)")
+        t = t.to(device=self._flat.device, dtype=torch.float64).reshape(-1)
+        if t.numel() != self._flat.numel():
+            raise ValueError(f"expected {self._flat.numel()} parameters, got {t.numel()}")
+        self._flat.copy_(t)
         self.params_changed()
 
     def params_changed(self):

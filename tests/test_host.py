@@ -1236,3 +1236,29 @@ def test_local_operator_refuses_imaginary_elements():
                                        constant=2 + 0j)
     assert op.constant == 2.0 and op._terms[(1,)].dtype == np.float64
     np.testing.assert_array_equal(op._terms[(1,)], [[0.0, 1.0], [1.0, 0.0]])
+
+
+def test_parameter_assignment_forms():
+    """vs.parameters accepts a pytree of NumPy arrays (as loaded from a file) and
+    tensors; complex values and a wrong size are refused, not cast."""
+    import torch
+    from netket_gb300 import vqs
+    from netket_gb300.models import RBM
+    vs = vqs.MCState.__new__(vqs.MCState)
+    vs.model = RBM(alpha=1)
+    vs.N, vs.M = 2, 2
+    vs._flat = torch.zeros(8, dtype=torch.float64)
+    vs._version, vs._samples, vs._cache = 0, None, None
+    p = {"Dense": {"bias": np.array([1.0, 2.0]), "kernel": np.arange(4.0).reshape(2, 2)},
+         "visible_bias": [7.0, 8.0]}
+    vs.parameters = p
+    np.testing.assert_array_equal(vs._flat.numpy(), [1, 2, 0, 1, 2, 3, 7, 8])
+    assert vs._version == 1
+    vs.flat_parameters = torch.arange(8, dtype=torch.float32)
+    np.testing.assert_array_equal(vs._flat.numpy(), np.arange(8.0))
+    with pytest.raises(TypeError, match="complex"):
+        vs.flat_parameters = np.ones(8) * (1 + 1j)
+    with pytest.raises(TypeError, match="complex"):
+        vs.parameters = dict(p, visible_bias=np.array([1j, 0]))
+    with pytest.raises(ValueError, match="expected 8"):
+        vs.flat_parameters = np.ones(7)
