@@ -11,6 +11,7 @@ the solver status); ``run`` adds the sampler's acceptance, as NetKet logs it.
 import numbers
 import sys
 import time
+import warnings
 from pathlib import Path
 
 import torch
@@ -223,12 +224,21 @@ class VMC_SR(AbstractVariationalDriver):
     def __init__(self, hamiltonian, optimizer, *, diag_shift, variational_state, use_ntk=None,
                  gram="structured", gram_mode=None, solve=None, refine_iters=3,
                  refine_tol=1e-10, jac_dtype=None, proj_reg=None, momentum=None,
-                 linear_solver=None, chunk_size_bwd=None, mode=None, on_the_fly=None):
+                 linear_solver=None, linear_solver_fn=None, chunk_size_bwd=None, mode=None,
+                 on_the_fly=None):
         # linear_solver: NetKet's cholesky_with_fallback (default), cholesky (no
         # fallback) or pinv_smooth (netket/optimizer/solver/solvers.py); chunk_size_bwd
         # has no effect (nothing is chunked: the Jacobian is never materialised);
         # on_the_fly selects NetKet's srt_onthefly / srt, which here are one path.
         from .optimizer import solver as _solvers
+        if linear_solver_fn is not None:
+            # the reference's deprecated name for linear_solver (vmc_sr.py:264-266)
+            if linear_solver is not None:
+                raise ValueError("pass linear_solver only (linear_solver_fn is its deprecated "
+                                 "name)")
+            warnings.warn("linear_solver_fn is deprecated; use linear_solver",
+                          FutureWarning, stacklevel=2)
+            linear_solver = linear_solver_fn
         if linear_solver is None or linear_solver is _solvers.cholesky_with_fallback:
             self._solver = "fallback"
         elif linear_solver is _solvers.cholesky:

@@ -436,6 +436,15 @@ def test_driver_and_state_arguments_refused_before_the_device():
     with pytest.raises(NotImplementedError, match="on_the_fly"):
         nk.driver.VMC_SR(H, opt, diag_shift=0.01, variational_state=None, use_ntk=False,
                          on_the_fly=True)
+    # linear_solver_fn: the reference's deprecated name for linear_solver
+    with pytest.warns(FutureWarning, match="linear_solver_fn"):
+        with pytest.raises(NotImplementedError, match="linear_solver"):
+            nk.driver.VMC_SR(H, opt, diag_shift=0.01, variational_state=None,
+                             linear_solver_fn=lambda A, b: (b, None))
+    with pytest.raises(ValueError, match="linear_solver only"):
+        nk.driver.VMC_SR(H, opt, diag_shift=0.01, variational_state=None,
+                         linear_solver=nk.optimizer.solver.cholesky,
+                         linear_solver_fn=nk.optimizer.solver.cholesky)
 
 
 def _replica_rank(rank, world, port, q):
