@@ -199,6 +199,12 @@ class VMC(AbstractVariationalDriver):
     """``expect_and_grad`` then an optional preconditioner (e.g. ``SR``)."""
 
     def __init__(self, hamiltonian, optimizer, *, variational_state, preconditioner=None):
+        if variational_state.hilbert != hamiltonian.hilbert:
+            # netket/driver/vmc.py:77-84
+            raise TypeError(f"the variational_state has hilbert space "
+                            f"{variational_state.hilbert} (this is normally defined by the "
+                            f"hilbert space in the sampler), but the hamiltonian has hilbert "
+                            f"space {hamiltonian.hilbert}. The two should match.")
         super().__init__(variational_state, optimizer)
         self._ham = hamiltonian
         self.preconditioner = preconditioner or identity_preconditioner

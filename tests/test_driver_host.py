@@ -369,3 +369,17 @@ def test_runtime_log_serialize_to_streams(tmp_path):
     back = nklog.RuntimeLog.deserialize(str(tmp_path / "run"))
     np.testing.assert_allclose(back["Energy"]["Mean"], [0.0, 1.0, 2.0])
     assert list(log["x"][1:].iters) == [1, 2]
+
+
+def test_vmc_checks_hilbert_spaces():
+    """VMC refuses a Hamiltonian on another Hilbert space (vmc.py:77-84)."""
+    import netket_gb300 as nk
+
+    class State:
+        hilbert = nk.hilbert.Spin(0.5, 4, total_sz=0)
+
+    H_same = nk.operator.Ising(nk.hilbert.Spin(0.5, 4, total_sz=0), nk.graph.Chain(4), h=1.0)
+    nk.driver.VMC(H_same, nk.optimizer.Sgd(0.1), variational_state=State())
+    H_other = nk.operator.Ising(nk.hilbert.Spin(0.5, 4), nk.graph.Chain(4), h=1.0)
+    with pytest.raises(TypeError, match="hilbert space"):
+        nk.driver.VMC(H_other, nk.optimizer.Sgd(0.1), variational_state=State())
