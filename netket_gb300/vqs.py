@@ -44,6 +44,16 @@ def _derive_seed(seed):
     return z ^ (z >> 31)
 
 
+def _progress_bar(verbose, total):
+    if not verbose:
+        return None
+    try:
+        from tqdm.auto import tqdm
+    except ImportError:
+        return None
+    return tqdm(total=total, desc="expect_to_precision", leave=False, dynamic_ncols=True)
+
+
 def _check_mutable(mutable):
     if mutable not in (None, False):
         raise NotImplementedError("mutable model collections are not supported (the RBM has "
@@ -277,7 +287,8 @@ class MCState:
         lp = self.model.apply(self.params_c, x)
         return log_psi_to_array(lp, normalize)
 
-    def expect_to_precision(self, op, *, atol=None, rtol=None, max_iter=10_000, max_lag=64):
+    def expect_to_precision(self, op, *, atol=None, rtol=None, max_iter=10_000, max_lag=64,
+                            verbose=True):
         """Sample until the standard error of the mean meets ``atol`` (absolute)
         and / or ``rtol`` (relative to |mean|); both must hold when both are given
         (``netket/_src/vqs/expect_to_precision.py:70-164``).  ``op`` is an operator
@@ -285,7 +296,8 @@ class MCState:
         accumulator (``max_lag`` lags of online autocorrelation), fed with the
         local estimators of every sampling round until it converges, and the
         accumulators are returned in the structure of ``op``.  Later rounds
-        discard no sweeps, as in the reference."""
+        discard no sweeps, as in the reference.  ``verbose`` shows a progress
+        bar of the rounds when tqdm is installed."""
         if atol is None and rtol is None:
             raise ValueError("At least one of 'atol' or 'rtol' must be specified.")
         if atol is not None and atol <= 0:
@@ -310,12 +322,18 @@ class MCState:
         self.sample()
         accs = accumulate(set(range(len(leaves))), [None] * len(leaves))
         active = [i for i in range(len(leaves)) if unconverged(accs[i])]
+        bar = _progress_bar(verbose, max_iter)
         it = 0
         while active and it < max_iter:
             self.sample(n_discard_per_chain=0)
             accs = accumulate(set(active), accs)
             active = [i for i in active if unconverged(accs[i])]
             it += 1
+            if bar is not None:
+                bar.set_postfix_str(f"{len(active)} not converged")
+                bar.update(1)
+        if bar is not None:
+            bar.close()
         self.last_precision_rounds = it
         if keys is not None:
             return dict(zip(keys, accs))

@@ -1271,3 +1271,18 @@ def test_parameter_assignment_forms():
         vs.parameters = dict(p, visible_bias=np.array([1j, 0]))
     with pytest.raises(ValueError, match="expected 8"):
         vs.flat_parameters = np.ones(7)
+
+
+def test_precision_progress_bar_switch():
+    """expect_to_precision(verbose=): no bar when False; a tqdm bar (or nothing
+    without tqdm) when True."""
+    from netket_gb300.vqs import _progress_bar
+    assert _progress_bar(False, 10) is None
+    bar = _progress_bar(True, 10)
+    try:
+        import tqdm  # noqa: F401
+        assert bar is not None
+        bar.update(1)
+        bar.close()
+    except ImportError:
+        assert bar is None
