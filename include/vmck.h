@@ -55,6 +55,15 @@ const char *vmck_last_error(void);
 /* Number of kernels this library has launched in this process (diagnostic;
  * cuBLAS / cuSOLVER launches are not included). */
 int64_t vmck_launch_count(void);
+/* Wall-time limit (ns, default 2e9) of the device-side waits for work: the
+ * tensor-core kernels' pipeline waits and the waits between CTAs of the
+ * persistent triangular solves.  A wait that runs out sets VMCK_DEV_TIMEOUT in
+ * the call's status word and the kernel winds down; copies and MMAs already
+ * issued are still waited for with the fixed 2 s limit, so no CTA exits with
+ * work in flight.  No counterpart in the reference (XLA's kernels have no
+ * device-side waits); the tests shorten it to make a wait run out. */
+int vmck_set_wait_limit_ns(uint64_t ns);
+uint64_t vmck_wait_limit_ns(void);
 
 /* Library context: owns cuBLAS / cuSOLVER handles and the solver workspace.
  * Replaces the XLA-managed handles behind jax.scipy.linalg.cho_factor

@@ -66,6 +66,8 @@ _SIGNATURES = {
     "vmck_error_string": ([c_i32], ctypes.c_char_p),
     "vmck_last_error": ([], ctypes.c_char_p),
     "vmck_launch_count": ([], c_i64),
+    "vmck_set_wait_limit_ns": ([c_u64], c_i32),
+    "vmck_wait_limit_ns": ([], c_u64),
     "vmck_ctx_create": ([ctypes.POINTER(c_vp)], c_i32),
     "vmck_ctx_destroy": ([c_vp], c_i32),
     "vmck_random_states": ([c_vp, c_vp, c_i64, c_i32, c_i32, c_u64, c_u64], c_i32),

@@ -20,11 +20,22 @@ static std::atomic<long long> g_launches{0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+static std::atomic<unsigned long long> g_wait_ns{2000000000ull};
+
+unsigned long long wait_limit_ns() { return g_wait_ns.load(std::memory_order_relaxed); }
+
 }  // namespace vmck
 
 extern "C" int64_t vmck_launch_count(void) { return vmck::g_launches.load(); }
 
 extern "C" int vmck_abi_version(void) { return VMCK_ABI_VERSION; }
+
+extern "C" int vmck_set_wait_limit_ns(uint64_t ns) {
+  vmck::g_wait_ns.store(ns, std::memory_order_relaxed);
+  return VMCK_OK;
+}
+
+extern "C" uint64_t vmck_wait_limit_ns(void) { return vmck::g_wait_ns.load(); }
 
 extern "C" const char *vmck_last_error(void) { return vmck::g_last_error; }
 

@@ -15,6 +15,9 @@ void set_last_error(const char *fmt, ...);
 
 void count_launch();
 
+// Wall-time limit (ns) of the device-side waits for work (vmck_set_wait_limit_ns).
+unsigned long long wait_limit_ns();
+
 // Every kernel launch of the library is followed by check_launch, which also
 // counts it (vmck_launch_count).
 inline int check_launch(const char *what) {

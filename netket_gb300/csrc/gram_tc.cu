@@ -84,13 +84,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: true on completion, false when TC_WAIT_NS elapsed.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded wait: true on completion, false when `limit` ns of wall time elapsed.
+// Waits for work use the library's wait limit (vmck_set_wait_limit_ns); the
+// wind-down waits for copies and MMAs already issued always use TC_WAIT_NS, so a
+// CTA never exits with a copy into its shared memory or an MMA still in flight.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned long long limit = TC_WAIT_NS) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (global_ns() - t0 > TC_WAIT_NS) return false;
+    if (global_ns() - t0 > limit) return false;
   }
 }
 
@@ -227,6 +231,7 @@ struct TcEpilogue {
   double *T64;
   float *T32;
   int32_t *status;
+  unsigned long long wait_ns;  // limit of the waits for work
 };
 
 __device__ inline void tc_tri_tile(int64_t bid, int64_t &I, int64_t &J) {
@@ -308,7 +313,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc_tri_tile(tile, I, J);
         for (int kb = 0; kb < num_kb; ++kb, ++it) {
           const int s = (int)(it % TC_STAGES);
-          if (it >= TC_STAGES && !mbar_wait(&empty[s], (uint32_t)(((it / TC_STAGES) - 1) & 1))) {
+          if (it >= TC_STAGES &&
+              !mbar_wait(&empty[s], (uint32_t)(((it / TC_STAGES) - 1) & 1), ep.wait_ns)) {
             fail();
             break;
           }
@@ -332,7 +338,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       bool issued_any = false;
       for (int64_t tile = blockIdx.x; tile < n_tiles && !*abort_flag; tile += gridDim.x, ++tcount) {
         const int b = (int)(tcount & 1);
-        if (tcount >= 2 && !mbar_wait(&tempty[b], (uint32_t)(((tcount >> 1) - 1) & 1))) {
+        if (tcount >= 2 &&
+            !mbar_wait(&tempty[b], (uint32_t)(((tcount >> 1) - 1) & 1), ep.wait_ns)) {
           fail();
           break;
         }
@@ -340,7 +347,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         bool ok = true;
         for (int kb = 0; kb < num_kb; ++kb, ++it) {
           const int s = (int)(it % TC_STAGES);
-          if (!mbar_wait(&full[s], (uint32_t)((it / TC_STAGES) & 1))) {
+          if (!mbar_wait(&full[s], (uint32_t)((it / TC_STAGES) & 1), ep.wait_ns)) {
             fail();
             ok = false;
             break;
@@ -423,7 +430,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const df32 wr_s0 = df_add(df32{wrow.x, wrow.y}, s0sq);
       const df32 nh_row = {-hrow.x, -hrow.y};
       __syncwarp();
-      if (!mbar_wait(&tfull[b], (uint32_t)((tcount >> 1) & 1))) {
+      if (!mbar_wait(&tfull[b], (uint32_t)((tcount >> 1) & 1), ep.wait_ns)) {
         fail();
         break;
       }
@@ -574,7 +581,8 @@ int gram_tc_launch(vmck_ctx *ctx, cudaStream_t st, const float *tanh_theta, cons
   VMCK_CUDA(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
   const int64_t nt = (n + TC_BM - 1) / TC_BM, tiles = nt * (nt + 1) / 2;
-  TcEpilogue ep{bits, words, N, n, h, w, s0sq, (float)inv_n, diag_shift, T64, T32, status};
+  TcEpilogue ep{bits, words, N, n, h, w, s0sq, (float)inv_n, diag_shift, T64, T32, status,
+                wait_limit_ns()};
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -581,11 +581,11 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsm_leaf_kernel(const float *__
 // are persistent: CTAs take block tickets in order from an atomic counter, so
 // every block a CTA waits for has been claimed by a CTA that is already running
 // and that never waits for a later block; a finished block is published with a
-// release store of the call's epoch into its flag.  Waits are bounded
-// (TRSV_WAIT_NS of wall time); a wait that runs out raises VMCK_DEV_TIMEOUT and
-// sets the abort word, which makes every other wait give up at once.
+// release store of the call's epoch into its flag.  Waits are bounded (the
+// library's wait limit, 2 s of wall time by default); a wait that runs out raises
+// VMCK_DEV_TIMEOUT and sets the abort word, which makes every other wait give up
+// at once.  A CTA holds nothing when it gives up (no copies or MMAs in flight).
 constexpr int TB = 128;
-constexpr unsigned long long TRSV_WAIT_NS = 2000000000ull;
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   unsigned v;
@@ -603,12 +603,12 @@ __device__ __forceinline__ unsigned long long wall_ns() {
 
 // Every lane of the warp spins; returns false if the solve was aborted.
 __device__ __forceinline__ bool trsv_wait(const unsigned *flag, unsigned epoch, unsigned *abort_w,
-                          int32_t *status) {
+                          int32_t *status, unsigned long long limit) {
   const unsigned long long t0 = wall_ns();
   for (unsigned it = 0;; ++it) {
     if (ld_acquire_u32(flag) == epoch) return true;
     if (ld_acquire_u32(abort_w) == epoch) return false;
-    if ((it & 63) == 63 && wall_ns() - t0 > TRSV_WAIT_NS) {
+    if (it >= 4 && wall_ns() - t0 > limit) {
       if (status) atomicOr(status, VMCK_DEV_TIMEOUT);
       atomicExch(abort_w, epoch);
       return false;
@@ -647,6 +647,7 @@ struct TrsvSync {
   unsigned *flags;   // nb
   unsigned *ticket;  // 1
   unsigned *abort_w; // 1
+  unsigned long long wait_ns;  // limit of each wait
 };
 
 // y = U^-T r.  Block K: z = r_K - sum_{J<K} U_JK^T y_J (warp w: columns 8w..8w+7 of
@@ -690,7 +691,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_fwd_kernel(const float *__r
         u[q] = (c < mk) ? __ldg(reinterpret_cast<const float4 *>(U + (k0 + c) * n + (int64_t)J * TB) + lane)
                         : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       }
-      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status);
+      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status, sy.wait_ns);
       if (!alive) break;
       const float4 yj = __ldcg(reinterpret_cast<const float4 *>(y + (int64_t)J * TB) + lane);
 #pragma unroll
@@ -773,7 +774,7 @@ __global__ void __launch_bounds__(LEAF_THREADS) trsv_bwd_kernel(const float *__r
                              rr + 2 < mk ? col[rr + 2] : 0.0f, 0.0f);
         }
       }
-      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status);
+      alive = trsv_wait(sy.flags + J, epoch, sy.abort_w, status, sy.wait_ns);
       if (!alive) break;
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
@@ -1263,8 +1264,8 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
   float *yinv = reinterpret_cast<float *>(aux + yinv_off);
   float *y32 = reinterpret_cast<float *>(aux + y32_off);
   unsigned *sync = reinterpret_cast<unsigned *>(aux + sync_off);
-  const TrsvSync sync_f{sync, sync + 2 * nb, sync + 2 * nb + 2};
-  const TrsvSync sync_b{sync + nb, sync + 2 * nb + 1, sync + 2 * nb + 2};
+  const TrsvSync sync_f{sync, sync + 2 * nb, sync + 2 * nb + 2, wait_limit_ns()};
+  const TrsvSync sync_b{sync + nb, sync + 2 * nb + 1, sync + 2 * nb + 2, wait_limit_ns()};
   if (factor_mode >= 2) {
     VMCK_BLAS(cublasSetMathMode(c->blas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
     VMCK_BLAS(cublasSetEmulationStrategy(c->blas, CUBLAS_EMULATION_STRATEGY_EAGER));

@@ -17,6 +17,7 @@
 // With no hoppable cluster the proposal is x itself with a NaN correction in
 // NetKet, which is never accepted; here it is rejected directly.
 #include <algorithm>
+#include <cstdlib>
 
 #include "common.cuh"
 
@@ -540,7 +541,11 @@ int launch_metropolis(cudaStream_t st, const void *params, int N, int M, int8_t 
   int grid = (B + wpb - 1) / wpb;
   const T *p = static_cast<const T *>(params);
   uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  if (sizeof(T) == 4 && rule == 1 && C <= 1024 && M <= 512) {
+  // VMCK_EXCHANGE_GENERIC=1 routes the Exchange rule to metropolis_kernel<float, 1>
+  // (read per call): the parity tests run both kernels on the same seeds.
+  const char *generic = getenv("VMCK_EXCHANGE_GENERIC");
+  const bool force_generic = generic && generic[0] == '1';
+  if (sizeof(T) == 4 && rule == 1 && C <= 1024 && M <= 512 && !force_generic) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

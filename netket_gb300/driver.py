@@ -172,7 +172,7 @@ class AbstractVariationalDriver:
             callbacks.on_run_end(self.step_count, self)
         except cb.StopRun as error:
             callbacks.on_run_end(self.step_count, self)
-            print("Stopping early because of : ", error)
+            print(f"run stopped before the last step: {error}")
         except KeyboardInterrupt as error:
             callbacks.on_run_error(self.step_count, error, self)
             if hasattr(sys, "ps1"):

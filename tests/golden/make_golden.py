@@ -31,8 +31,7 @@ Covered:
                  cholesky_with_fallback (optimizer/solver/solvers.py,
                  _src/solvers/nan_fallback.py:22-45)
 
-Run:  python tests/golden/make_golden.py [REFERENCE_ROOT]
-(default reference root: /root/reference).
+Run:  python tests/golden/make_golden.py REFERENCE_ROOT   (or set NETKET_REFERENCE_ROOT)
 """
 import __future__
 import ast
@@ -50,7 +49,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+# The reference checkout to read: the first argument or $NETKET_REFERENCE_ROOT
+# (required; the fixtures are generated from that tree's own source files).
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NETKET_REFERENCE_ROOT")
+if not REF:
+    sys.exit("usage: make_golden.py REFERENCE_ROOT (or set NETKET_REFERENCE_ROOT): the path of "
+             "the NetKet source tree whose functions generate the fixtures")
 NK = os.path.join(REF, "netket")
 
 

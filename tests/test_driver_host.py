@@ -154,7 +154,7 @@ def test_legacy_callback_falsy_return_stops_before_the_update(capsys):
     assert seen == [0, 1, 2] and drv.step_count == 2
     np.testing.assert_allclose(drv.state._flat.numpy(), np.arange(11.0) * 0.25)
     assert list(log["Energy"].iters) == [0, 1]
-    assert "Stopping early" in capsys.readouterr().out
+    assert "run stopped before the last step" in capsys.readouterr().out
 
     drv2 = FakeDriver()
     drv2.run(5, callback=lambda s, d, dr: None, show_progress=False)

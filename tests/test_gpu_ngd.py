@@ -345,3 +345,53 @@ def test_vmc_sr_spring_driver(nk):
                              use_ntk=False, proj_reg=0.1)
     with pytest.raises(ValueError, match="proj_reg"):
         drv_s.advance(1)
+
+
+def test_bounded_waits_run_out_and_recover(nk):
+    """Device-side waits are bounded (vmck_set_wait_limit_ns).  With the limit
+    shortened to 1 ns the tensor-core Gram (pipeline waits between its TMA, MMA
+    and epilogue warps) and the refined solve (waits between the CTAs of the
+    persistent triangular solves) wind down and report VMCK_DEV_TIMEOUT instead
+    of hanging; with the default restored the next calls on the same context give
+    the right results."""
+    L = nk._native.lib()
+    default = L.vmck_wait_limit_ns()
+    assert default == 2_000_000_000
+    N, alpha, n = 100, 4, 2048
+    model, flat, M, x, t, p = _problem(nk, N, alpha, n)
+    t32 = t.float().contiguous()
+    obar = nk.kernels.column_means(t, x, N, M)
+    st0 = torch.zeros(1, dtype=torch.int32, device="cuda")
+    T64, T32 = nk.kernels.gram_structured(t32, x, N, M, obar, 1e-3, mode=2, want_f32=True,
+                                          status=st0)
+    assert st0.item() == 0
+    T64, T32 = T64.clone(), T32.clone()
+    ns = 8192
+    rng = np.random.default_rng(5)
+    U = rng.normal(size=(ns, 200))
+    A = U @ U.T / 200 + 1e-3 * np.eye(ns)
+    b = rng.normal(size=ns)
+    At, bt = torch.as_tensor(A, device="cuda"), torch.as_tensor(b, device="cuda")
+    try:
+        L.vmck_set_wait_limit_ns(1)
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        nk.kernels.gram_structured(t32, x, N, M, obar, 1e-3, mode=2, want_f32=True, status=st)
+        torch.cuda.synchronize()
+        assert st.item() & nk._native.DEV_TIMEOUT
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        nk.kernels.cholesky_solve_refined(At, At.float().contiguous(), bt, st, max_iter=2)
+        torch.cuda.synchronize()
+        assert st.item() & nk._native.DEV_TIMEOUT
+    finally:
+        L.vmck_set_wait_limit_ns(default)
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    G64, G32 = nk.kernels.gram_structured(t32, x, N, M, obar, 1e-3, mode=2, want_f32=True,
+                                          status=st)
+    assert st.item() == 0
+    low = torch.tril(torch.ones(n, n, dtype=torch.bool, device="cuda"))
+    assert torch.equal(G64[low], T64[low]) and torch.equal(G32[low], T32[low])
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    xs, res = nk.kernels.cholesky_solve_refined(At, At.float().contiguous(), bt, st, max_iter=6)
+    assert st.item() == 0 and res.item() < 1e-10
+    ref = np.linalg.solve(A, b)
+    np.testing.assert_allclose(xs.cpu().numpy(), ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max())

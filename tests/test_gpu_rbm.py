@@ -61,16 +61,19 @@ def test_eloc_ising(nk, N, h, J):
     np.testing.assert_allclose(d32, ref, rtol=1e-4, atol=1e-4 * scale)
 
 
-@pytest.mark.parametrize("L,J,order", [(4, 1.0, 1), (6, [1.0, 0.5], 2), (10, [1.0, 0.5], 2)])
-def test_eloc_heisenberg(nk, L, J, order):
+@pytest.mark.parametrize("L,J,order,alpha,sign_rule", [
+    (4, 1.0, 1, 2, None), (6, [1.0, 0.5], 2, 2, None), (10, [1.0, 0.5], 2, 2, None),
+    # the benchmark's Hamiltonian and width: 10x10 J1-J2, Marshall sign on J1, M = 400
+    (10, [1.0, 0.5], 2, 4, [True, False])])
+def test_eloc_heisenberg(nk, L, J, order, alpha, sign_rule):
     N = L * L
-    model, flat, M = _setup(nk, N, 2, 4)
+    model, flat, M = _setup(nk, N, alpha, 4)
     g = nk.graph.Square(L, max_neighbor_order=order)
     hi = nk.hilbert.Spin(0.5, N, total_sz=0)
-    H = nk.operator.Heisenberg(hi, g, J=J)
+    H = nk.operator.Heisenberg(hi, g, J=J, sign_rule=sign_rule)
     x = hi.random_state(seed=9, size=300)
     ref = orbm.local_energies(oracle_params(flat, N, M), x.cpu().numpy(),
-                              oracle_heisenberg(g, J).get_conn_padded)
+                              oracle_heisenberg(g, J, sign_rule).get_conn_padded)
     e64 = nk.kernels.local_energies_fused(H, flat, x, N, M).cpu().numpy()
     d64 = nk.kernels.local_energies_dense(H, flat, x, N, M).cpu().numpy()
     e32 = nk.kernels.local_energies_fused(H, flat.float(), x, N, M).cpu().numpy()

@@ -84,6 +84,49 @@ def test_exchange_rule_distribution(nk, dtype, std, independent):
     assert _chi2_pvalues(nk, make, model, flat, N, 0, dtype, independent=independent) > 0.01
 
 
+@pytest.mark.parametrize("alpha,std", [(20, 0.12), (40, 0.09), (60, 0.07)])
+def test_exchange_smem_kernel_wide_hidden_layer_distribution(nk, alpha, std):
+    """The shared-memory Exchange kernel keeps M / 32 hidden units per lane in
+    registers and is instantiated for up to 4, 8, 13 and 16 of them.  M = 160,
+    320 and 480 (N = 8, Sz = 0, FP32) reach the 8-, 13- and 16-unit forms; the
+    13-unit form is the one the 10x10 alpha = 4 workload (M = 400) runs.  The
+    sample histogram must follow |psi|^2."""
+    N = 8
+    model = nk.models.RBM(alpha=alpha, kernel_init_std=std, hidden_bias_init_std=std,
+                          visible_bias_init_std=std)
+    flat = model.init_flat(21, N)
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    g = nk.graph.Chain(N, max_neighbor_order=2)
+    make = lambda nc: nk.sampler.MetropolisExchange(hi, graph=g, d_max=1, n_chains=nc)
+    assert _chi2_pvalues(nk, make, model, flat, N, 0, torch.float32, independent=True) > 0.01
+
+
+@pytest.mark.parametrize("L,alpha", [(10, 4), (10, 1), (10, 2), (6, 14)])
+def test_exchange_smem_kernel_matches_generic_kernel(nk, monkeypatch, L, alpha):
+    """At the benchmark's shape (10x10, nn + nnn clusters, FP32; M = 100, 200 and
+    400: the 4-, 8- and 13-unit forms) and on 6x6 with M = 504 (the 16-unit form;
+    at N = 100 its weights would not fit in shared memory) the shared-memory
+    Exchange kernel draws the same random numbers and evaluates the same
+    floating-point expressions as the generic warp-per-chain kernel: samples,
+    log-probabilities and acceptance counters are identical."""
+    N = L * L
+    model = nk.models.RBM(alpha=alpha)
+    flat = model.init_flat(4, N).float()
+    hi = nk.hilbert.Spin(0.5, N, total_sz=0)
+    g = nk.graph.Square(L, max_neighbor_order=2)
+    out = []
+    for generic in ("0", "1"):
+        monkeypatch.setenv("VMCK_EXCHANGE_GENERIC", generic)
+        sampler = nk.sampler.MetropolisExchange(hi, graph=g, d_max=1, n_chains=512)
+        st = sampler.init_state(model, flat, seed=17)
+        a, st = sampler.sample(model, flat, state=st, chain_length=4, n_discard=5)
+        out.append((a.clone(), st.log_prob.clone(), st.n_accepted_proc.clone()))
+    assert torch.equal(out[0][0], out[1][0])
+    assert torch.equal(out[0][1], out[1][1])
+    assert torch.equal(out[0][2], out[1][2])
+    assert torch.all(out[0][0].to(torch.int32).sum(-1) == 0)
+
+
 def test_sampler_bookkeeping(nk):
     N = 20
     model = nk.models.RBM(alpha=2)

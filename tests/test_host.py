@@ -290,7 +290,8 @@ def _header_prototypes():
     hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
     protos = {}
     for ret, name, args in re.findall(
-            r"\b(int64_t|int|const\s+char\s*\*)\s*(vmck_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", hdr):
+            r"\b(uint64_t|int64_t|int|const\s+char\s*\*)\s*(vmck_[a-z0-9_]+)\s*\(([^)]*)\)\s*;",
+            hdr):
         kinds = []
         for a in args.split(","):
             a = a.strip()
@@ -308,7 +309,7 @@ def _header_prototypes():
                 kinds.append("f64")
             else:
                 raise AssertionError(f"{name}: unclassified argument {a!r}")
-        rk = {"int": "i32", "int64_t": "i64"}.get(ret, "str")
+        rk = {"int": "i32", "int64_t": "i64", "uint64_t": "u64"}.get(ret, "str")
         protos[name] = (rk, kinds)
     return protos
 
@@ -331,7 +332,8 @@ def test_ctypes_signatures_match_header():
     for name, (args, res) in _native._SIGNATURES.items():
         rk, kinds = protos[name]
         assert [kind(a) for a in args] == kinds, name
-        exp_res = {"i32": ctypes.c_int32, "i64": ctypes.c_int64, "str": ctypes.c_char_p}[rk]
+        exp_res = {"i32": ctypes.c_int32, "i64": ctypes.c_int64, "u64": ctypes.c_uint64,
+                   "str": ctypes.c_char_p}[rk]
         assert res is exp_res, name
 
 
