@@ -1,0 +1,771 @@
+// Blocked Cholesky factorisation of an FP32 matrix on the tcgen05 tensor cores
+// (factor_mode 4 of vmck_cholesky_solve_refined): the factor of the FP32 copy
+// of T that iterative refinement against the FP64 matrix turns into an
+// FP64-accurate solve.  It replaces jax.scipy.linalg.cho_factor in
+// netket/optimizer/solver/solvers.py:266-268.
+//
+// Storage: the matrix is column-major with its UPPER triangle valid (row-major
+// lower triangle, the library's convention); the factor U (A = U^T U) replaces
+// it in place.
+//
+// Algorithm: right-looking, 512-row block rows, each factored in 128-row inner
+// panels:
+//   leaf   chol_leaf_kernel: one CTA factors the 128 x 128 diagonal block in
+//          shared memory and forms its inverse X = U_pp^-1;
+//   panel  U[r0:r1, r1:n] = X^T A[r0:r1, r1:n]  (a GEMM with K = 128);
+//   inner  A[r1:k1, r1:n] -= U[r0:r1, r1:k1]^T U[r0:r1, r1:n]  (K = 128), the
+//          rest of the block row;
+//   bulk   A[k1:n, k1:n] -= U[k0:k1, k1:n]^T U[k0:k1, k1:n]  (K = 512), once per
+//          block row.
+// Every GEMM runs in tc_gemm_kernel.  Its operands are FP32 values split into
+// two FP16 terms, t * s = hi + lo with s a power of two that keeps the operand
+// inside FP16's normal range (|t| s < 2^13), and it accumulates hi_a hi_b +
+// hi_a lo_b + lo_a hi_b in FP32 in tensor memory: 22 significant bits per
+// operand, so each product carries ~2^-21 relative error (lo_a lo_b, ~2^-22, is
+// dropped) - FP32-GEMM class, at three half-precision MMAs where a BF16 split
+// needs six.  Each GEMM's epilogue also writes the split form of the values the
+// next GEMM consumes (the panel rows), so no separate conversion pass runs.
+//
+// Scales: for SPD A every trailing-matrix entry is bounded by max_i A_ii and
+// every factor entry by sqrt(max_i A_ii); the leaf measures max |X| itself.
+// A matrix that is not SPD reports VMCK_DEV_NOT_SPD from the leaf (the pivot is
+// replaced by 1 so the run stays finite); the caller falls back.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "chol_tc.cuh"
+#include "tc_common.cuh"
+
+namespace vmck {
+
+// ------------------------------------------------------------ operand split
+// Power-of-two s with bound * s < 2^13 (exponent clamped); 1 for a bound that is
+// zero, negative or not finite.
+__device__ __forceinline__ float split_scale(float bound) {
+  if (!(bound > 0.0f) || !(bound <= 3.0e38f)) return 1.0f;
+  int e = 0;
+  frexpf(bound, &e);  // bound = f 2^e, f in [0.5, 1)
+  e = max(-100, min(100, e));
+  return ldexpf(1.0f, 13 - e);
+}
+
+__device__ __forceinline__ void split_f16(float v, float s, __half &hi, __half &lo) {
+  const float t = v * s;
+  hi = __float2half_rn(t);
+  lo = __float2half_rn(t - __half2float(hi));
+}
+
+// scales[0] = s(max diag A), scales[1] = s(sqrt(max diag A)); status gets
+// NONFINITE for a non-finite diagonal.  One block.
+__global__ void __launch_bounds__(256) chol_bounds_kernel(const float *__restrict__ A, int64_t n,
+                                                          float *scales, int32_t *status) {
+  __shared__ float red[8];
+  float m = 0.0f;
+  bool bad = false;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const float d = A[i + i * n];
+    bad |= !isfinite(d);
+    m = fmaxf(m, fabsf(d));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  bad = __syncthreads_or(bad);
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < 8; ++w) t = fmaxf(t, red[w]);
+    scales[0] = split_scale(t);
+    scales[1] = split_scale(sqrtf(t));
+    if (bad && status) atomicOr(status, VMCK_DEV_NONFINITE);
+  }
+}
+
+// B operand of the first panel GEMM: out[j * ldo + i] = split(A(r0 + i, c0 + j))
+// for i < rows (column-major A), zero for i in [rows, ldo).
+__global__ void chol_split_rows_kernel(const float *__restrict__ A, int64_t n, int64_t r0,
+                                       int64_t c0, int rows, int64_t cols, int ldo,
+                                       const float *scales, __half *oh, __half *ol) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= cols * ldo) return;
+  const int64_t j = e / ldo;
+  const int i = (int)(e - j * ldo);
+  __half hi = __float2half_rn(0.0f), lo = hi;
+  if (i < rows) split_f16(A[(r0 + i) + (c0 + j) * n], scales[0], hi, lo);
+  oh[e] = hi;
+  ol[e] = lo;
+}
+
+// ------------------------------------------------------------ the GEMM
+// C[m + nn ldc] = alpha (A_op B_op^T)(m, nn) / (sa sb) + beta C[m + nn ldc]
+// with A_op (M x K) and B_op (N x K) given as split FP16 pairs whose rows are
+// K-contiguous (TMA tensors: x = K, y = row).  tri: only m <= nn is written and
+// tiles wholly below the diagonal are skipped.  Optional split output of the
+// result: oh/ol[(nn - o_col0) ldo + m] = split(value * so) for m < o_rows,
+// nn >= o_col0.
+//
+// Persistent and warp-specialised like the Gram kernel: warp 0 streams 64-wide
+// K slabs of the four operand tiles with TMA (128-byte swizzle) into a 2-stage
+// ring, warp 1 issues three tcgen05.mma (kind::f16, M = 128, N = 256) per 16-wide
+// K step from one thread, warps 2-9 drain the tensor-memory accumulator (two
+// 256-column buffers, so a tile's epilogue overlaps the next tile's MMAs) with
+// coalesced column-major stores.  Waits for work are bounded by the library's
+// wait limit; a wait that runs out sets VMCK_DEV_TIMEOUT and the CTA winds down.
+constexpr int G_BM = 128, G_BN = 256, G_BK = 64, G_STAGES = 2;
+constexpr int G_EPI_WARPS = 8;
+constexpr int G_THREADS = 32 * (2 + G_EPI_WARPS);
+constexpr int G_TMEM_COLS = 2 * G_BN;
+constexpr int G_A_BYTES = G_BM * G_BK * 2;  // 16 KB (one of hi / lo)
+constexpr int G_B_BYTES = G_BN * G_BK * 2;  // 32 KB
+constexpr int G_STAGE_BYTES = 2 * G_A_BYTES + 2 * G_B_BYTES;
+constexpr int G_UMMA_K = 16;
+constexpr int G_CHUNK = 16;  // epilogue columns per tensor-memory load
+
+struct GemmParams {
+  int M, N, K;
+  int a_row0, b_row0, k_off;  // TMA coordinates of A_op row 0, B_op row 0, first K
+  float *C;
+  int64_t ldc;
+  float alpha, beta;
+  const float *sa, *sb;
+  int tri;
+  __half *oh, *ol;
+  int64_t ldo;
+  int o_rows, o_col0;
+  const float *so;
+  int32_t *status;
+  unsigned long long wait_ns;
+  int mt, nt;
+  int64_t tiles;
+};
+
+// Tile t -> (mi, ni).  Upper-triangular launches (BN = 2 BM, common origin):
+// column tile ni holds row tiles 0 .. min(mt, 2 ni + 2) - 1.
+__device__ __forceinline__ int64_t tri_cum(int64_t ni, int64_t mt) {
+  const int64_t h = mt / 2;
+  return ni <= h ? ni * (ni + 1) : h * (h + 1) + (ni - h) * mt;
+}
+__device__ __forceinline__ void gemm_tile(const GemmParams &g, int64_t t, int &mi, int &ni) {
+  if (!g.tri) {
+    mi = (int)(t % g.mt);
+    ni = (int)(t / g.mt);
+    return;
+  }
+  int lo = 0, hi = g.nt - 1;  // largest ni with tri_cum(ni) <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tri_cum(mid, g.mt) <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  ni = lo;
+  mi = (int)(t - tri_cum(lo, g.mt));
+}
+
+__global__ void __launch_bounds__(G_THREADS, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                   const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
+                   GemmParams g) {
+  extern __shared__ __align__(1024) unsigned char g_smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(g_smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + G_STAGES * G_STAGE_BYTES);
+  uint64_t *empty = full + G_STAGES;
+  uint64_t *tfull = empty + G_STAGES;  // [2]
+  uint64_t *tempty = tfull + 2;        // [2]
+  uint64_t *drain = tempty + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0)
+    *abort_flag =
+        (g.status && (*reinterpret_cast<volatile int32_t *>(g.status) & VMCK_DEV_TIMEOUT)) ? 1 : 0;
+  __syncthreads();
+  if (*abort_flag) return;
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(G_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < G_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], G_EPI_WARPS);
+    }
+    mbar_init(drain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mAh)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mAl)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mBh)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mBl)) : "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+  const int num_kb = (g.K + G_BK - 1) / G_BK;
+
+  auto fail = [&]() {
+    if (g.status) atomicOr(g.status, VMCK_DEV_TIMEOUT);
+    *abort_flag = 1;
+  };
+
+  if (warp == 0) {
+    // ---------------- TMA producer
+    if (lane == 0) {
+      int64_t it = 0;
+      for (int64_t tile = blockIdx.x; tile < g.tiles && !*abort_flag; tile += gridDim.x) {
+        int mi, ni;
+        gemm_tile(g, tile, mi, ni);
+        const int ya = g.a_row0 + mi * G_BM, yb = g.b_row0 + ni * G_BN;
+        for (int kb = 0; kb < num_kb; ++kb, ++it) {
+          const int s = (int)(it % G_STAGES);
+          if (it >= G_STAGES &&
+              !mbar_wait(&empty[s], (uint32_t)(((it / G_STAGES) - 1) & 1), g.wait_ns)) {
+            fail();
+            break;
+          }
+          if (*abort_flag) break;
+          unsigned char *st = smem + s * G_STAGE_BYTES;
+          const int x = g.k_off + kb * G_BK;
+          mbar_expect_tx(&full[s], G_STAGE_BYTES);
+          tma_load_2d(st, &mAh, &full[s], x, ya);
+          tma_load_2d(st + G_A_BYTES, &mAl, &full[s], x, ya);
+          tma_load_2d(st + 2 * G_A_BYTES, &mBh, &full[s], x, yb);
+          tma_load_2d(st + 2 * G_A_BYTES + G_B_BYTES / 2, &mBh, &full[s], x, yb + G_BN / 2);
+          tma_load_2d(st + 2 * G_A_BYTES + G_B_BYTES, &mBl, &full[s], x, yb);
+          tma_load_2d(st + 2 * G_A_BYTES + G_B_BYTES + G_B_BYTES / 2, &mBl, &full[s], x,
+                      yb + G_BN / 2);
+        }
+      }
+      // every copy issued must land before the CTA may exit
+      const int64_t first = it > G_STAGES ? it - G_STAGES : 0;
+      for (int64_t q = first; q < it; ++q)
+        mbar_wait(&full[q % G_STAGES], (uint32_t)((q / G_STAGES) & 1));
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = umma_idesc_f16(G_BM, G_BN);
+      int64_t it = 0, tcount = 0;
+      bool issued_any = false;
+      for (int64_t tile = blockIdx.x; tile < g.tiles && !*abort_flag;
+           tile += gridDim.x, ++tcount) {
+        const int b = (int)(tcount & 1);
+        if (tcount >= 2 &&
+            !mbar_wait(&tempty[b], (uint32_t)(((tcount >> 1) - 1) & 1), g.wait_ns)) {
+          fail();
+          break;
+        }
+        tc_fence_after();
+        const uint32_t dacc = tmem_base + (uint32_t)(b * G_BN);
+        bool ok = true;
+        for (int kb = 0; kb < num_kb; ++kb, ++it) {
+          const int s = (int)(it % G_STAGES);
+          if (!mbar_wait(&full[s], (uint32_t)((it / G_STAGES) & 1), g.wait_ns)) {
+            fail();
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t ah = smem_u32(smem + s * G_STAGE_BYTES);
+          const uint32_t al = ah + G_A_BYTES, bh = ah + 2 * G_A_BYTES, bl = bh + G_B_BYTES;
+#pragma unroll
+          for (int k = 0; k < G_BK / G_UMMA_K; ++k) {
+            const uint32_t off = k * G_UMMA_K * 2;
+            const uint64_t dah = umma_desc_sw128(ah + off), dal = umma_desc_sw128(al + off);
+            const uint64_t dbh = umma_desc_sw128(bh + off), dbl = umma_desc_sw128(bl + off);
+            umma_f16(dacc, dah, dbh, idesc, (kb == 0 && k == 0) ? 0u : 1u);
+            umma_f16(dacc, dah, dbl, idesc, 1u);
+            umma_f16(dacc, dal, dbh, idesc, 1u);
+          }
+          umma_commit(&empty[s]);
+          issued_any = true;
+        }
+        if (!ok) break;
+        umma_commit(&tfull[b]);
+      }
+      if (issued_any) {
+        umma_commit(drain);
+        mbar_wait(drain, 0);
+      }
+    }
+  } else {
+    // ---------------- epilogue: warp e reads TMEM lane quarter (warp & 3),
+    // columns [128 * (e >> 2), +128) of the 256-column accumulator
+    const int e = warp - 2, quarter = warp & 3, half = e >> 2;
+    const float inv_s = 1.0f / ((g.sa ? *g.sa : 1.0f) * (g.sb ? *g.sb : 1.0f));
+    const float alpha = g.alpha * inv_s;
+    const float so = g.so ? *g.so : 1.0f;
+    int64_t tcount = 0;
+    for (int64_t tile = blockIdx.x; tile < g.tiles; tile += gridDim.x, ++tcount) {
+      const int b = (int)(tcount & 1);
+      int mi, ni;
+      gemm_tile(g, tile, mi, ni);
+      const int m = mi * G_BM + quarter * 32 + lane;
+      const int nbase = ni * G_BN + half * 128;
+      if (!mbar_wait(&tfull[b], (uint32_t)((tcount >> 1) & 1), g.wait_ns)) {
+        fail();
+        break;
+      }
+      if (*abort_flag) break;
+      tc_fence_after();
+      const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) +
+                             (uint32_t)(b * G_BN + half * 128);
+      const bool row_ok = m < g.M;
+      float *Crow = g.C + m;
+#pragma unroll 1
+      for (int ch = 0; ch < 128 / G_CHUNK; ++ch) {
+        const int n0 = nbase + ch * G_CHUNK;
+        float old[G_CHUNK];
+        if (g.beta != 0.0f) {
+#pragma unroll
+          for (int j = 0; j < G_CHUNK; ++j) {
+            const int nn = n0 + j;
+            old[j] = (row_ok && nn < g.N && (!g.tri || m <= nn)) ? Crow[(int64_t)nn * g.ldc]
+                                                                   : 0.0f;
+          }
+        }
+        float v[G_CHUNK];
+        tmem_ld_16cols(taddr + ch * G_CHUNK, v);
+        tmem_wait_ld();
+        if (ch == 128 / G_CHUNK - 1) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[b]);
+        }
+#pragma unroll
+        for (int j = 0; j < G_CHUNK; ++j) {
+          const int nn = n0 + j;
+          if (!row_ok || nn >= g.N || (g.tri && m > nn)) continue;
+          float val = alpha * v[j];
+          if (g.beta != 0.0f) val = fmaf(g.beta, old[j], val);
+          Crow[(int64_t)nn * g.ldc] = val;
+          if (g.oh && m < g.o_rows && nn >= g.o_col0) {
+            __half hi, lo;
+            split_f16(val, so, hi, lo);
+            const int64_t o = (int64_t)(nn - g.o_col0) * g.ldo + m;
+            g.oh[o] = hi;
+            g.ol[o] = lo;
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(G_TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ------------------------------------------------------------ the leaf
+// One CTA factors the mp x mp (mp <= 128) diagonal block at (r0, r0) of the
+// column-major upper A in shared memory and forms X = U^-1:
+//   (a) per 32-wide sub-panel p, warp 0 factors the 32 x 32 diagonal block in
+//       registers (lane l holds column l) and inverts it (back substitution,
+//       lane l: column l of the inverse);
+//   (b) the panel row U(P+i, j) = sum_k X_pp(k, i) A(P+k, j), all threads;
+//   (c) the rank-32 update of the trailing block (4 x 4 register tiles);
+// then the off-diagonal 32 x 32 blocks of X by block back substitution.
+// Writes U in place, X split into K-contiguous rows (xh/xl[m * 128 + k] = X(k, m),
+// scale from max |X| into *scale_x) and Y = X^T zero-padded column-major
+// 128 x 128 (the refinement's triangular solves).  Rows / columns past mp are
+// the identity.  A non-positive or NaN pivot raises VMCK_DEV_NOT_SPD and is
+// replaced by 1.
+constexpr int LB = 128, LLD = LB + 1, LEAF_T = 256;
+constexpr size_t CHOL_LEAF_SMEM = (size_t)(2 * LB * LLD + 3 * 32 * 33) * sizeof(float);
+
+__global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A, int64_t n,
+                                                           int64_t r0, int mp,
+                                                           __half *__restrict__ xh,
+                                                           __half *__restrict__ xl,
+                                                           float *scale_x, float *__restrict__ yinv,
+                                                           int32_t *status) {
+  extern __shared__ float lsm[];
+  float *S = lsm;             // S[i * LLD + j] = U(i, j), i <= j; zero below
+  float *X = lsm + LB * LLD;  // X[i * LLD + j] = U^-1(i, j)
+  float *Tb = X + LB * LLD;   // 3 x [32][33] temporaries of the inverse
+  __shared__ float red[LEAF_T / 32];
+  __shared__ int not_spd;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) not_spd = 0;
+  for (int e = tid; e < LB * LB; e += LEAF_T) {
+    const int j = e / LB, i = e - j * LB;
+    float v = 0.0f;
+    if (i <= j) {
+      if (j < mp) v = A[(r0 + i) + (r0 + j) * n];
+      else if (i == j) v = 1.0f;
+    }
+    S[i * LLD + j] = v;
+    X[i * LLD + j] = 0.0f;
+  }
+  __syncthreads();
+  for (int p = 0; p < 4; ++p) {
+    const int P = 32 * p;
+    if (warp == 0) {
+      float c[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) c[i] = S[(P + i) * LLD + P + lane];
+      bool bad = false;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        float d = __shfl_sync(0xffffffffu, c[k], k);
+        if (!(d > 0.0f)) {
+          bad = true;
+          d = 1.0f;
+        }
+        const float ukk = sqrtf(d), rk = 1.0f / ukk;
+        if (lane == k) c[k] = ukk;
+        else if (lane > k) c[k] *= rk;
+#pragma unroll
+        for (int i = k + 1; i < 32; ++i) {
+          const float uki = __shfl_sync(0xffffffffu, c[k], i);
+          if (lane >= i) c[i] = fmaf(-uki, c[k], c[i]);
+        }
+      }
+      if (bad && lane == 0) not_spd = 1;
+      // inverse of the 32 x 32 upper block: lane l solves U x = e_l
+      float x[32];
+#pragma unroll
+      for (int i = 31; i >= 0; --i) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = i + 1; k < 32; ++k) {
+          const float uik = __shfl_sync(0xffffffffu, c[i], k);  // U(i, k) from lane k
+          if (k <= lane) acc = fmaf(uik, x[k], acc);
+        }
+        const float uii = __shfl_sync(0xffffffffu, c[i], i);
+        x[i] = (i == lane) ? 1.0f / uii : (i < lane ? -acc / uii : 0.0f);
+      }
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        S[(P + i) * LLD + P + lane] = (i <= lane) ? c[i] : 0.0f;
+        X[(P + i) * LLD + P + lane] = x[i];
+      }
+    }
+    __syncthreads();
+    const int ncols = LB - P - 32;
+    if (ncols > 0) {
+      // (b) panel row, in place: every thread reads its column first
+      const int tpc = ncols >= 96 ? 2 : (ncols >= 64 ? 4 : 8);  // threads per column
+      const int jj = tid % ncols, grp = tid / ncols;
+      const int j = P + 32 + jj;
+      const int per = 32 / tpc;
+      float in[32], out[16];
+      const bool active = grp < tpc;
+      if (active) {
+#pragma unroll
+        for (int k = 0; k < 32; ++k) in[k] = S[(P + k) * LLD + j];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          out[q] = 0.0f;
+          if (q < per) {
+            const int i = grp * per + q;
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+              if (k <= i) out[q] = fmaf(X[(P + k) * LLD + P + i], in[k], out[q]);
+          }
+        }
+      }
+      __syncthreads();
+      if (active) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (q < per) S[(P + grp * per + q) * LLD + j] = out[q];
+      }
+      __syncthreads();
+      // (c) trailing update of the upper triangle [P+32, 128)^2 in 4 x 4 tiles
+      const int T = ncols / 4, ntl = T * (T + 1) / 2;
+      const int base = P + 32;
+      for (int t = tid; t < ntl; t += LEAF_T) {
+        int tj = (int)((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
+        while (tj * (tj + 1) / 2 > t) --tj;
+        while ((tj + 1) * (tj + 2) / 2 <= t) ++tj;
+        const int ti = t - tj * (tj + 1) / 2;
+        const int i0 = base + 4 * ti, j0 = base + 4 * tj;
+        float acc[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[r][q] = S[(i0 + r) * LLD + j0 + q];
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+          const float *row = S + (P + k) * LLD;
+          float a[4], bq[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) a[r] = row[i0 + r];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) bq[q] = row[j0 + q];
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(-a[r], bq[q], acc[r][q]);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (i0 + r <= j0 + q) S[(i0 + r) * LLD + j0 + q] = acc[r][q];
+      }
+      __syncthreads();
+    }
+  }
+  // off-diagonal blocks of X: X_IJ = -X_II sum_{K=I+1..J} U_IK X_KJ, by distance d
+  for (int d = 1; d < 4; ++d) {
+    const int nblk = 4 - d;
+    // phase 1: Tb[blk] = sum_K U_IK X_KJ  (I = blk, J = blk + d)
+    for (int e = tid; e < nblk * 1024; e += LEAF_T) {
+      const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
+      const int I = blk, J = blk + d;
+      float acc = 0.0f;
+      for (int K = I + 1; K <= J; ++K) {
+        const float *urow = S + (32 * I + r) * LLD + 32 * K;
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) acc = fmaf(urow[k], X[(32 * K + k) * LLD + 32 * J + cc], acc);
+      }
+      Tb[blk * 32 * 33 + r * 33 + cc] = acc;
+    }
+    __syncthreads();
+    // phase 2: X_IJ = -X_II Tb[blk]
+    for (int e = tid; e < nblk * 1024; e += LEAF_T) {
+      const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
+      const int I = blk, J = blk + d;
+      const float *xrow = X + (32 * I + r) * LLD + 32 * I;
+      float acc = 0.0f;
+#pragma unroll 8
+      for (int k = 0; k < 32; ++k) acc = fmaf(xrow[k], Tb[blk * 32 * 33 + k * 33 + cc], acc);
+      X[(32 * I + r) * LLD + 32 * J + cc] = -acc;
+    }
+    __syncthreads();
+  }
+  // max |X| over the valid block -> split scale
+  float am = 0.0f;
+  for (int e = tid; e < mp * mp; e += LEAF_T) {
+    const int i = e / mp, j = e - i * mp;
+    if (i <= j) am = fmaxf(am, fabsf(X[i * LLD + j]));
+  }
+  for (int o = 16; o > 0; o >>= 1) am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
+  if (lane == 0) red[warp] = am;
+  __syncthreads();
+  float amax = 0.0f;
+#pragma unroll
+  for (int w = 0; w < LEAF_T / 32; ++w) amax = fmaxf(amax, red[w]);
+  const float sx = split_scale(amax);
+  if (tid == 0) {
+    *scale_x = sx;
+    if (not_spd && status) atomicOr(status, VMCK_DEV_NOT_SPD);
+  }
+  // outputs
+  for (int e = tid; e < mp * mp; e += LEAF_T) {
+    const int j = e / mp, i = e - j * mp;
+    if (i <= j) A[(r0 + i) + (r0 + j) * n] = S[i * LLD + j];
+  }
+  for (int e = tid; e < LB * LB; e += LEAF_T) {
+    const int m = e / LB, k = e - m * LB;  // row m of the split operand = column m of X
+    __half hi = __float2half_rn(0.0f), lo = hi;
+    if (m < mp && k < mp && k <= m) split_f16(X[k * LLD + m], sx, hi, lo);
+    xh[e] = hi;
+    xl[e] = lo;
+  }
+  for (int e = tid; e < LB * LB; e += LEAF_T) {
+    const int c = e / LB, r = e - c * LB;  // Y(r, c) = X(c, r)
+    yinv[e] = (c < mp && r < mp && c <= r) ? X[c * LLD + r] : 0.0f;
+  }
+}
+
+// ------------------------------------------------------------ host side
+static int make_f16_map(CUtensorMap *map, const __half *base, int64_t kdim, int64_t rows,
+                        int64_t ld) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_last_error("cuTensorMapEncodeTiled is unavailable");
+    return VMCK_ERR_CUDA;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)G_BK, (cuuint32_t)G_BM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half *>(base), dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_last_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return VMCK_ERR_CUDA;
+  }
+  return VMCK_OK;
+}
+
+struct SplitOperand {
+  const __half *hi, *lo;
+  int64_t ld;     // row stride (elements)
+  int64_t kdim;   // K extent seen by TMA (zero fill beyond)
+  int64_t rows;   // row extent seen by TMA (zero fill beyond)
+};
+
+static int num_sms_dev() {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+static size_t gemm_smem_bytes() { return 1024 + G_STAGES * G_STAGE_BYTES + 8 * 16 + 64; }
+
+int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOperand &b, int b_row0,
+            int k_off, int M, int N, int K, float *C, int64_t ldc, float alpha, float beta,
+            const float *sa, const float *sb, int tri, __half *oh, __half *ol, int64_t ldo,
+            int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas) {
+  if (M <= 0 || N <= 0 || K <= 0) return VMCK_OK;
+  CUtensorMap mAh, mAl, mBh, mBl;
+  int rc;
+  if ((rc = make_f16_map(&mAh, a.hi, a.kdim, a.rows, a.ld))) return rc;
+  if ((rc = make_f16_map(&mAl, a.lo, a.kdim, a.rows, a.ld))) return rc;
+  if ((rc = make_f16_map(&mBh, b.hi, b.kdim, b.rows, b.ld))) return rc;
+  if ((rc = make_f16_map(&mBl, b.lo, b.kdim, b.rows, b.ld))) return rc;
+  GemmParams g{};
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.a_row0 = a_row0;
+  g.b_row0 = b_row0;
+  g.k_off = k_off;
+  g.C = C;
+  g.ldc = ldc;
+  g.alpha = alpha;
+  g.beta = beta;
+  g.sa = sa;
+  g.sb = sb;
+  g.tri = tri;
+  g.oh = oh;
+  g.ol = ol;
+  g.ldo = ldo;
+  g.o_rows = o_rows;
+  g.o_col0 = o_col0;
+  g.so = so;
+  g.status = status;
+  g.wait_ns = wait_limit_ns();
+  g.mt = (M + G_BM - 1) / G_BM;
+  g.nt = (N + G_BN - 1) / G_BN;
+  if (tri) {
+    const int64_t h = g.mt / 2;
+    g.tiles = g.nt <= h ? (int64_t)g.nt * (g.nt + 1) : h * (h + 1) + (int64_t)(g.nt - h) * g.mt;
+  } else {
+    g.tiles = (int64_t)g.mt * g.nt;
+  }
+  const size_t smem = gemm_smem_bytes();
+  VMCK_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  const int sms = max_ctas > 0 ? max_ctas : num_sms_dev();
+  const unsigned grid = (unsigned)std::min<int64_t>(g.tiles, sms);
+  tc_gemm_kernel<<<grid, G_THREADS, smem, st>>>(mAh, mAl, mBh, mBl, g);
+  return check_launch("tc_gemm");
+}
+
+int64_t chol_tc_workspace_bytes(int64_t n) {
+  const int64_t nb = (n + LB - 1) / LB;
+  int64_t b = 0;
+  b += 2 * (int64_t)CHOL_BLOCK * n * 2;  // Ph hi / lo (K = 512 rows per column)
+  b += 2 * (int64_t)LB * n * 2;          // Bs hi / lo
+  b += 2 * (int64_t)LB * LB * 2;         // Xs hi / lo
+  b += 64;                               // scales
+  b += nb * LB * LB * 4;                 // Yinv
+  return b + 6 * 1024;                   // alignment
+}
+
+static char *align_up(char *p, size_t a) {
+  return reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + a - 1) & ~uintptr_t(a - 1));
+}
+
+int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *status,
+                   float **yinv_out) {
+  if (n <= 0) return VMCK_OK;
+  if (n >= (1ll << 30)) {
+    set_last_error("chol_tc: n must be below 2^30");
+    return VMCK_ERR_UNSUPPORTED;
+  }
+  char *p = align_up(static_cast<char *>(ws), 1024);
+  __half *ph_hi = reinterpret_cast<__half *>(p);
+  p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
+  __half *ph_lo = reinterpret_cast<__half *>(p);
+  p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
+  __half *bs_hi = reinterpret_cast<__half *>(p);
+  p = align_up(p + (size_t)LB * n * 2, 1024);
+  __half *bs_lo = reinterpret_cast<__half *>(p);
+  p = align_up(p + (size_t)LB * n * 2, 1024);
+  __half *xs_hi = reinterpret_cast<__half *>(p);
+  p = align_up(p + (size_t)LB * LB * 2, 1024);
+  __half *xs_lo = reinterpret_cast<__half *>(p);
+  p = align_up(p + (size_t)LB * LB * 2, 1024);
+  float *scales = reinterpret_cast<float *>(p);  // [0] A entries, [1] U entries, [2] X
+  p = align_up(p + 64, 1024);
+  float *yinv = reinterpret_cast<float *>(p);
+  if (yinv_out) *yinv_out = yinv;
+
+  int rc;
+  VMCK_CUDA(cudaFuncSetAttribute(chol_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)CHOL_LEAF_SMEM));
+  chol_bounds_kernel<<<1, 256, 0, st>>>(A, n, scales, status);
+  if ((rc = check_launch("chol_tc bounds"))) return rc;
+  {
+    const int rows = (int)std::min<int64_t>(LB, n);
+    const int64_t cols = n - rows;
+    if (cols > 0) {
+      chol_split_rows_kernel<<<ceil_div(cols * LB, 256), 256, 0, st>>>(
+          A, n, 0, rows, rows, cols, LB, scales, bs_hi, bs_lo);
+      if ((rc = check_launch("chol_tc split"))) return rc;
+    }
+  }
+  const SplitOperand xs{xs_hi, xs_lo, LB, LB, LB};
+  for (int64_t k0 = 0; k0 < n; k0 += CHOL_BLOCK) {
+    const int64_t k1 = std::min<int64_t>(n, k0 + CHOL_BLOCK), w = k1 - k0;
+    // the block row's split panel: row (c - k0) holds U(k0 .. k1, c) (K = w)
+    const SplitOperand ph{ph_hi, ph_lo, CHOL_BLOCK, w, n - k0};
+    for (int64_t r0 = k0; r0 < k1; r0 += LB) {
+      const int64_t r1 = std::min<int64_t>(k1, r0 + LB);
+      const int mp = (int)(r1 - r0), p = (int)((r0 - k0) / LB);
+      chol_leaf_kernel<<<1, LEAF_T, CHOL_LEAF_SMEM, st>>>(A, n, r0, mp, xs_hi, xs_lo, scales + 2,
+                                                          yinv + (r0 / LB) * LB * LB, status);
+      if ((rc = check_launch("chol_tc leaf"))) return rc;
+      if (r1 == n) break;
+      const SplitOperand xop{xs_hi, xs_lo, LB, mp, mp};
+      const SplitOperand bop{bs_hi, bs_lo, LB, mp, n - r1};
+      // panel: U[r0:r1, r1:n] = X^T A[r0:r1, r1:n], split copy into Ph
+      if ((rc = tc_gemm(st, xop, 0, bop, 0, 0, mp, (int)(n - r1), mp, A + r0 + r1 * n, n, 1.0f,
+                        0.0f, scales + 2, scales + 0, 0, ph_hi + (r1 - k0) * CHOL_BLOCK + p * LB,
+                        ph_lo + (r1 - k0) * CHOL_BLOCK + p * LB, CHOL_BLOCK, mp, 0, scales + 1,
+                        status, 0)))
+        return rc;
+      if (r1 < k1) {
+        // rest of the block row; rows [r1, r1 + next) feed the next panel (split)
+        const int next = (int)std::min<int64_t>(LB, k1 - r1);
+        const SplitOperand pk{ph_hi, ph_lo, CHOL_BLOCK, p * LB + mp, n - k0};
+        if ((rc = tc_gemm(st, pk, (int)(r1 - k0), pk, (int)(r1 - k0), p * LB, (int)(k1 - r1),
+                          (int)(n - r1), mp, A + r1 + r1 * n, n, -1.0f, 1.0f, scales + 1,
+                          scales + 1, 1, bs_hi, bs_lo, LB, next, next, scales + 0, status, 0)))
+          return rc;
+      }
+    }
+    if (k1 == n) break;
+    // trailing matrix by the whole block row; rows [k1, k1 + next) feed the next
+    // block row's first panel (split)
+    const int next = (int)std::min<int64_t>(LB, n - k1);
+    if ((rc = tc_gemm(st, ph, (int)w, ph, (int)w, 0, (int)(n - k1), (int)(n - k1), (int)w,
+                      A + k1 + k1 * n, n, -1.0f, 1.0f, scales + 1, scales + 1, 1, bs_hi, bs_lo,
+                      LB, next, next, scales + 0, status, 0)))
+      return rc;
+  }
+  return VMCK_OK;
+}
+
+}  // namespace vmck

@@ -1,0 +1,22 @@
+// Tensor-core blocked Cholesky (chol_tc.cu): the factor of the refined solve.
+#pragma once
+
+#include "common.cuh"
+
+namespace vmck {
+
+// Rows of a block row of the factorisation (the K of the trailing update).
+constexpr int CHOL_BLOCK = 512;
+
+// Device workspace (bytes) of chol_tc_factor for an n x n matrix.
+int64_t chol_tc_workspace_bytes(int64_t n);
+
+// In-place upper Cholesky A = U^T U of the column-major FP32 matrix A (n x n,
+// upper triangle valid, ld n).  ws: chol_tc_workspace_bytes(n) bytes.  On
+// return *yinv (inside ws) holds, per 128-row diagonal block K, Y_K = U_KK^-T as
+// a zero-padded column-major 128 x 128 matrix.  Failed pivots / non-finite
+// diagonals are OR-ed into *status.
+int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *status,
+                   float **yinv);
+
+}  // namespace vmck

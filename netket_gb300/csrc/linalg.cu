@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "chol_tc.cuh"
 #include "common.cuh"
 
 struct vmck_ctx {
@@ -37,6 +38,10 @@ struct vmck_ctx {
   cublasHandle_t blas2 = nullptr;
   cudaEvent_t *events = nullptr;
   int n_events = 0;
+  // tensor-core factorisation (factor_mode 4): split panels, leaf inverses, and
+  // the padded copy when n is not a multiple of 4
+  void *tcws = nullptr;
+  size_t tcws_bytes = 0;
 };
 
 namespace vmck {
@@ -142,10 +147,13 @@ __global__ void axpy_f2d_kernel(double *x, const float *d, int64_t n, const int 
   if (i < n) x[i] += (double)d[i];
 }
 
-// *done = 1 when ||r|| <= tol ||b|| (FP64 sums of squares, one block).
+// *done = 1 when ||r|| <= tol ||b|| (FP64 sums of squares, one block) or, with
+// prev (nullable), when ||r|| > prev / 2: the residual has stopped falling (the
+// FP64 rounding floor of the all-FP64 solve); prev then receives ||r||.
 __global__ void __launch_bounds__(256) refine_converged_kernel(const double *__restrict__ r,
                                                                const double *__restrict__ b,
-                                                               int64_t n, double tol, int *done) {
+                                                               int64_t n, double tol, int *done,
+                                                               double *prev = nullptr) {
   if (refine_done(done)) return;
   __shared__ double red[2][8];
   double sr = 0.0, sb = 0.0;
@@ -167,7 +175,12 @@ __global__ void __launch_bounds__(256) refine_converged_kernel(const double *__r
       tr += red[0][k];
       tb += red[1][k];
     }
-    if (sqrt(tr) <= tol * sqrt(tb)) *done = 1;  // false for NaN: the loop goes on
+    const double nr = sqrt(tr);
+    if (nr <= tol * sqrt(tb)) *done = 1;  // false for NaN: the loop goes on
+    if (prev) {
+      if (nr > 0.5 * *prev) *done = 1;
+      *prev = nr;
+    }
   }
 }
 
@@ -1137,14 +1150,107 @@ __global__ void symv_residual_reduce_kernel(const double *__restrict__ ws, int64
   r[i] = b[i] - s;
 }
 
+// The same tiling in plain FP64 arithmetic (FP64-pipe-bound): the residual of
+// the all-FP64 solve, whose accuracy must match a direct FP64 factorisation.
+__global__ void __launch_bounds__(256) symv_lower_partial_f64_kernel(
+    const double *__restrict__ A, int64_t n, const double *__restrict__ x,
+    double *__restrict__ ws, const int *done) {
+  if (refine_done(done)) return;
+  __shared__ double as[SY_T * SY_LD];
+  __shared__ double xr[SY_T], xc[SY_T];
+  __shared__ double part[4][SY_T];
+  int64_t I, J;
+  sy_tri_tile(blockIdx.x, I, J);
+  const int tid = threadIdx.x;
+  const int64_t r0 = I * SY_T, c0 = J * SY_T;
+  const bool diag = (I == J);
+  if (tid < SY_T) xc[tid] = (c0 + tid < n) ? x[c0 + tid] : 0.0;
+  else if (tid < 2 * SY_T) xr[tid - SY_T] = (r0 + tid - SY_T < n) ? x[r0 + tid - SY_T] : 0.0;
+  {
+    const int c = tid & 63, g = tid >> 6;
+    const bool cok = (c0 + c) < n;
+#pragma unroll 4
+    for (int k = 0; k < 16; ++k) {
+      const int r = g + 4 * k;
+      double v = 0.0;
+      if (cok && (r0 + r) < n && (!diag || r >= c)) v = A[(r0 + r) * n + c0 + c];
+      as[r * SY_LD + c] = v;
+    }
+  }
+  __syncthreads();
+  const int u = tid & 63, h = (tid >> 6) & 1;
+  double acc = 0.0;
+  if (tid < 128) {
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const int c = 32 * h + i;
+      acc = fma(as[u * SY_LD + c], xc[c], acc);
+    }
+  } else {
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const int r = 32 * h + i;
+      if (diag && r == u) continue;
+      acc = fma(as[r * SY_LD + u], xr[r], acc);
+    }
+  }
+  part[tid >> 6][u] = acc;
+  __syncthreads();
+  if (tid < SY_T) {
+    const int r = tid;
+    const double rs = part[0][r] + part[1][r];
+    const double cs = part[2][r] + part[3][r];
+    if (diag) {
+      if (r0 + r < n) ws[I * n + r0 + r] = rs + cs;
+    } else {
+      if (r0 + r < n) ws[J * n + r0 + r] = rs;
+      if (c0 + r < n) ws[I * n + c0 + r] = cs;
+    }
+  }
+}
+
 static int symv_residual(cudaStream_t st, const double *A, int64_t n, const double *x,
-                         const double *b, double *r, double *ws, const int *done) {
+                         const double *b, double *r, double *ws, const int *done,
+                         bool exact = false) {
   const int64_t nt = (n + SY_T - 1) / SY_T;
-  symv_lower_partial_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, st>>>(A, n, x, ws, done);
+  if (exact)
+    symv_lower_partial_f64_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, st>>>(A, n, x, ws,
+                                                                                 done);
+  else
+    symv_lower_partial_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, st>>>(A, n, x, ws, done);
   int rc = check_launch("symv partial");
   if (rc) return rc;
   symv_residual_reduce_kernel<<<ceil_div(n, 256), 256, 0, st>>>(ws, n, (int)nt, b, r, done);
   return check_launch("symv reduce");
+}
+
+// norms[0] = ||r||, norms[1] = ||b|| (FP64, one block, fixed reduction order).
+__global__ void __launch_bounds__(256) norms_kernel(const double *__restrict__ r,
+                                                    const double *__restrict__ b, int64_t n,
+                                                    double *norms) {
+  __shared__ double red[2][8];
+  double sr = 0.0, sb = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    sr = fma(r[i], r[i], sr);
+    sb = fma(b[i], b[i], sb);
+  }
+  sr = warp_sum(sr);
+  sb = warp_sum(sb);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][w] = sr;
+    red[1][w] = sb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tr = 0.0, tb = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      tr += red[0][k];
+      tb += red[1][k];
+    }
+    norms[0] = sqrt(tr);
+    norms[1] = sqrt(tb);
+  }
 }
 
 
@@ -1181,92 +1287,108 @@ extern "C" int vmck_ctx_destroy(vmck_ctx *c) {
   if (c->blas) cublasDestroy(c->blas);
   cudaFree(c->dwork);
   cudaFree(c->aux);
+  cudaFree(c->tcws);
   cudaFree(c->d_info);
   free(c->hwork);
   delete c;
   return VMCK_OK;
 }
 
-extern "C" int vmck_cholesky_solve(vmck_ctx *c, vmck_stream s, int32_t dtype, const void *A,
-                                   const void *b, void *x, int64_t n, int32_t *status) {
-  VMCK_REQUIRE(c && A && b && x && n > 0, "cholesky_solve arguments");
-  VMCK_REQUIRE(dtype == VMCK_F64 || dtype == VMCK_F32, "cholesky_solve dtype");
-  cudaStream_t st = as_stream(s);
-  int rc = bind(c, st);
-  if (rc) return rc;
-  const size_t es = dtype == VMCK_F64 ? 8 : 4;
-  const cudaDataType dt = dtype == VMCK_F64 ? CUDA_R_64F : CUDA_R_32F;
-  size_t dsize = 0, hsize = 0;
-  VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, dt, A,
-                                          n, dt, &dsize, &hsize));
-  const size_t fbytes = (size_t)n * n * es;
-  const size_t off = (fbytes + 255) & ~size_t(255);
-  if ((rc = grow(&c->dwork, &c->dwork_bytes, off + dsize + 256, st))) return rc;
-  if ((rc = grow_host(c, hsize))) return rc;
-  void *F = c->dwork;
-  void *work = static_cast<char *>(c->dwork) + off;
-  VMCK_CUDA(cudaMemcpyAsync(F, A, fbytes, cudaMemcpyDeviceToDevice, st));
-  VMCK_CUDA(cudaMemcpyAsync(x, b, (size_t)n * es, cudaMemcpyDeviceToDevice, st));
-  VMCK_SOLVER(cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, dt, F, n, dt, work,
-                               dsize, c->hwork, hsize, c->d_info));
-  VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, dt, F, n, dt, x,
-                               n, c->d_info));
-  if (dtype == VMCK_F64)
-    solve_check_kernel<double><<<1, 1024, 0, st>>>(c->d_info, static_cast<const double *>(x),
-                                                   static_cast<const double *>(b), n, status);
-  else
-    solve_check_kernel<float><<<1, 1024, 0, st>>>(c->d_info, static_cast<const float *>(x),
-                                                  static_cast<const float *>(b), n, status);
-  return check_launch("cholesky_solve check");
+namespace vmck {
+
+__global__ void pad_identity_kernel(float *F, int64_t n, int64_t np) {
+  for (int64_t i = n + threadIdx.x; i < np; i += blockDim.x) F[i + i * np] = 1.0f;
 }
 
-extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const double *A64,
-                                           float *A32, const double *b, double *x, int64_t n,
-                                           int32_t max_iter, double tol, int32_t factor_mode,
-                                           int32_t *status, double *residual_out) {
-  VMCK_REQUIRE(c && A64 && A32 && b && x && n > 0 && max_iter >= 1, "refined solve arguments");
-  VMCK_REQUIRE(factor_mode >= 0 && factor_mode <= 3, "factor_mode must be 0, 1, 2 or 3");
-  VMCK_REQUIRE(n < (1ll << 31), "refined solve size");
-  cudaStream_t st = as_stream(s);
-  int rc = bind(c, st);
-  if (rc) return rc;
-  const bool emulate = factor_mode != 0;
-  VMCK_SOLVER(cusolverDnSetMathMode(c->solver, emulate ? CUSOLVER_FP32_EMULATED_BF16X9_MATH
-                                                       : CUSOLVER_DEFAULT_MATH));
-  if (emulate)
-    VMCK_SOLVER(cusolverDnSetEmulationStrategy(c->solver, CUDA_EMULATION_STRATEGY_EAGER));
+__global__ void refine_init_kernel(double *norms, double *prev, int *done) {
+  if (threadIdx.x == 0) {
+    norms[0] = norms[1] = 0.0;
+    *prev = 1e300;
+    *done = 0;
+  }
+}
+
+struct RefineOpts {
+  int max_iter;
+  double stop_tol;   // stop once ||r|| <= stop_tol ||b||
+  double fail_tol;   // VMCK_DEV_NO_CONVERGE if the final ||r|| > fail_tol ||b||
+  int factor_mode;
+  bool exact;        // FP64 residual (else double-float, ~2^-46 per term)
+  bool stagnation;   // also stop when the residual stops falling
+};
+
+// FP32 factor of A32 (overwritten) + iterative refinement against A64.
+static int refined_solve(vmck_ctx *c, cudaStream_t st, const double *A64, float *A32,
+                         const double *b, double *x, int64_t n, const RefineOpts &o,
+                         int32_t *status, double *residual_out) {
+  const int factor_mode = o.factor_mode;
+  int rc = VMCK_OK;
   size_t dsize = 0, hsize = 0;
-  const int64_t fn = factor_mode == 2 ? std::min<int64_t>(n, CHOL_LEAF) : n;
-  VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, fn,
-                                          CUDA_R_32F, A32, n, CUDA_R_32F, &dsize, &hsize));
-  if ((rc = grow(&c->dwork, &c->dwork_bytes, dsize + 256, st))) return rc;
-  if ((rc = grow_host(c, hsize))) return rc;
-  // aux: r (n double), r32 (n float), two norms, symv slots (n_tiles x n double);
-  // factor_mode 3 adds the blocked solves' inverse diagonal blocks (nb x 128^2
-  // float), y32 (n float) and their flags / tickets (2 nb + 4 uint)
+  if (factor_mode <= 3) {
+    if ((rc = bind(c, st))) return rc;
+    const bool emulate = factor_mode != 0;
+    VMCK_SOLVER(cusolverDnSetMathMode(c->solver, emulate ? CUSOLVER_FP32_EMULATED_BF16X9_MATH
+                                                         : CUSOLVER_DEFAULT_MATH));
+    if (emulate)
+      VMCK_SOLVER(cusolverDnSetEmulationStrategy(c->solver, CUDA_EMULATION_STRATEGY_EAGER));
+    const int64_t fn = factor_mode == 2 ? std::min<int64_t>(n, CHOL_LEAF) : n;
+    VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, fn,
+                                            CUDA_R_32F, A32, n, CUDA_R_32F, &dsize, &hsize));
+    if ((rc = grow(&c->dwork, &c->dwork_bytes, dsize + 256, st))) return rc;
+    if ((rc = grow_host(c, hsize))) return rc;
+  }
+  // the triangular solves run on the factor F (ld np); mode 4 pads n to a
+  // multiple of 4 (identity rows) for their vector loads
+  const int64_t np = factor_mode == 4 ? ((n + 3) & ~int64_t(3)) : n;
+  const bool own_trsv = (factor_mode == 3 && n % 4 == 0) || factor_mode == 4;
+  // aux: r (n double), r32 (np float), two norms + done + prev, symv slots
+  // (n_tiles x n double), inverse diagonal blocks (mode 3), y32 (np float), flags
+  // and tickets (2 nb + 4 uint), leaf inverses (mode 3)
   const int64_t nt = (n + SY_T - 1) / SY_T;
-  const bool own_trsv = factor_mode == 3 && n % 4 == 0;
-  const int64_t nb = (n + TB - 1) / TB;
-  const size_t ws_off = (((size_t)n * 12 + 64) + 255) & ~size_t(255);
+  const int64_t nb = (np + TB - 1) / TB;
+  const size_t r32_off = ((size_t)n * 8 + 255) & ~size_t(255);
+  const size_t norms_off = (r32_off + (size_t)np * 4 + 255) & ~size_t(255);
+  const size_t ws_off = norms_off + 256;
   const size_t yinv_off = (ws_off + (size_t)nt * n * 8 + 255) & ~size_t(255);
-  const size_t y32_off = (yinv_off + (own_trsv ? (size_t)nb * TB * TB * 4 : 0) + 255) & ~size_t(255);
-  const size_t sync_off = (y32_off + (own_trsv ? (size_t)n * 4 : 0) + 255) & ~size_t(255);
+  const size_t y32_off =
+      (yinv_off + (factor_mode == 3 && own_trsv ? (size_t)nb * TB * TB * 4 : 0) + 255) &
+      ~size_t(255);
+  const size_t sync_off = (y32_off + (own_trsv ? (size_t)np * 4 : 0) + 255) & ~size_t(255);
   const size_t dinv_off = (sync_off + (own_trsv ? (size_t)(2 * nb + 4) * 4 : 0) + 255) & ~size_t(255);
   const size_t need = dinv_off + (factor_mode == 3 ? (size_t)nb * 4096 * 4 : 0);
   if ((rc = grow(&c->aux, &c->aux_bytes, need, st))) return rc;
   char *aux = static_cast<char *>(c->aux);
   double *r = static_cast<double *>(c->aux);
-  float *r32 = reinterpret_cast<float *>(r + n);
-  double *norms = reinterpret_cast<double *>(
-      (reinterpret_cast<uintptr_t>(r32 + n) + 15) & ~uintptr_t(15));
-  int *done = reinterpret_cast<int *>(norms + 2);  // inside the 64-byte slack after r32
+  float *r32 = reinterpret_cast<float *>(aux + r32_off);
+  double *norms = reinterpret_cast<double *>(aux + norms_off);
+  double *prev = norms + 2;
+  int *done = reinterpret_cast<int *>(norms + 3);
   double *sws = reinterpret_cast<double *>(aux + ws_off);
   float *yinv = reinterpret_cast<float *>(aux + yinv_off);
   float *y32 = reinterpret_cast<float *>(aux + y32_off);
   unsigned *sync = reinterpret_cast<unsigned *>(aux + sync_off);
   const TrsvSync sync_f{sync, sync + 2 * nb, sync + 2 * nb + 2, wait_limit_ns()};
   const TrsvSync sync_b{sync + nb, sync + 2 * nb + 1, sync + 2 * nb + 2, wait_limit_ns()};
-  if (factor_mode >= 2) {
+  float *F = A32;  // the factor the solves read
+  if (factor_mode == 4) {
+    const size_t pad_bytes = np != n ? (size_t)np * np * 4 : 0;
+    const size_t tc_off = (pad_bytes + 1023) & ~size_t(1023);
+    if ((rc = grow(&c->tcws, &c->tcws_bytes, tc_off + (size_t)chol_tc_workspace_bytes(np), st)))
+      return rc;
+    if (np != n) {
+      F = static_cast<float *>(c->tcws);
+      VMCK_CUDA(cudaMemsetAsync(F, 0, pad_bytes, st));
+      VMCK_CUDA(cudaMemcpy2DAsync(F, np * 4, A32, n * 4, n * 4, n, cudaMemcpyDeviceToDevice, st));
+      pad_identity_kernel<<<1, 32, 0, st>>>(F, n, np);
+      if ((rc = check_launch("refined solve padding"))) return rc;
+    }
+    rc = chol_tc_factor(st, F, np, static_cast<char *>(c->tcws) + tc_off, status, &yinv);
+    if (rc) return rc;
+    if (np != n)
+      VMCK_CUDA(cudaMemcpy2DAsync(A32, n * 4, F, np * 4, n * 4, n, cudaMemcpyDeviceToDevice, st));
+    VMCK_CUDA(cudaMemsetAsync(c->d_info, 0, sizeof(int), st));
+    VMCK_CUDA(cudaMemsetAsync(sync, 0, (size_t)(2 * nb + 4) * 4, st));
+  } else if (factor_mode >= 2) {
     VMCK_BLAS(cublasSetMathMode(c->blas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
     VMCK_BLAS(cublasSetEmulationStrategy(c->blas, CUBLAS_EMULATION_STRATEGY_EAGER));
     if (factor_mode == 2) {
@@ -1312,16 +1434,19 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
     if ((rc = check_launch("refined solve info"))) return rc;
   }
   VMCK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
-  VMCK_CUDA(cudaMemsetAsync(done, 0, sizeof(int), st));
+  refine_init_kernel<<<1, 32, 0, st>>>(norms, prev, done);  // norms 0, prev huge, done 0
+  if ((rc = check_launch("refined solve init"))) return rc;
+  if (np != n) VMCK_CUDA(cudaMemsetAsync(r32, 0, (size_t)np * 4, st));
   const int blocks = ceil_div(n, 256);
   // Iteration it > 0 first forms r = b - A x and stops the loop (on the device)
-  // once ||r|| <= tol ||b||; the kernels after that return at entry.
-  for (int it = 0; it < max_iter; ++it) {
+  // once it is small enough; the kernels after that return at entry.
+  for (int it = 0; it < o.max_iter; ++it) {
     if (it == 0) {
       VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
     } else {
-      if ((rc = symv_residual(st, A64, n, x, b, r, sws, done))) return rc;
-      refine_converged_kernel<<<1, 256, 0, st>>>(r, b, n, tol, done);
+      if ((rc = symv_residual(st, A64, n, x, b, r, sws, done, o.exact))) return rc;
+      refine_converged_kernel<<<1, 256, 0, st>>>(r, b, n, o.stop_tol, done,
+                                                 o.stagnation ? prev : nullptr);
       if ((rc = check_launch("refined solve convergence"))) return rc;
     }
     d2f_kernel<<<blocks, 256, 0, st>>>(r, r32, n, done);
@@ -1329,10 +1454,10 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
     if (own_trsv) {
       const unsigned grid = (unsigned)std::min<int64_t>(nb, 2 * (int64_t)num_sms());
       VMCK_CUDA(cudaMemsetAsync(sync + 2 * nb, 0, 2 * sizeof(unsigned), st));  // tickets
-      trsv_fwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(A32, n, yinv, r32, y32, sync_f,
+      trsv_fwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(F, np, yinv, r32, y32, sync_f,
                                                      (unsigned)(it + 1), status, done);
       if ((rc = check_launch("refined solve forward"))) return rc;
-      trsv_bwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(A32, n, yinv, y32, r32, sync_b,
+      trsv_bwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(F, np, yinv, y32, r32, sync_b,
                                                      (unsigned)(it + 1), status, done);
       if ((rc = check_launch("refined solve backward"))) return rc;
     } else {
@@ -1343,17 +1468,82 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
     if ((rc = check_launch("refined solve update"))) return rc;
   }
   // the final residual (skipped when the loop stopped early: r already belongs to x)
-  if ((rc = symv_residual(st, A64, n, x, b, r, sws, done))) return rc;
-  VMCK_BLAS(cublasSetPointerMode(c->blas, CUBLAS_POINTER_MODE_DEVICE));
-  cublasStatus_t s1 = cublasDnrm2(c->blas, (int)n, r, 1, norms);
-  cublasStatus_t s2 = cublasDnrm2(c->blas, (int)n, b, 1, norms + 1);
-  cublasSetPointerMode(c->blas, CUBLAS_POINTER_MODE_HOST);
-  if (s1 != CUBLAS_STATUS_SUCCESS || s2 != CUBLAS_STATUS_SUCCESS) {
-    set_last_error("refined solve: cublasDnrm2 failed");
-    return VMCK_ERR_LIBRARY;
-  }
-  refine_check_kernel<<<1, 1, 0, st>>>(norms, norms + 1, c->d_info, tol, status, residual_out);
+  if ((rc = symv_residual(st, A64, n, x, b, r, sws, done, o.exact))) return rc;
+  norms_kernel<<<1, 256, 0, st>>>(r, b, n, norms);
+  if ((rc = check_launch("refined solve norms"))) return rc;
+  refine_check_kernel<<<1, 1, 0, st>>>(norms, norms + 1, c->d_info, o.fail_tol, status,
+                                       residual_out);
   return check_launch("refined solve");
+}
+
+}  // namespace vmck
+
+__global__ void lower_f64_to_f32_kernel(const double *__restrict__ A, float *__restrict__ F,
+                                        int64_t n) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= n * n) return;
+  const int64_t i = e / n, j = e - i * n;
+  F[e] = j <= i ? (float)A[e] : 0.0f;
+}
+
+extern "C" int vmck_cholesky_solve(vmck_ctx *c, vmck_stream s, int32_t dtype, const void *A,
+                                   const void *b, void *x, int64_t n, int32_t *status) {
+  VMCK_REQUIRE(c && A && b && x && n > 0, "cholesky_solve arguments");
+  VMCK_REQUIRE(dtype == VMCK_F64 || dtype == VMCK_F32, "cholesky_solve dtype");
+  cudaStream_t st = as_stream(s);
+  int rc;
+  if (dtype == VMCK_F64) {
+    // FP32 tensor-core factor of fp32(A), then refinement with the FP64 residual
+    // b - A x until it stops falling (its FP64 rounding floor): the solution of
+    // a direct FP64 factorisation, to FP64 rounding.  A factor that fails or a
+    // refinement that does not converge (cond(A) beyond ~1e6) is reported.
+    VMCK_REQUIRE(n < (1ll << 30), "cholesky_solve size");
+    const size_t fbytes = ((size_t)n * n * 4 + 255) & ~size_t(255);
+    if ((rc = grow(&c->dwork, &c->dwork_bytes, fbytes, st))) return rc;
+    float *F = static_cast<float *>(c->dwork);
+    lower_f64_to_f32_kernel<<<ceil_div(n * n, 256), 256, 0, st>>>(static_cast<const double *>(A),
+                                                                    F, n);
+    if ((rc = check_launch("cholesky_solve cast"))) return rc;
+    const RefineOpts o{30, 0.0, 1e-10, 4, true, true};
+    if ((rc = refined_solve(c, st, static_cast<const double *>(A), F, static_cast<const double *>(b),
+                            static_cast<double *>(x), n, o, status, nullptr)))
+      return rc;
+    solve_check_kernel<double><<<1, 1024, 0, st>>>(c->d_info, static_cast<const double *>(x),
+                                                   static_cast<const double *>(b), n, status);
+    return check_launch("cholesky_solve check");
+  }
+  // FP32: cuSOLVER SPOTRF / SPOTRS (the plain FP32 path the benchmark compares against)
+  if ((rc = bind(c, st))) return rc;
+  size_t dsize = 0, hsize = 0;
+  VMCK_SOLVER(cusolverDnXpotrf_bufferSize(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n,
+                                          CUDA_R_32F, A, n, CUDA_R_32F, &dsize, &hsize));
+  const size_t fbytes = (size_t)n * n * 4;
+  const size_t off = (fbytes + 255) & ~size_t(255);
+  if ((rc = grow(&c->dwork, &c->dwork_bytes, off + dsize + 256, st))) return rc;
+  if ((rc = grow_host(c, hsize))) return rc;
+  void *Fm = c->dwork;
+  void *work = static_cast<char *>(c->dwork) + off;
+  VMCK_CUDA(cudaMemcpyAsync(Fm, A, fbytes, cudaMemcpyDeviceToDevice, st));
+  VMCK_CUDA(cudaMemcpyAsync(x, b, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+  VMCK_SOLVER(cusolverDnXpotrf(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, CUDA_R_32F, Fm, n,
+                               CUDA_R_32F, work, dsize, c->hwork, hsize, c->d_info));
+  VMCK_SOLVER(cusolverDnXpotrs(c->solver, c->params, CUBLAS_FILL_MODE_UPPER, n, 1, CUDA_R_32F, Fm,
+                               n, CUDA_R_32F, x, n, c->d_info));
+  solve_check_kernel<float><<<1, 1024, 0, st>>>(c->d_info, static_cast<const float *>(x),
+                                                static_cast<const float *>(b), n, status);
+  return check_launch("cholesky_solve check");
+}
+
+
+extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const double *A64,
+                                           float *A32, const double *b, double *x, int64_t n,
+                                           int32_t max_iter, double tol, int32_t factor_mode,
+                                           int32_t *status, double *residual_out) {
+  VMCK_REQUIRE(c && A64 && A32 && b && x && n > 0 && max_iter >= 1, "refined solve arguments");
+  VMCK_REQUIRE(factor_mode >= 0 && factor_mode <= 4, "factor_mode must be 0 - 4");
+  VMCK_REQUIRE(n < (1ll << 30), "refined solve size");
+  const RefineOpts o{max_iter, tol, tol, factor_mode, false, false};
+  return refined_solve(c, as_stream(s), A64, A32, b, x, n, o, status, residual_out);
 }
 
 extern "C" int vmck_pinv_smooth_solve(vmck_ctx *c, vmck_stream s, const double *A, const double *b,

@@ -17,7 +17,7 @@ from pathlib import Path
 import torch
 
 from . import callbacks as cb
-from ._native import DEV_NONFINITE, DEV_NOT_SPD, DEV_TIMEOUT, VmckError
+from ._native import DEV_NO_CONVERGE, DEV_NONFINITE, DEV_NOT_SPD, DEV_TIMEOUT, VmckError
 from .logging import JsonLog, RuntimeLog
 from .ngd import minsr_fallback, minsr_update, sr_update
 from .optimizer import identity_preconditioner
@@ -312,7 +312,10 @@ class VMC_SR(AbstractVariationalDriver):
             self.info["status"] = status
             if status & DEV_TIMEOUT:
                 raise VmckError("a device-side wait timed out in the minSR step")
-            failed = bool(status & (DEV_NOT_SPD | DEV_NONFINITE))
+            bad = DEV_NOT_SPD | DEV_NONFINITE
+            if self.solve == "cholesky":
+                bad |= DEV_NO_CONVERGE  # the FP64 solve's refinement did not converge
+            failed = bool(status & bad)
             if self._solver == "pinv_smooth" or (self._solver == "fallback" and failed):
                 dp = minsr_fallback(self.info)
             elif self._solver == "cholesky" and failed:

@@ -178,12 +178,14 @@ def cholesky_solve(A, b, status):
     return x
 
 
-def cholesky_solve_refined(A64, A32, b, status, max_iter=3, tol=1e-10, factor_mode=3):
+def cholesky_solve_refined(A64, A32, b, status, max_iter=3, tol=1e-10, factor_mode=4):
     """FP32-accurate Cholesky of A32 (overwritten by its factor) refined to an
-    FP64 residual against A64.  factor_mode 0: cuSOLVER SPOTRF; 1: SPOTRF with
-    BF16x9 emulation; 2: recursive GEMM-based factorisation on BF16x9-emulated
-    tensor cores; 3: blocked factorisation with this library's leaf kernel and
-    emulated-GEMM panel solves / trailing updates."""
+    FP64 residual against A64.  factor_mode 4 (default): this library's blocked
+    factorisation on the tcgen05 tensor cores (FP16 hi + lo operand split, FP32
+    accumulation) with its own leaf, panel and trailing-update kernels.  For
+    comparison: 0 cuSOLVER SPOTRF; 1 SPOTRF with BF16x9 emulation; 2 recursive
+    GEMM factorisation on BF16x9-emulated cuBLAS; 3 blocked factorisation with
+    the library's 128 x 128 leaf and emulated cuBLAS GEMMs."""
     x = torch.empty_like(b)
     res = torch.empty(1, dtype=torch.float64, device=b.device)
     nat.check(nat.lib().vmck_cholesky_solve_refined(nat.ctx(), nat.stream(), nat.ptr(A64),

@@ -22,7 +22,9 @@ Two ways to form T:
   * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
     and a cuBLAS SYRK.
 Solvers (``solve=``):
-  * ``"cholesky"``: cuSOLVER Cholesky in the Jacobian's precision;
+  * ``"cholesky"``: Cholesky in the Jacobian's precision (FP64: this library's
+    tensor-core FP32 factor refined with the FP64 residual to FP64 rounding;
+    FP32: cuSOLVER, the plain path);
   * ``"refined"``: FP32 Cholesky refined against the FP64 matrix (iterative
     refinement) until the FP64 residual is below ``tol``;
 with NetKet's ``cholesky_with_fallback`` behaviour: a failed factorisation or a
@@ -128,7 +130,8 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     if check:
         st = int(status.item())
         info["status"] = st
-        if st & (nat.DEV_NOT_SPD | nat.DEV_NONFINITE):
+        if st & (nat.DEV_NOT_SPD | nat.DEV_NONFINITE) or (
+                solve == "cholesky" and st & nat.DEV_NO_CONVERGE):
             return minsr_fallback(info), info
     raw = K.ot_v(t, x, N, M, aux)
     delta = K.center_update(raw, obar, aux, s)
@@ -237,7 +240,12 @@ def solve_with_fallback(A, b, rtol=1e-14, rtol_smooth=1e-14):
     x = K.cholesky_solve(A, b, status)
     info = SolveInfo(solver_fallback=False)
     st = int(status.item())
-    if st & (nat.DEV_NOT_SPD | nat.DEV_NONFINITE):
+    # the FP64 solve refines an FP32 factor; a refinement that does not converge
+    # (cond(A) beyond the FP32 factor's reach) counts as a failed factorisation
+    bad = nat.DEV_NOT_SPD | nat.DEV_NONFINITE
+    if A.dtype == torch.float64:
+        bad |= nat.DEV_NO_CONVERGE
+    if st & bad:
         full = torch.tril(A) + torch.tril(A, -1).T
         x = K.pinv_smooth_solve(full.contiguous(), b, rtol, rtol_smooth)
         info["solver_fallback"] = True

@@ -149,11 +149,16 @@ def test_solvers(nk, golden):
 
 
 @pytest.mark.parametrize("n,mode", [(700, 2), (2500, 0), (2500, 1), (2500, 2), (4100, 2),
-                                    (100, 3), (700, 3), (1278, 3), (2500, 3), (4100, 3)])
+                                    (100, 3), (700, 3), (1278, 3), (2500, 3), (4100, 3),
+                                    (100, 4), (128, 4), (700, 4), (1278, 4), (2500, 4),
+                                    (4100, 4), (5000, 4)])
 def test_refined_solve(nk, n, mode):
     """FP32-accurate factorisation (cuSOLVER, emulated cuSOLVER, recursive GEMM
-    Cholesky, blocked Cholesky with the library's leaf kernel) + refinement with a
-    double-float residual reaches the FP64 solution."""
+    Cholesky, blocked Cholesky with the library's leaf kernel, the library's
+    tensor-core Cholesky) + refinement with a double-float residual reaches the
+    FP64 solution.  Mode 4 covers a single leaf (100, 128), partial panels and
+    block rows (700, 1278: padded to a multiple of 4, 2500, 4100) and several
+    512-row block rows (5000)."""
     rng = np.random.default_rng(3)
     U = rng.normal(size=(n, 300))
     A = U @ U.T / 300 + 1e-3 * np.eye(n)
@@ -174,7 +179,7 @@ def test_refined_solve(nk, n, mode):
     np.testing.assert_allclose((L @ L.T).cpu().numpy(), A, atol=2e-5 * np.abs(A).max())
 
 
-@pytest.mark.parametrize("mode", [2, 3])
+@pytest.mark.parametrize("mode", [2, 3, 4])
 def test_refined_solve_flags_non_spd(nk, mode):
     n = 1500
     A = -np.eye(n)
