@@ -34,7 +34,7 @@
 
 #include <algorithm>
 #include <cmath>
-#include <vector>
+#include <cstdlib>
 
 #include "chol_tc.cuh"
 #include "tc_common.cuh"
@@ -105,22 +105,35 @@ __global__ void chol_split_rows_kernel(const float *__restrict__ A, int64_t n, i
 // result: oh/ol[(nn - o_col0) ldo + m] = split(value * so) for m < o_rows,
 // nn >= o_col0.
 //
-// Persistent and warp-specialised like the Gram kernel: warp 0 streams 64-wide
-// K slabs of the four operand tiles with TMA (128-byte swizzle) into a 2-stage
-// ring, warp 1 issues three tcgen05.mma (kind::f16, M = 128, N = 256) per 16-wide
-// K step from one thread, warps 2-9 drain the tensor-memory accumulator (two
-// 256-column buffers, so a tile's epilogue overlaps the next tile's MMAs) with
-// coalesced column-major stores.  Waits for work are bounded by the library's
-// wait limit; a wait that runs out sets VMCK_DEV_TIMEOUT and the CTA winds down.
+// Persistent and warp-specialised: warp 0 streams 64-wide K slabs of the four
+// operand tiles with TMA (128-byte swizzle) into a 2-stage ring; warp 1 issues
+// the tcgen05.mma (kind::f16, M = 128, N = 256) from one thread; warps 2-17 hold
+// the tile's FP32 sums in registers (64 per thread).
+//
+// Accumulation.  The tensor core adds each MMA's products into its FP32
+// accumulator with a truncating alignment, an error of up to an ulp of the
+// running sum per MMA that does not average out: over K = 512 (96 MMAs) it left
+// the factor's backward error at ~4e-6 and refinement converging by only ~0.08
+// per pass.  Here the large hi * hi products accumulate in tensor memory for one
+// 64-wide slab only (4 MMAs, region D1), and the epilogue adds each slab's sum
+// to its registers with round-to-nearest FP32 additions; the small cross terms
+// hi * lo + lo * hi (2^-11 of the sum) accumulate over the whole tile in region
+// D2.  The MMA thread issues a slab's cross terms first, so the epilogue drains
+// D1 of the previous slab meanwhile.  With beta != 0 the register sums start
+// from the old C values, loaded while the tile's first slab runs, so the
+// write-out only stores.  Waits for work are bounded by the library's wait limit; a wait that
+// runs out sets VMCK_DEV_TIMEOUT and the CTA winds down.
 constexpr int G_BM = 128, G_BN = 256, G_BK = 64, G_STAGES = 2;
-constexpr int G_EPI_WARPS = 8;
+constexpr int G_EPI_WARPS = 16;  // four per tensor-memory lane quarter, 64 columns each
 constexpr int G_THREADS = 32 * (2 + G_EPI_WARPS);
-constexpr int G_TMEM_COLS = 2 * G_BN;
+constexpr int G_TMEM_COLS = 2 * G_BN;  // D1 (hi * hi, one slab), D2 (cross terms, one tile)
+constexpr int G_COLS = G_BN / 4;       // columns per epilogue warp
 constexpr int G_A_BYTES = G_BM * G_BK * 2;  // 16 KB (one of hi / lo)
 constexpr int G_B_BYTES = G_BN * G_BK * 2;  // 32 KB
 constexpr int G_STAGE_BYTES = 2 * G_A_BYTES + 2 * G_B_BYTES;
 constexpr int G_UMMA_K = 16;
-constexpr int G_CHUNK = 16;  // epilogue columns per tensor-memory load
+constexpr int G_CHUNK = 8;  // epilogue columns per tensor-memory load
+constexpr int G_NCH = G_COLS / G_CHUNK;
 
 struct GemmParams {
   int M, N, K;
@@ -162,7 +175,7 @@ __device__ __forceinline__ void gemm_tile(const GemmParams &g, int64_t t, int &m
   mi = (int)(t - tri_cum(lo, g.mt));
 }
 
-__global__ void __launch_bounds__(G_THREADS, 1)
+__global__ void __maxnreg__(112)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
                    const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
                    GemmParams g) {
@@ -171,9 +184,11 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       (reinterpret_cast<uintptr_t>(g_smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + G_STAGES * G_STAGE_BYTES);
   uint64_t *empty = full + G_STAGES;
-  uint64_t *tfull = empty + G_STAGES;  // [2]
-  uint64_t *tempty = tfull + 2;        // [2]
-  uint64_t *drain = tempty + 2;
+  uint64_t *d1_full = empty + G_STAGES;
+  uint64_t *d1_empty = d1_full + 1;
+  uint64_t *d2_full = d1_empty + 1;
+  uint64_t *d2_empty = d2_full + 1;
+  uint64_t *drain = d2_empty + 1;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
@@ -195,10 +210,10 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], G_EPI_WARPS);
-    }
+    mbar_init(d1_full, 1);
+    mbar_init(d1_empty, G_EPI_WARPS);
+    mbar_init(d2_full, 1);
+    mbar_init(d2_empty, G_EPI_WARPS);
     mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mAh)) : "memory");
@@ -254,20 +269,17 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     // ---------------- MMA issuer
     if (lane == 0) {
       const uint32_t idesc = umma_idesc_f16(G_BM, G_BN);
-      int64_t it = 0, tcount = 0;
-      bool issued_any = false;
-      for (int64_t tile = blockIdx.x; tile < g.tiles && !*abort_flag;
+      const uint32_t d1 = tmem_base, d2 = tmem_base + G_BN;
+      int64_t it = 0, slab = 0, tcount = 0;
+      bool issued_any = false, ok = true;
+      for (int64_t tile = blockIdx.x; tile < g.tiles && ok && !*abort_flag;
            tile += gridDim.x, ++tcount) {
-        const int b = (int)(tcount & 1);
-        if (tcount >= 2 &&
-            !mbar_wait(&tempty[b], (uint32_t)(((tcount >> 1) - 1) & 1), g.wait_ns)) {
+        if (tcount > 0 && !mbar_wait(d2_empty, (uint32_t)((tcount - 1) & 1), g.wait_ns)) {
           fail();
           break;
         }
         tc_fence_after();
-        const uint32_t dacc = tmem_base + (uint32_t)(b * G_BN);
-        bool ok = true;
-        for (int kb = 0; kb < num_kb; ++kb, ++it) {
+        for (int kb = 0; kb < num_kb; ++kb, ++it, ++slab) {
           const int s = (int)(it % G_STAGES);
           if (!mbar_wait(&full[s], (uint32_t)((it / G_STAGES) & 1), g.wait_ns)) {
             fail();
@@ -277,20 +289,34 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           tc_fence_after();
           const uint32_t ah = smem_u32(smem + s * G_STAGE_BYTES);
           const uint32_t al = ah + G_A_BYTES, bh = ah + 2 * G_A_BYTES, bl = bh + G_B_BYTES;
+          // cross terms of this slab into D2 (accumulates over the tile)
 #pragma unroll
           for (int k = 0; k < G_BK / G_UMMA_K; ++k) {
             const uint32_t off = k * G_UMMA_K * 2;
-            const uint64_t dah = umma_desc_sw128(ah + off), dal = umma_desc_sw128(al + off);
-            const uint64_t dbh = umma_desc_sw128(bh + off), dbl = umma_desc_sw128(bl + off);
-            umma_f16(dacc, dah, dbh, idesc, (kb == 0 && k == 0) ? 0u : 1u);
-            umma_f16(dacc, dah, dbl, idesc, 1u);
-            umma_f16(dacc, dal, dbh, idesc, 1u);
+            umma_f16(d2, umma_desc_sw128(ah + off), umma_desc_sw128(bl + off), idesc,
+                     (kb == 0 && k == 0) ? 0u : 1u);
+            umma_f16(d2, umma_desc_sw128(al + off), umma_desc_sw128(bh + off), idesc, 1u);
+          }
+          // hi * hi of this slab into D1 once the epilogue has read the last slab
+          if (slab > 0 && !mbar_wait(d1_empty, (uint32_t)((slab - 1) & 1), g.wait_ns)) {
+            fail();
+            ok = false;
+            issued_any = true;
+            break;
+          }
+          tc_fence_after();
+#pragma unroll
+          for (int k = 0; k < G_BK / G_UMMA_K; ++k) {
+            const uint32_t off = k * G_UMMA_K * 2;
+            umma_f16(d1, umma_desc_sw128(ah + off), umma_desc_sw128(bh + off), idesc,
+                     k == 0 ? 0u : 1u);
           }
           umma_commit(&empty[s]);
+          umma_commit(d1_full);
           issued_any = true;
         }
         if (!ok) break;
-        umma_commit(&tfull[b]);
+        umma_commit(d2_full);
       }
       if (issued_any) {
         umma_commit(drain);
@@ -299,56 +325,85 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     }
   } else {
     // ---------------- epilogue: warp e reads TMEM lane quarter (warp & 3),
-    // columns [128 * (e >> 2), +128) of the 256-column accumulator
-    const int e = warp - 2, quarter = warp & 3, half = e >> 2;
+    // columns [64 * (e >> 2), +64) of the 256-column tile
+    const int e = warp - 2, quarter = warp & 3, part = e >> 2;
     const float inv_s = 1.0f / ((g.sa ? *g.sa : 1.0f) * (g.sb ? *g.sb : 1.0f));
-    const float alpha = g.alpha * inv_s;
+    const float alpha = g.alpha * inv_s;  // a power of two times +-1: exact scaling
+    const float cscale = g.beta / alpha;  // old C in units of the sums
     const float so = g.so ? *g.so : 1.0f;
-    int64_t tcount = 0;
-    for (int64_t tile = blockIdx.x; tile < g.tiles; tile += gridDim.x, ++tcount) {
-      const int b = (int)(tcount & 1);
+    const uint32_t lane_off = static_cast<uint32_t>(quarter * 32) << 16;
+    const uint32_t t1 = tmem_base + lane_off + (uint32_t)(part * G_COLS);
+    const uint32_t t2 = t1 + G_BN;
+    int64_t tcount = 0, slab = 0;
+    bool alive = true;
+    for (int64_t tile = blockIdx.x; tile < g.tiles && alive; tile += gridDim.x, ++tcount) {
       int mi, ni;
       gemm_tile(g, tile, mi, ni);
       const int m = mi * G_BM + quarter * 32 + lane;
-      const int nbase = ni * G_BN + half * 128;
-      if (!mbar_wait(&tfull[b], (uint32_t)((tcount >> 1) & 1), g.wait_ns)) {
+      const int nbase = ni * G_BN + part * G_COLS;
+      const bool row_ok = m < g.M;
+      float *Crow = g.C + m;
+      // the sums start from the old C values (loaded while the first slab's MMAs
+      // run), so the write-out only stores
+      float acc[G_COLS];
+      if (g.beta != 0.0f) {
+        const float *cp = Crow + (int64_t)nbase * g.ldc;
+#pragma unroll
+        for (int i = 0; i < G_COLS; ++i) {
+          const int nn = nbase + i;
+          acc[i] = (row_ok && nn < g.N && (!g.tri || m <= nn)) ? *cp * cscale : 0.0f;
+          cp += g.ldc;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < G_COLS; ++i) acc[i] = 0.0f;
+      }
+      for (int kb = 0; kb < num_kb; ++kb, ++slab) {
+        if (!mbar_wait(d1_full, (uint32_t)(slab & 1), g.wait_ns)) {
+          fail();
+          alive = false;
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int ch = 0; ch < G_NCH; ++ch) {
+          float v[G_CHUNK];
+          tmem_ld_8cols(t1 + ch * G_CHUNK, v);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < G_CHUNK; ++j) acc[ch * G_CHUNK + j] += v[j];
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(d1_empty);
+      }
+      if (!alive) break;
+      if (!mbar_wait(d2_full, (uint32_t)(tcount & 1), g.wait_ns)) {
         fail();
         break;
       }
-      if (*abort_flag) break;
       tc_fence_after();
-      const uint32_t taddr = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) +
-                             (uint32_t)(b * G_BN + half * 128);
-      const bool row_ok = m < g.M;
-      float *Crow = g.C + m;
-#pragma unroll 1
-      for (int ch = 0; ch < 128 / G_CHUNK; ++ch) {
-        const int n0 = nbase + ch * G_CHUNK;
-        float old[G_CHUNK];
-        if (g.beta != 0.0f) {
 #pragma unroll
-          for (int j = 0; j < G_CHUNK; ++j) {
-            const int nn = n0 + j;
-            old[j] = (row_ok && nn < g.N && (!g.tri || m <= nn)) ? Crow[(int64_t)nn * g.ldc]
-                                                                   : 0.0f;
-          }
-        }
+      for (int ch = 0; ch < G_NCH; ++ch) {
         float v[G_CHUNK];
-        tmem_ld_16cols(taddr + ch * G_CHUNK, v);
+        tmem_ld_8cols(t2 + ch * G_CHUNK, v);
         tmem_wait_ld();
-        if (ch == 128 / G_CHUNK - 1) {
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty[b]);
-        }
 #pragma unroll
-        for (int j = 0; j < G_CHUNK; ++j) {
-          const int nn = n0 + j;
-          if (!row_ok || nn >= g.N || (g.tri && m > nn)) continue;
-          float val = alpha * v[j];
-          if (g.beta != 0.0f) val = fmaf(g.beta, old[j], val);
-          Crow[(int64_t)nn * g.ldc] = val;
-          if (g.oh && m < g.o_rows && nn >= g.o_col0) {
+        for (int j = 0; j < G_CHUNK; ++j) acc[ch * G_CHUNK + j] += v[j];
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(d2_empty);
+      // write-out (stores only)
+      float *cp = Crow + (int64_t)nbase * g.ldc;
+      const bool split_row = g.oh && row_ok && m < g.o_rows;
+#pragma unroll
+      for (int i = 0; i < G_COLS; ++i) {
+        const int nn = nbase + i;
+        if (row_ok && nn < g.N && (!g.tri || m <= nn)) {
+          const float val = alpha * acc[i];
+          *cp = val;
+          if (split_row && nn >= g.o_col0) {
             __half hi, lo;
             split_f16(val, so, hi, lo);
             const int64_t o = (int64_t)(nn - g.o_col0) * g.ldo + m;
@@ -356,6 +411,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             g.ol[o] = lo;
           }
         }
+        cp += g.ldc;
       }
     }
   }
@@ -371,13 +427,19 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 
 // ------------------------------------------------------------ the leaf
 // One CTA factors the mp x mp (mp <= 128) diagonal block at (r0, r0) of the
-// column-major upper A in shared memory and forms X = U^-1:
-//   (a) per 32-wide sub-panel p, warp 0 factors the 32 x 32 diagonal block in
-//       registers (lane l holds column l) and inverts it (back substitution,
-//       lane l: column l of the inverse);
-//   (b) the panel row U(P+i, j) = sum_k X_pp(k, i) A(P+k, j), all threads;
-//   (c) the rank-32 update of the trailing block (4 x 4 register tiles);
-// then the off-diagonal 32 x 32 blocks of X by block back substitution.
+// column-major upper A in shared memory and forms X = U^-1.  Per 32-wide
+// sub-panel p:
+//   (a) warp 0 factors the 32 x 32 diagonal block, lane l holding column l in
+//       registers;
+//   (b) the panel row U_pp^-T A_p,j by forward substitution, one thread per
+//       column j;
+//   (c) the rank-32 update of the trailing block in 4 x 4 register tiles.
+// Then warps 0-3 invert the four 32 x 32 diagonal blocks (back substitution,
+// lane l: column l) and all threads form the off-diagonal blocks of X by block
+// back substitution.  Every sequential loop runs one compact body per step:
+// the register arrays are shifted by one row per step instead of being indexed
+// by the step, so the code stays small (one warp runs it once per launch, on an
+// SM whose instruction cache holds none of it).
 // Writes U in place, X split into K-contiguous rows (xh/xl[m * 128 + k] = X(k, m),
 // scale from max |X| into *scale_x) and Y = X^T zero-padded column-major
 // 128 x 128 (the refinement's triangular solves).  Rows / columns past mp are
@@ -400,94 +462,82 @@ __global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A
   __shared__ int not_spd;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) not_spd = 0;
-  for (int e = tid; e < LB * LB; e += LEAF_T) {
-    const int j = e / LB, i = e - j * LB;
-    float v = 0.0f;
-    if (i <= j) {
-      if (j < mp) v = A[(r0 + i) + (r0 + j) * n];
-      else if (i == j) v = 1.0f;
+  // load in batches of 16 elements per thread so that their global loads overlap
+#pragma unroll 1
+  for (int e0 = 0; e0 < LB * LB; e0 += 16 * LEAF_T) {
+    float v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * LEAF_T + tid;
+      const int j = e / LB, i = e - j * LB;
+      v[u] = 0.0f;
+      if (i <= j) {
+        if (j < mp) v[u] = A[(r0 + i) + (r0 + j) * n];
+        else if (i == j) v[u] = 1.0f;
+      }
     }
-    S[i * LLD + j] = v;
-    X[i * LLD + j] = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int e = e0 + u * LEAF_T + tid;
+      const int j = e / LB, i = e - j * LB;
+      S[i * LLD + j] = v[u];
+      X[i * LLD + j] = 0.0f;
+    }
   }
   __syncthreads();
+#pragma unroll 1
   for (int p = 0; p < 4; ++p) {
     const int P = 32 * p;
     if (warp == 0) {
+      // (a) at step k, c[i] holds row k + i of column P + lane
       float c[32];
 #pragma unroll
       for (int i = 0; i < 32; ++i) c[i] = S[(P + i) * LLD + P + lane];
       bool bad = false;
-#pragma unroll
+#pragma unroll 1
       for (int k = 0; k < 32; ++k) {
-        float d = __shfl_sync(0xffffffffu, c[k], k);
+        float d = __shfl_sync(0xffffffffu, c[0], k);
         if (!(d > 0.0f)) {
           bad = true;
           d = 1.0f;
         }
-        const float ukk = sqrtf(d), rk = 1.0f / ukk;
-        if (lane == k) c[k] = ukk;
-        else if (lane > k) c[k] *= rk;
+        const float inv = rsqrtf(d);
+        const float u = (lane == k) ? d * inv : (lane > k ? c[0] * inv : 0.0f);  // U(k, lane)
+        S[(P + k) * LLD + P + lane] = u;
 #pragma unroll
-        for (int i = k + 1; i < 32; ++i) {
-          const float uki = __shfl_sync(0xffffffffu, c[k], i);
-          if (lane >= i) c[i] = fmaf(-uki, c[k], c[i]);
+        for (int i = 1; i < 32; ++i) {
+          const float uk = __shfl_sync(0xffffffffu, u, min(k + i, 31));  // U(k, k + i)
+          c[i - 1] = (k + i < 32 && lane >= k + i) ? fmaf(-uk, u, c[i]) : c[i];
         }
+        c[31] = 0.0f;
       }
       if (bad && lane == 0) not_spd = 1;
-      // inverse of the 32 x 32 upper block: lane l solves U x = e_l
-      float x[32];
-#pragma unroll
-      for (int i = 31; i >= 0; --i) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int k = i + 1; k < 32; ++k) {
-          const float uik = __shfl_sync(0xffffffffu, c[i], k);  // U(i, k) from lane k
-          if (k <= lane) acc = fmaf(uik, x[k], acc);
-        }
-        const float uii = __shfl_sync(0xffffffffu, c[i], i);
-        x[i] = (i == lane) ? 1.0f / uii : (i < lane ? -acc / uii : 0.0f);
-      }
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        S[(P + i) * LLD + P + lane] = (i <= lane) ? c[i] : 0.0f;
-        X[(P + i) * LLD + P + lane] = x[i];
-      }
     }
     __syncthreads();
     const int ncols = LB - P - 32;
     if (ncols > 0) {
-      // (b) panel row, in place: every thread reads its column first
-      const int tpc = ncols >= 96 ? 2 : (ncols >= 64 ? 4 : 8);  // threads per column
-      const int jj = tid % ncols, grp = tid / ncols;
-      const int j = P + 32 + jj;
-      const int per = 32 / tpc;
-      float in[32], out[16];
-      const bool active = grp < tpc;
-      if (active) {
+      // (b) thread jj: column j = P + 32 + jj; at step k, y[i] holds row k + i
+      if (tid < ncols) {
+        const int j = P + 32 + tid;
+        float y[32];
 #pragma unroll
-        for (int k = 0; k < 32; ++k) in[k] = S[(P + k) * LLD + j];
+        for (int i = 0; i < 32; ++i) y[i] = S[(P + i) * LLD + j];
+#pragma unroll 1
+        for (int k = 0; k < 32; ++k) {
+          const float *urow = S + (P + k) * LLD + P + k;  // U(k, k ..)
+          const float yk = y[0] / urow[0];
+          S[(P + k) * LLD + j] = yk;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          out[q] = 0.0f;
-          if (q < per) {
-            const int i = grp * per + q;
-#pragma unroll
-            for (int k = 0; k < 32; ++k)
-              if (k <= i) out[q] = fmaf(X[(P + k) * LLD + P + i], in[k], out[q]);
-          }
+          for (int i = 1; i < 32; ++i)
+            y[i - 1] = (k + i < 32) ? fmaf(-urow[min(i, 31 - k)], yk, y[i]) : y[i];
+          y[31] = 0.0f;
         }
-      }
-      __syncthreads();
-      if (active) {
-#pragma unroll
-        for (int q = 0; q < 16; ++q)
-          if (q < per) S[(P + grp * per + q) * LLD + j] = out[q];
       }
       __syncthreads();
       // (c) trailing update of the upper triangle [P+32, 128)^2 in 4 x 4 tiles
       const int T = ncols / 4, ntl = T * (T + 1) / 2;
       const int base = P + 32;
+#pragma unroll 1
       for (int t = tid; t < ntl; t += LEAF_T) {
         int tj = (int)((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
         while (tj * (tj + 1) / 2 > t) --tj;
@@ -499,7 +549,7 @@ __global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A
         for (int r = 0; r < 4; ++r)
 #pragma unroll
           for (int q = 0; q < 4; ++q) acc[r][q] = S[(i0 + r) * LLD + j0 + q];
-#pragma unroll 8
+#pragma unroll 4
         for (int k = 0; k < 32; ++k) {
           const float *row = S + (P + k) * LLD;
           float a[4], bq[4];
@@ -521,7 +571,37 @@ __global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A
       __syncthreads();
     }
   }
+  // diagonal blocks of X: warp p inverts U_pp; lane l solves U x = e_l from the
+  // bottom row up, x[i] holding row 31 - s + i at step s (shifted down each step)
+  if (warp < 4) {
+    const int P = 32 * warp;
+    float x[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) x[i] = 0.0f;
+#pragma unroll 1
+    for (int s = 0; s < 32; ++s) {
+      const int i = 31 - s;
+      const float *urow = S + (P + i) * LLD + P;  // U(i, 0 ..)
+      float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+      // x[q] holds X(i + 1 + q, lane) for q < s (shifted: x[0] = row i + 1)
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        a0 = fmaf(urow[min(i + 1 + q, 31)], x[q], a0);
+        a1 = fmaf(urow[min(i + 2 + q, 31)], x[q + 1], a1);
+        a2 = fmaf(urow[min(i + 3 + q, 31)], x[q + 2], a2);
+        a3 = fmaf(urow[min(i + 4 + q, 31)], x[q + 3], a3);
+      }
+      const float uii = urow[i];
+      const float xi = (i == lane) ? 1.0f / uii : (i < lane ? -((a0 + a1) + (a2 + a3)) / uii : 0.0f);
+      X[(P + i) * LLD + P + lane] = xi;
+#pragma unroll
+      for (int q = 31; q > 0; --q) x[q] = x[q - 1];
+      x[0] = xi;
+    }
+  }
+  __syncthreads();
   // off-diagonal blocks of X: X_IJ = -X_II sum_{K=I+1..J} U_IK X_KJ, by distance d
+#pragma unroll 1
   for (int d = 1; d < 4; ++d) {
     const int nblk = 4 - d;
     // phase 1: Tb[blk] = sum_K U_IK X_KJ  (I = blk, J = blk + d)
@@ -551,10 +631,8 @@ __global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A
   }
   // max |X| over the valid block -> split scale
   float am = 0.0f;
-  for (int e = tid; e < mp * mp; e += LEAF_T) {
-    const int i = e / mp, j = e - i * mp;
-    if (i <= j) am = fmaxf(am, fabsf(X[i * LLD + j]));
-  }
+  for (int j = warp; j < mp; j += LEAF_T / 32)
+    for (int i = lane; i <= j; i += 32) am = fmaxf(am, fabsf(X[i * LLD + j]));
   for (int o = 16; o > 0; o >>= 1) am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
   if (lane == 0) red[warp] = am;
   __syncthreads();
@@ -567,10 +645,8 @@ __global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A
     if (not_spd && status) atomicOr(status, VMCK_DEV_NOT_SPD);
   }
   // outputs
-  for (int e = tid; e < mp * mp; e += LEAF_T) {
-    const int j = e / mp, i = e - j * mp;
-    if (i <= j) A[(r0 + i) + (r0 + j) * n] = S[i * LLD + j];
-  }
+  for (int j = warp; j < mp; j += LEAF_T / 32)
+    for (int i = lane; i <= j; i += 32) A[(r0 + i) + (r0 + j) * n] = S[i * LLD + j];
   for (int e = tid; e < LB * LB; e += LEAF_T) {
     const int m = e / LB, k = e - m * LB;  // row m of the split operand = column m of X
     __half hi = __float2half_rn(0.0f), lo = hi;
@@ -672,6 +748,15 @@ int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOpera
   return check_launch("tc_gemm");
 }
 
+int chol_block_rows() {
+  static const int rows = [] {
+    const char *v = getenv("VMCK_CHOL_BLOCK");
+    const int r = v ? atoi(v) : CHOL_BLOCK;
+    return (r == 128 || r == 256 || r == 512) ? r : CHOL_BLOCK;
+  }();
+  return rows;
+}
+
 int64_t chol_tc_workspace_bytes(int64_t n) {
   const int64_t nb = (n + LB - 1) / LB;
   int64_t b = 0;
@@ -726,9 +811,9 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
       if ((rc = check_launch("chol_tc split"))) return rc;
     }
   }
-  const SplitOperand xs{xs_hi, xs_lo, LB, LB, LB};
-  for (int64_t k0 = 0; k0 < n; k0 += CHOL_BLOCK) {
-    const int64_t k1 = std::min<int64_t>(n, k0 + CHOL_BLOCK), w = k1 - k0;
+  const int64_t blk = chol_block_rows();
+  for (int64_t k0 = 0; k0 < n; k0 += blk) {
+    const int64_t k1 = std::min<int64_t>(n, k0 + blk), w = k1 - k0;
     // the block row's split panel: row (c - k0) holds U(k0 .. k1, c) (K = w)
     const SplitOperand ph{ph_hi, ph_lo, CHOL_BLOCK, w, n - k0};
     for (int64_t r0 = k0; r0 < k1; r0 += LB) {

@@ -5,8 +5,12 @@
 
 namespace vmck {
 
-// Rows of a block row of the factorisation (the K of the trailing update).
+// Rows of a block row of the factorisation (the K of the trailing update): the
+// buffer stride of the split panel.  chol_block_rows() is the block-row height
+// used, CHOL_BLOCK unless VMCK_CHOL_BLOCK (128, 256 or 512; read once per
+// process) selects a shorter one.
 constexpr int CHOL_BLOCK = 512;
+int chol_block_rows();
 
 // Device workspace (bytes) of chol_tc_factor for an n x n matrix.
 int64_t chol_tc_workspace_bytes(int64_t n);
