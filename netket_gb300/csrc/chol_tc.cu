@@ -427,93 +427,47 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 
 // ------------------------------------------------------------ the leaf
 // One CTA factors the mp x mp (mp <= 128) diagonal block at (r0, r0) of the
-// column-major upper A in shared memory.  The right-looking elimination runs on
-// the augmented matrix [A | I]: scaling row k by 1 / sqrt(pivot) and
-// subtracting u_ki (row k) from every row i > k turns A into U (A = U^T U) and I
-// into M with M A = U, i.e. M = U^-T = X^T for X = U^-1 - the inverse comes out
-// of the same row operations.  Per 32-row panel p:
-//   (a) 32 elimination steps confined to the panel's rows, all 8 warps: scale
-//       row k (U part columns >= k, M part columns <= k), then update the panel
-//       rows below it;
-//   (b) the rank-32 update of every later row (U part: the trailing upper
-//       triangle; M part: columns < P + 32) in 4 x 4 register tiles.
-// Writes U in place, X split into K-contiguous rows (xh/xl[m * 128 + k] = X(k, m)
-// = M(m, k), scale from max |X| into *scale_x) and Y = X^T = M zero-padded
-// column-major 128 x 128 (the refinement's triangular solves).  Rows / columns
-// past mp are the identity.  A non-positive or NaN pivot raises
-// VMCK_DEV_NOT_SPD and is replaced by 1.
+// column-major upper A in shared memory and forms X = U^-1.  Per 32-wide
+// sub-panel p:
+//   (a) warp 0 factors the 32 x 32 diagonal block, lane l holding column l in
+//       registers: per pivot one shuffle and one FMA per row, the rows shifted
+//       down one register per step so the step loop has a single compact body
+//       (entries below the diagonal are updated too and never read);
+//   (b) the panel row U_pp^-T A_p,j by forward substitution, two threads per
+//       column j (even / odd rows), fully unrolled;
+//   (c) the rank-32 update of the trailing block in 4 x 4 register tiles.
+// Then warps 0-3 invert the four 32 x 32 diagonal blocks and all threads form
+// the off-diagonal blocks of X by block back substitution, four outputs per
+// thread at a time.
+// Writes U in place, X split into K-contiguous rows (xh/xl[m * 128 + k] = X(k, m),
+// scale from max |X| into *scale_x) and Y = X^T zero-padded column-major
+// 128 x 128 (the refinement's triangular solves).  Rows / columns past mp are
+// the identity.  A non-positive or NaN pivot raises VMCK_DEV_NOT_SPD and is
+// replaced by 1.
 constexpr int LB = 128, LLD = LB + 1, LEAF_T = 256;
-constexpr size_t CHOL_LEAF_SMEM = (size_t)(2 * LB * LLD) * sizeof(float);
+constexpr size_t CHOL_LEAF_SMEM = (size_t)(2 * LB * LLD + LB + 3 * 32 * 33) * sizeof(float);
 
-// Rank-32 update of rows [i_lo, 128) in 4 x 4 register tiles:
-//   upper:  S(i, j) -= sum_k S(P + k, i) S(P + k, j) for i_lo <= i <= j;
-//   lower:  M(i, c) -= sum_k S(P + k, i) M(P + k, c) for c < c_hi.
-__device__ __forceinline__ void leaf_rank32(float *S, float *Mx, int P, int i_lo, int c_hi,
-                                            int tid) {
-  const int T = (LB - i_lo) / 4, nup = T * (T + 1) / 2, nlo = T * (c_hi / 4);
-#pragma unroll 1
-  for (int t = tid; t < nup + nlo; t += LEAF_T) {
-    const bool up = t < nup;
-    int i0, j0;
-    if (up) {
-      int tj = (int)((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
-      while (tj * (tj + 1) / 2 > t) --tj;
-      while ((tj + 1) * (tj + 2) / 2 <= t) ++tj;
-      i0 = i_lo + 4 * (t - tj * (tj + 1) / 2);
-      j0 = i_lo + 4 * tj;
-    } else {
-      const int u = t - nup, nc = c_hi / 4;
-      i0 = i_lo + 4 * (u / nc);
-      j0 = 4 * (u % nc);
-    }
-    float *dst = up ? S : Mx;
-    float acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[r][q] = dst[(i0 + r) * LLD + j0 + q];
-#pragma unroll 4
-    for (int k = 0; k < 32; ++k) {
-      const float *urow = S + (P + k) * LLD;
-      const float *brow = dst + (P + k) * LLD;
-      float a[4], bq[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = urow[i0 + r];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) bq[q] = brow[j0 + q];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(-a[r], bq[q], acc[r][q]);
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (!up || i0 + r <= j0 + q) dst[(i0 + r) * LLD + j0 + q] = acc[r][q];
-  }
-}
-
-__global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A, int64_t n,
+__global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict__ A, int64_t n,
                                                            int64_t r0, int mp,
                                                            __half *__restrict__ xh,
                                                            __half *__restrict__ xl,
                                                            float *scale_x, float *__restrict__ yinv,
                                                            int32_t *status) {
   extern __shared__ float lsm[];
-  float *S = lsm;             // S[i * LLD + j]: A, then U (i <= j); zero below
-  float *Mx = lsm + LB * LLD; // Mx[i * LLD + c]: I, then M = U^-T (c <= i); zero above
+  float *S = lsm;             // S[i * LLD + j] = U(i, j), i <= j; zero below
+  float *X = lsm + LB * LLD;  // X[i * LLD + j] = U^-1(i, j)
+  float *rd = X + LB * LLD;   // rd[i] = 1 / U(i, i)
+  float *Tb = rd + LB;        // 3 x [32][33] temporaries of the inverse
   __shared__ float red[LEAF_T / 32];
   __shared__ int not_spd;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) not_spd = 0;
-  // load in batches of 16 elements per thread so that their global loads overlap
-#pragma unroll 1
-  for (int e0 = 0; e0 < LB * LB; e0 += 16 * LEAF_T) {
-    float v[16];
+  {
+    // all 64 of a thread's loads in flight at once
+    float v[LB * LB / LEAF_T];
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int e = e0 + u * LEAF_T + tid;
+    for (int u = 0; u < LB * LB / LEAF_T; ++u) {
+      const int e = u * LEAF_T + tid;
       const int j = e / LB, i = e - j * LB;
       v[u] = 0.0f;
       if (i <= j) {
@@ -522,59 +476,194 @@ __global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A
       }
     }
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int e = e0 + u * LEAF_T + tid;
+    for (int u = 0; u < LB * LB / LEAF_T; ++u) {
+      const int e = u * LEAF_T + tid;
       const int j = e / LB, i = e - j * LB;
       S[i * LLD + j] = v[u];
-      Mx[j * LLD + i] = (i == j) ? 1.0f : 0.0f;
+      X[i * LLD + j] = 0.0f;
     }
   }
   __syncthreads();
 #pragma unroll 1
   for (int p = 0; p < 4; ++p) {
     const int P = 32 * p;
-    // (a) elimination steps R = P .. P + 31 within the panel rows
+    if (warp == 0) {
+      // (a) at step k, c[i] holds row k + i of column P + lane
+      float c[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) c[i] = S[(P + i) * LLD + P + lane];
+      bool bad = false;
 #pragma unroll 1
-    for (int R = P; R < P + 32; ++R) {
-      float d = S[R * LLD + R];
-      if (!(d > 0.0f)) {
-        if (tid == 0) not_spd = 1;
-        d = 1.0f;
-      }
-      const float inv = rsqrtf(d);
-      __syncthreads();  // every thread has read the pivot
-      // scale row R: U part columns R..127 (thread t -> column R + t), M part
-      // columns 0..R (thread t -> column t - (128 - R))
-      if (tid < LB - R) {
-        const int j = R + tid;
-        S[R * LLD + j] = (j == R) ? d * inv : S[R * LLD + j] * inv;
-      } else if (tid <= LB) {
-        const int c = tid - (LB - R);
-        Mx[R * LLD + c] *= inv;
-      }
-      __syncthreads();
-      // rows i in (R, P + 31]: warp w takes rows R + 1 + w, + 8, ...; lanes
-      // stride over the row's U columns [i, 128) then M columns [0, R]
-      for (int i = R + 1 + warp; i < P + 32; i += LEAF_T / 32) {
-        const float f = S[R * LLD + i];  // U(R, i)
-        const int nu = LB - i;
-        for (int q = lane; q < nu + R + 1; q += 32) {
-          if (q < nu) S[i * LLD + i + q] = fmaf(-f, S[R * LLD + i + q], S[i * LLD + i + q]);
-          else Mx[i * LLD + q - nu] = fmaf(-f, Mx[R * LLD + q - nu], Mx[i * LLD + q - nu]);
+      for (int k = 0; k < 32; ++k) {
+        float d = __shfl_sync(0xffffffffu, c[0], k);
+        if (!(d > 0.0f)) {
+          bad = true;
+          d = 1.0f;
         }
+        const float inv = rsqrtf(d);
+        const float u = (lane == k) ? d * inv : (lane > k ? c[0] * inv : 0.0f);  // U(k, lane)
+        S[(P + k) * LLD + P + lane] = u;
+        if (lane == 0) rd[P + k] = inv;
+#pragma unroll
+        for (int i = 1; i < 32; ++i)
+          c[i - 1] = fmaf(-__shfl_sync(0xffffffffu, u, (k + i) & 31), u, c[i]);
+        c[31] = 0.0f;
+      }
+      if (bad && lane == 0) not_spd = 1;
+    }
+    __syncthreads();
+    const int ncols = LB - P - 32;
+    if (ncols > 0) {
+      // (b) thread pair (2 jj, 2 jj + 1): column j, rows P + g + 2 r
+      if (tid < 2 * ncols) {
+        const int g = tid & 1, j = P + 32 + (tid >> 1);
+        float y[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) y[r] = S[(P + g + 2 * r) * LLD + j];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          const float mine = (g == (k & 1)) ? y[k >> 1] * rd[P + k] : 0.0f;
+          const float yk = __shfl_sync(0xffffffffu, mine, (lane & ~1) | (k & 1));
+          if (g == (k & 1)) y[k >> 1] = yk;
+          const float *urow = S + (P + k) * LLD + P + g;  // U(k, P + g + 2 r) = urow[2 r]
+#pragma unroll
+          for (int r = 0; r < 16; ++r)
+            if (2 * r + 1 > k && 2 * r + g > k) y[r] = fmaf(-urow[2 * r], yk, y[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < 16; ++r) S[(P + g + 2 * r) * LLD + j] = y[r];
       }
       __syncthreads();
-    }
-    // (b) rank-32 update of the rows after the panel
-    if (P + 32 < LB) {
-      leaf_rank32(S, Mx, P, P + 32, P + 32, tid);
+      // (c) trailing update of the upper triangle [P+32, 128)^2 in 4 x 4 tiles
+      const int T = ncols / 4, ntl = T * (T + 1) / 2;
+      const int base = P + 32;
+#pragma unroll 1
+      for (int t = tid; t < ntl; t += LEAF_T) {
+        int tj = (int)((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
+        while (tj * (tj + 1) / 2 > t) --tj;
+        while ((tj + 1) * (tj + 2) / 2 <= t) ++tj;
+        const int ti = t - tj * (tj + 1) / 2;
+        const int i0 = base + 4 * ti, j0 = base + 4 * tj;
+        float acc[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[r][q] = S[(i0 + r) * LLD + j0 + q];
+#pragma unroll 4
+        for (int k = 0; k < 32; ++k) {
+          const float *row = S + (P + k) * LLD;
+          float a[4], bq[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) a[r] = row[i0 + r];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) bq[q] = row[j0 + q];
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(-a[r], bq[q], acc[r][q]);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (i0 + r <= j0 + q) S[(i0 + r) * LLD + j0 + q] = acc[r][q];
+      }
       __syncthreads();
     }
   }
-  // max |X| = max |M| over the valid block -> split scale
+  // diagonal blocks of X: warp p inverts U_pp; lane l solves U x = e_l from the
+  // bottom row up, x[q] holding row i + 1 + q at step s (i = 31 - s); rows past
+  // the block hold 0, so their products with the U entries read past the
+  // block's last column (finite values of the same smem array) vanish
+  if (warp < 4) {
+    const int P = 32 * warp;
+    float x[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) x[i] = 0.0f;
+#pragma unroll 1
+    for (int s2 = 0; s2 < 32; ++s2) {
+      const int i = 31 - s2;
+      const float *urow = S + (P + i) * LLD + P + i + 1;  // U(i, i + 1 + q) = urow[q]
+      float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        a0 = fmaf(urow[q], x[q], a0);
+        a1 = fmaf(urow[q + 1], x[q + 1], a1);
+        a2 = fmaf(urow[q + 2], x[q + 2], a2);
+        a3 = fmaf(urow[q + 3], x[q + 3], a3);
+      }
+      const float ri = rd[P + i];
+      const float xi = (i == lane) ? ri : (i < lane ? -((a0 + a1) + (a2 + a3)) * ri : 0.0f);
+      X[(P + i) * LLD + P + lane] = xi;
+#pragma unroll
+      for (int q = 31; q > 0; --q) x[q] = x[q - 1];
+      x[0] = xi;
+    }
+  }
+  __syncthreads();
+  // off-diagonal blocks of X: X_IJ = -X_II sum_{K=I+1..J} U_IK X_KJ, by distance d;
+  // a thread computes four outputs (e, e + 256, e + 512, e + 768) at a time
+#pragma unroll 1
+  for (int d = 1; d < 4; ++d) {
+    const int tot = (4 - d) * 1024;
+    // phase 1: Tb[blk] = sum_K U_IK X_KJ  (I = blk, J = blk + d)
+#pragma unroll 1
+    for (int e0 = tid; e0 < tot; e0 += 4 * LEAF_T) {
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      const float *ur[4];
+      const float *xc[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = min(e0 + u * LEAF_T, tot - 1);
+        const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
+        ur[u] = S + (32 * blk + r) * LLD + 32 * (blk + 1);  // U(32 I + r, 32 (I + 1) + k)
+        xc[u] = X + 32 * (blk + 1) * LLD + 32 * (blk + d) + cc;  // X(32 (I + 1) + k, 32 J + cc)
+      }
+#pragma unroll 4
+      for (int k = 0; k < 32 * d; ++k) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u] = fmaf(ur[u][k], xc[u][k * LLD], acc[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = e0 + u * LEAF_T;
+        if (e < tot) Tb[(e >> 10) * 32 * 33 + ((e >> 5) & 31) * 33 + (e & 31)] = acc[u];
+      }
+    }
+    __syncthreads();
+    // phase 2: X_IJ = -X_II Tb[blk]
+#pragma unroll 1
+    for (int e0 = tid; e0 < tot; e0 += 4 * LEAF_T) {
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      const float *xr[4];
+      const float *tc[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = min(e0 + u * LEAF_T, tot - 1);
+        const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
+        xr[u] = X + (32 * blk + r) * LLD + 32 * blk;
+        tc[u] = Tb + blk * 32 * 33 + cc;
+      }
+#pragma unroll 8
+      for (int k = 0; k < 32; ++k) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u] = fmaf(xr[u][k], tc[u][k * 33], acc[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = e0 + u * LEAF_T;
+        if (e < tot) {
+          const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
+          X[(32 * blk + r) * LLD + 32 * (blk + d) + cc] = -acc[u];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // max |X| over the valid block -> split scale
   float am = 0.0f;
-  for (int i = warp; i < mp; i += LEAF_T / 32)
-    for (int c = lane; c <= i; c += 32) am = fmaxf(am, fabsf(Mx[i * LLD + c]));
+  for (int j = warp; j < mp; j += LEAF_T / 32)
+    for (int i = lane; i <= j; i += 32) am = fmaxf(am, fabsf(X[i * LLD + j]));
   for (int o = 16; o > 0; o >>= 1) am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
   if (lane == 0) red[warp] = am;
   __syncthreads();
@@ -590,15 +679,15 @@ __global__ void __launch_bounds__(LEAF_T) chol_leaf_kernel(float *__restrict__ A
   for (int j = warp; j < mp; j += LEAF_T / 32)
     for (int i = lane; i <= j; i += 32) A[(r0 + i) + (r0 + j) * n] = S[i * LLD + j];
   for (int e = tid; e < LB * LB; e += LEAF_T) {
-    const int m = e / LB, k = e - m * LB;  // row m of the split operand: X(k, m) = M(m, k)
+    const int m = e / LB, k = e - m * LB;  // row m of the split operand = column m of X
     __half hi = __float2half_rn(0.0f), lo = hi;
-    if (m < mp && k <= m) split_f16(Mx[m * LLD + k], sx, hi, lo);
+    if (m < mp && k <= m) split_f16(X[k * LLD + m], sx, hi, lo);
     xh[e] = hi;
     xl[e] = lo;
   }
   for (int e = tid; e < LB * LB; e += LEAF_T) {
-    const int c = e / LB, r = e - c * LB;  // Y(r, c) = X(c, r) = M(r, c)
-    yinv[e] = (r < mp && c <= r) ? Mx[r * LLD + c] : 0.0f;
+    const int c = e / LB, r = e - c * LB;  // Y(r, c) = X(c, r)
+    yinv[e] = (r < mp && c <= r) ? X[c * LLD + r] : 0.0f;
   }
 }
 
