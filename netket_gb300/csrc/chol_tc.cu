@@ -445,7 +445,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 // the identity.  A non-positive or NaN pivot raises VMCK_DEV_NOT_SPD and is
 // replaced by 1.
 constexpr int LB = 128, LLD = LB + 1, LEAF_T = 256;
-constexpr size_t CHOL_LEAF_SMEM = (size_t)(2 * LB * LLD + LB + 3 * 32 * 33) * sizeof(float);
+constexpr int LPAD = 64;  // zeros after S: the diagonal inverse reads up to 31 floats past it
+constexpr size_t CHOL_LEAF_SMEM = (size_t)(2 * LB * LLD + LPAD + LB + 3 * 32 * 33) * sizeof(float);
 
 __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict__ A, int64_t n,
                                                            int64_t r0, int mp,
@@ -455,13 +456,14 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
                                                            int32_t *status) {
   extern __shared__ float lsm[];
   float *S = lsm;             // S[i * LLD + j] = U(i, j), i <= j; zero below
-  float *X = lsm + LB * LLD;  // X[i * LLD + j] = U^-1(i, j)
-  float *rd = X + LB * LLD;   // rd[i] = 1 / U(i, i)
+  float *X = lsm + LB * LLD + LPAD;  // X[i * LLD + j] = U^-1(i, j), blocks I <= J only
+  float *rd = X + LB * LLD;          // rd[i] = 1 / U(i, i)
   float *Tb = rd + LB;        // 3 x [32][33] temporaries of the inverse
   __shared__ float red[LEAF_T / 32];
   __shared__ int not_spd;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) not_spd = 0;
+  if (tid < LPAD) S[LB * LLD + tid] = 0.0f;
   {
     // all 64 of a thread's loads in flight at once
     float v[LB * LB / LEAF_T];
@@ -480,7 +482,6 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
       const int e = u * LEAF_T + tid;
       const int j = e / LB, i = e - j * LB;
       S[i * LLD + j] = v[u];
-      X[i * LLD + j] = 0.0f;
     }
   }
   __syncthreads();
@@ -573,8 +574,9 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
   }
   // diagonal blocks of X: warp p inverts U_pp; lane l solves U x = e_l from the
   // bottom row up, x[q] holding row i + 1 + q at step s (i = 31 - s); rows past
-  // the block hold 0, so their products with the U entries read past the
-  // block's last column (finite values of the same smem array) vanish
+  // the block hold 0, so their products with the entries read past the block's
+  // last column (finite: later S entries or the zero pad after S) vanish
+  float am = 0.0f;  // max |X| over the valid block (this thread's writes)
   if (warp < 4) {
     const int P = 32 * warp;
     float x[32];
@@ -595,75 +597,80 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
       const float ri = rd[P + i];
       const float xi = (i == lane) ? ri : (i < lane ? -((a0 + a1) + (a2 + a3)) * ri : 0.0f);
       X[(P + i) * LLD + P + lane] = xi;
+      if (P + lane < mp) am = fmaxf(am, fabsf(xi));
 #pragma unroll
       for (int q = 31; q > 0; --q) x[q] = x[q - 1];
       x[0] = xi;
     }
   }
   __syncthreads();
-  // off-diagonal blocks of X: X_IJ = -X_II sum_{K=I+1..J} U_IK X_KJ, by distance d;
-  // a thread computes four outputs (e, e + 256, e + 512, e + 768) at a time
+  // off-diagonal blocks of X: X_IJ = -X_II sum_{K=I+1..J} U_IK X_KJ, by distance d
+  // (I = blk, J = blk + d), each thread a 4 x 4 tile of one block (64 per block)
+  // in registers.  X below the block diagonal is never read.
 #pragma unroll 1
   for (int d = 1; d < 4; ++d) {
-    const int tot = (4 - d) * 1024;
-    // phase 1: Tb[blk] = sum_K U_IK X_KJ  (I = blk, J = blk + d)
-#pragma unroll 1
-    for (int e0 = tid; e0 < tot; e0 += 4 * LEAF_T) {
-      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      const float *ur[4];
-      const float *xc[4];
+    const int ntile = (4 - d) * 64;
+    const int blk = tid >> 6, r0t = 4 * ((tid >> 3) & 7), c0t = 4 * (tid & 7);
+    const bool act = tid < ntile;
+    float acc[4][4];
+    if (act) {
+      // phase 1: Tb[blk] = sum_K U_IK X_KJ over the 32 d columns right of block I
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int e = min(e0 + u * LEAF_T, tot - 1);
-        const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
-        ur[u] = S + (32 * blk + r) * LLD + 32 * (blk + 1);  // U(32 I + r, 32 (I + 1) + k)
-        xc[u] = X + 32 * (blk + 1) * LLD + 32 * (blk + d) + cc;  // X(32 (I + 1) + k, 32 J + cc)
-      }
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] = 0.0f;
+      const float *ur = S + (32 * blk + r0t) * LLD + 32 * (blk + 1);
+      const float *xc = X + 32 * (blk + 1) * LLD + 32 * (blk + d) + c0t;
 #pragma unroll 4
       for (int k = 0; k < 32 * d; ++k) {
+        float a[4], bq[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) acc[u] = fmaf(ur[u][k], xc[u][k * LLD], acc[u]);
+        for (int r = 0; r < 4; ++r) a[r] = ur[r * LLD + k];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) bq[q] = xc[k * LLD + q];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(a[r], bq[q], acc[r][q]);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int e = e0 + u * LEAF_T;
-        if (e < tot) Tb[(e >> 10) * 32 * 33 + ((e >> 5) & 31) * 33 + (e & 31)] = acc[u];
-      }
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Tb[blk * 32 * 33 + (r0t + r) * 33 + c0t + q] = acc[r][q];
     }
     __syncthreads();
-    // phase 2: X_IJ = -X_II Tb[blk]
-#pragma unroll 1
-    for (int e0 = tid; e0 < tot; e0 += 4 * LEAF_T) {
-      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      const float *xr[4];
-      const float *tc[4];
+    if (act) {
+      // phase 2: X_IJ = -X_II Tb[blk]
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int e = min(e0 + u * LEAF_T, tot - 1);
-        const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
-        xr[u] = X + (32 * blk + r) * LLD + 32 * blk;
-        tc[u] = Tb + blk * 32 * 33 + cc;
-      }
-#pragma unroll 8
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] = 0.0f;
+      const float *xr = X + (32 * blk + r0t) * LLD + 32 * blk;
+      const float *tc = Tb + blk * 32 * 33 + c0t;
+#pragma unroll 4
       for (int k = 0; k < 32; ++k) {
+        float a[4], bq[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) acc[u] = fmaf(xr[u][k], tc[u][k * 33], acc[u]);
+        for (int r = 0; r < 4; ++r) a[r] = xr[r * LLD + k];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) bq[q] = tc[k * 33 + q];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[r][q] = fmaf(a[r], bq[q], acc[r][q]);
       }
+      const int row0 = 32 * blk + r0t, col0 = 32 * (blk + d) + c0t;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int e = e0 + u * LEAF_T;
-        if (e < tot) {
-          const int blk = e >> 10, r = (e >> 5) & 31, cc = e & 31;
-          X[(32 * blk + r) * LLD + 32 * (blk + d) + cc] = -acc[u];
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          X[(row0 + r) * LLD + col0 + q] = -acc[r][q];
+          if (col0 + q < mp) am = fmaxf(am, fabsf(acc[r][q]));
         }
-      }
     }
     __syncthreads();
   }
   // max |X| over the valid block -> split scale
-  float am = 0.0f;
-  for (int j = warp; j < mp; j += LEAF_T / 32)
-    for (int i = lane; i <= j; i += 32) am = fmaxf(am, fabsf(X[i * LLD + j]));
   for (int o = 16; o > 0; o >>= 1) am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
   if (lane == 0) red[warp] = am;
   __syncthreads();
@@ -678,12 +685,13 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
   // outputs
   for (int j = warp; j < mp; j += LEAF_T / 32)
     for (int i = lane; i <= j; i += 32) A[(r0 + i) + (r0 + j) * n] = S[i * LLD + j];
-  for (int e = tid; e < LB * LB; e += LEAF_T) {
+  for (int e = 2 * tid; e < LB * LB; e += 2 * LEAF_T) {
     const int m = e / LB, k = e - m * LB;  // row m of the split operand = column m of X
-    __half hi = __float2half_rn(0.0f), lo = hi;
-    if (m < mp && k <= m) split_f16(X[k * LLD + m], sx, hi, lo);
-    xh[e] = hi;
-    xl[e] = lo;
+    __half h0 = __float2half_rn(0.0f), l0 = h0, h1 = h0, l1 = h0;
+    if (m < mp && k <= m) split_f16(X[k * LLD + m], sx, h0, l0);
+    if (m < mp && k + 1 <= m) split_f16(X[(k + 1) * LLD + m], sx, h1, l1);
+    reinterpret_cast<__half2 *>(xh)[e >> 1] = __halves2half2(h0, h1);
+    reinterpret_cast<__half2 *>(xl)[e >> 1] = __halves2half2(l0, l1);
   }
   for (int e = tid; e < LB * LB; e += LEAF_T) {
     const int c = e / LB, r = e - c * LB;  // Y(r, c) = X(c, r)
