@@ -464,6 +464,7 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) not_spd = 0;
   if (tid < LPAD) S[LB * LLD + tid] = 0.0f;
+  if (tid < LB) S[tid * LLD + LB] = 0.0f;  // each row's padding column
   {
     // all 64 of a thread's loads in flight at once
     float v[LB * LB / LEAF_T];
@@ -575,7 +576,8 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
   // diagonal blocks of X: warp p inverts U_pp; lane l solves U x = e_l from the
   // bottom row up, x[q] holding row i + 1 + q at step s (i = 31 - s); rows past
   // the block hold 0, so their products with the entries read past the block's
-  // last column (finite: later S entries or the zero pad after S) vanish
+  // last column (finite: later S entries, the zeroed padding column of each row
+  // or the zero pad after S) vanish
   float am = 0.0f;  // max |X| over the valid block (this thread's writes)
   if (warp < 4) {
     const int P = 32 * warp;
