@@ -106,7 +106,7 @@ def _work_lists(Ns, Ms, n_chains, n_samples, chains_per_item, samples_per_item):
 
 class BatchedTFIM:
     def __init__(self, instances, *, alpha=2, n_chains=1024, chain_length=4, n_discard=5,
-                 diag_shift=1e-4, lr=0.01, seed=0, gram_mode=1, refine_iters=3,
+                 diag_shift=1e-4, lr=0.01, seed=0, gram_mode=1, refine_iters=4,
                  launch=None, n_streams=8):
         nat.require_cuda()
         self.instances = list(instances)

@@ -228,8 +228,8 @@ class VMC_SR(AbstractVariationalDriver):
     """
 
     def __init__(self, hamiltonian, optimizer, *, diag_shift, variational_state, use_ntk=None,
-                 gram="structured", gram_mode=None, solve=None, refine_iters=3,
-                 refine_tol=1e-10, jac_dtype=None, proj_reg=None, momentum=None,
+                 gram="structured", gram_mode=None, solve=None, refine_iters=4,
+                 refine_tol=1e-8, jac_dtype=None, proj_reg=None, momentum=None,
                  linear_solver=None, linear_solver_fn=None, chunk_size_bwd=None, mode=None,
                  on_the_fly=None):
         # linear_solver: NetKet's cholesky_with_fallback (default), cholesky (no

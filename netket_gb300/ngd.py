@@ -25,8 +25,14 @@ Solvers (``solve=``):
   * ``"cholesky"``: Cholesky in the Jacobian's precision (FP64: this library's
     tensor-core FP32 factor refined with the FP64 residual to FP64 rounding;
     FP32: cuSOLVER, the plain path);
-  * ``"refined"``: FP32 Cholesky refined against the FP64 matrix (iterative
-    refinement) until the FP64 residual is below ``tol``;
+  * ``"refined"``: FP32 Cholesky (this library's tensor-core factorisation)
+    refined against the FP64 matrix (iterative refinement) until the relative
+    FP64 residual is below ``refine_tol`` (default 1e-8, at most ``refine_iters``
+    correction solves; the loop stops on the device once it is reached).  The
+    residual bound matters little beyond that: with T = O_L O_L^T + lambda I a
+    residual r moves delta = O_L^T aux by at most |r| / (2 sqrt(lambda)), and the
+    mixed path's Gram rounding already puts delta ~3e-5 (relative) from the
+    all-FP64 update;
 with NetKet's ``cholesky_with_fallback`` behaviour: a failed factorisation or a
 non-finite result switches to ``pinv_smooth`` (``netket/optimizer/solver/
 solvers.py:305-340``).
@@ -56,7 +62,7 @@ def _o_l_v(t, x, N, M, obar, s, v):
 
 
 def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram_mode=None,
-                 solve="cholesky", refine_iters=3, refine_tol=1e-10, rtol=1e-14,
+                 solve="cholesky", refine_iters=4, refine_tol=1e-8, rtol=1e-14,
                  rtol_smooth=1e-14, jac_dtype=None, check=True, phase_timer=None,
                  proj_reg=None, momentum=None, old_updates=None):
     """Returns (delta (P,) FP64, info).  ``t`` = tanh(theta) (n, M) in the compute
