@@ -4,7 +4,7 @@ Workload (the configuration the metric is quoted on): 10x10 periodic square
 lattice, J1 = 1, J2 = 0.5, total Sz = 0; RBM alpha = 4 (M = 400, P = 40,500);
 MetropolisExchange on the 400 nearest and next-nearest bonds, 4096 chains,
 16,384 samples per step (4 per chain), 5 discarded sweeps per chain; minSR with
-T = O_L O_L^T + 1e-4 I (16,384 x 16,384) solved in FP64; SGD lr 0.01.
+T = O_L O_L^T + 1e-4 I (16,384 x 16,384) solved to an FP64 residual; SGD lr 0.01.
 Synthetic: random RBM initialisation (Normal(0, 0.01)), no dataset.
 
 A step = one VMC_SR step (sample, local energies, statistics, T, solve,
@@ -12,12 +12,16 @@ parameter update), through ``netket_gb300.driver.VMC_SR.advance``.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-``--impl reference`` times the reference algorithm on the host cores (the
+The line carries: ``roofline`` (the solve, the step's largest phase),
+``roofline_gram``, ``matched_energy`` (each arm's energy error against an
+all-FP64 run over a few steps on the same samples), ``plain_fp32`` (the plain
+FP32 GPU path), ``cpu_baseline`` and ``e2e`` (host buffers through the public
+API).  ``--impl reference`` times the reference algorithm on the host cores (the
 numpy FP64 restatement in ``oracle/``; NetKet's own JAX path cannot be
-installed here) on a bounded sample of the same workload and scales it to the
-full step phase by phase.  Under torchrun every rank runs an independent
-replica (the path has no cross-GPU exchange on a single-GPU machine); rank 0
-prints one JSON line.
+installed here): every phase of the full 16,384-sample step is measured, the
+per-sample phases on a 1/32 slice of the chains.  Under torchrun every rank
+runs an independent replica (the path has no cross-GPU exchange on a
+single-GPU machine); rank 0 prints one JSON line.
 """
 import argparse
 import json
@@ -145,6 +149,61 @@ def dist_setup():
     return world, rank, local
 
 
+def _pin_samples(vs):
+    """Make ``vs`` take its samples from ``box["x"]`` instead of its own sampler."""
+    box = {}
+    vs.reset = lambda: None
+
+    def sample(**kw):
+        vs._samples = box["x"]
+        return vs._samples
+    vs.sample = sample
+    return box
+
+
+def matched_energy(nk, steps, n_chains, n_samples, seed):
+    """Energy error of each arm against the all-FP64 run over ``steps`` minSR steps
+    from the same initial parameters: the mixed path (this library's default) and
+    the plain FP32 GPU path (dense connected elements, materialised Jacobian,
+    cuBLAS SSYRK, cuSOLVER SPOTRF) take the FP64 run's samples at every step and
+    their own parameters, so the energies differ by arithmetic only.  Target:
+    within 1e-4 relative of the FP64 run."""
+    import torch
+    _, v64, d64 = build_problem(nk, "fp64", seed=seed, n_chains=n_chains, n_samples=n_samples)
+    arms = {}
+    for name, prec in (("mixed", "mixed"), ("fp32_plain", "fp32")):
+        _, v, d = build_problem(nk, prec, seed=seed, n_chains=n_chains, n_samples=n_samples)
+        if name == "fp32_plain":
+            v.local_estimator = "dense"
+            d.gram = "dense"
+            d.solve = "cholesky"
+        v.flat_parameters = v64.flat_parameters.clone()
+        arms[name] = (v, d, _pin_samples(v))
+    dev = {k: 0.0 for k in arms}
+    e64 = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s64, u64 = d64.compute_loss_and_update()
+        x = v64.samples.clone()
+        d64.update_parameters(u64)
+        d64.step_count += 1
+        e64.append(s64.mean)
+        for name, (v, d, box) in arms.items():
+            box["x"] = x
+            s, u = d.compute_loss_and_update()
+            d.update_parameters(u)
+            d.step_count += 1
+            dev[name] = max(dev[name], abs(s.mean - s64.mean) / abs(s64.mean))
+    torch.cuda.synchronize()
+    return {"steps": steps, "target_rel": 1e-4,
+            "max_rel_energy_error_vs_fp64": {k: float(f"{v:.3e}") for k, v in dev.items()},
+            "within_target": {k: v <= 1e-4 for k, v in dev.items()},
+            "fp64_energy_per_site_first_last": [round(e64[0] / 100, 8), round(e64[-1] / 100, 8)],
+            "wall_s": round(time.perf_counter() - t0, 1),
+            "how": "the mixed and plain FP32 arms run on the FP64 run's samples (same "
+                   "initial parameters, own parameters afterwards)"}
+
+
 def run_ours(args):
     import torch
     import netket_gb300 as nk
@@ -237,31 +296,48 @@ def run_ours(args):
         if dist:
             dist.destroy_process_group()
         return None
-    gram_ms = phases.get("gram")
+    peaks = load_peaks()
     n = vs.n_samples
-    flops = float(n) * (n + 1) * 400  # lower triangle of t t^T (n x n x M), 2 flop per FMA
-    # tcgen05 mode 2: hi*hi, hi*lo, lo*hi, lo*lo over K = 400 padded to 448
-    executed = float(n) * (n + 1) * 4 * 448
-    # DRAM bytes per launch from the n = 8,192 ncu capture (profiles/gram_tc_kernel_n8192.md),
-    # scaled by the number of T entries
-    traffic = args.gram_traffic if args.gram_traffic is not None else \
-        (73.9e6 + 346.2e6) * (n / 8192.0) ** 2
+    # dominant phase: the solve (FP32 tensor-core Cholesky of T + refinement against
+    # the FP64 T), algorithmic work n^3 / 3 flop of the factorisation
+    solve_ms = phases.get("solve")
     roof = None
-    if gram_ms:
-        peaks = load_peaks()
-        achieved = flops / (gram_ms * 1e-3) / 1e12
-        roof = {"kernel": "structured Gram T = O_L O_L^T (gram_tc_kernel, tcgen05)",
+    if solve_ms:
+        chol_flops = float(n) ** 3 / 3.0
+        achieved = chol_flops / (solve_ms * 1e-3) / 1e12
+        roof = {"kernel": "minSR solve: Cholesky of T (chol_leaf_kernel + tcgen05 tc_gemm_kernel, "
+                          "FP16 hi/lo split, 3 products) + iterative refinement (trsv, symv)",
                 "bound": "tensor", "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"],
                 "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 5),
-                "traffic": traffic, "peak_source": peaks["source"],
-                "algorithmic_flops_per_launch": flops,
-                "executed_tensor_tflops": round(executed / (gram_ms * 1e-3) / 1e12, 3),
-                "launch_ms": round(gram_ms, 4),
-                "note": "Gram phase time (shift, g vector, operand split, kernel); the step's "
-                        "largest phase is the Cholesky solve (profiles/)"}
+                "traffic": args.solve_traffic, "peak_source": peaks["source"],
+                "algorithmic_flops_per_launch": chol_flops,
+                "executed_tensor_tflops": round(3 * chol_flops / (solve_ms * 1e-3) / 1e12, 3),
+                "launch_ms": round(solve_ms, 4),
+                "note": "one 'launch' = the solve phase of one step (CUDA events around it); "
+                        "executed tensor flops count the three FP16 products per FP32 "
+                        "multiply-add of the factorisation; traffic = DRAM bytes of one solve "
+                        "from the ncu capture in profiles/"}
+    gram_ms = phases.get("gram")
+    roof_gram = None
+    if gram_ms:
+        flops = float(n) * (n + 1) * 400  # lower triangle of t t^T (n x n x M), 2 flop per FMA
+        executed = float(n) * (n + 1) * 4 * 448  # hi*hi, hi*lo, lo*hi, lo*lo over K padded to 448
+        achieved = flops / (gram_ms * 1e-3) / 1e12
+        traffic = args.gram_traffic if args.gram_traffic is not None else \
+            (73.9e6 + 346.2e6) * (n / 8192.0) ** 2
+        roof_gram = {"kernel": "structured Gram T = O_L O_L^T (gram_tc_kernel, tcgen05)",
+                     "bound": "tensor", "achieved": round(achieved, 3),
+                     "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": round(achieved / peaks["bf16_tflops"], 5), "traffic": traffic,
+                     "algorithmic_flops_per_launch": flops,
+                     "executed_tensor_tflops": round(executed / (gram_ms * 1e-3) / 1e12, 3),
+                     "launch_ms": round(gram_ms, 4)}
+    matched = None
+    if args.matched_steps > 0:
+        matched = matched_energy(nk, args.matched_steps, args.n_chains, args.n_samples, rank)
     cpu = None
     if not args.no_cpu_baseline:
-        cpu = run_cpu_baseline(n_samples=args.cpu_samples)
+        cpu = run_cpu_baseline()
     line = {
         "metric": METRIC, "value": round(value, 5), "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max, 4),
@@ -273,6 +349,8 @@ def run_ours(args):
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         "plain_fp32": plain,
         "roofline": roof,
+        "roofline_gram": roof_gram,
+        "matched_energy": matched,
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_value, 5), "unit": "steps/s",
                 "h2d_bytes_per_step": P * 8, "d2h_bytes_per_step": P * 8 + 6 * 8},
@@ -296,51 +374,58 @@ def load_peaks():
                 "source": "fallback"}
 
 
-def run_cpu_baseline(n_samples=512, repeats=1):
-    """The reference algorithm (numpy FP64, all host threads) on a bounded
-    sample: n_samples samples from n_samples/4 chains (chain length 4, 5
-    discarded sweeps) of the same 10x10 J1-J2 / alpha=4 problem; each phase is
-    scaled to 16,384 samples by its complexity (sampling, local energies,
-    Jacobian and update ~ n; T ~ n^2; Cholesky ~ n^3)."""
-    import numpy as np
-    from oracle import graph as og, hilbert as oh, operator as oop, rbm as orbm, vmc_step
+class CpuReference:
+    """The reference algorithm on the host cores (numpy / scipy FP64, all host
+    threads): ``oracle/vmc_step.py``'s step of the same 10x10 J1-J2 / alpha = 4
+    workload at 16,384 samples, measured rather than modelled.  The
+    per-sample phases (sampling, local energies, Jacobian rows, O_L^T aux) run on
+    a slice of 128 chains x 4 samples (1/32 of the step's independent work), the
+    Gram matrix as that slice's 512 rows of T against a full-size Jacobian, and
+    the 16,384 x 16,384 Cholesky at full size once per run."""
 
-    g = og.Square(10, max_neighbor_order=2)
-    op = oop.heisenberg(100, g, [1.0, 0.5], sign_rule=[True, False])
-    tables = vmc_step.two_site_tables(op)
-    clusters = np.array(g.edges(), dtype=np.int64)
-    clusters = np.sort(clusters, axis=1)
-    order = np.lexsort((clusters[:, 1], clusters[:, 0]))
-    clusters = clusters[order]
-    import scipy.linalg as sla
-    rng = np.random.default_rng(0)
-    params = orbm.init_params(rng, 100, 4, 0.01)
-    B = max(1, n_samples // 4)
-    x = oh.random_state(rng, B, 100, 0)
-    best = None
-    t_start = time.perf_counter()
-    for _ in range(repeats):
-        params, x, st, t = vmc_step.timed_step(params, x, rng, clusters, tables, 5, 4, 1e-4, 0.01)
-        # the Cholesky of a few-hundred matrix is overhead-bound: time it at n_c
-        n_c = 3072
-        A = rng.normal(size=(n_c, 256))
-        A = A @ A.T / 256 + 1e-4 * np.eye(n_c)
-        b = rng.normal(size=n_c)
-        c0 = time.perf_counter()
-        cf = sla.cho_factor(A, lower=False, overwrite_a=True, check_finite=False)
-        sla.cho_solve(cf, b, check_finite=False)
-        t["solve"] = (time.perf_counter() - c0) * (B * 4 / n_c) ** 3
-        tot = sum(t[k] * (16384 / (B * 4)) ** vmc_step.PHASE_SCALING[k] for k in t)
-        if best is None or tot < best[0]:
-            best = (tot, t)
-    wall = time.perf_counter() - t_start
-    full_s, phases = best
+    N_SLICE_CHAINS = 128
+
+    def __init__(self, n_samples=16384, seed=0):
+        import numpy as np
+        from oracle import graph as og, hilbert as oh, operator as oop, rbm as orbm, vmc_step
+        self.np, self.vmc_step = np, vmc_step
+        g = og.Square(10, max_neighbor_order=2)
+        op = oop.heisenberg(100, g, [1.0, 0.5], sign_rule=[True, False])
+        self.tables = vmc_step.two_site_tables(op)
+        clusters = np.sort(np.array(g.edges(), dtype=np.int64), axis=1)
+        self.clusters = clusters[np.lexsort((clusters[:, 1], clusters[:, 0]))]
+        self.rng = np.random.default_rng(seed)
+        self.params = orbm.init_params(self.rng, 100, 4, 0.01)
+        self.x = oh.random_state(self.rng, self.N_SLICE_CHAINS, 100, 0)
+        self.n_samples = n_samples
+        t0 = time.perf_counter()
+        self.chol_s = vmc_step.full_size_cholesky_seconds(n_samples, 1e-4, self.rng)
+        self.setup_s = time.perf_counter() - t0
+
+    def step(self):
+        """Seconds of one full-size step and its phases."""
+        phases, reps = self.vmc_step.measured_full_step(
+            self.params, self.x, self.rng, self.clusters, self.tables, 5, 4, 1e-4, 0.01,
+            self.n_samples, self.chol_s)
+        self.reps = reps
+        return sum(phases.values()), phases
+
+    def describe(self):
+        return (f"every phase of the {self.n_samples}-sample step measured: sampling, local "
+                f"energies, Jacobian rows and O_L^T aux on {self.N_SLICE_CHAINS} chains x 4 "
+                f"samples (1/{self.reps} of the step's independent per-sample work, times "
+                f"{self.reps}); T = O_L O_L^T as those 512 rows against a full-size "
+                f"{self.n_samples} x 40500 FP64 Jacobian (times {self.reps}); the "
+                f"{self.n_samples} x {self.n_samples} FP64 cho_factor + cho_solve at full size "
+                f"({self.chol_s:.2f} s, timed once); numpy/scipy FP64 with {NPROC} host threads")
+
+
+def run_cpu_baseline():
+    ref = CpuReference()
+    full_s, phases = ref.step()
     return {"value": round(1.0 / full_s, 6), "unit": "steps/s", "cores": NPROC, "kind": "port",
-            "sample": (f"{B * 4} samples ({B} chains x 4, 5 discarded sweeps) of the same "
-                       f"workload (Cholesky timed at n=3072), numpy FP64 reference algorithm, "
-                       f"each phase scaled to 16384 samples by its complexity; "
-                       f"measured {wall:.1f} s"),
-            "phase_s_at_sample": {k: round(v, 4) for k, v in phases.items()},
+            "sample": ref.describe(),
+            "phase_s": {k: round(v, 3) for k, v in phases.items()},
             "full_step_s": round(full_s, 3)}
 
 
@@ -348,24 +433,32 @@ def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
         return None
-    vals = []
+    t_start = time.perf_counter()
+    ref = CpuReference()
     for _ in range(args.warmup):
-        run_cpu_baseline(n_samples=args.cpu_samples)
+        ref.step()
+    steps = []
     for _ in range(args.steps):
-        vals.append(run_cpu_baseline(n_samples=args.cpu_samples))
-    v = pystats.median([c["value"] for c in vals])
-    c = vals[-1]
+        steps.append(ref.step())
+    full = [s for s, _ in steps]
+    v = 1.0 / pystats.median(full)
+    phases = {k: round(pystats.median(p[k] for _, p in steps), 3) for k in steps[0][1]}
     return {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / v, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": dict(WORKLOAD, precision="fp64",
-                                            parallelism="host cores"),
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": NPROC, "kind": "port",
-                         "sample": c["sample"]},
-        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": "steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000.0 / v, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(WORKLOAD, precision="fp64", parallelism="host cores"),
+        "cpu_baseline": {"value": round(v, 6), "unit": "steps/s", "cores": NPROC, "kind": "port",
+                         "sample": ref.describe()},
+        "phase_s": phases,
+        "e2e": {"value": round(v, 6), "unit": "steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": round(time.perf_counter() - t_start, 1),
         "note": "NetKet's JAX CPU path cannot be installed here (no jax/flax/optax/numba); "
-                "the numpy FP64 restatement of the same algorithm is timed instead",
+                "the numpy FP64 restatement of the same algorithm is timed instead. Each "
+                "step's value is the full-size step assembled from measured phases (see "
+                "sample); wall_s is this process's own run time",
     }
 
 
@@ -380,9 +473,12 @@ def main():
     ap.add_argument("--n-chains", type=int, default=WORKLOAD["n_chains"],
                     help="smaller cases for profiling; the metric is quoted at the default")
     ap.add_argument("--n-samples", type=int, default=WORKLOAD["n_samples"])
-    ap.add_argument("--cpu-samples", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gram-traffic", type=float, default=None)
+    ap.add_argument("--solve-traffic", type=float, default=None,
+                    help="DRAM bytes of one solve (ncu); reported as roofline.traffic")
+    ap.add_argument("--matched-steps", type=int, default=8,
+                    help="steps of the matched-energy comparison (0 skips it)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

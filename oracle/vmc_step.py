@@ -13,8 +13,8 @@ is a fair CPU baseline of the reference:
   * dense centred Jacobian, ``T = O_L O_L^T + lambda I``, Cholesky solve and
     ``delta = O_L^T aux`` (``netket/_src/ngd/srt.py:22-96``);
   * SGD.
-``timed_step`` returns the wall time of each phase so a reduced sample can be
-scaled to the full workload phase by phase.
+``timed_step`` returns the wall time of each phase; ``measured_full_step``
+times the full-size step without modelling how any phase grows with size.
 """
 import time
 
@@ -129,5 +129,62 @@ def timed_step(params, x_chains, rng, clusters, tables, n_discard, chain_length,
     return orbm.unravel(flat, N, M), x_chains, st, t
 
 
-# how each phase grows from a reduced sample count n_s to the full n
-PHASE_SCALING = {"sample": 1, "eloc": 1, "jacobian": 1, "gram": 2, "solve": 3, "update": 1}
+def full_size_cholesky_seconds(n, diag_shift, rng, rank=256):
+    """Wall time of ``cho_factor`` + ``cho_solve`` (``netket/optimizer/solver/
+    solvers.py:266-268``) on an n x n FP64 SPD matrix of the minSR form
+    G G^T / rank + diag_shift I (synthetic values: the factorisation's cost does
+    not depend on them)."""
+    G = rng.normal(size=(n, rank))
+    T = G @ G.T / rank
+    del G
+    T[np.diag_indices(n)] += diag_shift
+    b = rng.normal(size=n)
+    t0 = time.perf_counter()
+    c, low = sla.cho_factor(T, lower=False, overwrite_a=True, check_finite=False)
+    sla.cho_solve((c, low), b, check_finite=False)
+    return time.perf_counter() - t0
+
+
+def measured_full_step(params, x_chains, rng, clusters, tables, n_discard, chain_length,
+                       diag_shift, lr, n_full, chol_seconds):
+    """The reference step at n_full samples, every phase measured at the full
+    size or as an exact fraction of it:
+      * sampling, local energies, Jacobian rows and delta = O_L^T aux act on each
+        sample independently: they run on the given slice of chains
+        (n_slice = chains x chain_length samples) and the full step is
+        n_full / n_slice such slices;
+      * T = O_L O_L^T: the slice's rows of T against a full-size O_L (n_full x P,
+        the slice's rows repeated), 1 / (n_full / n_slice) of the full product;
+      * the n_full x n_full Cholesky: ``chol_seconds`` from
+        ``full_size_cholesky_seconds`` (timed once per run).
+    Returns (phase seconds of the full step, slice count)."""
+    N = x_chains.shape[1]
+    M = params["bias"].shape[0]
+    t0 = time.perf_counter()
+    samples, x_chains = sample_exchange(params, x_chains, rng, clusters, n_discard, chain_length, N)
+    t1 = time.perf_counter()
+    x = samples.reshape(-1, N)
+    xp, mels = conn_two_site(x, tables)
+    lp = orbm.logpsi(params, x)
+    lpc = orbm.logpsi(params, xp.reshape(-1, N)).reshape(mels.shape)
+    e = np.sum(mels * np.exp(lpc - lp[:, None]), axis=1)
+    ost.statistics(e.reshape(x_chains.shape[0], -1))
+    t2 = time.perf_counter()
+    n = x.shape[0]
+    reps = n_full // n
+    O = orbm.jacobian(params, x, center=True) / np.sqrt(n_full)
+    t3 = time.perf_counter()
+    O_full = np.tile(O, (reps, 1))
+    t4 = time.perf_counter()
+    T_rows = O @ O_full.T
+    T_rows[np.arange(n), np.arange(n)] += diag_shift
+    t5 = time.perf_counter()
+    del O_full, T_rows
+    aux = rng.normal(size=n)
+    t6 = time.perf_counter()
+    delta = O.T @ aux
+    orbm.ravel(params) - lr * delta
+    t7 = time.perf_counter()
+    phases = {"sample": reps * (t1 - t0), "eloc": reps * (t2 - t1), "jacobian": reps * (t3 - t2),
+              "gram": reps * (t5 - t4), "solve": chol_seconds, "update": reps * (t7 - t6)}
+    return phases, reps
