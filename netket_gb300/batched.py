@@ -15,9 +15,10 @@ bit-identical to running it alone:
   (``capture()`` / ``run()``), so a step costs one graph launch plus one small
   device-to-host read of all energies and solver statuses.
 
-The persistent launch shape (chains per work item, CTAs per SM) is picked by a
-small autotuner that times the candidates on the first step and caches the
-choice per size signature in ``VMCK_AUTOTUNE_CACHE`` (a JSON file).
+The persistent launch shapes (sampler: chains per work item and CTAs; local
+energies: samples per work item and CTAs) are picked by a small autotuner that
+times the candidates on the first step and caches the choice per size
+signature in ``VMCK_AUTOTUNE_CACHE`` (a JSON file).
 """
 import json
 import os
@@ -292,12 +293,30 @@ class BatchedTFIM:
                 ms = a.elapsed_time(b)
                 if best is None or ms < best[0]:
                     best = (ms, dict(cand))
+        # local-energy launch shape (a pure function of the samples just drawn)
+        self.launch = dict(best[1])
+        best_e = None
+        for spi in (4, 8, 16):
+            for per_sm in (4, 8, 16):
+                self.launch.update(samples_per_item=spi, eloc_ctas=sms * per_sm)
+                self._build_work()
+                self._local_energies()
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                self._local_energies()
+                b.record()
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b)
+                if best_e is None or ms < best_e[0]:
+                    best_e = (ms, spi, sms * per_sm)
+        best[1].update(samples_per_item=best_e[1], eloc_ctas=best_e[2])
         for s, v in zip(self.sigma, saved):
             s.copy_(v)
         for s, v in zip(self.nacc, saved_acc):
             s.copy_(v)
         # the tuning launches advanced the proposal counters: rebuild the tables
         self._build_tables()
-        choice = dict(best[1], tuned_ms=round(best[0], 4))
+        choice = dict(best[1], tuned_ms=round(best[0], 4), tuned_eloc_ms=round(best_e[0], 4))
         _store_tune_choice(path, sig, choice)
         return choice

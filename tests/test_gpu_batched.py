@@ -53,3 +53,27 @@ def test_batched_equals_single(nk, tmp_path, monkeypatch):
         p, e = _single(nk, N, h, 10 + i, steps, B, L, nd, shift, lr)
         assert torch.equal(p, bt.instance_parameters(i)), f"instance {i} differs"
         np.testing.assert_array_equal(np.array(e), np.array([row[i] for row in e_b]))
+
+
+def test_batched_equals_single_at_workload_size(nk, tmp_path, monkeypatch):
+    """Three instances of the 64-instance workload's distribution, at its sizes
+    (1024 chains x 4 samples, the largest N = 144 among them), stepped by the
+    batched runner (two eager steps and one captured-graph step) equal their
+    single-instance runs bit for bit."""
+    monkeypatch.setenv("VMCK_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    full = nk.batched.tfim_instances(64, seed=0)
+    big = max(full, key=lambda t: t[0])
+    small = min(full, key=lambda t: t[0])
+    inst = [big, full[1], small]
+    B, L, nd, shift, lr = 1024, 4, 5, 1e-4, 0.01
+    bt = nk.batched.BatchedTFIM(inst, n_chains=B, chain_length=L, n_discard=nd,
+                                diag_shift=shift, lr=lr, seed=20)
+    for _ in range(2):
+        _, status = bt.step()
+        assert np.all(status == 0)
+    bt.capture()
+    _, status = bt.step()
+    assert np.all(status == 0)
+    for i, (N, h) in enumerate(inst):
+        p, _ = _single(nk, N, h, 20 + i, bt.step_count, B, L, nd, shift, lr)
+        assert torch.equal(p, bt.instance_parameters(i)), f"instance {i} (N={N}) differs"
