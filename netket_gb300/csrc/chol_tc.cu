@@ -801,12 +801,28 @@ int chol_block_rows() {
 int64_t chol_tc_workspace_bytes(int64_t n) {
   const int64_t nb = (n + LB - 1) / LB;
   int64_t b = 0;
-  b += 2 * (int64_t)CHOL_BLOCK * n * 2;  // Ph hi / lo (K = 512 rows per column)
+  b += 4 * (int64_t)CHOL_BLOCK * n * 2;  // Ph hi / lo, two buffers (K = 512 rows per column)
   b += 2 * (int64_t)LB * n * 2;          // Bs hi / lo
   b += 2 * (int64_t)LB * LB * 2;         // Xs hi / lo
   b += 64;                               // scales
   b += nb * LB * LB * 4;                 // Yinv
-  return b + 6 * 1024;                   // alignment
+  return b + 8 * 1024;                   // alignment
+}
+
+int chol_events_needed(int64_t n) {
+  const int64_t blk = chol_block_rows();
+  return (int)(3 * ((n + blk - 1) / blk) + 2);
+}
+
+// Trailing-update CTAs of the side stream: every SM but VMCK_CHOL_RESERVE (read
+// once per process, default 32), which stay free for the chain's kernels.
+static int side_ctas(int sms) {
+  static const int reserve = [] {
+    const char *v = getenv("VMCK_CHOL_RESERVE");
+    const int r = v ? atoi(v) : 32;
+    return r < 0 ? 0 : r;
+  }();
+  return std::max(8, sms - reserve);
 }
 
 static char *align_up(char *p, size_t a) {
@@ -814,17 +830,20 @@ static char *align_up(char *p, size_t a) {
 }
 
 int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *status,
-                   float **yinv_out) {
+                   float **yinv_out, const CholStreams *ls) {
   if (n <= 0) return VMCK_OK;
   if (n >= (1ll << 30)) {
     set_last_error("chol_tc: n must be below 2^30");
     return VMCK_ERR_UNSUPPORTED;
   }
   char *p = align_up(static_cast<char *>(ws), 1024);
-  __half *ph_hi = reinterpret_cast<__half *>(p);
-  p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
-  __half *ph_lo = reinterpret_cast<__half *>(p);
-  p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
+  __half *ph_hi[2], *ph_lo[2];
+  for (int q = 0; q < 2; ++q) {
+    ph_hi[q] = reinterpret_cast<__half *>(p);
+    p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
+    ph_lo[q] = reinterpret_cast<__half *>(p);
+    p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
+  }
   __half *bs_hi = reinterpret_cast<__half *>(p);
   p = align_up(p + (size_t)LB * n * 2, 1024);
   __half *bs_lo = reinterpret_cast<__half *>(p);
@@ -838,58 +857,117 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
   float *yinv = reinterpret_cast<float *>(p);
   if (yinv_out) *yinv_out = yinv;
 
+  const int64_t blk = chol_block_rows();
+  const int nblocks = (int)((n + blk - 1) / blk);
+  // look-ahead: the chain stream factors block row b and updates block row b + 1
+  // (LA); the side stream updates rows b + 2 .. with block row b, first block row
+  // b + 2 (event E[b]: LA(b + 1) waits for it), then the rest (event G[b]: block
+  // row b + 2 reuses block row b's split-panel buffer).  F[b]: block row b's
+  // panel is complete.
+  const bool two = ls && ls->chain && ls->side && ls->n_events >= 3 * nblocks + 2;
+  cudaStream_t chain = two ? ls->chain : st, side = two ? ls->side : st;
+  cudaEvent_t *F = two ? ls->events : nullptr, *E = F ? F + nblocks : nullptr;
+  cudaEvent_t *G = E ? E + nblocks : nullptr;
   int rc;
+  if (two) {
+    VMCK_CUDA(cudaEventRecord(ls->events[3 * nblocks], st));
+    VMCK_CUDA(cudaStreamWaitEvent(chain, ls->events[3 * nblocks], 0));
+    VMCK_CUDA(cudaStreamWaitEvent(side, ls->events[3 * nblocks], 0));
+  }
+  const int side_grid = two ? side_ctas(num_sms_dev()) : 0;
   VMCK_CUDA(cudaFuncSetAttribute(chol_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)CHOL_LEAF_SMEM));
-  chol_bounds_kernel<<<1, 256, 0, st>>>(A, n, scales, status);
+  chol_bounds_kernel<<<1, 256, 0, chain>>>(A, n, scales, status);
   if ((rc = check_launch("chol_tc bounds"))) return rc;
   {
     const int rows = (int)std::min<int64_t>(LB, n);
     const int64_t cols = n - rows;
     if (cols > 0) {
-      chol_split_rows_kernel<<<ceil_div(cols * LB, 256), 256, 0, st>>>(
+      chol_split_rows_kernel<<<ceil_div(cols * LB, 256), 256, 0, chain>>>(
           A, n, 0, rows, rows, cols, LB, scales, bs_hi, bs_lo);
       if ((rc = check_launch("chol_tc split"))) return rc;
     }
   }
-  const int64_t blk = chol_block_rows();
-  for (int64_t k0 = 0; k0 < n; k0 += blk) {
+  for (int b = 0; b < nblocks; ++b) {
+    const int64_t k0 = b * blk;
     const int64_t k1 = std::min<int64_t>(n, k0 + blk), w = k1 - k0;
+    const int64_t k2 = std::min<int64_t>(n, k1 + blk), k3 = std::min<int64_t>(n, k2 + blk);
+    __half *qh = ph_hi[two ? (b & 1) : 0], *ql = ph_lo[two ? (b & 1) : 0];
     // the block row's split panel: row (c - k0) holds U(k0 .. k1, c) (K = w)
-    const SplitOperand ph{ph_hi, ph_lo, CHOL_BLOCK, w, n - k0};
+    const SplitOperand ph{qh, ql, CHOL_BLOCK, w, n - k0};
+    if (two && b >= 2)
+      VMCK_CUDA(cudaStreamWaitEvent(chain, G[b - 2], 0));  // side is done with this buffer
     for (int64_t r0 = k0; r0 < k1; r0 += LB) {
       const int64_t r1 = std::min<int64_t>(k1, r0 + LB);
-      const int mp = (int)(r1 - r0), p = (int)((r0 - k0) / LB);
-      chol_leaf_kernel<<<1, LEAF_T, CHOL_LEAF_SMEM, st>>>(A, n, r0, mp, xs_hi, xs_lo, scales + 2,
-                                                          yinv + (r0 / LB) * LB * LB, status);
+      const int mp = (int)(r1 - r0), pp = (int)((r0 - k0) / LB);
+      chol_leaf_kernel<<<1, LEAF_T, CHOL_LEAF_SMEM, chain>>>(A, n, r0, mp, xs_hi, xs_lo,
+                                                             scales + 2,
+                                                             yinv + (r0 / LB) * LB * LB, status);
       if ((rc = check_launch("chol_tc leaf"))) return rc;
       if (r1 == n) break;
       const SplitOperand xop{xs_hi, xs_lo, LB, mp, mp};
       const SplitOperand bop{bs_hi, bs_lo, LB, mp, n - r1};
       // panel: U[r0:r1, r1:n] = X^T A[r0:r1, r1:n], split copy into Ph
-      if ((rc = tc_gemm(st, xop, 0, bop, 0, 0, mp, (int)(n - r1), mp, A + r0 + r1 * n, n, 1.0f,
-                        0.0f, scales + 2, scales + 0, 0, ph_hi + (r1 - k0) * CHOL_BLOCK + p * LB,
-                        ph_lo + (r1 - k0) * CHOL_BLOCK + p * LB, CHOL_BLOCK, mp, 0, scales + 1,
+      if ((rc = tc_gemm(chain, xop, 0, bop, 0, 0, mp, (int)(n - r1), mp, A + r0 + r1 * n, n,
+                        1.0f, 0.0f, scales + 2, scales + 0, 0,
+                        qh + (r1 - k0) * CHOL_BLOCK + pp * LB,
+                        ql + (r1 - k0) * CHOL_BLOCK + pp * LB, CHOL_BLOCK, mp, 0, scales + 1,
                         status, 0)))
         return rc;
       if (r1 < k1) {
         // rest of the block row; rows [r1, r1 + next) feed the next panel (split)
         const int next = (int)std::min<int64_t>(LB, k1 - r1);
-        const SplitOperand pk{ph_hi, ph_lo, CHOL_BLOCK, p * LB + mp, n - k0};
-        if ((rc = tc_gemm(st, pk, (int)(r1 - k0), pk, (int)(r1 - k0), p * LB, (int)(k1 - r1),
-                          (int)(n - r1), mp, A + r1 + r1 * n, n, -1.0f, 1.0f, scales + 1,
-                          scales + 1, 1, bs_hi, bs_lo, LB, next, next, scales + 0, status, 0)))
+        const SplitOperand pk{qh, ql, CHOL_BLOCK, pp * LB + mp, n - k0};
+        if ((rc = tc_gemm(chain, pk, (int)(r1 - k0), pk, (int)(r1 - k0), pp * LB,
+                          (int)(k1 - r1), (int)(n - r1), mp, A + r1 + r1 * n, n, -1.0f, 1.0f,
+                          scales + 1, scales + 1, 1, bs_hi, bs_lo, LB, next, next, scales + 0,
+                          status, 0)))
           return rc;
       }
     }
     if (k1 == n) break;
-    // trailing matrix by the whole block row; rows [k1, k1 + next) feed the next
-    // block row's first panel (split)
     const int next = (int)std::min<int64_t>(LB, n - k1);
-    if ((rc = tc_gemm(st, ph, (int)w, ph, (int)w, 0, (int)(n - k1), (int)(n - k1), (int)w,
+    if (!two) {
+      // trailing matrix by the whole block row; rows [k1, k1 + next) feed the
+      // next block row's first panel (split)
+      if ((rc = tc_gemm(st, ph, (int)w, ph, (int)w, 0, (int)(n - k1), (int)(n - k1), (int)w,
+                        A + k1 + k1 * n, n, -1.0f, 1.0f, scales + 1, scales + 1, 1, bs_hi, bs_lo,
+                        LB, next, next, scales + 0, status, 0)))
+        return rc;
+      continue;
+    }
+    VMCK_CUDA(cudaEventRecord(F[b], chain));
+    // LA(b): block row b + 1 by this block row, once the side stream has applied
+    // the previous block row to it
+    if (b >= 1) VMCK_CUDA(cudaStreamWaitEvent(chain, E[b - 1], 0));
+    if ((rc = tc_gemm(chain, ph, (int)w, ph, (int)w, 0, (int)(k2 - k1), (int)(n - k1), (int)w,
                       A + k1 + k1 * n, n, -1.0f, 1.0f, scales + 1, scales + 1, 1, bs_hi, bs_lo,
                       LB, next, next, scales + 0, status, 0)))
       return rc;
+    // side: block row b + 2, then the rest
+    VMCK_CUDA(cudaStreamWaitEvent(side, F[b], 0));
+    if (k2 < n) {
+      const int off2 = (int)(k2 - k0);
+      if ((rc = tc_gemm(side, ph, off2, ph, off2, 0, (int)(k3 - k2), (int)(n - k2), (int)w,
+                        A + k2 + k2 * n, n, -1.0f, 1.0f, scales + 1, scales + 1, 1, nullptr,
+                        nullptr, 0, 0, 0, nullptr, status, side_grid)))
+        return rc;
+    }
+    VMCK_CUDA(cudaEventRecord(E[b], side));
+    if (k3 < n) {
+      const int off3 = (int)(k3 - k0);
+      if ((rc = tc_gemm(side, ph, off3, ph, off3, 0, (int)(n - k3), (int)(n - k3), (int)w,
+                        A + k3 + k3 * n, n, -1.0f, 1.0f, scales + 1, scales + 1, 1, nullptr,
+                        nullptr, 0, 0, 0, nullptr, status, side_grid)))
+        return rc;
+    }
+    VMCK_CUDA(cudaEventRecord(G[b], side));
+  }
+  if (two) {
+    VMCK_CUDA(cudaEventRecord(ls->events[3 * nblocks], chain));
+    VMCK_CUDA(cudaStreamWaitEvent(st, ls->events[3 * nblocks], 0));
+    VMCK_CUDA(cudaEventRecord(ls->events[3 * nblocks + 1], side));
+    VMCK_CUDA(cudaStreamWaitEvent(st, ls->events[3 * nblocks + 1], 0));
   }
   return VMCK_OK;
 }

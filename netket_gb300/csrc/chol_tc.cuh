@@ -15,12 +15,24 @@ int chol_block_rows();
 // Device workspace (bytes) of chol_tc_factor for an n x n matrix.
 int64_t chol_tc_workspace_bytes(int64_t n);
 
+// Streams and events of the look-ahead factorisation (owned by the caller):
+// chain (high priority) runs the latency-bound panel chain, side the bulk of the
+// trailing updates; events: chol_events_needed(n).
+struct CholStreams {
+  cudaStream_t chain, side;
+  cudaEvent_t *events;
+  int n_events;
+};
+int chol_events_needed(int64_t n);
+
 // In-place upper Cholesky A = U^T U of the column-major FP32 matrix A (n x n,
 // upper triangle valid, ld n).  ws: chol_tc_workspace_bytes(n) bytes.  On
 // return *yinv (inside ws) holds, per 128-row diagonal block K, Y_K = U_KK^-T as
 // a zero-padded column-major 128 x 128 matrix.  Failed pivots / non-finite
-// diagonals are OR-ed into *status.
+// diagonals are OR-ed into *status.  With ls the trailing updates overlap the
+// panel chain on two streams (the caller's stream waits for both at the end);
+// without it everything runs on st.
 int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *status,
-                   float **yinv);
+                   float **yinv, const CholStreams *ls = nullptr);
 
 }  // namespace vmck

@@ -927,15 +927,15 @@ static int chol_rec(RecChol &R, float *A, int64_t lda, int64_t n) {
 // left), overlapping the next panels' latency-bound factorisation.  Events:
 // F[q] (panel q final) orders the side stream's use of it; U[q] (block row q+2
 // updated by panel q) orders the caller's update of that row by panel q+1.
-static int chol_lookahead_setup(vmck_ctx *c, int panels) {
+// The context's look-ahead streams (chain: highest priority; side: lowest) and
+// at least `need` events, created on first use.
+static int streams_setup(vmck_ctx *c, int need) {
   if (!c->side) {
     int lo = 0, hi = 0;
     VMCK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    VMCK_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    VMCK_CUDA(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, lo));
     VMCK_CUDA(cudaStreamCreateWithPriority(&c->chain, cudaStreamNonBlocking, hi));
-    VMCK_BLAS(cublasCreate(&c->blas2));
   }
-  const int need = 2 * panels + 2;
   if (c->n_events < need) {
     cudaEvent_t *ev = static_cast<cudaEvent_t *>(malloc(sizeof(cudaEvent_t) * need));
     if (!ev) return VMCK_ERR_NOMEM;
@@ -946,6 +946,13 @@ static int chol_lookahead_setup(vmck_ctx *c, int panels) {
     c->events = ev;
     c->n_events = need;
   }
+  return VMCK_OK;
+}
+
+static int chol_lookahead_setup(vmck_ctx *c, int panels) {
+  int rc = streams_setup(c, 2 * panels + 2);
+  if (rc) return rc;
+  if (!c->blas2) VMCK_BLAS(cublasCreate(&c->blas2));
   VMCK_BLAS(cublasSetStream(c->blas2, c->side));
   VMCK_BLAS(cublasSetMathMode(c->blas2, CUBLAS_FP32_EMULATED_BF16X9_MATH));
   VMCK_BLAS(cublasSetEmulationStrategy(c->blas2, CUBLAS_EMULATION_STRATEGY_EAGER));
@@ -1382,7 +1389,9 @@ static int refined_solve(vmck_ctx *c, cudaStream_t st, const double *A64, float 
       pad_identity_kernel<<<1, 32, 0, st>>>(F, n, np);
       if ((rc = check_launch("refined solve padding"))) return rc;
     }
-    rc = chol_tc_factor(st, F, np, static_cast<char *>(c->tcws) + tc_off, status, &yinv);
+    if ((rc = streams_setup(c, chol_events_needed(np)))) return rc;
+    const CholStreams ls{c->chain, c->side, c->events, c->n_events};
+    rc = chol_tc_factor(st, F, np, static_cast<char *>(c->tcws) + tc_off, status, &yinv, &ls);
     if (rc) return rc;
     if (np != n)
       VMCK_CUDA(cudaMemcpy2DAsync(A32, n * 4, F, np * 4, n * 4, n, cudaMemcpyDeviceToDevice, st));
