@@ -815,11 +815,11 @@ int chol_events_needed(int64_t n) {
 }
 
 // Trailing-update CTAs of the side stream: every SM but VMCK_CHOL_RESERVE (read
-// once per process, default 32), which stay free for the chain's kernels.
+// once per process, default 48), which stay free for the chain's kernels.
 static int side_ctas(int sms) {
   static const int reserve = [] {
     const char *v = getenv("VMCK_CHOL_RESERVE");
-    const int r = v ? atoi(v) : 32;
+    const int r = v ? atoi(v) : 48;
     return r < 0 ? 0 : r;
   }();
   return std::max(8, sms - reserve);
