@@ -305,6 +305,8 @@ def run_ours(args):
     if solve_ms:
         chol_flops = float(n) ** 3 / 3.0
         achieved = chol_flops / (solve_ms * 1e-3) / 1e12
+        if args.n_samples != WORKLOAD["n_samples"]:
+            args.solve_traffic = None  # measured for the 16,384 case only
         roof = {"kernel": "minSR solve: Cholesky of T (chol_leaf_kernel + tcgen05 tc_gemm_kernel, "
                           "FP16 hi/lo split, 3 products) + iterative refinement (trsv, symv)",
                 "bound": "tensor", "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"],
@@ -626,7 +628,9 @@ def main():
     ap.add_argument("--n-samples", type=int, default=WORKLOAD["n_samples"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gram-traffic", type=float, default=None)
-    ap.add_argument("--solve-traffic", type=float, default=None,
+    # DRAM bytes of one n = 16,384 solve, summed over its 473 launches in one ncu
+    # capture (profiles/cholesky_solve_dram_n16384.md)
+    ap.add_argument("--solve-traffic", type=float, default=18.88e9,
                     help="DRAM bytes of one solve (ncu); reported as roofline.traffic")
     ap.add_argument("--matched-steps", type=int, default=8,
                     help="steps of the matched-energy comparison (0 skips it)")
