@@ -105,7 +105,9 @@ __global__ void chol_split_rows_kernel(const float *__restrict__ A, int64_t n, i
 // result: oh/ol[(nn - o_col0) ldo + m] = split(value * so) for m < o_rows,
 // nn >= o_col0.
 //
-// Persistent and warp-specialised: warp 0 streams 64-wide K slabs of the four
+// Launched with programmatic dependent launch: the prologue (tensor-memory
+// allocation, barriers, descriptor prefetch) overlaps the previous kernel of the
+// stream.  Persistent and warp-specialised: warp 0 streams 64-wide K slabs of the four
 // operand tiles with TMA (128-byte swizzle) into a 2-stage ring; warp 1 issues
 // the tcgen05.mma (kind::f16, M = 128, N = 256) from one thread; warps 2-17 hold
 // the tile's FP32 sums in registers (64 per thread).
@@ -226,6 +228,10 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
   const int num_kb = (g.K + G_BK - 1) / G_BK;
+  // the prologue above overlaps the previous kernel of the stream; its output
+  // (operands, C) is read only from here on
+  pdl_wait();
+  pdl_trigger();
 
   auto fail = [&]() {
     if (g.status) atomicOr(g.status, VMCK_DEV_TIMEOUT);
@@ -464,6 +470,8 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) not_spd = 0;
   if (tid < LPAD) S[LB * LLD + tid] = 0.0f;
+  pdl_wait();  // the block was written by the previous kernel of the stream
+  pdl_trigger();
   if (tid < LB) S[tid * LLD + LB] = 0.0f;  // each row's padding column
   {
     // all 64 of a thread's loads in flight at once
@@ -785,7 +793,17 @@ int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOpera
                                  (int)smem));
   const int sms = max_ctas > 0 ? max_ctas : num_sms_dev();
   const unsigned grid = (unsigned)std::min<int64_t>(g.tiles, sms);
-  tc_gemm_kernel<<<grid, G_THREADS, smem, st>>>(mAh, mAl, mBh, mBl, g);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(G_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  VMCK_CUDA(cudaLaunchKernelEx(&cfg, tc_gemm_kernel, mAh, mAl, mBh, mBl, g));
   return check_launch("tc_gemm");
 }
 
@@ -900,10 +918,21 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
     for (int64_t r0 = k0; r0 < k1; r0 += LB) {
       const int64_t r1 = std::min<int64_t>(k1, r0 + LB);
       const int mp = (int)(r1 - r0), pp = (int)((r0 - k0) / LB);
-      chol_leaf_kernel<<<1, LEAF_T, CHOL_LEAF_SMEM, chain>>>(A, n, r0, mp, xs_hi, xs_lo,
-                                                             scales + 2,
-                                                             yinv + (r0 / LB) * LB * LB, status);
-      if ((rc = check_launch("chol_tc leaf"))) return rc;
+      {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(1);
+        cfg.blockDim = dim3(LEAF_T);
+        cfg.dynamicSmemBytes = CHOL_LEAF_SMEM;
+        cfg.stream = chain;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        VMCK_CUDA(cudaLaunchKernelEx(&cfg, chol_leaf_kernel, A, n, r0, mp, xs_hi, xs_lo,
+                                     scales + 2, yinv + (r0 / LB) * LB * LB, status));
+        if ((rc = check_launch("chol_tc leaf"))) return rc;
+      }
       if (r1 == n) break;
       const SplitOperand xop{xs_hi, xs_lo, LB, mp, mp};
       const SplitOperand bop{bs_hi, bs_lo, LB, mp, n - r1};

@@ -165,6 +165,16 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream-serialisation attribute may start while its predecessor in the stream
+// still runs; griddepcontrol.wait blocks (in hardware) until the predecessor
+// has completed and its memory is visible, and launch_dependents lets the next
+// kernel start early.  Both are no-ops for a kernel launched without it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // UMMA instruction descriptor for kind::f16 with FP16 A and B (format 0), FP32
 // accumulate, both K-major.
 __host__ __device__ constexpr uint32_t umma_idesc_f16(int M, int N) {
