@@ -731,12 +731,28 @@ static int make_f16_map(CUtensorMap *map, const __half *base, int64_t kdim, int6
   return VMCK_OK;
 }
 
-struct SplitOperand {
-  const __half *hi, *lo;
-  int64_t ld;     // row stride (elements)
-  int64_t kdim;   // K extent seen by TMA (zero fill beyond)
-  int64_t rows;   // row extent seen by TMA (zero fill beyond)
-};
+
+__global__ void tc_split_rows_kernel(const float *__restrict__ src, int64_t rows, int K, int ldk,
+                                     float bound, __half *__restrict__ hi,
+                                     __half *__restrict__ lo, float *scale) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const float s = split_scale(bound);
+  if (e == 0) *scale = s;
+  if (e >= rows * ldk) return;
+  const int64_t r = e / ldk;
+  const int k = (int)(e - r * ldk);
+  __half h = __float2half_rn(0.0f), l = h;
+  if (k < K) split_f16(src[r * K + k], s, h, l);
+  hi[e] = h;
+  lo[e] = l;
+}
+
+int tc_split_rows(cudaStream_t st, const float *src, int64_t rows, int K, int ldk, float bound,
+                  __half *hi, __half *lo, float *scale) {
+  tc_split_rows_kernel<<<ceil_div(rows * ldk, 256), 256, 0, st>>>(src, rows, K, ldk, bound, hi,
+                                                                  lo, scale);
+  return check_launch("tc split rows");
+}
 
 static int num_sms_dev() {
   int dev = 0, sms = 148;

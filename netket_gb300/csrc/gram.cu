@@ -14,6 +14,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "chol_tc.cuh"
 #include "gram_tc.cuh"
 
 namespace vmck {
@@ -232,6 +233,41 @@ __device__ __forceinline__ df32 gram_value_df(float Ac, float2 ws, float2 wc, df
   return v;
 }
 
+// ---------------------------------------------------------------- assembly (mode 4)
+// T from Ac = c c^T (FP32, already in T32's lower triangle, written by the
+// tensor-core GEMM): the same double-float epilogue as the SIMT Gram.  Block
+// (x, y) covers columns [256 x, +256) of rows [64 y, +64), lower triangle only;
+// a thread keeps its column's sign bits and pairs in registers, the row's are
+// warp-uniform loads.
+constexpr int GA_ROWS = 64;
+__global__ void __launch_bounds__(256) gram_assemble_kernel(
+    const uint32_t *__restrict__ bits, int words, int N, int64_t n,
+    const float2 *__restrict__ hdf, const float2 *__restrict__ wdf,
+    const float2 *__restrict__ s0sq_p, float inv_n, df32 shift, double *__restrict__ T64,
+    float *__restrict__ T32) {
+  const int64_t c0 = (int64_t)blockIdx.x * 256;
+  const int64_t r0 = (int64_t)blockIdx.y * GA_ROWS;
+  const int64_t r1 = r0 + GA_ROWS < n ? r0 + GA_ROWS : n;
+  if (r1 <= c0) return;  // the whole block lies above the diagonal
+  const int64_t c = c0 + threadIdx.x;
+  if (c >= n) return;
+  uint32_t cb[9];
+#pragma unroll
+  for (int w = 0; w < 9; ++w) cb[w] = w < words ? bits[c * words + w] : 0u;
+  const float2 wc = wdf[c], hc = hdf[c], q = *s0sq_p;
+  for (int64_t r = r0 > c ? r0 : c; r < r1; ++r) {
+    int diff = 0;
+#pragma unroll
+    for (int w = 0; w < 9; ++w)
+      if (w < words) diff += __popc(cb[w] ^ __ldg(bits + r * words + w));
+    const int64_t e = r * n + c;
+    const df32 v = gram_value_df(T32[e], wdf[r], wc, df32{q.x, q.y}, N - 2 * diff, hdf[r], hc,
+                                 inv_n, r == c, shift);
+    T32[e] = v.hi + v.lo;
+    if (T64) T64[e] = df_to_double(v);
+  }
+}
+
 // ---------------------------------------------------------------- SIMT Gram
 constexpr int GT = 64, GK = 16;
 
@@ -362,8 +398,10 @@ static GramWs gram_ws_layout(double *ws, int N, int M, int64_t n) {
 extern "C" int64_t vmck_gram_workspace_size(int32_t N, int32_t M, int64_t n) {
   const int64_t words = gram_words(N);
   const int64_t P = (int64_t)M + (int64_t)N * M + N;
+  // the tail: the tensor-core Gram's panels, or the split rows of mode 4
+  const int64_t split = ((n * ((M + 7) & ~7) + 511) & ~int64_t(511)) * 2 * 2 / 8 + (1024 + 16) / 8;
   return n + 2 + (n * words + 1) / 2 + P + n + n + 2 + (M + 1) / 2 + 2 + (n * (int64_t)M + 1) / 2 +
-         2 + vmck::gram_tc_workspace_doubles(M, n) + 8;
+         2 + std::max(vmck::gram_tc_workspace_doubles(M, n), split) + 8;
 }
 
 extern "C" int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t dtype,
@@ -375,8 +413,8 @@ extern "C" int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t
                "rbm_gram arguments");
   VMCK_REQUIRE(N <= 288, "rbm_gram supports N <= 288");
   VMCK_REQUIRE(workspace_len >= vmck_gram_workspace_size(N, M, n), "rbm_gram workspace too small");
-  VMCK_REQUIRE((mode == 0 && dtype == VMCK_F64) || (mode >= 1 && mode <= 3 && dtype == VMCK_F32),
-               "rbm_gram: mode/dtype combination (0: F64, 1-3: F32 tanh input)");
+  VMCK_REQUIRE((mode == 0 && dtype == VMCK_F64) || (mode >= 1 && mode <= 4 && dtype == VMCK_F32),
+               "rbm_gram: mode/dtype combination (0: F64, 1-4: F32 tanh input)");
   VMCK_REQUIRE(mode < 2 || T32, "rbm_gram: tensor-core modes write T32");
   cudaStream_t st = as_stream(s);
   const int words = (int)gram_words(N);
@@ -406,6 +444,28 @@ extern "C" int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t
   h_df_kernel<<<ceil_div(n, 256), 256, 0, st>>>(w.g, w.cptr, n, w.hdf);
   if ((rc = check_launch("gram h pairs"))) return rc;
   const double inv_n = 1.0 / (double)n;
+  if (mode == 4) {
+    VMCK_REQUIRE(n < (int64_t)INT32_MAX && (n + GA_ROWS - 1) / GA_ROWS <= 65535,
+                 "rbm_gram mode 4: too many samples");
+    // c c^T on the tensor cores: c = t - s0 (|c| <= 2) split into FP16 hi / lo,
+    // the triangular split GEMM into T32, then the double-float assembly
+    const int ldk = (M + 7) & ~7;
+    __half *hi = reinterpret_cast<__half *>(
+        (reinterpret_cast<uintptr_t>(w.tc) + 1023) & ~uintptr_t(1023));
+    __half *lo = hi + ((n * ldk + 511) & ~int64_t(511));
+    float *scale = reinterpret_cast<float *>(lo + ((n * ldk + 511) & ~int64_t(511)));
+    if ((rc = tc_split_rows(st, w.c, n, M, ldk, 2.0f, hi, lo, scale))) return rc;
+    const SplitOperand op{hi, lo, ldk, M, n};
+    if ((rc = tc_gemm(st, op, 0, op, 0, 0, (int)n, (int)n, M, T32, n, 1.0f, 0.0f, scale, scale,
+                      1, nullptr, nullptr, 0, 0, 0, nullptr, status, 0)))
+      return rc;
+    const df32 shift = {(float)diag_shift, (float)(diag_shift - (double)(float)diag_shift)};
+    gram_assemble_kernel<<<dim3((unsigned)((n + 255) / 256),
+                                (unsigned)((n + GA_ROWS - 1) / GA_ROWS)),
+                           256, 0, st>>>(w.bits, words, N, n, w.hdf, w.wdf, w.s0sq,
+                                         (float)inv_n, shift, T64, T32);
+    return check_launch("gram assemble");
+  }
   if (mode >= 2)
     return gram_tc_launch(ctx, st, w.c, w.bits, words, N, M, n, w.hdf, w.wdf, w.s0sq, inv_n,
                           diag_shift, T64, T32, w.tc, mode == 2 ? 1 : 0, status);

@@ -146,7 +146,8 @@ def jacobian_dense(tanh_t, x, N, M, col_mean, scale, out_dtype):
 def gram_structured(tanh_t, x, N, M, obar, diag_shift, mode, want_f32=False, status=None):
     """Lower triangle of T = O_L O_L^T + diag_shift I (n, n) FP64 (+ FP32 copy).
     mode 0: FP64 CUDA cores; 1: FP32 CUDA cores; 2: tcgen05 BF16 hi/lo split;
-    3: tcgen05 single BF16."""
+    3: tcgen05 single BF16; 4: tcgen05 FP16 hi/lo split with per-slab drained
+    accumulation (the blocked-Cholesky GEMM) and a double-float assembly pass."""
     n = x.shape[0]
     T64 = torch.empty((n, n), dtype=torch.float64, device=x.device)
     T32 = torch.empty((n, n), dtype=torch.float32, device=x.device) if want_f32 else None

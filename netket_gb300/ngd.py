@@ -16,9 +16,12 @@ Two ways to form T:
     hi * hi part accumulates apart from the small cross terms), ``3`` with one
     BF16, ``1`` in FP32 on the CUDA cores.  At n = 16,384, M = 400 and
     diag_shift 1e-4 the minSR update of mode 2 is within 1.2e-4 (relative) of
-    the all-FP64 one, mode 1 within 2.5e-4, mode 3 within 2.4e-2.  With M = 2048
-    (16 x 16, alpha 8) mode 2's T is no longer positive definite, so the default
-    is mode 2 only for M <= ``TC_GRAM_MAX_M`` and mode 1 above;
+    the all-FP64 one, mode 1 within 2.5e-4, mode 3 within 2.4e-2.  The tensor
+    cores' FP32 accumulation loses bits in proportion to the MMA chain length, so
+    at M = 2048 (16 x 16, alpha 8) mode 2's T is no longer positive definite;
+    above ``TC_GRAM_MAX_M`` the default is mode 4, FP16 hi/lo operands whose
+    accumulators are drained into FP32 registers every 64 columns of K (the
+    factorisation's trailing-update GEMM) followed by the double-float assembly;
   * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
     and a cuBLAS SYRK.
 Solvers (``solve=``):
@@ -88,8 +91,9 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
             mode = 0
         else:
             # the tensor cores' FP32 accumulation over K = M of the hi * hi term keeps T
-            # positive definite at M = 400 (diag_shift 1e-4) but not at M = 2048
-            mode = 2 if M <= TC_GRAM_MAX_M else 1
+            # positive definite at M = 400 (diag_shift 1e-4) but not at M = 2048:
+            # there the per-slab drained GEMM
+            mode = 2 if M <= TC_GRAM_MAX_M else 4
     obar = K.column_means(t, x, N, M)
     dv = K.center_scale(e, mean_dev, 2.0 * s)
     if momentum is not None and old_updates is not None:

@@ -102,7 +102,8 @@ def _round_terms(v, terms):
 def test_fp32_and_tensor_core_gram(nk, N, alpha, n):
     """FP32 Gram modes contract c = round(t - s0) (s0 = fp32 column mean of t;
     mode 1 FP32, mode 2 hi + lo BF16 pairs on tcgen05, mode 3 one BF16 on
-    tcgen05) and add the shift back exactly: T equals the FP64 Gram of the
+    tcgen05, mode 4 FP16 hi + lo with per-slab drained accumulation and a
+    separate assembly pass) and add the shift back exactly: T equals the FP64 Gram of the
     Jacobian of t_eff = c + s0 centred at the given obar, to FP32 accumulation
     accuracy, and is positive definite."""
     model, flat, M, x, t, p = _problem(nk, N, alpha, n)
@@ -112,7 +113,7 @@ def test_fp32_and_tensor_core_gram(nk, N, alpha, n):
     obar = nk.kernels.column_means(t, x, N, M)
     s0 = obar[:M].float()
     ob = obar.cpu().numpy()
-    for mode, terms in ((1, 0), (2, 2), (3, 1)):
+    for mode, terms in ((1, 0), (2, 2), (3, 1), (4, 0)):
         teff = (_round_terms(t32 - s0, terms).double() + s0.double()).cpu().numpy()
         O = (_jacobian_from_t(teff, xs) - ob) / math.sqrt(n)
         ref = O @ O.T + 1e-3 * np.eye(n)
@@ -127,6 +128,46 @@ def test_fp32_and_tensor_core_gram(nk, N, alpha, n):
         np.testing.assert_allclose(T32.cpu().numpy()[low], got[low], rtol=1e-6, atol=1e-7 * scale)
         full = np.tril(got) + np.tril(got, -1).T
         np.linalg.cholesky(full)  # positive definite
+
+
+def _structured_gram_f64(teff, xs, ob, n, shift):
+    """O_L O_L^T + shift I in FP64 from the identity O(s).O(s') =
+    (t_s.t_s')(1 + x_s.x_s') + x_s.x_s' and g = O obar, without forming O."""
+    N, M = xs.shape[1], teff.shape[1]
+    X = xs @ xs.T
+    G = (teff @ teff.T) * (1.0 + X) + X
+    Wb = ob[M:M + N * M].reshape(N, M)
+    g = teff @ ob[:M] + np.einsum("si,ij,sj->s", xs, Wb, teff) + xs @ ob[M + N * M:]
+    return (G - g[:, None] - g[None, :] + ob @ ob) / n + shift * np.eye(n)
+
+
+@pytest.mark.parametrize("N,alpha,n", [(256, 8, 2048), (64, 10, 1500)])
+def test_tensor_core_gram_large_m(nk, N, alpha, n):
+    """M > 512 (the 16 x 16, alpha 8 model's M = 2048): the default mode 4 Gram
+    equals the FP64 Gram of t_eff = fp32(t - s0) + s0 to 2e-6 of its largest
+    entry and is positive definite at diag_shift 1e-4 with the model's default
+    N(0, 0.01) initialisation; it is the mode minsr_update picks there."""
+    model, flat, M, x, t, p = _problem(nk, N, alpha, n, std=0.01)
+    assert M > nk.ngd.TC_GRAM_MAX_M
+    xs = x.cpu().numpy().astype(np.float64)
+    low = np.tril_indices(n)
+    t32 = t.float().contiguous()
+    obar = nk.kernels.column_means(t, x, N, M)
+    s0 = obar[:M].float()
+    ob = obar.cpu().numpy()
+    teff = ((t32 - s0).double() + s0.double()).cpu().numpy()
+    ref = _structured_gram_f64(teff, xs, ob, n, 1e-4)
+    scale = np.abs(ref).max()
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    T64, T32 = nk.kernels.gram_structured(t32, x, N, M, obar, 1e-4, mode=4, want_f32=True,
+                                          status=st)
+    assert st.item() == 0
+    got = T64.cpu().numpy()
+    err = np.abs(got[low] - ref[low]).max() / scale
+    assert err < 2e-6, err
+    np.testing.assert_allclose(T32.cpu().numpy()[low], got[low], rtol=1e-6, atol=1e-7 * scale)
+    full = np.tril(got) + np.tril(got, -1).T
+    np.linalg.cholesky(full)
 
 
 def test_solvers(nk, golden):
