@@ -47,9 +47,22 @@ WORKLOAD = {
     "solver": "minSR, T 16384x16384, diag_shift=1e-4", "lr": 0.01,
 }
 METRIC = "VMC steps/s"
+# the large configuration (``--workload large``): 16x16 Heisenberg, alpha 8,
+# 65,536 samples, a 65,536 x 65,536 T
+LARGE = {
+    "workload": "heisenberg_16x16_alpha8_minsr",
+    "lattice": "16x16 periodic square, J=1, total_sz=0, sign_rule=True",
+    "model": "RBM alpha=8 (M=2048, P=526592)",
+    "sampler": "MetropolisExchange nn bonds (512 clusters)",
+    "n_chains": 16384, "n_samples": 65536, "n_discard_per_chain": 5,
+    "solver": "minSR, T 65536x65536, diag_shift=1e-4", "lr": 0.005,
+}
 
 
 def workload_config(args, world):
+    if args.workload == "large":
+        return dict(LARGE, precision=args.precision, parallelism=f"replicas{world}",
+                    l2="per-step working set > L2: T64 34.4 GB + T32 17.2 GB")
     cfg = dict(WORKLOAD, precision=args.precision, parallelism=f"replicas{world}",
                l2="per-step working set > L2: T64 2.1 GB + T32 1.1 GB")
     if (args.n_chains, args.n_samples) != (WORKLOAD["n_chains"], WORKLOAD["n_samples"]):
@@ -58,6 +71,22 @@ def workload_config(args, world):
                    solver=f"minSR, T {n}x{n}, diag_shift=1e-4",
                    l2=f"T64 {8 * n * n / 1e9:.2f} GB + T32 {4 * n * n / 1e9:.2f} GB")
     return cfg
+
+
+def build_large(nk, precision, seed=0):
+    """16x16 Heisenberg (J = 1, Marshall sign rule, total Sz = 0), RBM alpha 8,
+    MetropolisExchange on the nearest-neighbour bonds, 16,384 chains x 4 samples,
+    minSR with diag_shift 1e-4, SGD lr 0.005 (at lr 0.01 this run diverges after
+    about ten steps: the energy turns back up and the local energies blow up)."""
+    g = nk.graph.Square(16)
+    hi = nk.hilbert.Spin(0.5, N=256, total_sz=0)
+    H = nk.operator.Heisenberg(hi, g, J=1.0, sign_rule=True)
+    sampler = nk.sampler.MetropolisExchange(hi, graph=g, n_chains=LARGE["n_chains"])
+    vs = nk.vqs.MCState(sampler, nk.models.RBM(alpha=8), n_samples=LARGE["n_samples"],
+                        n_discard_per_chain=5, seed=seed, precision=precision)
+    drv = nk.driver.VMC_SR(H, nk.optimizer.Sgd(LARGE["lr"]), diag_shift=1e-4,
+                           variational_state=vs, use_ntk=True)
+    return H, vs, drv
 
 
 def build_problem(nk, precision, seed=0, n_chains=4096, n_samples=16384):
@@ -222,8 +251,12 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    H, vs, drv = build_problem(nk, args.precision, seed=rank, n_chains=args.n_chains,
-                               n_samples=args.n_samples)
+    large = args.workload == "large"
+    if large:
+        H, vs, drv = build_large(nk, args.precision, seed=rank)
+    else:
+        H, vs, drv = build_problem(nk, args.precision, seed=rank, n_chains=args.n_chains,
+                                   n_samples=args.n_samples)
     drv.advance(args.warmup)
     barrier()
     L = _native.lib()
@@ -243,7 +276,7 @@ def run_ours(args):
     ms = start.elapsed_time(stop) / args.steps
     ms_max = max_over_ranks(ms, dist, "cuda")
     value = replica_throughput(world, ms_max)
-    energy = st.mean / 100
+    energy = st.mean / vs.N
 
     # ---------------- end to end through the public API, host buffers
     P = vs.n_parameters
@@ -270,7 +303,9 @@ def run_ours(args):
 
     # ---------------- the plain FP32 GPU path (reference algorithm on the GPU)
     plain = None
-    if args.plain_steps > 0:
+    if large:
+        plain = {"skipped": "the dense FP32 Jacobian of this size (65536 x 526592) is 138 GB"}
+    elif args.plain_steps > 0:
         _, vs32, drv32 = build_problem(nk, "fp32", seed=rank, n_chains=args.n_chains,
                                        n_samples=args.n_samples)
         vs32.local_estimator = "dense"
@@ -305,7 +340,7 @@ def run_ours(args):
     if solve_ms:
         chol_flops = float(n) ** 3 / 3.0
         achieved = chol_flops / (solve_ms * 1e-3) / 1e12
-        if args.n_samples != WORKLOAD["n_samples"]:
+        if large or args.n_samples != WORKLOAD["n_samples"]:
             args.solve_traffic = None  # measured for the 16,384 case only
         roof = {"kernel": "minSR solve: Cholesky of T (chol_leaf_kernel + tcgen05 tc_gemm_kernel, "
                           "FP16 hi/lo split, 3 products) + iterative refinement (trsv, symv)",
@@ -322,12 +357,22 @@ def run_ours(args):
     gram_ms = phases.get("gram")
     roof_gram = None
     if gram_ms:
-        flops = float(n) * (n + 1) * 400  # lower triangle of t t^T (n x n x M), 2 flop per FMA
-        executed = float(n) * (n + 1) * 4 * 448  # hi*hi, hi*lo, lo*hi, lo*lo over K padded to 448
+        M = vs.M
+        flops = float(n) * (n + 1) * M  # lower triangle of t t^T (n x n x M), 2 flop per FMA
+        if M <= nk.ngd.TC_GRAM_MAX_M:
+            # hi*hi, hi*lo, lo*hi, lo*lo over K padded to a multiple of 64
+            executed = float(n) * (n + 1) * 4 * (-(-M // 64) * 64)
+            kname = "structured Gram T = O_L O_L^T (gram_tc_kernel, tcgen05, fused epilogue)"
+            traffic = args.gram_traffic if args.gram_traffic is not None else \
+                (73.9e6 + 346.2e6) * (n / 8192.0) ** 2
+        else:
+            # hi*hi, hi*lo, lo*hi, lo*lo over K padded to 64
+            executed = float(n) * (n + 1) * 4 * (-(-M // 64) * 64)
+            kname = ("structured Gram T = O_L O_L^T (tcgen05 tc_gemm_kernel, FP16 hi/lo, "
+                     "drained accumulation, + gram_assemble_kernel)")
+            traffic = args.gram_traffic
         achieved = flops / (gram_ms * 1e-3) / 1e12
-        traffic = args.gram_traffic if args.gram_traffic is not None else \
-            (73.9e6 + 346.2e6) * (n / 8192.0) ** 2
-        roof_gram = {"kernel": "structured Gram T = O_L O_L^T (gram_tc_kernel, tcgen05)",
+        roof_gram = {"kernel": kname,
                      "bound": "tensor", "achieved": round(achieved, 3),
                      "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": round(achieved / peaks["bf16_tflops"], 5), "traffic": traffic,
@@ -335,10 +380,12 @@ def run_ours(args):
                      "executed_tensor_tflops": round(executed / (gram_ms * 1e-3) / 1e12, 3),
                      "launch_ms": round(gram_ms, 4)}
     matched = None
-    if args.matched_steps > 0:
+    if large:
+        matched = {"skipped": "the all-FP64 arm at this size is measured by --precision fp64"}
+    elif args.matched_steps > 0:
         matched = matched_energy(nk, args.matched_steps, args.n_chains, args.n_samples, rank)
     cpu = None
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and not large:
         cpu = run_cpu_baseline()
     line = {
         "metric": METRIC, "value": round(value, 5), "unit": "steps/s", "n_gpus": world,
@@ -618,9 +665,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="minsr", choices=["minsr", "batched", "serving"],
+    ap.add_argument("--workload", default="minsr",
+                    choices=["minsr", "batched", "serving", "large"],
                     help="minsr: the 10x10 J1-J2 step (the metric); batched: 64 TFIM "
-                         "instances per step; serving: the request-stream sweep")
+                         "instances per step; serving: the request-stream sweep; large: the "
+                         "16x16 alpha-8 step with 65,536 samples")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     ap.add_argument("--plain-steps", type=int, default=4)
     ap.add_argument("--n-chains", type=int, default=WORKLOAD["n_chains"],

@@ -380,7 +380,7 @@ int vmck_rbm_jacobian(vmck_stream s, int32_t dtype, const void *tanh_theta,
  * mode 0: FP64 contraction (CUDA cores); 1: FP32 contraction (CUDA cores);
  * 2: tensor cores (tcgen05, TMA) on t rounded to hi + lo BF16 pairs (all four
  * products, FP32 accumulation); 3: tensor cores on t rounded to one BF16;
- * 4: tensor cores on t split into FP16 hi + lo (three products) with the FP32
+ * 4: tensor cores on t split into FP16 hi + lo (all four products) with the FP32
  * accumulators drained to registers every 64-wide slab (the accuracy of mode 2
  * at any M: the tensor cores' accumulation error grows with the chain length),
  * the exact terms added by a separate assembly pass.
@@ -425,6 +425,21 @@ int vmck_cholesky_solve_refined(vmck_ctx *ctx, vmck_stream s, const double *A64,
                                 float *A32, const double *b, double *x, int64_t n,
                                 int32_t max_iter, double tol, int32_t factor_mode,
                                 int32_t *status, double *residual_out);
+/* The solution of the FP64 Cholesky solve (netket/optimizer/solver/solvers.py
+ * cholesky, the minSR solve of netket/_src/ngd/srt.py:76-79) when the FP32
+ * factor of A fails (cond(A) beyond FP32): A + mu I is factored on the tensor
+ * cores, mu = shift_rel trace(A) (x16 per failed attempt, at most six), and
+ * preconditions flexible conjugate gradients against A64 (FP64 products) until
+ * ||b - A x|| <= tol ||b|| or max_iter iterations.  A32 (nullable: context
+ * workspace) is overwritten by the factor.  status (device) gets NOT_SPD when
+ * CG meets non-positive curvature (A not positive definite) or every factor
+ * failed, NO_CONVERGE when tol is not reached, NONFINITE.  residual_out
+ * (device, nullable) receives the final relative FP64 residual, *shift_out
+ * (host, nullable) the shift used.  Synchronises the stream. */
+int vmck_cholesky_solve_pcg(vmck_ctx *ctx, vmck_stream s, const double *A64,
+                            float *A32, const double *b, double *x, int64_t n,
+                            int32_t max_iter, double tol, double shift_rel,
+                            int32_t *status, double *residual_out, double *shift_out);
 /* pinv_smooth (solvers.py:33-139) via a symmetric eigendecomposition (FP64). */
 int vmck_pinv_smooth_solve(vmck_ctx *ctx, vmck_stream s, const double *A,
                            const double *b, double *x, int64_t n, double rtol,

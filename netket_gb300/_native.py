@@ -116,6 +116,8 @@ _SIGNATURES = {
     "vmck_cholesky_solve": ([c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp], c_i32),
     "vmck_cholesky_solve_refined": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i32, c_dbl,
                                      c_i32, c_vp, c_vp], c_i32),
+    "vmck_cholesky_solve_pcg": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i32, c_dbl, c_dbl,
+                                 c_vp, c_vp, c_vp], c_i32),
     "vmck_pinv_smooth_solve": ([c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_dbl, c_dbl], c_i32),
     "vmck_center_scale": ([c_vp, c_vp, c_vp, c_i64, c_dbl, c_vp], c_i32),
     "vmck_center_update": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_dbl, c_vp], c_i32),

@@ -120,7 +120,10 @@ __global__ void chol_split_rows_kernel(const float *__restrict__ A, int64_t n, i
 // 64-wide slab only (4 MMAs, region D1), and the epilogue adds each slab's sum
 // to its registers with round-to-nearest FP32 additions; the small cross terms
 // hi * lo + lo * hi (2^-11 of the sum) accumulate over the whole tile in region
-// D2.  The MMA thread issues a slab's cross terms first, so the epilogue drains
+// D2 (with lolo also lo * lo: the result is then the exact product of the split
+// operands up to FP32 summation, so a Gram matrix stays positive semidefinite;
+// without it the missing 2^-22 part is a positive semidefinite matrix taken
+// away).  The MMA thread issues a slab's cross terms first, so the epilogue drains
 // D1 of the previous slab meanwhile.  With beta != 0 the register sums start
 // from the old C values, loaded while the tile's first slab runs, so the
 // write-out only stores.  Waits for work are bounded by the library's wait limit; a wait that
@@ -145,6 +148,7 @@ struct GemmParams {
   float alpha, beta;
   const float *sa, *sb;
   int tri;
+  int lolo;  // also lo * lo (a Gram matrix of the split operand stays one)
   __half *oh, *ol;
   int64_t ldo;
   int o_rows, o_col0;
@@ -302,6 +306,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             umma_f16(d2, umma_desc_sw128(ah + off), umma_desc_sw128(bl + off), idesc,
                      (kb == 0 && k == 0) ? 0u : 1u);
             umma_f16(d2, umma_desc_sw128(al + off), umma_desc_sw128(bh + off), idesc, 1u);
+            if (g.lolo)
+              umma_f16(d2, umma_desc_sw128(al + off), umma_desc_sw128(bl + off), idesc, 1u);
           }
           // hi * hi of this slab into D1 once the epilogue has read the last slab
           if (slab > 0 && !mbar_wait(d1_empty, (uint32_t)((slab - 1) & 1), g.wait_ns)) {
@@ -732,28 +738,6 @@ static int make_f16_map(CUtensorMap *map, const __half *base, int64_t kdim, int6
 }
 
 
-__global__ void tc_split_rows_kernel(const float *__restrict__ src, int64_t rows, int K, int ldk,
-                                     float bound, __half *__restrict__ hi,
-                                     __half *__restrict__ lo, float *scale) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const float s = split_scale(bound);
-  if (e == 0) *scale = s;
-  if (e >= rows * ldk) return;
-  const int64_t r = e / ldk;
-  const int k = (int)(e - r * ldk);
-  __half h = __float2half_rn(0.0f), l = h;
-  if (k < K) split_f16(src[r * K + k], s, h, l);
-  hi[e] = h;
-  lo[e] = l;
-}
-
-int tc_split_rows(cudaStream_t st, const float *src, int64_t rows, int K, int ldk, float bound,
-                  __half *hi, __half *lo, float *scale) {
-  tc_split_rows_kernel<<<ceil_div(rows * ldk, 256), 256, 0, st>>>(src, rows, K, ldk, bound, hi,
-                                                                  lo, scale);
-  return check_launch("tc split rows");
-}
-
 static int num_sms_dev() {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
@@ -766,7 +750,7 @@ static size_t gemm_smem_bytes() { return 1024 + G_STAGES * G_STAGE_BYTES + 8 * 1
 int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOperand &b, int b_row0,
             int k_off, int M, int N, int K, float *C, int64_t ldc, float alpha, float beta,
             const float *sa, const float *sb, int tri, __half *oh, __half *ol, int64_t ldo,
-            int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas) {
+            int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas, int lolo) {
   if (M <= 0 || N <= 0 || K <= 0) return VMCK_OK;
   CUtensorMap mAh, mAl, mBh, mBl;
   int rc;
@@ -788,6 +772,7 @@ int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOpera
   g.sa = sa;
   g.sb = sb;
   g.tri = tri;
+  g.lolo = lolo;
   g.oh = oh;
   g.ol = ol;
   g.ldo = ldo;

@@ -26,16 +26,12 @@ struct SplitOperand {
 
 // C[m + nn ldc] = alpha (A_op B_op^T)(m, nn) / (sa sb) + beta C (tri: m <= nn
 // only) on the tensor cores (chol_tc.cu); optional split output of the result.
+// Products hi hi + hi lo + lo hi, and lo lo with lolo.
 int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOperand &b,
             int b_row0, int k_off, int M, int N, int K, float *C, int64_t ldc, float alpha,
             float beta, const float *sa, const float *sb, int tri, __half *oh, __half *ol,
-            int64_t ldo, int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas);
-
-// hi / lo[r * ldk + k] = split(src[r * K + k] * s) for k < K, zero for k in
-// [K, ldk), with s the power of two for `bound` (|src| <= bound), written to
-// *scale.  rows x K FP32 row-major input.
-int tc_split_rows(cudaStream_t st, const float *src, int64_t rows, int K, int ldk, float bound,
-                  __half *hi, __half *lo, float *scale);
+            int64_t ldo, int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas,
+            int lolo = 0);
 
 // Device workspace (bytes) of chol_tc_factor for an n x n matrix.
 int64_t chol_tc_workspace_bytes(int64_t n);

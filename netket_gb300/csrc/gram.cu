@@ -144,8 +144,9 @@ __global__ void __launch_bounds__(256) g_vector_df_kernel(const float *__restric
 }
 
 // Shift of the FP32 contraction: s0 = fp32(mean of t) from obar, and
-// c = round(t - s0) with terms = 0 (FP32), 1 (one BF16) or 2 (hi + lo BF16);
-// c is exactly what the contraction multiplies.  A = t t^T is then
+// c = round(t - s0) with terms = 0 (FP32), 1 (one BF16), 2 (hi + lo BF16) or
+// 3 (a multiple of 2^-19, the fixed-point grid of mode 4's split); c is exactly
+// what the contraction multiplies.  A = t t^T is then
 // c c^T + w 1^T + 1 w^T + |s0|^2 with w_s = c_s . s0, and only c c^T is
 // accumulated in FP32 -- its entries are small where hidden units are biased,
 // which keeps the centred T free of catastrophic cancellation.
@@ -159,6 +160,8 @@ __global__ void gram_shift_kernel(const float *__restrict__ t, const double *__r
   const float v = __fsub_rn(t[e], __double2float_rn(obar[j]));
   if (terms == 0) {
     c[e] = v;
+  } else if (terms == 3) {
+    c[e] = rintf(v * 524288.0f) * (1.0f / 524288.0f);  // |v| < 2: exact scalings
   } else {
     const float hi = __bfloat162float(__float2bfloat16(v));
     c[e] = (terms == 1) ? hi : __fadd_rn(hi, __bfloat162float(__float2bfloat16(__fsub_rn(v, hi))));
@@ -231,6 +234,36 @@ __device__ __forceinline__ df32 gram_value_df(float Ac, float2 ws, float2 wc, df
   v = df_mul(v, inv_n);
   if (diag) v = df_add(v, shift);
   return v;
+}
+
+// ---------------------------------------------------------------- fixed-point split (mode 4)
+// c (|c| < 2) -> hi + lo with u = c 2^8: hi = rint(u), an integer of at most
+// 512 in magnitude, and lo = rint((u - hi) 2^11) 2^-11, so c = (hi + lo) 2^-8 to
+// 2^-20 (exactly: the shift kernel has put c on the 2^-19 grid, so that the
+// shift terms w and g see the same c as the contraction).  Both are exact in FP16.  Every hi * hi product is an integer below
+// 2^18 and a 64-wide slab of them sums to an integer of at most 2^24: the
+// tensor core forms each slab's large part exactly, whatever its rounding, and
+// the only rounding of it is the round-to-nearest FP32 sum over slabs in
+// registers.  (A floating split leaves the tensor core's truncating alignment
+// in the slab sums, an error of ~2^-22 of the sum that is biased toward zero;
+// amplified by T's centring it pushed the smallest eigenvalue of T below
+// diag_shift 1e-4 at n = 65,536, M = 2048.)  The scale 2^8 goes to *scale.
+__global__ void gram_split_fixed_kernel(const float *__restrict__ c, int64_t n, int M, int ldk,
+                                        __half *__restrict__ hi, __half *__restrict__ lo,
+                                        float *scale) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e == 0) *scale = 256.0f;
+  if (e >= n * ldk) return;
+  const int64_t r = e / ldk;
+  const int k = (int)(e - r * ldk);
+  float h = 0.0f, l = 0.0f;
+  if (k < M) {
+    const float u = c[r * M + k] * 256.0f;  // exact: a power-of-two scaling
+    h = rintf(u);
+    l = rintf((u - h) * 2048.0f) * (1.0f / 2048.0f);  // u - h is exact (Sterbenz)
+  }
+  hi[e] = __float2half_rn(h);
+  lo[e] = __float2half_rn(l);
 }
 
 // ---------------------------------------------------------------- assembly (mode 4)
@@ -428,7 +461,7 @@ extern "C" int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t
     g_vector_kernel<double><<<gblocks, 256, 0, st>>>(static_cast<const double *>(tanh_theta), x,
                                                      N, M, n, obar, w.g);
   } else {
-    const int terms = mode == 2 ? 2 : (mode == 3 ? 1 : 0);
+    const int terms = mode == 2 ? 2 : (mode == 3 ? 1 : (mode == 4 ? 3 : 0));
     gram_shift_kernel<<<ceil_div(n * (int64_t)M, 256), 256, 0, st>>>(
         static_cast<const float *>(tanh_theta), obar, n, M, terms, w.c, w.s0);
     if ((rc = check_launch("gram shift"))) return rc;
@@ -447,17 +480,20 @@ extern "C" int vmck_rbm_gram(vmck_ctx *ctx, vmck_stream s, int32_t mode, int32_t
   if (mode == 4) {
     VMCK_REQUIRE(n < (int64_t)INT32_MAX && (n + GA_ROWS - 1) / GA_ROWS <= 65535,
                  "rbm_gram mode 4: too many samples");
-    // c c^T on the tensor cores: c = t - s0 (|c| <= 2) split into FP16 hi / lo,
-    // the triangular split GEMM into T32, then the double-float assembly
+    // c c^T on the tensor cores: c = t - s0 (|c| < 2) split into fixed-point
+    // FP16 hi / lo, the triangular split GEMM (all four products: the Gram
+    // matrix of hi + lo) into T32, then the double-float assembly
     const int ldk = (M + 7) & ~7;
     __half *hi = reinterpret_cast<__half *>(
         (reinterpret_cast<uintptr_t>(w.tc) + 1023) & ~uintptr_t(1023));
     __half *lo = hi + ((n * ldk + 511) & ~int64_t(511));
     float *scale = reinterpret_cast<float *>(lo + ((n * ldk + 511) & ~int64_t(511)));
-    if ((rc = tc_split_rows(st, w.c, n, M, ldk, 2.0f, hi, lo, scale))) return rc;
+    gram_split_fixed_kernel<<<ceil_div(n * ldk, 256), 256, 0, st>>>(w.c, n, M, ldk, hi, lo,
+                                                                     scale);
+    if ((rc = check_launch("gram split"))) return rc;
     const SplitOperand op{hi, lo, ldk, M, n};
     if ((rc = tc_gemm(st, op, 0, op, 0, 0, (int)n, (int)n, M, T32, n, 1.0f, 0.0f, scale, scale,
-                      1, nullptr, nullptr, 0, 0, 0, nullptr, status, 0)))
+                      1, nullptr, nullptr, 0, 0, 0, nullptr, status, 0, 1)))
       return rc;
     const df32 shift = {(float)diag_shift, (float)(diag_shift - (double)(float)diag_shift)};
     gram_assemble_kernel<<<dim3((unsigned)((n + 255) / 256),

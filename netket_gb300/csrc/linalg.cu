@@ -42,6 +42,8 @@ struct vmck_ctx {
   // the padded copy when n is not a multiple of 4
   void *tcws = nullptr;
   size_t tcws_bytes = 0;
+  // the shifted-preconditioner fallback: per-attempt status word
+  int32_t *d_attempt = nullptr;
 };
 
 namespace vmck {
@@ -195,6 +197,112 @@ __global__ void refine_check_kernel(const double *nr, const double *nb, const in
     else if (!(rel <= tol)) s |= VMCK_DEV_NO_CONVERGE;
     if (s) atomicOr(status, s);
   }
+}
+
+// ---- flexible preconditioned CG (the fallback of a failed FP32 factor)
+// One block: fixed reduction order, so the iteration is deterministic.
+__device__ __forceinline__ double block_sum_1024(double v, double *red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+  return t;  // valid in thread 0
+}
+
+// sc: [0] r.z, [1] alpha, [2] beta
+__global__ void __launch_bounds__(1024) pcg_start_kernel(const double *__restrict__ r,
+                                                         const double *__restrict__ z,
+                                                         int64_t n, double *sc) {
+  __shared__ double red[32];
+  double a = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) a = fma(r[i], z[i], a);
+  a = block_sum_1024(a, red);
+  if (threadIdx.x == 0) sc[0] = a;
+}
+
+// alpha = r.z / p.A p with qn = -A p; a direction of non-positive curvature
+// (A not positive definite) or a non-finite value ends the iteration.
+__global__ void __launch_bounds__(1024) pcg_alpha_kernel(const double *__restrict__ p,
+                                                         const double *__restrict__ qn,
+                                                         int64_t n, double *sc, int32_t *status,
+                                                         int *done) {
+  if (refine_done(done)) return;
+  __shared__ double red[32];
+  double a = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) a = fma(p[i], qn[i], a);
+  a = block_sum_1024(a, red);
+  if (threadIdx.x == 0) {
+    const double pq = -a;
+    const double alpha = sc[0] / pq;
+    if (!(pq > 0.0) || !isfinite(alpha)) {
+      atomicOr(status, isfinite(pq) ? VMCK_DEV_NOT_SPD : VMCK_DEV_NONFINITE);
+      *done = 1;
+    }
+    sc[1] = alpha;
+  }
+}
+
+__global__ void pcg_update_kernel(double *__restrict__ x, double *__restrict__ r,
+                                  const double *__restrict__ p, const double *__restrict__ qn,
+                                  int64_t n, const double *sc, const int *done) {
+  if (refine_done(done)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double alpha = sc[1];
+  x[i] = fma(alpha, p[i], x[i]);
+  r[i] = fma(alpha, qn[i], r[i]);  // r - alpha A p
+}
+
+__global__ void f2d_copy_kernel(const float *__restrict__ in, double *__restrict__ out, int64_t n,
+                                const int *done) {
+  if (refine_done(done)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+
+// Polak-Ribiere beta = z.(r - r_old) / (r_old.z_old), r - r_old = alpha qn:
+// stays a conjugate-gradient step when the FP32 preconditioner is not exactly
+// the same linear map from one application to the next.
+__global__ void __launch_bounds__(1024) pcg_beta_kernel(const double *__restrict__ r,
+                                                        const double *__restrict__ z,
+                                                        const double *__restrict__ qn,
+                                                        int64_t n, double *sc, const int *done) {
+  if (refine_done(done)) return;
+  __shared__ double red[32];
+  double a = 0.0, b = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    a = fma(r[i], z[i], a);
+    b = fma(z[i], qn[i], b);
+  }
+  a = block_sum_1024(a, red);
+  b = block_sum_1024(b, red);
+  if (threadIdx.x == 0) {
+    sc[2] = sc[1] * b / sc[0];
+    sc[0] = a;
+  }
+}
+
+__global__ void pcg_direction_kernel(double *__restrict__ p, const double *__restrict__ z,
+                                     int64_t n, const double *sc, const int *done) {
+  if (refine_done(done)) return;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = fma(sc[2], p[i], z[i]);
+}
+
+__global__ void status_or_kernel(int32_t *status, const int32_t *bits) {
+  if (*bits) atomicOr(status, *bits);
+}
+
+__global__ void trace_kernel(const double *__restrict__ A, int64_t n, double *out) {
+  __shared__ double red[32];
+  double a = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) a += A[i * n + i];
+  a = block_sum_1024(a, red);
+  if (threadIdx.x == 0) *out = a;
 }
 
 __global__ void pinv_filter_kernel(const double *w, double *y, int64_t n, double rtol,
@@ -1295,6 +1403,7 @@ extern "C" int vmck_ctx_destroy(vmck_ctx *c) {
   cudaFree(c->dwork);
   cudaFree(c->aux);
   cudaFree(c->tcws);
+  cudaFree(c->d_attempt);
   cudaFree(c->d_info);
   free(c->hwork);
   delete c;
@@ -1322,6 +1431,8 @@ struct RefineOpts {
   int factor_mode;
   bool exact;        // FP64 residual (else double-float, ~2^-46 per term)
   bool stagnation;   // also stop when the residual stops falling
+  bool pcg = false;  // flexible PCG with the factor as preconditioner (factor_mode 4)
+  bool *factor_failed = nullptr;  // pcg: set when the factor failed (no iteration ran)
 };
 
 // FP32 factor of A32 (overwritten) + iterative refinement against A64.
@@ -1362,7 +1473,10 @@ static int refined_solve(vmck_ctx *c, cudaStream_t st, const double *A64, float 
       ~size_t(255);
   const size_t sync_off = (y32_off + (own_trsv ? (size_t)np * 4 : 0) + 255) & ~size_t(255);
   const size_t dinv_off = (sync_off + (own_trsv ? (size_t)(2 * nb + 4) * 4 : 0) + 255) & ~size_t(255);
-  const size_t need = dinv_off + (factor_mode == 3 ? (size_t)nb * 4096 * 4 : 0);
+  const size_t pcg_off = (dinv_off + (factor_mode == 3 ? (size_t)nb * 4096 * 4 : 0) + 255) &
+                        ~size_t(255);
+  const size_t vec_bytes = ((size_t)n * 8 + 255) & ~size_t(255);
+  const size_t need = pcg_off + (o.pcg ? 4 * vec_bytes + 256 : 0);
   if ((rc = grow(&c->aux, &c->aux_bytes, need, st))) return rc;
   char *aux = static_cast<char *>(c->aux);
   double *r = static_cast<double *>(c->aux);
@@ -1441,6 +1555,87 @@ static int refined_solve(vmck_ctx *c, cudaStream_t st, const double *A64, float 
     }
     info_accumulate_kernel<<<1, 1, 0, st>>>(c->d_info, status);
     if ((rc = check_launch("refined solve info"))) return rc;
+  }
+  if (o.pcg) {
+    VMCK_REQUIRE(own_trsv, "the PCG fallback runs on the tensor-core factor (factor_mode 4)");
+    // a failed factor is reported before any iteration: the caller retries with
+    // a larger shift
+    int32_t fstat = 0;
+    VMCK_CUDA(cudaMemcpyAsync(&fstat, status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    VMCK_CUDA(cudaStreamSynchronize(st));
+    if (fstat & (VMCK_DEV_NOT_SPD | VMCK_DEV_NONFINITE | VMCK_DEV_TIMEOUT)) {
+      if (o.factor_failed) *o.factor_failed = !(fstat & VMCK_DEV_TIMEOUT);
+      return VMCK_OK;
+    }
+    double *z = reinterpret_cast<double *>(aux + pcg_off);
+    double *p = reinterpret_cast<double *>(aux + pcg_off + vec_bytes);
+    double *qn = reinterpret_cast<double *>(aux + pcg_off + 2 * vec_bytes);
+    double *zero = reinterpret_cast<double *>(aux + pcg_off + 3 * vec_bytes);
+    double *sc = reinterpret_cast<double *>(aux + pcg_off + 4 * vec_bytes);
+    const int blocks = ceil_div(n, 256);
+    const unsigned grid = (unsigned)std::min<int64_t>(nb, 2 * (int64_t)num_sms());
+    VMCK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
+    VMCK_CUDA(cudaMemsetAsync(zero, 0, (size_t)n * 8, st));
+    VMCK_CUDA(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    refine_init_kernel<<<1, 32, 0, st>>>(norms, prev, done);
+    if ((rc = check_launch("pcg init"))) return rc;
+    if (np != n) VMCK_CUDA(cudaMemsetAsync(r32, 0, (size_t)np * 4, st));
+    unsigned epoch = 0;
+    // z = M^-1 r: the two triangular solves on the factor of A32
+    auto precondition = [&]() -> int {
+      int e;
+      d2f_kernel<<<blocks, 256, 0, st>>>(r, r32, n, done);
+      if ((e = check_launch("pcg cast"))) return e;
+      ++epoch;
+      VMCK_CUDA(cudaMemsetAsync(sync + 2 * nb, 0, 2 * sizeof(unsigned), st));  // tickets
+      trsv_fwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(F, np, yinv, r32, y32, sync_f, epoch,
+                                                     status, done);
+      if ((e = check_launch("pcg forward"))) return e;
+      trsv_bwd_kernel<<<grid, LEAF_THREADS, 0, st>>>(F, np, yinv, y32, r32, sync_b, epoch,
+                                                     status, done);
+      if ((e = check_launch("pcg backward"))) return e;
+      f2d_copy_kernel<<<blocks, 256, 0, st>>>(r32, z, n, done);
+      return check_launch("pcg z");
+    };
+    if ((rc = precondition())) return rc;
+    VMCK_CUDA(cudaMemcpyAsync(p, z, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    pcg_start_kernel<<<1, 1024, 0, st>>>(r, z, n, sc);
+    if ((rc = check_launch("pcg start"))) return rc;
+    for (int it = 0; it < o.max_iter; ++it) {
+      if ((rc = symv_residual(st, A64, n, p, zero, qn, sws, done, o.exact))) return rc;
+      pcg_alpha_kernel<<<1, 1024, 0, st>>>(p, qn, n, sc, status, done);
+      if ((rc = check_launch("pcg alpha"))) return rc;
+      pcg_update_kernel<<<blocks, 256, 0, st>>>(x, r, p, qn, n, sc, done);
+      if ((rc = check_launch("pcg update"))) return rc;
+      // every 32nd iteration the recursive residual is replaced by the true
+      // b - A x (FP64 rounding makes them drift apart), and the loop also stops
+      // once that has not halved since the last replacement: its FP64 floor
+      // ~eps ||A|| ||x||
+      const bool replace = (it & 31) == 31;
+      if (replace && (rc = symv_residual(st, A64, n, x, b, r, sws, done, o.exact))) return rc;
+      refine_converged_kernel<<<1, 256, 0, st>>>(r, b, n, o.stop_tol, done,
+                                                 replace ? prev : nullptr);
+      if ((rc = check_launch("pcg convergence"))) return rc;
+      if ((rc = precondition())) return rc;
+      pcg_beta_kernel<<<1, 1024, 0, st>>>(r, z, qn, n, sc, done);
+      if ((rc = check_launch("pcg beta"))) return rc;
+      pcg_direction_kernel<<<blocks, 256, 0, st>>>(p, z, n, sc, done);
+      if ((rc = check_launch("pcg direction"))) return rc;
+      if ((it & 31) == 31) {  // stop enqueueing once the device has converged
+        int h_done = 0;
+        VMCK_CUDA(cudaMemcpyAsync(&h_done, done, sizeof(int), cudaMemcpyDeviceToHost, st));
+        VMCK_CUDA(cudaStreamSynchronize(st));
+        if (h_done) break;
+      }
+    }
+    // the true residual b - A x (the recursive one drifts)
+    VMCK_CUDA(cudaMemsetAsync(done, 0, sizeof(int), st));
+    if ((rc = symv_residual(st, A64, n, x, b, r, sws, done, o.exact))) return rc;
+    norms_kernel<<<1, 256, 0, st>>>(r, b, n, norms);
+    if ((rc = check_launch("pcg norms"))) return rc;
+    refine_check_kernel<<<1, 1, 0, st>>>(norms, norms + 1, c->d_info, o.fail_tol, status,
+                                         residual_out);
+    return check_launch("pcg check");
   }
   VMCK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, st));
   refine_init_kernel<<<1, 32, 0, st>>>(norms, prev, done);  // norms 0, prev huge, done 0
@@ -1553,6 +1748,62 @@ extern "C" int vmck_cholesky_solve_refined(vmck_ctx *c, vmck_stream s, const dou
   VMCK_REQUIRE(n < (1ll << 30), "refined solve size");
   const RefineOpts o{max_iter, tol, tol, factor_mode, false, false};
   return refined_solve(c, as_stream(s), A64, A32, b, x, n, o, status, residual_out);
+}
+
+extern "C" int vmck_cholesky_solve_pcg(vmck_ctx *c, vmck_stream s, const double *A64,
+                                       float *A32, const double *b, double *x, int64_t n,
+                                       int32_t max_iter, double tol, double shift_rel,
+                                       int32_t *status, double *residual_out,
+                                       double *shift_out) {
+  VMCK_REQUIRE(c && A64 && b && x && status && n > 0 && max_iter >= 1 && shift_rel > 0.0,
+               "pcg solve arguments");
+  VMCK_REQUIRE(n < (1ll << 30), "pcg solve size");
+  cudaStream_t st = as_stream(s);
+  int rc;
+  float *F = A32;
+  if (!F) {
+    const size_t fbytes = ((size_t)n * n * 4 + 255) & ~size_t(255);
+    if ((rc = grow(&c->dwork, &c->dwork_bytes, fbytes, st))) return rc;
+    F = static_cast<float *>(c->dwork);
+  }
+  if (!c->d_attempt && cudaMalloc(&c->d_attempt, 16) != cudaSuccess) {
+    set_last_error("pcg solve: status word allocation failed");
+    return VMCK_ERR_NOMEM;
+  }
+  double *d_trace = reinterpret_cast<double *>(c->d_attempt + 2);
+  trace_kernel<<<1, 1024, 0, st>>>(A64, n, d_trace);
+  if ((rc = check_launch("pcg trace"))) return rc;
+  double trace = 0.0;
+  VMCK_CUDA(cudaMemcpyAsync(&trace, d_trace, sizeof(double), cudaMemcpyDeviceToHost, st));
+  VMCK_CUDA(cudaStreamSynchronize(st));
+  if (!(std::isfinite(trace) && trace > 0.0)) {  // not SPD, or not finite: no attempt
+    const int32_t bits = std::isfinite(trace) ? VMCK_DEV_NOT_SPD : VMCK_DEV_NONFINITE;
+    VMCK_CUDA(cudaMemcpyAsync(c->d_attempt, &bits, sizeof(bits), cudaMemcpyHostToDevice, st));
+    VMCK_CUDA(cudaStreamSynchronize(st));
+    status_or_kernel<<<1, 1, 0, st>>>(status, c->d_attempt);
+    return check_launch("pcg status");
+  }
+  double mu = shift_rel * trace;
+  RefineOpts o{max_iter, tol, tol, 4, true, false};
+  o.pcg = true;
+  bool failed = false;
+  o.factor_failed = &failed;
+  for (int attempt = 0; attempt < 6; ++attempt, mu *= 16.0) {
+    failed = false;
+    lower_f64_to_f32_kernel<<<ceil_div(n * n, 256), 256, 0, st>>>(A64, F, n);
+    if ((rc = check_launch("pcg cast"))) return rc;
+    add_diag_kernel<<<ceil_div(n, 256), 256, 0, st>>>(F, VMCK_F32, n, mu);
+    if ((rc = check_launch("pcg shift"))) return rc;
+    VMCK_CUDA(cudaMemsetAsync(c->d_attempt, 0, sizeof(int32_t), st));
+    if ((rc = refined_solve(c, st, A64, F, b, x, n, o, c->d_attempt, residual_out))) return rc;
+    // the factor of A + mu I failed (mu below its rounding error): a larger
+    // shift.  (CG meeting non-positive curvature -- A itself not positive
+    // definite -- also reports NOT_SPD, after a successful factor: no retry.)
+    if (!(failed && attempt < 5)) break;
+  }
+  if (shift_out) *shift_out = mu;
+  status_or_kernel<<<1, 1, 0, st>>>(status, c->d_attempt);
+  return check_launch("pcg status");
 }
 
 extern "C" int vmck_pinv_smooth_solve(vmck_ctx *c, vmck_stream s, const double *A, const double *b,

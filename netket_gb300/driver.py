@@ -316,10 +316,13 @@ class VMC_SR(AbstractVariationalDriver):
             if self.solve == "cholesky":
                 bad |= DEV_NO_CONVERGE  # the FP64 solve's refinement did not converge
             failed = bool(status & bad)
-            if self._solver == "pinv_smooth" or (self._solver == "fallback" and failed):
-                dp = minsr_fallback(self.info)
-            elif self._solver == "cholesky" and failed:
-                dp = torch.full_like(dp, float("nan"))  # a failed cho_factor gives NaN
+            if self._solver == "pinv_smooth":
+                dp = minsr_fallback(self.info, try_pcg=False)
+            elif failed:
+                # the FP32 factor failed: the FP64 solution by shifted-factor PCG,
+                # else pinv_smooth (fallback) or NaN (a failed cho_factor)
+                fb = minsr_fallback(self.info, pinv=self._solver == "fallback")
+                dp = fb if fb is not None else torch.full_like(dp, float("nan"))
             stats = Stats.from_array(host[:5].numpy())
             if mom is not None:
                 dp = dp + mom * old  # SPRING (netket/_src/ngd/srt.py:79-82)

@@ -146,7 +146,7 @@ def jacobian_dense(tanh_t, x, N, M, col_mean, scale, out_dtype):
 def gram_structured(tanh_t, x, N, M, obar, diag_shift, mode, want_f32=False, status=None):
     """Lower triangle of T = O_L O_L^T + diag_shift I (n, n) FP64 (+ FP32 copy).
     mode 0: FP64 CUDA cores; 1: FP32 CUDA cores; 2: tcgen05 BF16 hi/lo split;
-    3: tcgen05 single BF16; 4: tcgen05 FP16 hi/lo split with per-slab drained
+    3: tcgen05 single BF16; 4: tcgen05 FP16 hi/lo split (four products) with per-slab drained
     accumulation (the blocked-Cholesky GEMM) and a double-float assembly pass."""
     n = x.shape[0]
     T64 = torch.empty((n, n), dtype=torch.float64, device=x.device)
@@ -195,6 +195,22 @@ def cholesky_solve_refined(A64, A32, b, status, max_iter=3, tol=1e-10, factor_mo
                                                     int(factor_mode), nat.ptr(status),
                                                     nat.ptr(res)))
     return x, res
+
+
+def cholesky_solve_pcg(A64, b, status, max_iter=2000, tol=1e-10, shift_rel=1e-7, A32=None):
+    """Solution of A64 x = b (A64 SPD, lower triangle set) when its FP32 factor
+    fails: the tensor-core factor of A + mu I (mu = shift_rel trace(A), x16 per
+    failed attempt) preconditions flexible CG with FP64 products of A64.
+    Returns (x, relative residual (device), mu).  A32 (optional, n x n FP32) is
+    used as the factor's storage.  Synchronises the stream."""
+    x = torch.empty_like(b)
+    res = torch.zeros(1, dtype=torch.float64, device=b.device)
+    mu = ctypes.c_double(0.0)
+    nat.check(nat.lib().vmck_cholesky_solve_pcg(
+        nat.ctx(), nat.stream(), nat.ptr(A64), nat.ptr(A32) if A32 is not None else None,
+        nat.ptr(b), nat.ptr(x), A64.shape[0], int(max_iter), float(tol), float(shift_rel),
+        nat.ptr(status), nat.ptr(res), ctypes.byref(mu)))
+    return x, res, mu.value
 
 
 def pinv_smooth_solve(A, b, rtol=1e-14, rtol_smooth=1e-14):

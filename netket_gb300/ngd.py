@@ -19,7 +19,8 @@ Two ways to form T:
     the all-FP64 one, mode 1 within 2.5e-4, mode 3 within 2.4e-2.  The tensor
     cores' FP32 accumulation loses bits in proportion to the MMA chain length, so
     at M = 2048 (16 x 16, alpha 8) mode 2's T is no longer positive definite;
-    above ``TC_GRAM_MAX_M`` the default is mode 4, FP16 hi/lo operands whose
+    above ``TC_GRAM_MAX_M`` the default is mode 4, FP16 hi/lo operands (all four
+    products, so T stays the Gram matrix of hi + lo) whose
     accumulators are drained into FP32 registers every 64 columns of K (the
     factorisation's trailing-update GEMM) followed by the double-float assembly;
   * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
@@ -72,7 +73,8 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     dtype, ``e`` = local energies (n,) FP64, ``mean_dev`` = their mean (device).
 
     With ``check=False`` the device status is not read here: ``info["status_dev"]``
-    holds it and ``minsr_fallback(info)`` recomputes delta with pinv_smooth if the
+    holds it and ``minsr_fallback(info)`` recomputes delta (shifted-factor PCG,
+    then pinv_smooth) if the
     caller finds a failed factorisation (one host read per step).
 
     SPRING (``netket/_src/ngd/srt.py:34-35, 63-66``): ``proj_reg`` adds
@@ -137,6 +139,9 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     if ph:
         ph.mark("solve")
     info["_fallback_args"] = (t, x, N, M, obar, dv, Tfb, s, rtol, rtol_smooth)
+    if gram == "structured":
+        # the FP64 system of a failed FP32 factor: shifted-factor PCG first
+        info["_pcg"] = (T32, refine_tol if solve == "refined" else 1e-10)
     if check:
         st = int(status.item())
         info["status"] = st
@@ -150,9 +155,29 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
     return delta, info
 
 
-def minsr_fallback(info):
-    """delta from pinv_smooth on the same T (``cholesky_with_fallback``)."""
+def minsr_fallback(info, try_pcg=True, pinv=True):
+    """delta after a failed solve (``try_pcg=False``: pinv_smooth directly;
+    ``pinv=False``: None where pinv_smooth would be the answer).  The FP64 Cholesky of the reference solves T
+    up to cond(T) ~ 1e15; the FP32 factor here stops near 1e7.  So a failed
+    factor of a finite, structured T is first retried as shifted-factor PCG
+    against the FP64 T (``kernels.cholesky_solve_pcg``: the FP64 solution);
+    only if that fails too -- T not positive definite, or not finite -- does it
+    switch to pinv_smooth as ``cholesky_with_fallback`` does
+    (``netket/optimizer/solver/solvers.py:305-340``)."""
     t, x, N, M, obar, dv, T, s, rtol, rtol_smooth = info["_fallback_args"]
+    # (a failed pivot also reads as non-finite: the PCG itself reports a T that is)
+    if try_pcg and "_pcg" in info and T.dtype == torch.float64:
+        T32, tol = info["_pcg"]
+        pst = _status()
+        aux, res, mu = K.cholesky_solve_pcg(T, dv, pst, tol=tol, A32=T32)
+        pst = int(pst.item())
+        info["pcg"] = {"status": pst, "shift": mu, "residual": float(res.item())}
+        if pst == 0:
+            info["aux"] = aux
+            raw = K.ot_v(t, x, N, M, aux)
+            return K.center_update(raw, obar, aux, s)
+    if not pinv:
+        return None
     A = T.to(torch.float64)
     A = torch.tril(A) + torch.tril(A, -1).T
     aux = K.pinv_smooth_solve(A.contiguous(), dv, rtol, rtol_smooth)

@@ -94,6 +94,8 @@ def _jacobian_from_t(t, x):
 def _round_terms(v, terms):
     if terms == 0:
         return v
+    if terms == 3:  # mode 4: the 2^-19 fixed-point grid
+        return torch.round(v * 524288.0) / 524288.0
     hi = v.to(torch.bfloat16).float()
     return hi if terms == 1 else hi + (v - hi).to(torch.bfloat16).float()
 
@@ -102,8 +104,8 @@ def _round_terms(v, terms):
 def test_fp32_and_tensor_core_gram(nk, N, alpha, n):
     """FP32 Gram modes contract c = round(t - s0) (s0 = fp32 column mean of t;
     mode 1 FP32, mode 2 hi + lo BF16 pairs on tcgen05, mode 3 one BF16 on
-    tcgen05, mode 4 FP16 hi + lo with per-slab drained accumulation and a
-    separate assembly pass) and add the shift back exactly: T equals the FP64 Gram of the
+    tcgen05, mode 4 rounded to 2^-19 and split into fixed-point FP16 hi + lo
+    whose slab sums are exact) and add the shift back exactly: T equals the FP64 Gram of the
     Jacobian of t_eff = c + s0 centred at the given obar, to FP32 accumulation
     accuracy, and is positive definite."""
     model, flat, M, x, t, p = _problem(nk, N, alpha, n)
@@ -113,7 +115,7 @@ def test_fp32_and_tensor_core_gram(nk, N, alpha, n):
     obar = nk.kernels.column_means(t, x, N, M)
     s0 = obar[:M].float()
     ob = obar.cpu().numpy()
-    for mode, terms in ((1, 0), (2, 2), (3, 1), (4, 0)):
+    for mode, terms in ((1, 0), (2, 2), (3, 1), (4, 3)):
         teff = (_round_terms(t32 - s0, terms).double() + s0.double()).cpu().numpy()
         O = (_jacobian_from_t(teff, xs) - ob) / math.sqrt(n)
         ref = O @ O.T + 1e-3 * np.eye(n)
@@ -144,7 +146,8 @@ def _structured_gram_f64(teff, xs, ob, n, shift):
 @pytest.mark.parametrize("N,alpha,n", [(256, 8, 2048), (64, 10, 1500)])
 def test_tensor_core_gram_large_m(nk, N, alpha, n):
     """M > 512 (the 16 x 16, alpha 8 model's M = 2048): the default mode 4 Gram
-    equals the FP64 Gram of t_eff = fp32(t - s0) + s0 to 2e-6 of its largest
+    equals the FP64 Gram of t_eff = c + s0, c = fp32(t - s0) rounded to a
+    multiple of 2^-19, to 2e-6 of its largest
     entry and is positive definite at diag_shift 1e-4 with the model's default
     N(0, 0.01) initialisation; it is the mode minsr_update picks there."""
     model, flat, M, x, t, p = _problem(nk, N, alpha, n, std=0.01)
@@ -155,7 +158,7 @@ def test_tensor_core_gram_large_m(nk, N, alpha, n):
     obar = nk.kernels.column_means(t, x, N, M)
     s0 = obar[:M].float()
     ob = obar.cpu().numpy()
-    teff = ((t32 - s0).double() + s0.double()).cpu().numpy()
+    teff = (_round_terms(t32 - s0, 3).double() + s0.double()).cpu().numpy()
     ref = _structured_gram_f64(teff, xs, ob, n, 1e-4)
     scale = np.abs(ref).max()
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -229,6 +232,64 @@ def test_refined_solve_flags_non_spd(nk, mode):
     nk.kernels.cholesky_solve_refined(At, At.float().contiguous(), torch.ones(n, device="cuda",
                                       dtype=torch.float64), st, max_iter=2, factor_mode=mode)
     assert st.item() & nk._native.DEV_NOT_SPD
+
+
+def _ill_conditioned(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    d = np.logspace(np.log10(hi), np.log10(lo), n)
+    return (Q * d) @ Q.T, rng.normal(size=n)
+
+
+@pytest.mark.parametrize("n", [1000, 1536])
+def test_pcg_solves_beyond_the_fp32_factor(nk, n):
+    """cond(A) = 1e8: the FP32 factor (and its refinement) cannot solve A, the
+    FP64 Cholesky of the reference can; the shifted-factor PCG reaches an FP64
+    residual of 1e-8 ||b|| (FP64's own floor eps ||A|| ||x|| is ~2e-9 ||b||
+    here) and the FP64 solution to 1e-6 (n = 1000 also runs the padded factor)."""
+    A, b = _ill_conditioned(n, 1e-6, 1e2, seed=n)
+    At = torch.as_tensor(np.tril(A), device="cuda")
+    bt = torch.as_tensor(b, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nk.kernels.cholesky_solve_refined(At, At.float().contiguous(), bt, st, max_iter=8,
+                                      tol=1e-8)
+    assert st.item() != 0  # the mixed solve does not get there
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    x, res, mu = nk.kernels.cholesky_solve_pcg(At, bt, st, tol=1e-8)
+    assert st.item() == 0, (st.item(), res.item(), mu)
+    assert mu > 0
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(A @ xs - b) <= 2e-8 * np.linalg.norm(b)
+    assert res.item() <= 1e-8
+    ref = np.linalg.solve(A, b)
+    assert np.linalg.norm(xs - ref) <= 1e-6 * np.linalg.norm(ref)
+
+
+def test_minsr_falls_back_to_pcg(nk):
+    """Repeated samples (an exactly singular O_L O_L^T) and diag_shift = ||T|| / 1e8:
+    the FP32 factor of T fails; minsr_update (refined solve, FP64 T) then solves
+    T by shifted-factor PCG -- not pinv_smooth -- to its refine_tol of 1e-7 (the
+    FP64 floor eps cond(T) is ~1e-8)."""
+    N, n = 16, 512
+    model, flat, M, x, t, p = _problem(nk, N, 2, 64, seed=9)
+    x = x.repeat(8, 1)
+    _, _, t = nk.kernels.rbm_forward(flat, x, N, M, want_tanh=True)
+    g = nk.graph.Chain(N)
+    H = nk.operator.Heisenberg(nk.hilbert.Spin(0.5, N), g)
+    e = nk.kernels.local_energies_fused(H, flat, x, N, M)
+    obar = nk.kernels.column_means(t, x, N, M)
+    T0, _ = nk.kernels.gram_structured(t, x, N, M, obar, 0.0, 0)
+    T0 = torch.tril(T0) + torch.tril(T0, -1).T
+    shift = float(torch.linalg.eigvalsh(T0)[-1]) / 1e8
+    dp, info = nk.ngd.minsr_update(t, x, N, M, e, e.mean().reshape(1), shift, solve="refined",
+                                   refine_tol=1e-7)
+    assert info["status"] != 0
+    assert info["pcg"]["status"] == 0 and not info["solver_fallback"], info["pcg"]
+    T = (T0 + shift * torch.eye(n, dtype=torch.float64, device="cuda")).cpu().numpy()
+    dv = (2 * (e - e.mean()) / math.sqrt(n)).cpu().numpy()
+    aux = info["aux"].cpu().numpy()
+    assert np.linalg.norm(T @ aux - dv) <= 2e-7 * np.linalg.norm(dv)
+    assert np.all(np.isfinite(dp.cpu().numpy()))
 
 
 @pytest.mark.parametrize("name", ["minsr", "sr", "minsr_big_shift"])
