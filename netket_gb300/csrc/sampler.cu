@@ -501,6 +501,250 @@ __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem
   }
 }
 
+// ------------------------------------------------------------ Exchange, W in L2
+// The same chain for hidden layers too wide for shared-memory weights (N M >
+// ~48 K): W, b, a are read through L2 (2 MB for N = 256, M = 2048), theta lives
+// in registers (lane l holds units l + 32 r, r < R) and log_cosh(theta) in the
+// warp's shared memory; an accepted move recomputes theta' and its log_cosh
+// (the same expressions, so the same bits) instead of keeping the proposal.
+// That holds a chain in ~8 KB of shared memory and ~R + 40 registers per lane:
+// 16 chains per SM at M = 2048, where metropolis_kernel's four M-vectors in
+// shared memory leave 4.  Warps loop over chains (b += gridDim.x wpb).  Random
+// stream, proposal order and every floating-point expression match
+// metropolis_kernel<float, 1>, so the samples are identical.
+constexpr int XL_WARPS = 16;
+
+template <int R>
+__global__ void __launch_bounds__(32 * XL_WARPS, 1) metropolis_exchange_l2_kernel(
+    const float *__restrict__ params, int N, int M, int8_t *sigma, double *log_prob,
+    int64_t *n_accepted, int B, int sweep, int n_discard, int L, int8_t *samples, uint32_t k0,
+    uint32_t k1, uint64_t counter, const int32_t *__restrict__ clusters, int C) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nwords = (C + 31) >> 5;
+  const float *Wg = params + M, *bg = params, *ag = params + M + (int64_t)N * M;
+  float *logtab = reinterpret_cast<float *>(smem_raw);                // C + 1
+  int16_t *cl = reinterpret_cast<int16_t *>(logtab + C + 1);          // 2C
+  int16_t *inc = cl + 2 * C;                                          // N x XS_MAXDEG
+  int *deg = reinterpret_cast<int *>(                                 // N
+      (reinterpret_cast<uintptr_t>(inc + (size_t)N * XS_MAXDEG) + 3) & ~uintptr_t(3));
+  __shared__ int overflow;
+  unsigned char *per_warp_base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(deg + N) + 15) & ~uintptr_t(15));
+  const size_t per_warp = 4 * (size_t)M + (((size_t)N + 15) & ~size_t(15)) + 4 * (size_t)nwords;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wpb = (int)(blockDim.x >> 5);
+  {  // clusters and incidence lists
+    for (int i = tid; i < N; i += blockDim.x) deg[i] = 0;
+    for (int k = tid; k <= C; k += blockDim.x) logtab[k] = logf((float)k);
+    for (int q = tid; q < 2 * C; q += blockDim.x) cl[q] = (int16_t)clusters[q];
+    if (tid == 0) overflow = 0;
+    __syncthreads();
+    for (int q = tid; q < C; q += blockDim.x) {
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int site = cl[2 * q + e];
+        const int pos = atomicAdd(&deg[site], 1);
+        if (pos < XS_MAXDEG) inc[site * XS_MAXDEG + pos] = (int16_t)q;
+        else overflow = 1;
+      }
+    }
+    __syncthreads();
+  }
+  const bool full_recount = overflow != 0;
+  float *lcs = reinterpret_cast<float *>(per_warp_base + warp * per_warp);  // M
+  int8_t *xs = reinterpret_cast<int8_t *>(lcs + M);
+  uint32_t *mask = reinterpret_cast<uint32_t *>(xs + ((N + 15) & ~15));
+  for (int b = blockIdx.x * wpb + warp; b < B; b += gridDim.x * wpb) {
+    int8_t *sigma_row = sigma + (int64_t)b * N;
+    __syncwarp();
+    for (int i = lane; i < N; i += 32) xs[i] = sigma_row[i];
+    __syncwarp();
+    int hop = 0;
+    for (int w = lane; w < nwords; w += 32) {
+      uint32_t bits = 0u;
+      for (int t = 0; t < 32; ++t) {
+        const int q = 32 * w + t;
+        if (q < C && xs[cl[2 * q]] != xs[cl[2 * q + 1]]) bits |= 1u << t;
+      }
+      mask[w] = bits;
+      hop += __popc(bits);
+    }
+    hop = warp_sum_int(hop);
+    __syncwarp();
+    float th[R];
+    float logpsi = 0.0f;
+    auto recompute = [&]() {
+      float part = 0.0f;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int j = lane + 32 * r;
+        th[r] = 0.0f;
+        if (j < M) {
+          float acc = __ldg(bg + j);
+          for (int i = 0; i < N; ++i) acc += (float)xs[i] * __ldg(Wg + (int64_t)i * M + j);
+          th[r] = acc;
+          const float l = log_cosh_fast(acc);
+          lcs[j] = l;
+          part += l;
+        }
+      }
+      for (int i = lane; i < N; i += 32) part += (float)xs[i] * __ldg(ag + i);
+      logpsi = warp_sum(part);
+      __syncwarp();
+    };
+    int64_t acc_count = 0;
+    const int total = n_discard + L;
+    for (int step = 0; step < total; ++step) {
+      recompute();
+      for (int p = 0; p < sweep; ++p) {
+        const uint64_t pidx = counter + (uint64_t)step * sweep + p;
+        u32x4 rr = philox4x32_10(u32x4{(uint32_t)pidx, (uint32_t)(pidx >> 32), (uint32_t)b, 0u},
+                                 k0, k1);
+        if (hop == 0) continue;  // no move possible: rejected
+        int k = (int)below(rr.x, (uint32_t)hop);
+        const uint32_t wbits = lane < nwords ? mask[lane] : 0u;
+        const int cnt = __popc(wbits);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int excl = incl - cnt;
+        const bool owner = excl <= k && k < incl;
+        const unsigned ob = __ballot_sync(0xffffffffu, owner);
+        if (ob == 0u) continue;  // unreachable while hop matches the mask
+        const int src = __ffs(ob) - 1;
+        int pick = -1;
+        if (owner) pick = 32 * lane + nth_set_bit(wbits, k - excl);
+        pick = __shfl_sync(0xffffffffu, pick, src);
+        if (pick < 0 || pick >= C) continue;  // likewise unreachable; never out of range
+        const int su = cl[2 * pick], sv = cl[2 * pick + 1];
+        const int8_t xu = xs[su], xv = xs[sv];
+        const float du = (float)(xv - xu), dv = (float)(xu - xv);
+        int q = -1, newh = 0;
+        int hop_new;
+        if (!full_recount) {
+          const int site = lane < 16 ? su : sv, slot = lane & 15;
+          if (slot < deg[site]) {
+            q = inc[site * XS_MAXDEG + slot];
+            const int a0 = cl[2 * q], a1 = cl[2 * q + 1];
+            if (lane >= 16 && (a0 == su || a1 == su)) q = -1;
+            if (q >= 0) {
+              const int8_t x0 = a0 == su ? xv : (a0 == sv ? xu : xs[a0]);
+              const int8_t x1 = a1 == su ? xv : (a1 == sv ? xu : xs[a1]);
+              newh = x0 != x1;
+            }
+          }
+          const int oldh = q >= 0 ? (int)((mask[q >> 5] >> (q & 31)) & 1u) : 0;
+          hop_new = hop + warp_sum_int(q >= 0 ? newh - oldh : 0);
+        } else {
+          int h2 = 0;
+          for (int q0 = 0; q0 < C; q0 += 32) {
+            const int qq = q0 + lane;
+            if (qq < C) {
+              const int a0 = cl[2 * qq], a1 = cl[2 * qq + 1];
+              const int8_t x0 = a0 == su ? xv : (a0 == sv ? xu : xs[a0]);
+              const int8_t x1 = a1 == su ? xv : (a1 == sv ? xu : xs[a1]);
+              h2 += x0 != x1;
+            }
+          }
+          hop_new = warp_sum_int(h2);
+        }
+        const float corr = logtab[hop] - logtab[hop_new];
+        float sacc = 0.0f;
+        const float *Wu = Wg + (int64_t)su * M, *Wv = Wg + (int64_t)sv * M;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int j = lane + 32 * r;
+          if (j < M) {
+            float t = th[r] + du * __ldg(Wu + j);
+            t += dv * __ldg(Wv + j);
+            sacc += log_cosh_fast(t) - lcs[j];
+          }
+        }
+        float s = warp_sum(sacc);
+        s += du * __ldg(ag + su);
+        s += dv * __ldg(ag + sv);
+        const float dlp = 2.0f * s;
+        const float u = u01f(rr.y);
+        if (u < expf(dlp + corr)) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int j = lane + 32 * r;
+            if (j < M) {
+              float t = th[r] + du * __ldg(Wu + j);
+              t += dv * __ldg(Wv + j);
+              th[r] = t;
+              lcs[j] = log_cosh_fast(t);
+            }
+          }
+          __syncwarp();
+          if (lane == 0) {
+            xs[su] = (int8_t)(xu + (int)du);
+            xs[sv] = (int8_t)(xv + (int)dv);
+          }
+          if (!full_recount) {
+            if (q >= 0) {
+              const uint32_t bit = 1u << (q & 31);
+              if (newh) atomicOr(&mask[q >> 5], bit);
+              else atomicAnd(&mask[q >> 5], ~bit);
+            }
+          } else {
+            __syncwarp();
+            for (int w = lane; w < nwords; w += 32) {
+              uint32_t bits = 0u;
+              for (int t = 0; t < 32; ++t) {
+                const int qq = 32 * w + t;
+                if (qq < C && xs[cl[2 * qq]] != xs[cl[2 * qq + 1]]) bits |= 1u << t;
+              }
+              mask[w] = bits;
+            }
+          }
+          hop = hop_new;
+          logpsi += s;
+          ++acc_count;
+        }
+        __syncwarp();
+      }
+      if (step >= n_discard) {
+        int8_t *dst = samples + ((int64_t)b * L + (step - n_discard)) * N;
+        for (int i = lane; i < N; i += 32) dst[i] = xs[i];
+      }
+    }
+    recompute();
+    for (int i = lane; i < N; i += 32) sigma_row[i] = xs[i];
+    if (lane == 0) {
+      log_prob[b] = 2.0 * (double)logpsi;
+      n_accepted[b] += acc_count;
+    }
+  }
+}
+
+static size_t exchange_l2_smem_bytes(int N, int M, int C, int wpb) {
+  const int nwords = (C + 31) >> 5;
+  size_t bytes = (size_t)(C + 1) * 4 + (size_t)C * 4 + (size_t)N * XS_MAXDEG * 2 + 4 +
+                 (size_t)N * 4 + 16;
+  bytes += (size_t)wpb * (4 * (size_t)M + (((size_t)N + 15) & ~size_t(15)) + 4 * (size_t)nwords);
+  return bytes + 64;
+}
+
+template <int R>
+static int launch_exchange_l2(cudaStream_t st, const float *p, int N, int M, int8_t *sigma,
+                              double *log_prob, int64_t *n_acc, int B, int sweep, int n_discard,
+                              int L, int8_t *samples, uint32_t k0, uint32_t k1, uint64_t counter,
+                              const int32_t *clusters, int C, int sms) {
+  const int wpb = XL_WARPS;
+  const size_t smem = exchange_l2_smem_bytes(N, M, C, wpb);
+  VMCK_CUDA(cudaFuncSetAttribute(metropolis_exchange_l2_kernel<R>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int grid = (int)std::min<int64_t>(((int64_t)B + wpb - 1) / wpb, sms);
+  metropolis_exchange_l2_kernel<R><<<grid, 32 * wpb, smem, st>>>(
+      p, N, M, sigma, log_prob, n_acc, B, sweep, n_discard, L, samples, k0, k1, counter, clusters,
+      C);
+  return check_launch("metropolis_sample (exchange, weights through L2)");
+}
+
 static size_t exchange_smem_bytes(int N, int M, int C, int wpb) {
   const int nwords = (C + 31) >> 5;
   size_t bytes = (size_t)N * M * 4 + (size_t)M * 4 + (size_t)N * 4 + (size_t)(C + 1) * 4 +
@@ -564,6 +808,18 @@ int launch_metropolis(cudaStream_t st, const void *params, int N, int M, int8_t 
       return launch_exchange_smem<16>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard,
                                       L, samples, k0, k1, counter, clusters, C, sms);
     }
+  }
+  if (sizeof(T) == 4 && rule == 1 && C <= 1024 && M > 512 && M <= 2048 && !force_generic &&
+      exchange_l2_smem_bytes(N, M, C, XL_WARPS) <= 200 * 1024) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const float *pf = reinterpret_cast<const float *>(params);
+    if (M <= 1024)
+      return launch_exchange_l2<32>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard, L,
+                                    samples, k0, k1, counter, clusters, C, sms);
+    return launch_exchange_l2<64>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard, L,
+                                  samples, k0, k1, counter, clusters, C, sms);
   }
   if (rule == 0) {
     if (smem > 48 * 1024)

@@ -101,14 +101,18 @@ def test_exchange_smem_kernel_wide_hidden_layer_distribution(nk, alpha, std):
     assert _chi2_pvalues(nk, make, model, flat, N, 0, torch.float32, independent=True) > 0.01
 
 
-@pytest.mark.parametrize("L,alpha", [(10, 4), (10, 1), (10, 2), (6, 14)])
+@pytest.mark.parametrize("L,alpha", [(10, 4), (10, 1), (10, 2), (6, 14), (10, 8), (16, 8),
+                                     (6, 40)])
 def test_exchange_smem_kernel_matches_generic_kernel(nk, monkeypatch, L, alpha):
     """At the benchmark's shape (10x10, nn + nnn clusters, FP32; M = 100, 200 and
     400: the 4-, 8- and 13-unit forms) and on 6x6 with M = 504 (the 16-unit form;
     at N = 100 its weights would not fit in shared memory) the shared-memory
     Exchange kernel draws the same random numbers and evaluates the same
     floating-point expressions as the generic warp-per-chain kernel: samples,
-    log-probabilities and acceptance counters are identical."""
+    log-probabilities and acceptance counters are identical.  The same holds for
+    the kernel that reads wider weights through L2: 10x10 alpha 8 (M = 800, 32
+    units per lane), 16x16 alpha 8 (M = 2048, the large configuration's model;
+    64 units) and 6x6 alpha 40 (M = 1440, a partly filled 64-unit form)."""
     N = L * L
     model = nk.models.RBM(alpha=alpha)
     flat = model.init_flat(4, N).float()
