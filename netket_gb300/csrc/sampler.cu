@@ -503,18 +503,18 @@ __global__ void __launch_bounds__(32 * XS_MAX_WARPS, 1) metropolis_exchange_smem
 
 // ------------------------------------------------------------ Exchange, W in L2
 // The same chain for hidden layers too wide for shared-memory weights (N M >
-// ~48 K): W, b, a are read through L2 (2 MB for N = 256, M = 2048), theta lives
-// in registers (lane l holds units l + 32 r, r < R) and log_cosh(theta) in the
-// warp's shared memory; an accepted move recomputes theta' and its log_cosh
-// (the same expressions, so the same bits) instead of keeping the proposal.
-// That holds a chain in ~8 KB of shared memory and ~R + 40 registers per lane:
-// 16 chains per SM at M = 2048, where metropolis_kernel's four M-vectors in
-// shared memory leave 4.  Warps loop over chains (b += gridDim.x wpb).  Random
-// stream, proposal order and every floating-point expression match
-// metropolis_kernel<float, 1>, so the samples are identical.
-constexpr int XL_WARPS = 16;
+// ~48 K): W, b, a are read through L2 (2 MB for N = 256, M = 2048) and theta
+// lives in the warp's shared memory (M floats); log_cosh(theta) is recomputed
+// where it is needed instead of stored (the same function of the same value,
+// so the same bits), and an accepted move recomputes theta'.  A chain then
+// holds ~8.3 KB of shared memory and few registers: 24 chains per SM at
+// M = 2048, where metropolis_kernel's four M-vectors leave 4 (a version with
+// theta in registers, 64 per lane, was register-bound at 16 and stalled on the
+// L2 loads of W: 25 % warps active).  Warps loop over chains (b += gridDim.x
+// wpb).  Random stream, proposal order and every floating-point expression
+// match metropolis_kernel<float, 1>, so the samples are identical.
+constexpr int XL_WARPS = 24;
 
-template <int R>
 __global__ void __launch_bounds__(32 * XL_WARPS, 1) metropolis_exchange_l2_kernel(
     const float *__restrict__ params, int N, int M, int8_t *sigma, double *log_prob,
     int64_t *n_accepted, int B, int sweep, int n_discard, int L, int8_t *samples, uint32_t k0,
@@ -551,8 +551,8 @@ __global__ void __launch_bounds__(32 * XL_WARPS, 1) metropolis_exchange_l2_kerne
     __syncthreads();
   }
   const bool full_recount = overflow != 0;
-  float *lcs = reinterpret_cast<float *>(per_warp_base + warp * per_warp);  // M
-  int8_t *xs = reinterpret_cast<int8_t *>(lcs + M);
+  float *ths = reinterpret_cast<float *>(per_warp_base + warp * per_warp);  // theta, M
+  int8_t *xs = reinterpret_cast<int8_t *>(ths + M);
   uint32_t *mask = reinterpret_cast<uint32_t *>(xs + ((N + 15) & ~15));
   for (int b = blockIdx.x * wpb + warp; b < B; b += gridDim.x * wpb) {
     int8_t *sigma_row = sigma + (int64_t)b * N;
@@ -571,22 +571,14 @@ __global__ void __launch_bounds__(32 * XL_WARPS, 1) metropolis_exchange_l2_kerne
     }
     hop = warp_sum_int(hop);
     __syncwarp();
-    float th[R];
     float logpsi = 0.0f;
     auto recompute = [&]() {
       float part = 0.0f;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int j = lane + 32 * r;
-        th[r] = 0.0f;
-        if (j < M) {
-          float acc = __ldg(bg + j);
-          for (int i = 0; i < N; ++i) acc += (float)xs[i] * __ldg(Wg + (int64_t)i * M + j);
-          th[r] = acc;
-          const float l = log_cosh_fast(acc);
-          lcs[j] = l;
-          part += l;
-        }
+      for (int j = lane; j < M; j += 32) {
+        float acc = __ldg(bg + j);
+        for (int i = 0; i < N; ++i) acc += (float)xs[i] * __ldg(Wg + (int64_t)i * M + j);
+        ths[j] = acc;
+        part += log_cosh_fast(acc);
       }
       for (int i = lane; i < N; i += 32) part += (float)xs[i] * __ldg(ag + i);
       logpsi = warp_sum(part);
@@ -654,14 +646,12 @@ __global__ void __launch_bounds__(32 * XL_WARPS, 1) metropolis_exchange_l2_kerne
         const float corr = logtab[hop] - logtab[hop_new];
         float sacc = 0.0f;
         const float *Wu = Wg + (int64_t)su * M, *Wv = Wg + (int64_t)sv * M;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int j = lane + 32 * r;
-          if (j < M) {
-            float t = th[r] + du * __ldg(Wu + j);
-            t += dv * __ldg(Wv + j);
-            sacc += log_cosh_fast(t) - lcs[j];
-          }
+#pragma unroll 8
+        for (int j = lane; j < M; j += 32) {
+          const float th = ths[j];
+          float t = th + du * __ldg(Wu + j);
+          t += dv * __ldg(Wv + j);
+          sacc += log_cosh_fast(t) - log_cosh_fast(th);
         }
         float s = warp_sum(sacc);
         s += du * __ldg(ag + su);
@@ -669,15 +659,11 @@ __global__ void __launch_bounds__(32 * XL_WARPS, 1) metropolis_exchange_l2_kerne
         const float dlp = 2.0f * s;
         const float u = u01f(rr.y);
         if (u < expf(dlp + corr)) {
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const int j = lane + 32 * r;
-            if (j < M) {
-              float t = th[r] + du * __ldg(Wu + j);
-              t += dv * __ldg(Wv + j);
-              th[r] = t;
-              lcs[j] = log_cosh_fast(t);
-            }
+#pragma unroll 8
+          for (int j = lane; j < M; j += 32) {
+            float t = ths[j] + du * __ldg(Wu + j);
+            t += dv * __ldg(Wv + j);
+            ths[j] = t;
           }
           __syncwarp();
           if (lane == 0) {
@@ -729,17 +715,29 @@ static size_t exchange_l2_smem_bytes(int N, int M, int C, int wpb) {
   return bytes + 64;
 }
 
-template <int R>
+// Dynamic shared memory a block may use on this GPU (227 KB on sm_100 / sm_103),
+// less the kernel's static variable.
+constexpr size_t XL_SMEM_MAX = 227 * 1024 - 64;
+
+// Chains per block of the L2 kernel: as many as fit (at most XL_WARPS), 0 if
+// fewer than 4 do.
+static int exchange_l2_warps(int N, int M, int C) {
+  int w = XL_WARPS;
+  while (w >= 4 && exchange_l2_smem_bytes(N, M, C, w) > XL_SMEM_MAX) --w;
+  return w >= 4 ? w : 0;
+}
+
 static int launch_exchange_l2(cudaStream_t st, const float *p, int N, int M, int8_t *sigma,
                               double *log_prob, int64_t *n_acc, int B, int sweep, int n_discard,
                               int L, int8_t *samples, uint32_t k0, uint32_t k1, uint64_t counter,
                               const int32_t *clusters, int C, int sms) {
-  const int wpb = XL_WARPS;
+  const int wpb = exchange_l2_warps(N, M, C);
+  VMCK_REQUIRE(wpb >= 4, "exchange L2 kernel: M too large");
   const size_t smem = exchange_l2_smem_bytes(N, M, C, wpb);
-  VMCK_CUDA(cudaFuncSetAttribute(metropolis_exchange_l2_kernel<R>,
+  VMCK_CUDA(cudaFuncSetAttribute(metropolis_exchange_l2_kernel,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = (int)std::min<int64_t>(((int64_t)B + wpb - 1) / wpb, sms);
-  metropolis_exchange_l2_kernel<R><<<grid, 32 * wpb, smem, st>>>(
+  metropolis_exchange_l2_kernel<<<grid, 32 * wpb, smem, st>>>(
       p, N, M, sigma, log_prob, n_acc, B, sweep, n_discard, L, samples, k0, k1, counter, clusters,
       C);
   return check_launch("metropolis_sample (exchange, weights through L2)");
@@ -809,17 +807,14 @@ int launch_metropolis(cudaStream_t st, const void *params, int N, int M, int8_t 
                                       L, samples, k0, k1, counter, clusters, C, sms);
     }
   }
-  if (sizeof(T) == 4 && rule == 1 && C <= 1024 && M > 512 && M <= 2048 && !force_generic &&
-      exchange_l2_smem_bytes(N, M, C, XL_WARPS) <= 200 * 1024) {
+  if (sizeof(T) == 4 && rule == 1 && C <= 1024 && M > 512 && !force_generic &&
+      exchange_l2_warps(N, M, C) > 0) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const float *pf = reinterpret_cast<const float *>(params);
-    if (M <= 1024)
-      return launch_exchange_l2<32>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard, L,
-                                    samples, k0, k1, counter, clusters, C, sms);
-    return launch_exchange_l2<64>(st, pf, N, M, sigma, log_prob, n_acc, B, sweep, n_discard, L,
-                                  samples, k0, k1, counter, clusters, C, sms);
+    return launch_exchange_l2(st, reinterpret_cast<const float *>(params), N, M, sigma, log_prob,
+                              n_acc, B, sweep, n_discard, L, samples, k0, k1, counter, clusters, C,
+                              sms);
   }
   if (rule == 0) {
     if (smem > 48 * 1024)
