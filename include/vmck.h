@@ -162,6 +162,18 @@ int vmck_get_conn_local(vmck_stream s, const vmck_local_op *op, const int8_t *x,
 int vmck_rbm_logpsi(vmck_stream s, int32_t dtype, const void *params, int32_t N,
                     int32_t M, const int8_t *x, int64_t n, void *logpsi,
                     void *theta_out, void *tanh_out);
+/* The same for FP32 parameters with x W on the tensor cores (tcgen05; W split
+ * into FP16 hi + lo, x exact; FP32 accumulation drained every 64 sites), then
+ * one pass for b, tanh and the log_cosh row sums.  workspace: caller-owned
+ * device bytes, at least vmck_rbm_logpsi_tc_workspace_size(N, M, n,
+ * theta_out != NULL).  status (device, nullable): VMCK_DEV_TIMEOUT if a
+ * bounded wait ran out. */
+int64_t vmck_rbm_logpsi_tc_workspace_size(int32_t N, int32_t M, int64_t n,
+                                          int32_t with_theta_out);
+int vmck_rbm_logpsi_tc(vmck_stream s, const float *params, int32_t N, int32_t M,
+                       const int8_t *x, int64_t n, float *logpsi, float *theta_out,
+                       float *tanh_out, void *workspace, int64_t workspace_bytes,
+                       int32_t *status);
 
 /* ---------------------------------------------------------------- a9 (plain)
  * local_value_kernel_jax reduction (netket/vqs/mc/kernels.py:62-71) from
@@ -362,6 +374,15 @@ int64_t vmck_ot_v_workspace_size(int32_t N, int32_t M, int64_t n);
 int vmck_rbm_ot_v(vmck_stream s, int32_t dtype, const void *tanh_theta,
                   const int8_t *x, int32_t N, int32_t M, int64_t n, const double *v,
                   double *out, double *workspace, int64_t workspace_len);
+/* O^T v for FP32 tanh(theta) on the tensor cores: one GEMM of v (.) [t, 1]
+ * (split into FP16 hi + lo) with [x, 1] over the samples (split into chunks,
+ * partial sums added in FP64 in chunk order) gives the kernel, hidden-bias and
+ * visible-bias parts at once.  workspace: caller-owned device bytes, at least
+ * vmck_rbm_ot_v_tc_workspace_size(N, M, n).  status as vmck_rbm_logpsi_tc. */
+int64_t vmck_rbm_ot_v_tc_workspace_size(int32_t N, int32_t M, int64_t n);
+int vmck_rbm_ot_v_tc(vmck_stream s, const float *tanh_theta, const int8_t *x, int32_t N,
+                     int32_t M, int64_t n, const double *v, double *out, void *workspace,
+                     int64_t workspace_bytes, int32_t *status);
 
 /* Dense centred, scaled Jacobian O_L = (O - mean O) * scale, (n, P) in out_dtype,
  * from tanh(theta) (dtype) and the column means (FP64, P) -- nkjax.jacobian

@@ -80,6 +80,12 @@ _SIGNATURES = {
     "vmck_rbm_eloc_pauli": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64,
                              ctypes.POINTER(PauliStringsStruct), c_vp, c_vp], c_i32),
     "vmck_rbm_logpsi": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp], c_i32),
+    "vmck_rbm_logpsi_tc_workspace_size": ([c_i32, c_i32, c_i64, c_i32], c_i64),
+    "vmck_rbm_logpsi_tc": ([c_vp, c_vp, c_i32, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i64,
+                            c_vp], c_i32),
+    "vmck_rbm_ot_v_tc_workspace_size": ([c_i32, c_i32, c_i64], c_i64),
+    "vmck_rbm_ot_v_tc": ([c_vp, c_vp, c_vp, c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_i64, c_vp],
+                         c_i32),
     "vmck_eloc_from_logpsi": ([c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp], c_i32),
     "vmck_rbm_eloc_ising": ([c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i64, c_vp, c_i32, c_dbl,
                              c_dbl, c_vp, c_vp], c_i32),

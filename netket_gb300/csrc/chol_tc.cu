@@ -41,23 +41,6 @@
 
 namespace vmck {
 
-// ------------------------------------------------------------ operand split
-// Power-of-two s with bound * s < 2^13 (exponent clamped); 1 for a bound that is
-// zero, negative or not finite.
-__device__ __forceinline__ float split_scale(float bound) {
-  if (!(bound > 0.0f) || !(bound <= 3.0e38f)) return 1.0f;
-  int e = 0;
-  frexpf(bound, &e);  // bound = f 2^e, f in [0.5, 1)
-  e = max(-100, min(100, e));
-  return ldexpf(1.0f, 13 - e);
-}
-
-__device__ __forceinline__ void split_f16(float v, float s, __half &hi, __half &lo) {
-  const float t = v * s;
-  hi = __float2half_rn(t);
-  lo = __float2half_rn(t - __half2float(hi));
-}
-
 // scales[0] = s(max diag A), scales[1] = s(sqrt(max diag A)); status gets
 // NONFINITE for a non-finite diagonal.  One block.
 __global__ void __launch_bounds__(256) chol_bounds_kernel(const float *__restrict__ A, int64_t n,
@@ -149,6 +132,10 @@ struct GemmParams {
   const float *sa, *sb;
   int tri;
   int lolo;  // also lo * lo (a Gram matrix of the split operand stays one)
+  // split K: tile t of kz * base_tiles covers K range [z kchunk, +kchunk) of
+  // output tile t % base_tiles, z = t / base_tiles, into C + z zstride
+  int kz, kchunk;
+  int64_t zstride, base_tiles;
   __half *oh, *ol;
   int64_t ldo;
   int o_rows, o_col0;
@@ -179,6 +166,18 @@ __device__ __forceinline__ void gemm_tile(const GemmParams &g, int64_t t, int &m
   }
   ni = lo;
   mi = (int)(t - tri_cum(lo, g.mt));
+}
+
+// Tile t -> (mi, ni), its K slab range [kb0, kb0 + nkb) and output C.
+__device__ __forceinline__ void gemm_work(const GemmParams &g, int64_t t, int &mi, int &ni,
+                                          int &kb0, int &nkb, float *&C) {
+  const int64_t z = t / g.base_tiles;
+  gemm_tile(g, t - z * g.base_tiles, mi, ni);
+  const int k0 = (int)z * g.kchunk;
+  const int k1 = min(g.K, k0 + g.kchunk);
+  kb0 = k0 / G_BK;
+  nkb = (k1 - k0 + G_BK - 1) / G_BK;
+  C = g.C + z * g.zstride;
 }
 
 __global__ void __launch_bounds__(G_THREADS, 1)
@@ -231,7 +230,6 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
-  const int num_kb = (g.K + G_BK - 1) / G_BK;
   // the prologue above overlaps the previous kernel of the stream; its output
   // (operands, C) is read only from here on
   pdl_wait();
@@ -247,8 +245,9 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     if (lane == 0) {
       int64_t it = 0;
       for (int64_t tile = blockIdx.x; tile < g.tiles && !*abort_flag; tile += gridDim.x) {
-        int mi, ni;
-        gemm_tile(g, tile, mi, ni);
+        int mi, ni, kb0, num_kb;
+        float *Ct;
+        gemm_work(g, tile, mi, ni, kb0, num_kb, Ct);
         const int ya = g.a_row0 + mi * G_BM, yb = g.b_row0 + ni * G_BN;
         for (int kb = 0; kb < num_kb; ++kb, ++it) {
           const int s = (int)(it % G_STAGES);
@@ -259,7 +258,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           }
           if (*abort_flag) break;
           unsigned char *st = smem + s * G_STAGE_BYTES;
-          const int x = g.k_off + kb * G_BK;
+          const int x = g.k_off + (kb0 + kb) * G_BK;
           mbar_expect_tx(&full[s], G_STAGE_BYTES);
           tma_load_2d(st, &mAh, &full[s], x, ya);
           tma_load_2d(st + G_A_BYTES, &mAl, &full[s], x, ya);
@@ -289,6 +288,9 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           break;
         }
         tc_fence_after();
+        int mi, ni, kb0, num_kb;
+        float *Ct;
+        gemm_work(g, tile, mi, ni, kb0, num_kb, Ct);
         for (int kb = 0; kb < num_kb; ++kb, ++it, ++slab) {
           const int s = (int)(it % G_STAGES);
           if (!mbar_wait(&full[s], (uint32_t)((it / G_STAGES) & 1), g.wait_ns)) {
@@ -349,12 +351,13 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     int64_t tcount = 0, slab = 0;
     bool alive = true;
     for (int64_t tile = blockIdx.x; tile < g.tiles && alive; tile += gridDim.x, ++tcount) {
-      int mi, ni;
-      gemm_tile(g, tile, mi, ni);
+      int mi, ni, kb0, num_kb;
+      float *Ct;
+      gemm_work(g, tile, mi, ni, kb0, num_kb, Ct);
       const int m = mi * G_BM + quarter * 32 + lane;
       const int nbase = ni * G_BN + part * G_COLS;
       const bool row_ok = m < g.M;
-      float *Crow = g.C + m;
+      float *Crow = Ct + m;
       // the sums start from the old C values (loaded while the first slab's MMAs
       // run), so the write-out only stores
       float acc[G_COLS];
@@ -750,8 +753,14 @@ static size_t gemm_smem_bytes() { return 1024 + G_STAGES * G_STAGE_BYTES + 8 * 1
 int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOperand &b, int b_row0,
             int k_off, int M, int N, int K, float *C, int64_t ldc, float alpha, float beta,
             const float *sa, const float *sb, int tri, __half *oh, __half *ol, int64_t ldo,
-            int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas, int lolo) {
+            int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas, int lolo,
+            int kchunk, int64_t zstride) {
   if (M <= 0 || N <= 0 || K <= 0) return VMCK_OK;
+  if (kchunk <= 0 || kchunk >= K) kchunk = K;
+  if (kchunk < K && (kchunk % G_BK != 0 || tri || oh || beta != 0.0f)) {
+    set_last_error("tc_gemm: split K needs kchunk %% %d == 0, no tri / split output / beta", G_BK);
+    return VMCK_ERR_ARG;
+  }
   CUtensorMap mAh, mAl, mBh, mBl;
   int rc;
   if ((rc = make_f16_map(&mAh, a.hi, a.kdim, a.rows, a.ld))) return rc;
@@ -785,10 +794,14 @@ int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOpera
   g.nt = (N + G_BN - 1) / G_BN;
   if (tri) {
     const int64_t h = g.mt / 2;
-    g.tiles = g.nt <= h ? (int64_t)g.nt * (g.nt + 1) : h * (h + 1) + (int64_t)(g.nt - h) * g.mt;
+    g.base_tiles = g.nt <= h ? (int64_t)g.nt * (g.nt + 1) : h * (h + 1) + (int64_t)(g.nt - h) * g.mt;
   } else {
-    g.tiles = (int64_t)g.mt * g.nt;
+    g.base_tiles = (int64_t)g.mt * g.nt;
   }
+  g.kchunk = kchunk;
+  g.kz = (K + kchunk - 1) / kchunk;
+  g.zstride = zstride;
+  g.tiles = g.base_tiles * g.kz;
   const size_t smem = gemm_smem_bytes();
   VMCK_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));

@@ -24,14 +24,33 @@ struct SplitOperand {
   int64_t rows;
 };
 
+// Power-of-two s with bound * s < 2^13 (exponent clamped); 1 for a bound that is
+// zero, negative or not finite.
+__device__ __forceinline__ float split_scale(float bound) {
+  if (!(bound > 0.0f) || !(bound <= 3.0e38f)) return 1.0f;
+  int e = 0;
+  frexpf(bound, &e);  // bound = f 2^e, f in [0.5, 1)
+  e = max(-100, min(100, e));
+  return ldexpf(1.0f, 13 - e);
+}
+
+// v s = hi + lo, both FP16 (22 significant bits together).
+__device__ __forceinline__ void split_f16(float v, float s, __half &hi, __half &lo) {
+  const float t = v * s;
+  hi = __float2half_rn(t);
+  lo = __float2half_rn(t - __half2float(hi));
+}
+
 // C[m + nn ldc] = alpha (A_op B_op^T)(m, nn) / (sa sb) + beta C (tri: m <= nn
 // only) on the tensor cores (chol_tc.cu); optional split output of the result.
-// Products hi hi + hi lo + lo hi, and lo lo with lolo.
+// Products hi hi + hi lo + lo hi, and lo lo with lolo.  Split K (kchunk > 0, a
+// multiple of 64, below K): the K range [z kchunk, +kchunk) of every output
+// tile goes to C + z zstride (partial sums, beta 0, no tri / split output).
 int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOperand &b,
             int b_row0, int k_off, int M, int N, int K, float *C, int64_t ldc, float alpha,
             float beta, const float *sa, const float *sb, int tri, __half *oh, __half *ol,
             int64_t ldo, int o_rows, int o_col0, const float *so, int32_t *status, int max_ctas,
-            int lolo = 0);
+            int lolo = 0, int kchunk = 0, int64_t zstride = 0);
 
 // Device workspace (bytes) of chol_tc_factor for an n x n matrix.
 int64_t chol_tc_workspace_bytes(int64_t n);

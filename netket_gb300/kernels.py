@@ -18,13 +18,36 @@ def _dev():
 
 
 # ------------------------------------------------------------------ RBM forward
-def rbm_forward(params_c, x, N, M, want_theta=False, want_tanh=False):
-    """logpsi (n,), optional theta and tanh(theta) (n, M), in params_c.dtype."""
+# FP32 contractions of at least this many sample x hidden-unit products run on
+# the tensor cores (vmck_rbm_logpsi_tc / vmck_rbm_ot_v_tc); smaller ones on the
+# CUDA cores, where the operand preparation would cost more than the product.
+TC_MIN_WORK = 1 << 22
+
+
+def _use_tc(dt, n, M, use_tc):
+    if use_tc is None:
+        return dt == torch.float32 and n * M >= TC_MIN_WORK
+    if use_tc and dt != torch.float32:
+        raise ValueError("the tensor-core RBM contractions take FP32 inputs")
+    return bool(use_tc)
+
+
+def rbm_forward(params_c, x, N, M, want_theta=False, want_tanh=False, use_tc=None):
+    """logpsi (n,), optional theta and tanh(theta) (n, M), in params_c.dtype.
+    ``use_tc``: None picks the tensor-core x W for large FP32 problems."""
     n = x.shape[0]
     dt = params_c.dtype
     lp = torch.empty(n, dtype=dt, device=x.device)
     th = torch.empty((n, M), dtype=dt, device=x.device) if want_theta else None
     tt = torch.empty((n, M), dtype=dt, device=x.device) if want_tanh else None
+    if _use_tc(dt, n, M, use_tc):
+        L = nat.lib()
+        nb = L.vmck_rbm_logpsi_tc_workspace_size(N, M, n, int(th is not None))
+        ws = torch.empty(nb, dtype=torch.uint8, device=x.device)
+        nat.check(L.vmck_rbm_logpsi_tc(nat.stream(), nat.ptr(params_c), N, M, nat.ptr(x), n,
+                                       nat.ptr(lp), nat.ptr(th), nat.ptr(tt), nat.ptr(ws), nb,
+                                       None))
+        return lp, th, tt
     nat.check(nat.lib().vmck_rbm_logpsi(nat.stream(), nat.dtype_code(dt), nat.ptr(params_c), N, M,
                                         nat.ptr(x), n, nat.ptr(lp), nat.ptr(th), nat.ptr(tt)))
     return lp, th, tt
@@ -105,11 +128,19 @@ def online_stats_update(data2d, state, max_lag, buf_len, decay, mean_f32):
 
 
 # ------------------------------------------------------------------ Jacobian products
-def ot_v(tanh_t, x, N, M, v):
-    """O^T v (P,) FP64 for the RBM Jacobian, never materialising O."""
+def ot_v(tanh_t, x, N, M, v, use_tc=None):
+    """O^T v (P,) FP64 for the RBM Jacobian, never materialising O.  ``use_tc``:
+    None picks the tensor-core GEMM for large FP32 problems."""
     n = x.shape[0]
     P = M + N * M + N
     out = torch.empty(P, dtype=torch.float64, device=x.device)
+    if _use_tc(tanh_t.dtype, n, M, use_tc):
+        L = nat.lib()
+        nb = L.vmck_rbm_ot_v_tc_workspace_size(N, M, n)
+        ws = torch.empty(nb, dtype=torch.uint8, device=x.device)
+        nat.check(L.vmck_rbm_ot_v_tc(nat.stream(), nat.ptr(tanh_t), nat.ptr(x), N, M, n,
+                                     nat.ptr(v.contiguous()), nat.ptr(out), nat.ptr(ws), nb, None))
+        return out
     ws = torch.empty(nat.lib().vmck_ot_v_workspace_size(N, M, n), dtype=torch.float64,
                      device=x.device)
     nat.check(nat.lib().vmck_rbm_ot_v(nat.stream(), nat.dtype_code(tanh_t.dtype), nat.ptr(tanh_t),

@@ -41,6 +41,56 @@ def test_logpsi(nk, N, alpha):
     np.testing.assert_allclose(tt.cpu().numpy(), np.tanh(rth), rtol=1e-12, atol=1e-13)
 
 
+TC_CASES = [(100, 4, 3000), (256, 8, 1500), (37, 3, 777)]
+
+
+@pytest.mark.parametrize("N,alpha,n", TC_CASES)
+def test_logpsi_tensor_cores(nk, N, alpha, n):
+    """theta = x W on tcgen05 (W split into FP16 hi + lo, x exact) for FP32
+    parameters: the 10x10 alpha-4 and 16x16 alpha-8 widths and an odd N (site
+    padding) with n not a multiple of the tile: logpsi, theta and tanh theta
+    against the FP64 oracle of the same FP32 parameters (FP32 tolerances) and
+    against the CUDA-core FP32 kernel."""
+    model, flat, M = _setup(nk, N, alpha, N + 3)
+    f32 = flat.float()
+    x = nk.hilbert.Spin(0.5, N).random_state(seed=2, size=n)
+    lp, th, tt = nk.kernels.rbm_forward(f32, x, N, M, want_theta=True, want_tanh=True,
+                                        use_tc=True)
+    p = oracle_params(f32.double(), N, M)
+    xs = x.cpu().numpy()
+    rth = orbm.theta(p, xs)
+    np.testing.assert_allclose(th.cpu().numpy(), rth, rtol=1e-5, atol=2e-5)
+    np.testing.assert_allclose(tt.cpu().numpy(), np.tanh(rth), rtol=1e-5, atol=2e-5)
+    np.testing.assert_allclose(lp.cpu().numpy(), orbm.logpsi(p, xs), rtol=2e-5, atol=2e-5)
+    lp_c, _, _ = nk.kernels.rbm_forward(f32, x, N, M, use_tc=False)
+    np.testing.assert_allclose(lp.cpu().numpy(), lp_c.cpu().numpy(), rtol=2e-5, atol=2e-5)
+    # without a theta buffer the pre-activation lives in the workspace
+    lp2, _, tt2 = nk.kernels.rbm_forward(f32, x, N, M, want_tanh=True, use_tc=True)
+    assert torch.equal(lp2, lp) and torch.equal(tt2, tt)
+
+
+@pytest.mark.parametrize("N,alpha,n", TC_CASES)
+def test_ot_v_tensor_cores(nk, N, alpha, n):
+    """O^T v on tcgen05 (v t split into FP16 hi + lo, samples split into K
+    chunks, partial sums in FP64): the kernel, hidden-bias and visible-bias parts
+    against the FP64 product with the same FP32 t, and against the CUDA-core
+    FP32 kernel (FP32 tolerances, 1e-4 relative)."""
+    model, flat, M = _setup(nk, N, alpha, N + 5)
+    f32 = flat.float()
+    x = nk.hilbert.Spin(0.5, N).random_state(seed=3, size=n)
+    _, _, t = nk.kernels.rbm_forward(f32, x, N, M, want_tanh=True, use_tc=False)
+    v = torch.as_tensor(np.random.default_rng(n).normal(size=n), device="cuda")
+    got = nk.kernels.ot_v(t, x, N, M, v, use_tc=True).cpu().numpy()
+    tn = t.double().cpu().numpy()
+    xs = x.cpu().numpy().astype(np.float64)
+    O = np.concatenate([tn, (xs[:, :, None] * tn[:, None, :]).reshape(n, N * M), xs], axis=1)
+    ref = O.T @ v.cpu().numpy()
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(got, ref, rtol=1e-4, atol=1e-5 * scale)
+    simt = nk.kernels.ot_v(t, x, N, M, v, use_tc=False).cpu().numpy()
+    np.testing.assert_allclose(got, simt, rtol=1e-4, atol=1e-5 * scale)
+
+
 @pytest.mark.parametrize("N,h,J", [(16, 1.0, 1.0), (24, 0.6, -1.0), (9, 0.0, 1.0)])
 def test_eloc_ising(nk, N, h, J):
     model, flat, M = _setup(nk, N, 2, 3)
