@@ -143,7 +143,7 @@ def _structured_gram_f64(teff, xs, ob, n, shift):
     return (G - g[:, None] - g[None, :] + ob @ ob) / n + shift * np.eye(n)
 
 
-@pytest.mark.parametrize("N,alpha,n", [(256, 8, 2048), (64, 10, 1500)])
+@pytest.mark.parametrize("N,alpha,n", [(256, 8, 2048), (64, 10, 1500), (256, 8, 8192)])
 def test_tensor_core_gram_large_m(nk, N, alpha, n):
     """M > 512 (the 16 x 16, alpha 8 model's M = 2048): the default mode 4 Gram
     equals the FP64 Gram of t_eff = c + s0, c = fp32(t - s0) rounded to a
