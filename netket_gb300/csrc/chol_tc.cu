@@ -171,6 +171,13 @@ __device__ __forceinline__ void gemm_tile(const GemmParams &g, int64_t t, int &m
 // Tile t -> (mi, ni), its K slab range [kb0, kb0 + nkb) and output C.
 __device__ __forceinline__ void gemm_work(const GemmParams &g, int64_t t, int &mi, int &ni,
                                           int &kb0, int &nkb, float *&C) {
+  if (g.kz == 1) {  // no split: skip the 64-bit division
+    gemm_tile(g, t, mi, ni);
+    kb0 = 0;
+    nkb = (g.K + G_BK - 1) / G_BK;
+    C = g.C;
+    return;
+  }
   const int64_t z = t / g.base_tiles;
   gemm_tile(g, t - z * g.base_tiles, mi, ni);
   const int k0 = (int)z * g.kchunk;
