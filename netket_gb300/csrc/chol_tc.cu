@@ -828,19 +828,23 @@ int tc_gemm(cudaStream_t st, const SplitOperand &a, int a_row0, const SplitOpera
   return check_launch("tc_gemm");
 }
 
-int chol_block_rows() {
-  static const int rows = [] {
+int chol_block_rows(int64_t n) {
+  static const int forced = [] {
     const char *v = getenv("VMCK_CHOL_BLOCK");
-    const int r = v ? atoi(v) : CHOL_BLOCK;
-    return (r == 128 || r == 256 || r == 512) ? r : CHOL_BLOCK;
+    const int r = v ? atoi(v) : 0;
+    return (r == 128 || r == 256 || r == 512 || r == 1024 || r == 2048 || r == 4096) ? r : 0;
   }();
-  return rows;
+  if (forced) return forced;
+  // measured on GB300 (factor + refinement): n = 16,384: 18.5 / 18.2 / 19.7 ms
+  // for 512 / 1024 / 2048 rows; 32,768: 86 / 68 / 71 ms; 65,536: 609 / 440 /
+  // 385 / 412 ms (4096)
+  return n >= 3 * CHOL_BIG_N / 2 ? 2048 : (n >= CHOL_BIG_N / 2 ? 1024 : CHOL_BLOCK);
 }
 
 int64_t chol_tc_workspace_bytes(int64_t n) {
   const int64_t nb = (n + LB - 1) / LB;
   int64_t b = 0;
-  b += 4 * (int64_t)CHOL_BLOCK * n * 2;  // Ph hi / lo, two buffers (K = 512 rows per column)
+  b += 4 * (int64_t)chol_block_rows(n) * n * 2;  // Ph hi / lo, two buffers (K = block rows)
   b += 2 * (int64_t)LB * n * 2;          // Bs hi / lo
   b += 2 * (int64_t)LB * LB * 2;         // Xs hi / lo
   b += 64;                               // scales
@@ -849,7 +853,7 @@ int64_t chol_tc_workspace_bytes(int64_t n) {
 }
 
 int chol_events_needed(int64_t n) {
-  const int64_t blk = chol_block_rows();
+  const int64_t blk = chol_block_rows(n);
   return (int)(3 * ((n + blk - 1) / blk) + 2);
 }
 
@@ -875,13 +879,14 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
     set_last_error("chol_tc: n must be below 2^30");
     return VMCK_ERR_UNSUPPORTED;
   }
+  const int64_t blk = chol_block_rows(n);
   char *p = align_up(static_cast<char *>(ws), 1024);
   __half *ph_hi[2], *ph_lo[2];
   for (int q = 0; q < 2; ++q) {
     ph_hi[q] = reinterpret_cast<__half *>(p);
-    p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
+    p = align_up(p + (size_t)blk * n * 2, 1024);
     ph_lo[q] = reinterpret_cast<__half *>(p);
-    p = align_up(p + (size_t)CHOL_BLOCK * n * 2, 1024);
+    p = align_up(p + (size_t)blk * n * 2, 1024);
   }
   __half *bs_hi = reinterpret_cast<__half *>(p);
   p = align_up(p + (size_t)LB * n * 2, 1024);
@@ -896,7 +901,6 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
   float *yinv = reinterpret_cast<float *>(p);
   if (yinv_out) *yinv_out = yinv;
 
-  const int64_t blk = chol_block_rows();
   const int nblocks = (int)((n + blk - 1) / blk);
   // look-ahead: the chain stream factors block row b and updates block row b + 1
   // (LA); the side stream updates rows b + 2 .. with block row b, first block row
@@ -933,7 +937,7 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
     const int64_t k2 = std::min<int64_t>(n, k1 + blk), k3 = std::min<int64_t>(n, k2 + blk);
     __half *qh = ph_hi[two ? (b & 1) : 0], *ql = ph_lo[two ? (b & 1) : 0];
     // the block row's split panel: row (c - k0) holds U(k0 .. k1, c) (K = w)
-    const SplitOperand ph{qh, ql, CHOL_BLOCK, w, n - k0};
+    const SplitOperand ph{qh, ql, blk, w, n - k0};
     if (two && b >= 2)
       VMCK_CUDA(cudaStreamWaitEvent(chain, G[b - 2], 0));  // side is done with this buffer
     for (int64_t r0 = k0; r0 < k1; r0 += LB) {
@@ -960,14 +964,14 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
       // panel: U[r0:r1, r1:n] = X^T A[r0:r1, r1:n], split copy into Ph
       if ((rc = tc_gemm(chain, xop, 0, bop, 0, 0, mp, (int)(n - r1), mp, A + r0 + r1 * n, n,
                         1.0f, 0.0f, scales + 2, scales + 0, 0,
-                        qh + (r1 - k0) * CHOL_BLOCK + pp * LB,
-                        ql + (r1 - k0) * CHOL_BLOCK + pp * LB, CHOL_BLOCK, mp, 0, scales + 1,
+                        qh + (r1 - k0) * blk + pp * LB, ql + (r1 - k0) * blk + pp * LB, blk,
+                        mp, 0, scales + 1,
                         status, 0)))
         return rc;
       if (r1 < k1) {
         // rest of the block row; rows [r1, r1 + next) feed the next panel (split)
         const int next = (int)std::min<int64_t>(LB, k1 - r1);
-        const SplitOperand pk{qh, ql, CHOL_BLOCK, pp * LB + mp, n - k0};
+        const SplitOperand pk{qh, ql, blk, pp * LB + mp, n - k0};
         if ((rc = tc_gemm(chain, pk, (int)(r1 - k0), pk, (int)(r1 - k0), pp * LB,
                           (int)(k1 - r1), (int)(n - r1), mp, A + r1 + r1 * n, n, -1.0f, 1.0f,
                           scales + 1, scales + 1, 1, bs_hi, bs_lo, LB, next, next, scales + 0,

@@ -7,12 +7,16 @@
 
 namespace vmck {
 
-// Rows of a block row of the factorisation (the K of the trailing update): the
-// buffer stride of the split panel.  chol_block_rows() is the block-row height
-// used, CHOL_BLOCK unless VMCK_CHOL_BLOCK (128, 256 or 512; read once per
-// process) selects a shorter one.
+// Rows of a block row of the factorisation (the K of the trailing update, and
+// the K stride of the split panel): chol_block_rows(n) is CHOL_BLOCK below
+// n = CHOL_BIG_N / 2, 1024 up to 1.5 CHOL_BIG_N and 2048 above (each block step
+// reads and writes the trailing matrix once, so at large n a taller block cuts
+// that traffic while the leaf chain no longer bounds the time), unless
+// VMCK_CHOL_BLOCK (128 ... 4096, powers of two; read once per process) forces
+// one.
 constexpr int CHOL_BLOCK = 512;
-int chol_block_rows();
+constexpr int64_t CHOL_BIG_N = 32768;
+int chol_block_rows(int64_t n);
 
 // An operand of tc_gemm: FP16 hi / lo rows of a split FP32 matrix, K contiguous
 // (element (row, k) at hi[row * ld + k]); TMA sees kdim x rows and fills zeros

@@ -223,6 +223,48 @@ def test_refined_solve(nk, n, mode):
     np.testing.assert_allclose((L @ L.T).cpu().numpy(), A, atol=2e-5 * np.abs(A).max())
 
 
+_TALL_BLOCKS = r"""
+import sys
+import numpy as np, torch
+sys.path.insert(0, {root!r})
+import netket_gb300 as nk
+n = {n}
+rng = np.random.default_rng(5)
+U = rng.normal(size=(n, 300))
+A = U @ U.T / 300 + 1e-3 * np.eye(n)
+b = rng.normal(size=n)
+At = torch.as_tensor(A, device="cuda")
+A32 = At.float().contiguous()
+st = torch.zeros(1, dtype=torch.int32, device="cuda")
+x, res = nk.kernels.cholesky_solve_refined(At, A32, torch.as_tensor(b, device="cuda"), st,
+                                           max_iter=6, tol=1e-10)
+ref = np.linalg.solve(A, b)
+L = torch.tril(A32).double()
+print(st.item(), res.item(), np.abs(x.cpu().numpy() - ref).max() / np.abs(ref).max(),
+      np.abs((L @ L.T).cpu().numpy() - A).max() / np.abs(A).max())
+"""
+
+
+@pytest.mark.parametrize("blk,n", [(1024, 2600), (1024, 4100), (2048, 4100), (2048, 5000)])
+def test_refined_solve_tall_row_blocks(nk, blk, n):
+    """The 1024- and 2048-row block rows the factorisation takes from n = 16,384
+    and 49,152 on (8 / 16 inner panels per block row, K = 1024 / 2048 trailing
+    updates), forced on smaller matrices with partial block rows
+    (VMCK_CHOL_BLOCK is read once per process: a child process): the factor
+    equals A to FP32 accuracy and the refined solve the FP64 solution."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, VMCK_CHOL_BLOCK=str(blk))
+    out = subprocess.run([sys.executable, "-c", _TALL_BLOCKS.format(root=root, n=n)], env=env,
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    st, res, xerr, ferr = out.stdout.split()[-4:]
+    assert int(st) == 0 and float(res) < 1e-10, out.stdout
+    assert float(xerr) < 1e-9 and float(ferr) < 2e-5, out.stdout
+
+
 @pytest.mark.parametrize("mode", [2, 3, 4])
 def test_refined_solve_flags_non_spd(nk, mode):
     n = 1500
