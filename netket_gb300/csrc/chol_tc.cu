@@ -857,14 +857,17 @@ int chol_events_needed(int64_t n) {
   return (int)(3 * ((n + blk - 1) / blk) + 2);
 }
 
-// Trailing-update CTAs of the side stream: every SM but VMCK_CHOL_RESERVE (read
-// once per process, default 48), which stay free for the chain's kernels.
-static int side_ctas(int sms) {
-  static const int reserve = [] {
+// Trailing-update CTAs of the side stream: every SM but a reserve that stays
+// free for the chain's kernels: 48 below n = CHOL_BIG_N, 24 from there on
+// (measured: the chain's share of the work shrinks with n; n = 65,536: 385 /
+// 366 / 371 ms with 48 / 24 / 12), unless VMCK_CHOL_RESERVE (read once per
+// process) sets it.
+static int side_ctas(int sms, int64_t n) {
+  static const int forced = [] {
     const char *v = getenv("VMCK_CHOL_RESERVE");
-    const int r = v ? atoi(v) : 48;
-    return r < 0 ? 0 : r;
+    return v ? std::max(0, atoi(v)) : -1;
   }();
+  const int reserve = forced >= 0 ? forced : (n >= CHOL_BIG_N ? 24 : 48);
   return std::max(8, sms - reserve);
 }
 
@@ -917,7 +920,7 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
     VMCK_CUDA(cudaStreamWaitEvent(chain, ls->events[3 * nblocks], 0));
     VMCK_CUDA(cudaStreamWaitEvent(side, ls->events[3 * nblocks], 0));
   }
-  const int side_grid = two ? side_ctas(num_sms_dev()) : 0;
+  const int side_grid = two ? side_ctas(num_sms_dev(), n) : 0;
   VMCK_CUDA(cudaFuncSetAttribute(chol_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)CHOL_LEAF_SMEM));
   chol_bounds_kernel<<<1, 256, 0, chain>>>(A, n, scales, status);
