@@ -854,7 +854,7 @@ int64_t chol_tc_workspace_bytes(int64_t n) {
 
 int chol_events_needed(int64_t n) {
   const int64_t blk = chol_block_rows(n);
-  return (int)(3 * ((n + blk - 1) / blk) + 2);
+  return (int)(3 * ((n + blk - 1) / blk) + 2 + 2 * ((n + LB - 1) / LB));
 }
 
 // Trailing-update CTAs of the side stream: every SM but a reserve that stays
@@ -914,11 +914,17 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
   cudaStream_t chain = two ? ls->chain : st, side = two ? ls->side : st;
   cudaEvent_t *F = two ? ls->events : nullptr, *E = F ? F + nblocks : nullptr;
   cudaEvent_t *G = E ? E + nblocks : nullptr;
+  // split block-row updates: PA[p] panel p's rows are written (chain), PB[p] the
+  // update of the rows below panel p + 1 by panel p is done (chain2)
+  const int npanels = (int)((n + LB - 1) / LB);
+  const bool split = two && ls->chain2 && ls->n_events >= 3 * nblocks + 2 + 2 * npanels;
+  cudaEvent_t *PA = split ? G + nblocks + 2 : nullptr, *PB = split ? PA + npanels : nullptr;
   int rc;
   if (two) {
     VMCK_CUDA(cudaEventRecord(ls->events[3 * nblocks], st));
     VMCK_CUDA(cudaStreamWaitEvent(chain, ls->events[3 * nblocks], 0));
     VMCK_CUDA(cudaStreamWaitEvent(side, ls->events[3 * nblocks], 0));
+    if (split) VMCK_CUDA(cudaStreamWaitEvent(ls->chain2, ls->events[3 * nblocks], 0));
   }
   const int side_grid = two ? side_ctas(num_sms_dev(), n) : 0;
   VMCK_CUDA(cudaFuncSetAttribute(chol_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -943,9 +949,11 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
     const SplitOperand ph{qh, ql, blk, w, n - k0};
     if (two && b >= 2)
       VMCK_CUDA(cudaStreamWaitEvent(chain, G[b - 2], 0));  // side is done with this buffer
+    bool pb_pending = false;  // PB[pi - 1] recorded in this block row
     for (int64_t r0 = k0; r0 < k1; r0 += LB) {
       const int64_t r1 = std::min<int64_t>(k1, r0 + LB);
       const int mp = (int)(r1 - r0), pp = (int)((r0 - k0) / LB);
+      const int pi = (int)(r0 / LB);
       {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(1);
@@ -975,11 +983,34 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
         // rest of the block row; rows [r1, r1 + next) feed the next panel (split)
         const int next = (int)std::min<int64_t>(LB, k1 - r1);
         const SplitOperand pk{qh, ql, blk, pp * LB + mp, n - k0};
-        if ((rc = tc_gemm(chain, pk, (int)(r1 - k0), pk, (int)(r1 - k0), pp * LB,
-                          (int)(k1 - r1), (int)(n - r1), mp, A + r1 + r1 * n, n, -1.0f, 1.0f,
-                          scales + 1, scales + 1, 1, bs_hi, bs_lo, LB, next, next, scales + 0,
-                          status, 0)))
-          return rc;
+        if (!split) {
+          if ((rc = tc_gemm(chain, pk, (int)(r1 - k0), pk, (int)(r1 - k0), pp * LB,
+                            (int)(k1 - r1), (int)(n - r1), mp, A + r1 + r1 * n, n, -1.0f, 1.0f,
+                            scales + 1, scales + 1, 1, bs_hi, bs_lo, LB, next, next,
+                            scales + 0, status, 0)))
+            return rc;
+        } else {
+          // the next panel's rows on the chain (after the previous panel's update
+          // of the same rows on chain2), the rows below them on chain2
+          const int64_t r2 = r1 + next;
+          if (r2 < k1) VMCK_CUDA(cudaEventRecord(PA[pi], chain));
+          if (pb_pending) VMCK_CUDA(cudaStreamWaitEvent(chain, PB[pi - 1], 0));
+          pb_pending = false;
+          if ((rc = tc_gemm(chain, pk, (int)(r1 - k0), pk, (int)(r1 - k0), pp * LB, next,
+                            (int)(n - r1), mp, A + r1 + r1 * n, n, -1.0f, 1.0f, scales + 1,
+                            scales + 1, 1, bs_hi, bs_lo, LB, next, next, scales + 0, status, 0)))
+            return rc;
+          if (r2 < k1) {
+            VMCK_CUDA(cudaStreamWaitEvent(ls->chain2, PA[pi], 0));
+            if ((rc = tc_gemm(ls->chain2, pk, (int)(r2 - k0), pk, (int)(r2 - k0), pp * LB,
+                              (int)(k1 - r2), (int)(n - r2), mp, A + r2 + r2 * n, n, -1.0f,
+                              1.0f, scales + 1, scales + 1, 1, nullptr, nullptr, 0, 0, 0,
+                              nullptr, status, 0)))
+              return rc;
+            VMCK_CUDA(cudaEventRecord(PB[pi], ls->chain2));
+            pb_pending = true;
+          }
+        }
       }
     }
     if (k1 == n) break;
@@ -1025,6 +1056,10 @@ int chol_tc_factor(cudaStream_t st, float *A, int64_t n, void *ws, int32_t *stat
     VMCK_CUDA(cudaStreamWaitEvent(st, ls->events[3 * nblocks], 0));
     VMCK_CUDA(cudaEventRecord(ls->events[3 * nblocks + 1], side));
     VMCK_CUDA(cudaStreamWaitEvent(st, ls->events[3 * nblocks + 1], 0));
+    if (split) {  // (already ordered through the chain; kept explicit)
+      VMCK_CUDA(cudaEventRecord(ls->events[3 * nblocks], ls->chain2));
+      VMCK_CUDA(cudaStreamWaitEvent(st, ls->events[3 * nblocks], 0));
+    }
   }
   return VMCK_OK;
 }

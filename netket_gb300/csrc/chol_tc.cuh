@@ -61,11 +61,15 @@ int64_t chol_tc_workspace_bytes(int64_t n);
 
 // Streams and events of the look-ahead factorisation (owned by the caller):
 // chain (high priority) runs the latency-bound panel chain, side the bulk of the
-// trailing updates; events: chol_events_needed(n).
+// trailing updates, chain2 (high priority, optional) the rest of each panel's
+// block-row update; events: chol_events_needed(n).
 struct CholStreams {
   cudaStream_t chain, side;
   cudaEvent_t *events;
   int n_events;
+  // (optional, high priority) the part of a panel's block-row update below the
+  // next panel's rows, off the chain
+  cudaStream_t chain2 = nullptr;
 };
 int chol_events_needed(int64_t n);
 

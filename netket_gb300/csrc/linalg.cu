@@ -35,6 +35,7 @@ struct vmck_ctx {
   // updates and a pool of events (two per panel), created on first use
   cudaStream_t side = nullptr;
   cudaStream_t chain = nullptr;  // highest priority: the factorisation's critical path
+  cudaStream_t chain2 = nullptr;  // highest priority: the rest of each panel's block-row update
   cublasHandle_t blas2 = nullptr;
   cudaEvent_t *events = nullptr;
   int n_events = 0;
@@ -1043,6 +1044,7 @@ static int streams_setup(vmck_ctx *c, int need) {
     VMCK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     VMCK_CUDA(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, lo));
     VMCK_CUDA(cudaStreamCreateWithPriority(&c->chain, cudaStreamNonBlocking, hi));
+    VMCK_CUDA(cudaStreamCreateWithPriority(&c->chain2, cudaStreamNonBlocking, hi));
   }
   if (c->n_events < need) {
     cudaEvent_t *ev = static_cast<cudaEvent_t *>(malloc(sizeof(cudaEvent_t) * need));
@@ -1397,6 +1399,7 @@ extern "C" int vmck_ctx_destroy(vmck_ctx *c) {
   if (c->blas2) cublasDestroy(c->blas2);
   if (c->side) cudaStreamDestroy(c->side);
   if (c->chain) cudaStreamDestroy(c->chain);
+  if (c->chain2) cudaStreamDestroy(c->chain2);
   if (c->params) cusolverDnDestroyParams(c->params);
   if (c->solver) cusolverDnDestroy(c->solver);
   if (c->blas) cublasDestroy(c->blas);
@@ -1504,7 +1507,7 @@ static int refined_solve(vmck_ctx *c, cudaStream_t st, const double *A64, float 
       if ((rc = check_launch("refined solve padding"))) return rc;
     }
     if ((rc = streams_setup(c, chol_events_needed(np)))) return rc;
-    const CholStreams ls{c->chain, c->side, c->events, c->n_events};
+    const CholStreams ls{c->chain, c->side, c->events, c->n_events, c->chain2};
     rc = chol_tc_factor(st, F, np, static_cast<char *>(c->tcws) + tc_off, status, &yinv, &ls);
     if (rc) return rc;
     if (np != n)
