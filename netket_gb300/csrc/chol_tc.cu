@@ -519,9 +519,9 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
 #pragma unroll
       for (int i = 0; i < 32; ++i) c[i] = S[(P + i) * LLD + P + lane];
       bool bad = false;
+      float d = __shfl_sync(0xffffffffu, c[0], 0);
 #pragma unroll 1
       for (int k = 0; k < 32; ++k) {
-        float d = __shfl_sync(0xffffffffu, c[0], k);
         if (!(d > 0.0f)) {
           bad = true;
           d = 1.0f;
@@ -530,10 +530,16 @@ __global__ void __launch_bounds__(LEAF_T, 1) chol_leaf_kernel(float *__restrict_
         const float u = (lane == k) ? d * inv : (lane > k ? c[0] * inv : 0.0f);  // U(k, lane)
         S[(P + k) * LLD + P + lane] = u;
         if (lane == 0) rd[P + k] = inv;
+        // the next pivot's row first and its diagonal broadcast at once: the
+        // dependency from one pivot to the next is then these two steps, and
+        // the other 30 row updates issue while the broadcast is in flight
+        c[0] = fmaf(-__shfl_sync(0xffffffffu, u, (k + 1) & 31), u, c[1]);
+        const float dn = __shfl_sync(0xffffffffu, c[0], (k + 1) & 31);
 #pragma unroll
-        for (int i = 1; i < 32; ++i)
+        for (int i = 2; i < 32; ++i)
           c[i - 1] = fmaf(-__shfl_sync(0xffffffffu, u, (k + i) & 31), u, c[i]);
         c[31] = 0.0f;
+        d = dn;
       }
       if (bad && lane == 0) not_spd = 1;
     }
