@@ -677,9 +677,9 @@ def main():
     ap.add_argument("--n-samples", type=int, default=WORKLOAD["n_samples"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gram-traffic", type=float, default=None)
-    # DRAM bytes of one n = 16,384 solve, summed over its 473 launches in one ncu
+    # DRAM bytes of one n = 16,384 solve, summed over its 537 launches in one ncu
     # capture (profiles/cholesky_solve_dram_n16384.md)
-    ap.add_argument("--solve-traffic", type=float, default=18.88e9,
+    ap.add_argument("--solve-traffic", type=float, default=15.69e9,
                     help="DRAM bytes of one solve (ncu); reported as roofline.traffic")
     ap.add_argument("--matched-steps", type=int, default=8,
                     help="steps of the matched-energy comparison (0 skips it)")
