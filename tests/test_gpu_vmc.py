@@ -137,6 +137,45 @@ def test_vmc_sr_minsr_step_mixed_matches_fp64(nk):
     assert u_err < 1.2e-4, u_err
 
 
+def _heisenberg16(nk, precision, seed):
+    """The large configuration's model at 4,096 samples: 16x16 Heisenberg (J = 1,
+    Marshall sign, Sz = 0), RBM alpha 8 (M = 2048), Exchange sampler on the nn
+    clusters, minSR with diag_shift 1e-4, SGD lr 0.005."""
+    g = nk.graph.Square(16)
+    hi = nk.hilbert.Spin(0.5, N=256, total_sz=0)
+    H = nk.operator.Heisenberg(hi, g, J=1.0, sign_rule=True)
+    vs = nk.vqs.MCState(nk.sampler.MetropolisExchange(hi, graph=g, n_chains=1024),
+                        nk.models.RBM(alpha=8), n_samples=4096, n_discard_per_chain=5,
+                        seed=seed, precision=precision)
+    drv = nk.driver.VMC_SR(H, nk.optimizer.Sgd(0.005), diag_shift=1e-4, variational_state=vs,
+                           use_ntk=True)
+    return H, vs, drv
+
+
+def test_minsr_step_mixed_matches_fp64_at_alpha8(nk):
+    """One minSR step of the large configuration's model (16x16, alpha 8, M =
+    2048) at 4,096 samples: the mixed path -- the Exchange kernel that reads W
+    through L2, x W and O^T v on tcgen05, the mode-4 tensor-core Gram (M > 512),
+    the FP32 factor refined to an FP64 residual -- on the FP64 path's samples,
+    after two FP64 steps.  Bounds: energy 1e-7 relative, update 1e-4 relative
+    (measured on a GB300: 3.1e-8 and 1.8e-5)."""
+    _, vs64, drv64 = _heisenberg16(nk, "fp64", 2)
+    _, vsm, drvm = _heisenberg16(nk, "mixed", 2)
+    box = _pin_samples(vsm)
+    drv64.advance(2)
+    vsm.flat_parameters = vs64.flat_parameters.clone()
+    s64, d64 = drv64.compute_loss_and_update()
+    box["x"] = vs64.samples.clone()
+    sm, dm = drvm.compute_loss_and_update()
+    assert drvm.info["status"] == 0
+    e_err = abs(sm.mean - s64.mean) / abs(s64.mean)
+    d64, dm = d64.cpu().numpy(), dm.cpu().numpy()
+    u_err = np.linalg.norm(dm - d64) / np.linalg.norm(d64)
+    print(f"mixed vs fp64 at 16x16 alpha 8, n=4096: energy {e_err:.3e}, update {u_err:.3e}")
+    assert e_err < 1e-7, e_err
+    assert u_err < 1e-4, u_err
+
+
 def test_mixed_trajectory_tracks_fp64(nk):
     """Matched energy error: 50 minSR steps of a 6x6 J1-J2 model (alpha 2, 1,024
     samples) from the same initial parameters.  The mixed run takes the FP64 run's
