@@ -10,19 +10,17 @@ Two ways to form T:
     ``O(s).O(s') = (t_s.t_s')(1 + x_s.x_s') + x_s.x_s'`` (t = tanh theta) turns
     the (n x n x P) contraction into (n x n x M), and O is never stored.  For an
     FP32 t the contraction is shifted by the column mean and the shift is added
-    back in double-float (no cancellation); ``gram_mode=2`` (default) contracts
-    on the tensor cores (tcgen05) with t rounded to hi + lo BF16 pairs (all four
-    products, so T is the Gram matrix of a 16-bit-mantissa Jacobian; the large
-    hi * hi part accumulates apart from the small cross terms), ``3`` with one
-    BF16, ``1`` in FP32 on the CUDA cores.  At n = 16,384, M = 400 and
-    diag_shift 1e-4 the minSR update of mode 2 is within 1.2e-4 (relative) of
-    the all-FP64 one, mode 1 within 2.5e-4, mode 3 within 2.4e-2.  The tensor
-    cores' FP32 accumulation loses bits in proportion to the MMA chain length, so
-    at M = 2048 (16 x 16, alpha 8) mode 2's T is no longer positive definite;
-    above ``TC_GRAM_MAX_M`` the default is mode 4, FP16 hi/lo operands (all four
-    products, so T stays the Gram matrix of hi + lo) whose
-    accumulators are drained into FP32 registers every 64 columns of K (the
-    factorisation's trailing-update GEMM) followed by the double-float assembly;
+    back in double-float (no cancellation).  ``gram_mode=4`` (default) contracts
+    on the tensor cores (tcgen05) with t - s0 on a 2^-19 grid split into
+    fixed-point FP16 hi + lo (all four products, so T is the Gram matrix of
+    that Jacobian; every 64-wide slab of hi * hi sums exactly and the slabs add
+    in FP32 registers), then a double-float assembly pass; ``2`` rounds t to hi +
+    lo BF16 pairs and accumulates in tensor memory over the whole K (its T lost
+    positive definiteness at M = 2048: the accumulation error grows with the MMA
+    chain), ``3`` one BF16, ``1`` FP32 on the CUDA cores.  At the 10 x 10 alpha-4
+    workload (n = 4,096, diag_shift 1e-4) the minSR update of mode 4 is within
+    1.1e-5 (relative) of the all-FP64 one, mode 2 within 2.9e-5; at n = 16,384
+    mode 4 takes 2.0 ms for T, mode 2 2.5 ms;
   * ``gram="dense"``: the reference algorithm, a materialised (n, P) Jacobian
     and a cuBLAS SYRK.
 Solvers (``solve=``):
@@ -57,7 +55,9 @@ def _status():
     return torch.zeros(1, dtype=torch.int32, device=nat.device())
 
 
-TC_GRAM_MAX_M = 512
+# FP32 Jacobians with M up to this use gram_mode 2 by default, larger ones mode 4
+# (0: mode 4 everywhere -- faster and closer to FP64 at every size measured)
+TC_GRAM_MAX_M = 0
 
 
 def _o_l_v(t, x, N, M, obar, s, v):
@@ -92,9 +92,6 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
         elif t.dtype == torch.float64:
             mode = 0
         else:
-            # the tensor cores' FP32 accumulation over K = M of the hi * hi term keeps T
-            # positive definite at M = 400 (diag_shift 1e-4) but not at M = 2048:
-            # there the per-slab drained GEMM
             mode = 2 if M <= TC_GRAM_MAX_M else 4
     obar = K.column_means(t, x, N, M)
     dv = K.center_scale(e, mean_dev, 2.0 * s)

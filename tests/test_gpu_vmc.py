@@ -115,11 +115,12 @@ def _pin_samples(vs):
 def test_vmc_sr_minsr_step_mixed_matches_fp64(nk):
     """One minSR step at the benchmark's shape (10x10 J1-J2, alpha 4, M = 400) with
     4,096 samples: the mixed path (FP32 sampler / local-energy kernels, tensor-core
-    Gram of t rounded to hi + lo BF16 pairs, FP32 factor refined to an FP64
-    residual) on the FP64 path's samples.  Bounds: energy 1e-7 relative, update
-    1.2e-4 relative (measured on a GB300: 1.2e-8 and 2.9e-5; the Gram matrix of
-    the 16-bit-mantissa Jacobian differs from the FP64 one by ~1e-6 relative, and
-    minSR amplifies it by the conditioning of T at diag_shift 1e-4)."""
+    Gram of t - s0 on a 2^-19 grid, FP32 factor refined to an FP64 residual) on
+    the FP64 path's samples.  Bounds: energy 1e-7 relative, update 1.2e-4
+    relative (measured on a GB300: 1.2e-8 and 1.1e-5; with the BF16 hi + lo Gram,
+    gram_mode 2, 2.9e-5: the Gram matrix of the rounded Jacobian differs from
+    the FP64 one by ~1e-6 relative, and minSR amplifies it by the conditioning of
+    T at diag_shift 1e-4)."""
     _, vs64, drv64 = _j1j2(nk, 10, 4, 1024, 4096, 1, "fp64")
     H, vsm, drvm = _j1j2(nk, 10, 4, 1024, 4096, 1, "mixed")
     box = _pin_samples(vsm)
