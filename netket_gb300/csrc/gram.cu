@@ -288,25 +288,16 @@ __global__ void __launch_bounds__(256) gram_assemble_kernel(
 #pragma unroll
   for (int w = 0; w < 9; ++w) cb[w] = w < words ? bits[c * words + w] : 0u;
   const float2 wc = wdf[c], hc = hdf[c], q = *s0sq_p;
-  // four rows at a time: their T32 loads are in flight together
-  for (int64_t rb = r0 > c ? r0 : c; rb < r1; rb += 4) {
-    float a[4];
+  for (int64_t r = r0 > c ? r0 : c; r < r1; ++r) {
+    int diff = 0;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) a[u] = rb + u < r1 ? T32[(rb + u) * n + c] : 0.0f;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int64_t r = rb + u;
-      if (r >= r1) break;
-      int diff = 0;
-#pragma unroll
-      for (int w = 0; w < 9; ++w)
-        if (w < words) diff += __popc(cb[w] ^ __ldg(bits + r * words + w));
-      const int64_t e = r * n + c;
-      const df32 v = gram_value_df(a[u], wdf[r], wc, df32{q.x, q.y}, N - 2 * diff, hdf[r], hc,
-                                   inv_n, r == c, shift);
-      T32[e] = v.hi + v.lo;
-      if (T64) T64[e] = df_to_double(v);
-    }
+    for (int w = 0; w < 9; ++w)
+      if (w < words) diff += __popc(cb[w] ^ __ldg(bits + r * words + w));
+    const int64_t e = r * n + c;
+    const df32 v = gram_value_df(T32[e], wdf[r], wc, df32{q.x, q.y}, N - 2 * diff, hdf[r], hc,
+                                 inv_n, r == c, shift);
+    T32[e] = v.hi + v.lo;
+    if (T64) T64[e] = df_to_double(v);
   }
 }
 
