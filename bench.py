@@ -370,7 +370,10 @@ def run_ours(args):
             executed = float(n) * (n + 1) * 4 * (-(-M // 64) * 64)
             kname = ("structured Gram T = O_L O_L^T (tcgen05 tc_gemm_kernel, FP16 hi/lo, "
                      "drained accumulation, + gram_assemble_kernel)")
-            traffic = args.gram_traffic
+            # DRAM bytes of the GEMM and the assembly pass at n = 16,384 (ncu,
+            # profiles/j1j2_10x10_minsr_step_launches.md), n^2 for other sizes
+            traffic = args.gram_traffic if args.gram_traffic is not None else \
+                (0.525e9 + 2.085e9) * (n / 16384.0) ** 2
         achieved = flops / (gram_ms * 1e-3) / 1e12
         roof_gram = {"kernel": kname,
                      "bound": "tensor", "achieved": round(achieved, 3),
@@ -679,7 +682,7 @@ def main():
     ap.add_argument("--gram-traffic", type=float, default=None)
     # DRAM bytes of one n = 16,384 solve, summed over its 537 launches in one ncu
     # capture (profiles/cholesky_solve_dram_n16384.md)
-    ap.add_argument("--solve-traffic", type=float, default=15.69e9,
+    ap.add_argument("--solve-traffic", type=float, default=15.72e9,
                     help="DRAM bytes of one solve (ncu); reported as roofline.traffic")
     ap.add_argument("--matched-steps", type=int, default=8,
                     help="steps of the matched-energy comparison (0 skips it)")
