@@ -154,8 +154,9 @@ def minsr_update(t, x, N, M, e, mean_dev, diag_shift, *, gram="structured", gram
 
 def minsr_fallback(info, try_pcg=True, pinv=True):
     """delta after a failed solve (``try_pcg=False``: pinv_smooth directly;
-    ``pinv=False``: None where pinv_smooth would be the answer).  The FP64 Cholesky of the reference solves T
-    up to cond(T) ~ 1e15; the FP32 factor here stops near 1e7.  So a failed
+    ``pinv=False``: None where pinv_smooth would be the answer).  The FP64
+    Cholesky of the reference solves T up to cond(T) ~ 1e15; the FP32 factor
+    here stops near 1e7.  So a failed
     factor of a finite, structured T is first retried as shifted-factor PCG
     against the FP64 T (``kernels.cholesky_solve_pcg``: the FP64 solution);
     only if that fails too -- T not positive definite, or not finite -- does it
