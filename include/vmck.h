@@ -401,10 +401,11 @@ int vmck_rbm_jacobian(vmck_stream s, int32_t dtype, const void *tanh_theta,
  * mode 0: FP64 contraction (CUDA cores); 1: FP32 contraction (CUDA cores);
  * 2: tensor cores (tcgen05, TMA) on t rounded to hi + lo BF16 pairs (all four
  * products, FP32 accumulation); 3: tensor cores on t rounded to one BF16;
- * 4: tensor cores on t split into FP16 hi + lo (all four products) with the FP32
- * accumulators drained to registers every 64-wide slab (the accuracy of mode 2
- * at any M: the tensor cores' accumulation error grows with the chain length),
- * the exact terms added by a separate assembly pass.
+ * 4: tensor cores on t - fp32(tbar) rounded to a multiple of 2^-19 and split
+ * into fixed-point FP16 hi + lo (all four products): every 64-wide slab of the
+ * hi * hi products sums exactly, the slabs add in FP32 registers (mode 2's
+ * accumulation error grows with the MMA chain and lost positive definiteness
+ * at M = 2048), and a separate assembly pass adds the exact terms.
  * Modes 1-4 take tanh_theta in FP32 and contract the shifted c = t - fp32(tbar)
  * (tbar = obar[0:M]), adding the shift back exactly in a double-float epilogue,
  * so T is the exact Gram matrix of the contracted Jacobian (positive
